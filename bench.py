@@ -1,0 +1,352 @@
+"""Benchmark: bases/s into the filtered k-mer graph on one GB300.
+
+Workload (one step = one full graph build over one batch of reads):
+  seeded synthetic genome of 5 Mbp (GC 50%), 2.5M reads x 100 bp sampled
+  from both strands at 50x, 1% iid substitutions + 0.1% single-base indels,
+  k=31, c=5 (uint64 keys, saturating uint8 multiplicities).
+A step = occurrence prefix + tile table + HyperLogLog sizing + table clear +
+K1 extract/count + K2 cutoff/compaction, with the packed reads resident in
+HBM. L2 is flushed (a 256 MiB write) before every timed step.
+
+Prints ONE JSON line (rank 0). `e2e` repeats the measurement through the
+C-ABI call on HOST (pinned) packed reads, with the host->device copy of the
+reads and the device->host copy of the filtered graph inside the timed
+region. `--impl reference` times the reference's CPU path instead.
+
+Multi-GPU (torchrun): every rank builds its own replica of the workload
+(independent samples, no data-path collective); value = all bases / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "swap-assembler_gb300"))
+
+METRIC = "bases/s into filtered k-mer graph on 1 GB300"
+WORKLOAD = dict(seed=2, genome_len=5_000_000, gc=0.5, n_reads=2_500_000, read_len=100,
+                sub_rate=0.01, indel_rate=0.001)
+K, CUTOFF = 31, 5
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-probe", action="store_true", help="skip the random-access probe")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def config_dict() -> dict:
+    return {"workload": "plain single-sample build: 5 Mbp genome (GC 50%), 2.5M x 100 bp reads "
+                        "at 50x from both strands, 1% subs + 0.1% indels, k=31, c=5",
+            "genome_bp": WORKLOAD["genome_len"], "reads": WORKLOAD["n_reads"],
+            "read_len": WORKLOAD["read_len"], "k": K, "c": CUTOFF,
+            "inputs": "packed 2-bit reads resident in HBM", "l2": "flushed before every step"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict | None:
+        rows = []
+        for l in self.lines:
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i in range(4) if r[i] == "Active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            pass
+    return {}
+
+
+def k_count_traffic_per_occ() -> tuple[float | None, str | None]:
+    p = ROOT / "profiles" / "k_count_ncu.json"
+    if not p.exists():
+        return None, None
+    d = json.loads(p.read_text())
+    return d.get("dram_bytes_per_occurrence"), d.get("source")
+
+
+def cpu_baseline(text: bytes, n_bases: int, budget_s: float = 20.0) -> dict:
+    """The oracle port timed on this host's cores on a bounded prefix sample."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    threads = oracle.cores()
+    # calibrate on ~2% of the reads, then size the sample for about budget_s
+    cut = lambda frac: text[: text.index(b"\n>", int(len(text) * frac)) + 1]
+    t0 = time.perf_counter()
+    small = cut(0.02)
+    oracle.records(small, K, CUTOFF, threads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    frac = min(1.0, 0.02 * budget_s / dt / 2)
+    sample = text if frac >= 1.0 else cut(frac)
+    nb = oracle.parse(sample, K)["n_bases"]
+    t0 = time.perf_counter()
+    oracle.records(sample, K, CUTOFF, threads)
+    dt = time.perf_counter() - t0
+    return {"value": nb / dt, "unit": "bases/s", "cores": threads, "kind": "port",
+            "sample": "first %d of %d bases (framing + count + cutoff, sorted records), %.1f s"
+                      % (nb, n_bases, dt)}
+
+
+def run_reference_arm(args) -> int:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import swapgb
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    text = swapgb.synth_fasta(**WORKLOAD)
+    kind = "port"
+    threads = oracle.cores()
+    # bounded sample: about one quarter of the workload's reads per step
+    sample = text[: text.index(b"\n>", len(text) // 4) + 1]
+    nb = oracle.parse(sample, K)["n_bases"]
+    for _ in range(max(args.warmup, 0)):
+        oracle.records(sample, K, CUTOFF, threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.records(sample, K, CUTOFF, threads)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * statistics.mean(times)
+    value = nb / (ms * 1e-3)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "bases/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic", "config": config_dict(),
+        "cpu_baseline": {"value": value, "unit": "bases/s", "cores": threads, "kind": kind,
+                         "sample": "first %d bases of the workload per step (framing + count + "
+                                   "cutoff), the reference's algorithm restated in C with one "
+                                   "thread per MPI rank" % nb},
+        "e2e": {"value": value, "unit": "bases/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main() -> int:
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import swapgb
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    text = swapgb.synth_fasta(**WORKLOAD)
+    reads = swapgb.reads_from_fasta(text, K)
+    n_bases = reads.n_bases
+    n_occ = int((reads.len.astype(np.int64) - K + 1).clip(min=0).sum())
+    stream = torch.cuda.current_stream(dev)
+    opts = swapgb.Opts(k=K, cutoff=CUTOFF, stream=stream.cuda_stream)
+
+    d_packed = torch.from_numpy(reads.packed.view(np.int32).copy()).to(dev)
+    d_off = torch.from_numpy(reads.off.view(np.int64).copy()).to(dev)
+    d_len = torch.from_numpy(reads.len.view(np.int32).copy()).to(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    g = swapgb.Graph()
+
+    def step():
+        g.build_device(opts, d_packed.data_ptr(), d_packed.numel(), d_off.data_ptr(),
+                       d_len.data_ptr(), d_off.numel())
+
+    for _ in range(max(args.warmup, 3)):
+        flush.fill_(1)
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    count_ms, launches = [], 0
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        t_wall0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(i)
+            evs[i][0].record(stream)
+            step()
+            evs[i][1].record(stream)
+            ms, nl = g.timings()
+            count_ms.append(ms[2])
+            launches += nl
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall0
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    ms_per_step = statistics.mean(step_ms)
+    if world > 1:
+        t = torch.tensor([ms_per_step], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_per_step = float(t.item())
+    value = world * n_bases / (ms_per_step * 1e-3)
+    survivors, distinct = g.size(), g.distinct()
+
+    # ---- end to end through the C ABI on pinned host buffers ----
+    h_packed = torch.from_numpy(reads.packed.view(np.int32).copy()).pin_memory()
+    h_off = torch.from_numpy(reads.off.view(np.int64).copy()).pin_memory()
+    h_len = torch.from_numpy(reads.len.view(np.int32).copy()).pin_memory()
+    h_keys = torch.empty(max(survivors, 1) + (1 << 20), dtype=torch.int64).pin_memory()
+    h_mult = torch.empty_like(h_keys)
+    g2 = swapgb.Graph()
+    lib = swapgb.lib()
+
+    def e2e_step() -> int:
+        swapgb._check(lib.swg_graph_build(g2._h, swapgb.C.byref(opts), h_packed.data_ptr(),
+                                          h_packed.numel(), h_off.data_ptr(), h_len.data_ptr(),
+                                          h_off.numel()), "swg_graph_build")
+        n = swapgb.C.c_uint64()
+        swapgb._check(lib.swg_graph_copy_out(g2._h, h_keys.data_ptr(), h_mult.data_ptr(),
+                                             h_keys.numel(), 0, swapgb.C.byref(n)), "copy_out")
+        return n.value
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_t = []
+    for _ in range(max(3, min(args.steps, 10))):
+        t0 = time.perf_counter()
+        n_e2e = e2e_step()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(e2e_t)
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = h_packed.numel() * 4 + h_off.numel() * 8 + h_len.numel() * 4
+    d2h = n_e2e * 16
+
+    # ---- roofline of the dominant kernel (K1 extract+count) ----
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    peak_src = "of measured" if hbm else "of fallback"
+    hbm = hbm or 6800.0
+    k1_ms = statistics.mean(count_ms)
+    algo_bytes = n_occ * 64 + n_bases / 4 + reads.n_reads * 12
+    achieved = algo_bytes / (k1_ms * 1e-3) / 1e9
+    tpo, tsrc = k_count_traffic_per_occ()
+    roofline = {"kernel": "k_count", "bound": "hbm", "achieved": achieved, "peak": hbm,
+                "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src,
+                "traffic": (tpo * n_occ) if tpo else None, "traffic_source": tsrc,
+                "algorithmic_bytes": algo_bytes,
+                "bytes_model": "64 B per k-mer occurrence (one 32 B sector of the hash-table "
+                               "entry read + written back) + 0.25 B per base + 12 B per read",
+                "k_count_ms": k1_ms}
+    atomic = None
+    if not args.no_probe and rank == 0:
+        table_bytes = 16 << 30
+        r_red = swapgb.probe_random_access("red_add_u32", table_bytes, 1 << 31, stream.cuda_stream)
+        r_pat = swapgb.probe_random_access("load16_cas128", table_bytes, 1 << 30, stream.cuda_stream)
+        # per read of length L: (L-k+1) key probes + 2(L-k) slot increments
+        ops = n_occ + 2 * (n_occ - int((reads.len >= K).sum()))
+        achieved_ops = ops / (k1_ms * 1e-3)
+        atomic = {"R_red_add_u32_per_s": r_red, "load16_cas128_per_s": r_pat,
+                  "table_bytes": table_bytes, "ops_per_step": ops,
+                  "achieved_ops_per_s": achieved_ops, "frac_of_R": achieved_ops / r_red,
+                  "occurrences_per_s": n_occ / (k1_ms * 1e-3),
+                  "frac_occ_vs_load16_cas128": (n_occ / (k1_ms * 1e-3)) / r_pat}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(text, n_bases)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "bases/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (seeded generator, no dataset)", "config": config_dict(),
+            "e2e": {"value": world * n_bases / e2e_s, "unit": "bases/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "path": "swg_graph_build on pinned host packed reads + swg_graph_copy_out"},
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "random_access": atomic,
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "kmers_per_s": world * n_occ / (ms_per_step * 1e-3),
+            "occurrences": n_occ, "distinct": distinct, "survivors": survivors,
+            "wall_s_timed_region": t_wall,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,165 @@
+/*
+ * swapgb.h — C ABI of the GB300 k-mer graph builder.
+ *
+ * The library builds SWAP-Assembler's filtered k-mer graph (every canonical
+ * k-molecule with its 8 strand-oriented edge multiplicities, after the -c
+ * cutoff) on one GPU. All entry points are plain C: pointers, sizes and
+ * status codes; no exceptions cross the boundary and nothing calls exit().
+ *
+ * Reference seams each entry point replaces (files of the reference project):
+ *   parameter::getopt / getParameters ......... sequence.cpp:4-183 (CLI `swap`)
+ *   MPIEnviroment::File_read + read framing .... mympi.cpp:108-120,
+ *                                                kmerGraph.cpp:95-233 -> swg_reads_from_fasta
+ *   kmerGraph::constructKmerGraph +
+ *   distNodeGraph::constructDistNodeGraph +
+ *   distNodeGraph::cutoffGraph ................. kmerGraph.cpp:95-310, graph.cpp:1049-1114
+ *                                                -> swg_build, swg_build_device, swg_graph_build*
+ *   distNodeGraph::kmolecules (hash_map<u64,arc>) graph.cpp:36-40,353 -> swg_graph_copy_out,
+ *                                                swg_graph_device_view
+ *   distNodeGraph::graphStatistics ............. graph.cpp:1569-1627 -> swg_graph_stats
+ *   distNodeGraph::printKmerGraph (-s output) .. graph.cpp:3352-3440 -> swg_graph_write_kmer_graph
+ *   distNodeGraph::printLocalNodeGraph ......... graph.cpp:555-572 -> swg_graph_write_node_lines
+ *
+ * Packed read layout (host or device memory):
+ *   packed   uint32 words; base i of the concatenated read stream sits in
+ *            word i/16 at bits [31-2*(i%16), 30-2*(i%16)] (first base most
+ *            significant, the reference's encoding order, kmerGraph.cpp:16-24),
+ *            codes A=0 C=1 G=2 T=3 (sequence.cpp:164-168).
+ *   read_off base offset of each read in the stream (uint64).
+ *   read_len length of each read (uint32). Reads shorter than k contribute
+ *            nothing (kmerGraph.cpp:182-187).
+ *
+ * Results: keys are canonical k-molecules, max(kmer, reverse complement)
+ * (kmerGraph.cpp:246-247); mult holds 8 bytes per key, slot t = the
+ * reference's arc::multiplicity[t] (graph.cpp:36-40): saturating uint8
+ * counts (graph.cpp:1076) after the cutoff (graph.cpp:1105).
+ *
+ * Threading: distinct handles may be used from distinct host threads; one
+ * handle must not be used concurrently. Every device operation of a call is
+ * ordered on the stream given in swg_opts (or the library's own stream).
+ */
+#ifndef SWAPGB_H
+#define SWAPGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum swg_status {
+    SWG_OK = 0,
+    SWG_ERR_BAD_INPUT = 1,  /* bad argument, k out of range, malformed FASTA */
+    SWG_ERR_TABLE_FULL = 2, /* hash table probe limit hit after all internal retries */
+    SWG_ERR_OOM = 3,        /* device or host allocation failed */
+    SWG_ERR_ADMISSION = 4,  /* server: request larger than the memory budget */
+    SWG_ERR_TIMEOUT = 5,    /* a bounded device-side retry loop gave up */
+    SWG_ERR_CUDA = 6,       /* CUDA runtime error (message in swg_last_error) */
+    SWG_ERR_NO_DEVICE = 7,  /* no CUDA device visible */
+    SWG_ERR_BAD_STATE = 8,  /* handle used in a state that does not allow the call */
+    SWG_ERR_IO = 9,         /* file could not be read or written */
+    SWG_ERR_NOT_READY = 10  /* server: result not finished yet */
+} swg_status;
+
+typedef struct swg_opts {
+    int k;                      /* 1..31; the CLI enforces the reference's odd 19..31 */
+    int cutoff;                 /* -c: slot kept iff multiplicity >= cutoff */
+    double load_factor;         /* target hash-table load, (0,0.9]; 0 selects 0.6 */
+    uint64_t expected_distinct; /* table sizing hint; 0 = estimate on the device */
+    void *stream;               /* cudaStream_t; NULL = the library's own stream */
+} swg_opts;
+
+typedef struct swg_reads swg_reads; /* host-side packed reads */
+typedef struct swg_graph swg_graph; /* device-resident filtered k-mer graph + workspace */
+
+/* ---- status ---------------------------------------------------------- */
+const char *swg_status_string(swg_status s);
+/* Last error message of the calling thread ("" if none). */
+const char *swg_last_error(void);
+/* Library version string. */
+const char *swg_version(void);
+
+/* ---- host FASTA framing and 2-bit packing ----------------------------- */
+/* Reproduces the reference's framing (kmerGraph.cpp:113-114,160-233): from the
+ * first '>', alternating header / single sequence line, each ended by '\n';
+ * acgt upper-cased, any other byte read as 'A'; reads shorter than k dropped.
+ * Input the reference never finishes (last record without '\n', NUL bytes,
+ * no '>') returns SWG_ERR_BAD_INPUT. */
+swg_status swg_reads_from_fasta(const char *text, uint64_t len, int k, swg_reads **out);
+swg_status swg_reads_from_fasta_file(const char *path, int k, swg_reads **out);
+/* Borrowed views into the packed read set (valid until swg_reads_free). */
+swg_status swg_reads_view(const swg_reads *r, const uint32_t **packed, uint64_t *n_words,
+                          const uint64_t **read_off, const uint32_t **read_len,
+                          uint64_t *n_reads, uint64_t *n_bases);
+/* Records seen while framing, including those shorter than k. */
+uint64_t swg_reads_records(const swg_reads *r);
+void swg_reads_free(swg_reads *r);
+
+/* ---- graph build ------------------------------------------------------ */
+/* Create an empty graph handle on the current CUDA device. Its device
+ * workspace (table, tiles, outputs) is kept and reused by later builds. */
+swg_status swg_graph_create(swg_graph **out);
+void swg_graph_free(swg_graph *g);
+
+/* Build from packed reads in HOST memory: copies them to the device, builds,
+ * leaves the result on the device. */
+swg_status swg_graph_build(swg_graph *g, const swg_opts *o, const uint32_t *packed,
+                           uint64_t n_words, const uint64_t *read_off,
+                           const uint32_t *read_len, uint64_t n_reads);
+/* Same with the packed reads already in DEVICE memory. */
+swg_status swg_graph_build_device(swg_graph *g, const swg_opts *o, const uint32_t *d_packed,
+                                  uint64_t n_words, const uint64_t *d_read_off,
+                                  const uint32_t *d_read_len, uint64_t n_reads);
+/* Convenience: create + build from host packed reads. */
+swg_status swg_build(const swg_opts *o, const uint32_t *packed, uint64_t n_words,
+                     const uint64_t *read_off, const uint32_t *read_len, uint64_t n_reads,
+                     swg_graph **out);
+/* Convenience: frame + pack a FASTA held in host memory, then build. */
+swg_status swg_build_fasta(const swg_opts *o, const char *text, uint64_t len, swg_graph **out);
+
+/* ---- results ---------------------------------------------------------- */
+/* Number of surviving k-molecules (after the cutoff). */
+swg_status swg_graph_size(const swg_graph *g, uint64_t *n);
+/* Distinct k-molecules before the cutoff (all keys ever inserted). */
+swg_status swg_graph_distinct(const swg_graph *g, uint64_t *n);
+/* Device pointers to the unordered result: keys[n], mult[n] (8 bytes per key
+ * packed in a uint64, byte t = slot t). Valid until the next build or free. */
+swg_status swg_graph_device_view(const swg_graph *g, const uint64_t **d_keys,
+                                 const uint64_t **d_mult, uint64_t *n);
+/* Copy the result to host memory, sorted by key when sorted != 0.
+ * keys[cap], mult[8*cap]; *n receives the count (SWG_ERR_BAD_INPUT if cap < n). */
+swg_status swg_graph_copy_out(const swg_graph *g, uint64_t *keys, uint8_t *mult, uint64_t cap,
+                              int sorted, uint64_t *n);
+/* graph.cpp:1613-1625 totals: nodes, edges, edge-length sum, tips, bubbles. */
+swg_status swg_graph_stats(const swg_graph *g, int64_t out[5]);
+/* kmerGraph.txt exactly as the reference's -s run writes it (graph.cpp:3352-3440,
+ * including its neighbour-id quirk), lines sorted by their first token. */
+swg_status swg_graph_write_kmer_graph(const swg_graph *g, const char *path);
+/* Node lines "K A# # ...# m0 .. m7" (graph.cpp:569), sorted by key; readable by
+ * the reference's readDistNodeGraph (graph.cpp:898-941). */
+swg_status swg_graph_write_node_lines(const swg_graph *g, const char *path);
+/* Host-only writers for records already in host memory (keys[n], mult[8*n],
+ * any order): the same two file formats as above. */
+swg_status swg_records_write_kmer_graph(const uint64_t *keys, const uint8_t *mult, uint64_t n,
+                                        int k, const char *path);
+swg_status swg_records_write_node_lines(const uint64_t *keys, const uint8_t *mult, uint64_t n,
+                                        const char *path);
+/* Device times (ms) of the last build's phases, from CUDA events on the build
+ * stream: [0] estimate, [1] table clear, [2] extract+count, [3] cutoff+compaction,
+ * [4] whole build. Also the launch count of the last build. */
+swg_status swg_graph_last_timings(const swg_graph *g, float ms[5], int *launches);
+
+/* ---- roofline probe ----------------------------------------------------- */
+/* Random-access throughput on this GPU: n_ops operations at uniformly random
+ * 16-byte-aligned addresses of a table of table_bytes bytes (allocated and
+ * freed inside). kind: 0 = 32-bit atomicAdd (no return), 1 = 64-bit CAS,
+ * 2 = 128-bit CAS, 3 = 16-byte load, 4 = 16-byte load + 128-bit CAS on the
+ * same address. Writes operations per second (device time). */
+swg_status swg_probe_random_access(int kind, uint64_t table_bytes, uint64_t n_ops, void *stream,
+                                   double *ops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWAPGB_H */

@@ -1,0 +1,180 @@
+"""Python binding of the CPU restatement (liboracle.so) and runners for the
+reference binaries built from the reference's own sources (oracle/_ref).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check and by the
+CPU-baseline leg of bench.py, always as the checker or the timed CPU
+baseline, never as the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "build" / "liboracle.so"
+ORACLE_BIN = HERE / "build" / "swap_oracle"
+REF_SWAP = HERE / "_ref" / "swap"
+REF_DUMP = HERE / "_ref" / "ref_dump"
+
+ERRORS = {0: "ok", -1: "no record start", -2: "unterminated record", -3: "NUL byte",
+          -4: "bad k", -5: "out of memory"}
+
+
+class OracleReads(C.Structure):
+    _fields_ = [("codes", C.c_void_p), ("off", C.c_void_p), ("len", C.c_void_p),
+                ("n_reads", C.c_uint64), ("n_bases", C.c_uint64), ("n_records", C.c_uint64)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            subprocess.run(["make", "-s", "-C", str(HERE), "restatement"], check=True)
+        L = C.CDLL(str(LIB_PATH))
+        P, u64, i32 = C.c_void_p, C.c_uint64, C.c_int
+        L.oracle_parse_fasta.argtypes = [C.c_char_p, u64, i32, C.POINTER(OracleReads)]
+        L.oracle_parse_fasta.restype = i32
+        L.oracle_reads_free.argtypes = [C.POINTER(OracleReads)]
+        L.oracle_build.argtypes = [C.POINTER(OracleReads), i32, i32, i32, i32]
+        L.oracle_build.restype = P
+        L.oracle_graph_size.argtypes = [P]
+        L.oracle_graph_size.restype = u64
+        L.oracle_graph_get.argtypes = [P, P, P]
+        L.oracle_graph_free.argtypes = [P]
+        L.oracle_write_kmer_graph.argtypes = [P, i32, C.c_char_p]
+        L.oracle_write_node_lines.argtypes = [P, C.c_char_p]
+        L.oracle_graph_stats.argtypes = [P, i32, C.POINTER(C.c_int64)]
+        L.oracle_kmer_graph_neighbour.argtypes = [u64, i32, i32]
+        L.oracle_kmer_graph_neighbour.restype = u64
+        L.oracle_revcomp.argtypes = [u64, i32]
+        L.oracle_revcomp.restype = u64
+        _lib = L
+    return _lib
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code: int):
+        super().__init__("oracle: %s" % ERRORS.get(code, code))
+        self.code = code
+
+
+def parse(text: bytes, k: int) -> dict:
+    """Framing + normalisation; returns codes/off/len numpy copies."""
+    r = OracleReads()
+    e = lib().oracle_parse_fasta(text, len(text), k, C.byref(r))
+    if e:
+        raise OracleError(e)
+    try:
+        out = {
+            "n_reads": r.n_reads, "n_bases": r.n_bases, "n_records": r.n_records,
+            "codes": np.ctypeslib.as_array((C.c_uint8 * max(r.n_bases, 1)).from_address(r.codes))[: r.n_bases].copy(),
+            "off": np.ctypeslib.as_array((C.c_uint64 * max(r.n_reads, 1)).from_address(r.off))[: r.n_reads].copy(),
+            "len": np.ctypeslib.as_array((C.c_uint32 * max(r.n_reads, 1)).from_address(r.len))[: r.n_reads].copy(),
+        }
+    finally:
+        lib().oracle_reads_free(C.byref(r))
+    return out
+
+
+class OracleGraph:
+    def __init__(self, handle: int, k: int):
+        self._h = C.c_void_p(handle)
+        self.k = k
+
+    def __del__(self):
+        if self._h:
+            lib().oracle_graph_free(self._h)
+            self._h = C.c_void_p()
+
+    def records(self) -> tuple[np.ndarray, np.ndarray]:
+        n = lib().oracle_graph_size(self._h)
+        keys = np.zeros(n, dtype=np.uint64)
+        mult = np.zeros((n, 8), dtype=np.uint8)
+        if n:
+            lib().oracle_graph_get(self._h, keys.ctypes.data, mult.ctypes.data)
+        return keys, mult
+
+    def write_kmer_graph(self, path: str) -> None:
+        lib().oracle_write_kmer_graph(self._h, self.k, str(path).encode())
+
+    def write_node_lines(self, path: str) -> None:
+        lib().oracle_write_node_lines(self._h, str(path).encode())
+
+    def stats(self) -> list[int]:
+        out = (C.c_int64 * 5)()
+        lib().oracle_graph_stats(self._h, self.k, out)
+        return list(out)
+
+
+def build(text: bytes, k: int, cutoff: int, threads: int = 0, apply_cutoff: bool = True) -> OracleGraph:
+    r = OracleReads()
+    e = lib().oracle_parse_fasta(text, len(text), k, C.byref(r))
+    if e:
+        raise OracleError(e)
+    try:
+        h = lib().oracle_build(C.byref(r), k, cutoff, int(apply_cutoff), threads)
+    finally:
+        lib().oracle_reads_free(C.byref(r))
+    if not h:
+        raise OracleError(-5)
+    return OracleGraph(h, k)
+
+
+def records(text: bytes, k: int, cutoff: int, threads: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    return build(text, k, cutoff, threads).records()
+
+
+def kmer_graph_neighbour(key: int, slot: int, k: int) -> int:
+    return lib().oracle_kmer_graph_neighbour(key, slot, k)
+
+
+def revcomp(x: int, k: int) -> int:
+    return lib().oracle_revcomp(x, k)
+
+
+# ---- the reference itself (only where it was compiled from its sources) ----
+
+def reference_available() -> bool:
+    return REF_SWAP.exists() and REF_DUMP.exists()
+
+
+def run_reference(fasta_path: str, k: int, cutoff: int, outdir: str, timeout: float = 600) -> dict:
+    """Run the reference's `swap -s` and its node dump on one FASTA.
+
+    Returns the sorted kmerGraph.txt lines, the sorted node lines and the
+    reference's stdout totals. outdir must not exist (the reference creates
+    it, sequence.cpp:128-133)."""
+    out = {}
+    a, b = str(outdir) + "_s", str(outdir) + "_n"
+    r = subprocess.run([str(REF_SWAP), "-k", str(k), "-c", str(cutoff), "-i", str(fasta_path),
+                        "-o", a, "-s"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                       timeout=timeout, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference swap failed: %s" % r.stdout[-2000:])
+    out["kmer_graph"] = sorted(Path(a, "kmerGraph.txt").read_text().splitlines(),
+                               key=lambda s: int(s.split()[0]))
+    totals = {}
+    for line in r.stdout.splitlines():
+        if line.startswith("recv") and "=" in line:
+            name, val = line.split("=")
+            totals[name.strip()] = int(val)
+    out["totals"] = totals
+    r = subprocess.run([str(REF_DUMP), "-k", str(k), "-c", str(cutoff), "-i", str(fasta_path),
+                        "-o", b], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                       timeout=timeout, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference node dump failed: %s" % r.stdout[-2000:])
+    out["nodes"] = sorted(Path(b, "nodes.txt").read_text().splitlines(),
+                          key=lambda s: int(s.split()[0]))
+    return out
+
+
+def cores() -> int:
+    return os.cpu_count() or 1

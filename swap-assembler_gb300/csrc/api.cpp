@@ -1,0 +1,551 @@
+// C ABI of the k-mer graph builder (declared in include/swapgb.h).
+//
+// A build runs on one CUDA stream:
+//   occurrence prefix (3 launches) -> tile table -> [HyperLogLog estimate]
+//   -> table clear -> K1 extract+count -> K2 cutoff+compaction
+// with two host synchronisations (occurrence total, then the distinct-count
+// estimate) and one at the end (status, survivor count). A table that fills
+// up is detected on the device and the build is repeated with a larger table.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "swg_internal.h"
+
+namespace swg {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+}  // namespace swg
+
+using swg::BuildArgs;
+using swg::Entry;
+
+struct Control {  // device-side control block
+    unsigned status;
+    unsigned pad;
+    unsigned long long counters[2];  // inserted keys, survivors
+    uint64_t occ_total;
+};
+
+struct swg_graph {
+    int device = 0;
+    cudaStream_t own = nullptr;
+    // device workspace, grown on demand and reused by later builds
+    uint32_t *d_packed = nullptr;
+    uint64_t packed_cap = 0;
+    uint64_t *d_off = nullptr;
+    uint32_t *d_len = nullptr;
+    uint64_t reads_cap = 0;
+    uint64_t *d_prefix = nullptr;
+    uint64_t prefix_cap = 0;
+    uint64_t *d_scan = nullptr;
+    uint64_t scan_cap = 0;
+    uint32_t *d_tiles = nullptr;
+    uint64_t tiles_cap = 0;
+    Entry *d_table = nullptr;
+    uint64_t table_cap = 0;
+    unsigned long long *d_out_keys = nullptr;
+    unsigned long long *d_out_mult = nullptr;
+    uint64_t out_cap = 0;
+    unsigned *d_hll = nullptr;
+    Control *d_ctl = nullptr;
+    // pinned host mirrors
+    Control *h_ctl = nullptr;
+    unsigned *h_hll = nullptr;
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    // result of the last build
+    bool built = false;
+    int k = 0;
+    int cutoff = 0;
+    uint64_t n_out = 0;
+    uint64_t n_distinct = 0;
+    uint64_t cap_used = 0;
+    float ms[5] = {0, 0, 0, 0, 0};
+    int launches = 0;
+};
+
+namespace {
+
+swg_status cuda_fail(cudaError_t e, const char *what) {
+    swg::set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? SWG_ERR_OOM : SWG_ERR_CUDA;
+}
+
+#define SWG_CUDA(call, what)                            \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+template <typename T>
+swg_status ensure(T **p, uint64_t *cap, uint64_t want, const char *what) {
+    if (*cap >= want && *p) return SWG_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    const uint64_t n = std::max<uint64_t>(want, 1);
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_fail(e, what);
+    }
+    *cap = n;
+    return SWG_OK;
+}
+
+swg_status check_opts(const swg_opts *o) {
+    if (!o) {
+        swg::set_error("opts is NULL");
+        return SWG_ERR_BAD_INPUT;
+    }
+    if (o->k < 1 || o->k > 31) {
+        swg::set_error("k must be in 1..31");
+        return SWG_ERR_BAD_INPUT;
+    }
+    if (o->load_factor < 0 || o->load_factor > 0.9) {
+        swg::set_error("load_factor must be in (0, 0.9] (0 = default)");
+        return SWG_ERR_BAD_INPUT;
+    }
+    return SWG_OK;
+}
+
+cudaStream_t stream_of(swg_graph *g, const swg_opts *o) {
+    return o->stream ? (cudaStream_t)o->stream : g->own;
+}
+
+swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, uint64_t n_words,
+                      const uint64_t *off, const uint32_t *len, uint64_t n_reads) {
+    swg_status st = check_opts(o);
+    if (st) return st;
+    if (n_reads >= 0xffffffffull) {
+        swg::set_error("at most 2^32-2 reads per build");
+        return SWG_ERR_BAD_INPUT;
+    }
+    if (n_reads && (!packed || !off || !len)) {
+        swg::set_error("NULL read buffer");
+        return SWG_ERR_BAD_INPUT;
+    }
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    cudaStream_t s = stream_of(g, o);
+    g->built = false;
+    g->k = o->k;
+    g->cutoff = o->cutoff;
+    g->launches = 0;
+    const double load = o->load_factor > 0 ? o->load_factor : 0.6;
+
+    BuildArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.packed = packed;
+    a.n_words = n_words;
+    a.read_off = off;
+    a.read_len = len;
+    a.n_reads = n_reads;
+    a.k = o->k;
+    a.cutoff = o->cutoff;
+
+    if ((st = ensure(&g->d_prefix, &g->prefix_cap, n_reads + 1, "occurrence prefix"))) return st;
+    if ((st = ensure(&g->d_scan, &g->scan_cap, swg::scan_block_count(n_reads) + 1, "scan scratch")))
+        return st;
+    a.occ_prefix = g->d_prefix;
+    a.scan_blocks = g->d_scan;
+    a.hll = g->d_hll;
+    a.status = &g->d_ctl->status;
+    a.counters = g->d_ctl->counters;
+
+    SWG_CUDA(cudaEventRecord(g->ev[0], s), "event");
+    SWG_CUDA(cudaMemsetAsync(g->d_ctl, 0, sizeof(Control), s), "memset control");
+    SWG_CUDA(cudaMemsetAsync(g->d_prefix, 0, sizeof(uint64_t), s), "memset prefix");
+    g->launches += swg::launch_occ_scan(a, s);
+    SWG_CUDA(cudaGetLastError(), "occurrence scan launch");
+    SWG_CUDA(cudaMemcpyAsync(&g->h_ctl->occ_total, g->d_prefix + n_reads, sizeof(uint64_t),
+                             cudaMemcpyDeviceToHost, s),
+             "read occurrence total");
+    SWG_CUDA(cudaStreamSynchronize(s), "occurrence scan");
+    a.total_occ = g->h_ctl->occ_total;
+    a.n_tiles = (a.total_occ + swg::kTileOcc - 1) / swg::kTileOcc;
+    if ((st = ensure(&g->d_tiles, &g->tiles_cap, a.n_tiles, "tile table"))) return st;
+    a.tile_first_read = g->d_tiles;
+    g->launches += swg::launch_tiles(a, s);
+    SWG_CUDA(cudaGetLastError(), "tile launch");
+
+    // table sizing: caller's hint, else a HyperLogLog estimate on the device
+    double est;
+    if (o->expected_distinct) {
+        est = (double)o->expected_distinct;
+    } else if (a.total_occ == 0) {
+        est = 0;
+    } else {
+        SWG_CUDA(cudaMemsetAsync(g->d_hll, 0, sizeof(unsigned) << swg::kHllBits, s), "memset hll");
+        g->launches += swg::launch_hll(a, s);
+        SWG_CUDA(cudaGetLastError(), "hll launch");
+        SWG_CUDA(cudaMemcpyAsync(g->h_hll, g->d_hll, sizeof(unsigned) << swg::kHllBits,
+                                 cudaMemcpyDeviceToHost, s),
+                 "read hll");
+        SWG_CUDA(cudaStreamSynchronize(s), "hll");
+        est = swg::hll_estimate(g->h_hll) * 1.06;  // ~3.7 standard errors of margin
+    }
+    est = std::min(est, (double)a.total_occ);
+    uint64_t cap = (uint64_t)std::ceil(std::max(est, 1.0) / load) + 64;
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        if ((st = ensure(&g->d_table, &g->table_cap, cap, "hash table"))) return st;
+        if (g->out_cap < cap || !g->d_out_keys || !g->d_out_mult) {
+            cudaFree(g->d_out_keys);
+            cudaFree(g->d_out_mult);
+            g->d_out_keys = g->d_out_mult = nullptr;
+            g->out_cap = 0;
+            SWG_CUDA(cudaMalloc(&g->d_out_keys, cap * sizeof(unsigned long long)), "output keys");
+            SWG_CUDA(cudaMalloc(&g->d_out_mult, cap * sizeof(unsigned long long)),
+                     "output multiplicities");
+            g->out_cap = cap;
+        }
+        a.table = g->d_table;
+        a.cap = cap;
+        a.out_keys = g->d_out_keys;
+        a.out_mult = g->d_out_mult;
+        a.out_cap = cap;
+        SWG_CUDA(cudaEventRecord(g->ev[1], s), "event");
+        SWG_CUDA(cudaMemsetAsync(g->d_table, 0, cap * sizeof(Entry), s), "clear table");
+        SWG_CUDA(cudaMemsetAsync(g->d_ctl, 0, sizeof(Control) - sizeof(uint64_t), s),
+                 "clear control");
+        SWG_CUDA(cudaEventRecord(g->ev[2], s), "event");
+        g->launches += swg::launch_count(a, s);
+        SWG_CUDA(cudaGetLastError(), "count launch");
+        SWG_CUDA(cudaEventRecord(g->ev[3], s), "event");
+        g->launches += swg::launch_compact(a, s);
+        SWG_CUDA(cudaGetLastError(), "compact launch");
+        SWG_CUDA(cudaEventRecord(g->ev[4], s), "event");
+        SWG_CUDA(cudaMemcpyAsync(g->h_ctl, g->d_ctl, sizeof(Control) - sizeof(uint64_t),
+                                 cudaMemcpyDeviceToHost, s),
+                 "read status");
+        SWG_CUDA(cudaStreamSynchronize(s), "build");
+        const unsigned status = g->h_ctl->status;
+        if (status & swg::kStatusCasLimit) {
+            swg::set_error("a bounded CAS retry loop gave up on the device");
+            return SWG_ERR_TIMEOUT;
+        }
+        if (status & swg::kStatusTableFull) {
+            const double inserted = (double)g->h_ctl->counters[0];
+            cap = (uint64_t)std::ceil(std::max(2.0 * (double)cap, inserted * 2.0 / load)) + 64;
+            continue;
+        }
+        g->n_distinct = g->h_ctl->counters[0];
+        g->n_out = g->h_ctl->counters[1];
+        g->cap_used = cap;
+        g->built = true;
+        float t[5] = {0, 0, 0, 0, 0};
+        cudaEventElapsedTime(&t[0], g->ev[0], g->ev[1]);
+        cudaEventElapsedTime(&t[1], g->ev[1], g->ev[2]);
+        cudaEventElapsedTime(&t[2], g->ev[2], g->ev[3]);
+        cudaEventElapsedTime(&t[3], g->ev[3], g->ev[4]);
+        cudaEventElapsedTime(&t[4], g->ev[0], g->ev[4]);
+        std::memcpy(g->ms, t, sizeof(t));
+        return SWG_OK;
+    }
+    swg::set_error("hash table still full after 6 enlargements");
+    return SWG_ERR_TABLE_FULL;
+}
+
+swg_status fetch_sorted(const swg_graph *g, std::vector<uint64_t> &keys,
+                        std::vector<uint64_t> &mult) {
+    if (!g || !g->built) {
+        swg::set_error("graph has not been built");
+        return SWG_ERR_BAD_STATE;
+    }
+    keys.resize(g->n_out);
+    mult.resize(g->n_out);
+    if (g->n_out) {
+        SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+        SWG_CUDA(cudaMemcpy(keys.data(), g->d_out_keys, g->n_out * 8, cudaMemcpyDeviceToHost),
+                 "copy keys");
+        SWG_CUDA(cudaMemcpy(mult.data(), g->d_out_mult, g->n_out * 8, cudaMemcpyDeviceToHost),
+                 "copy multiplicities");
+    }
+    swg::sort_records(keys.data(), mult.data(), g->n_out);
+    return SWG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *swg_status_string(swg_status s) {
+    switch (s) {
+        case SWG_OK: return "ok";
+        case SWG_ERR_BAD_INPUT: return "bad input";
+        case SWG_ERR_TABLE_FULL: return "hash table full";
+        case SWG_ERR_OOM: return "out of memory";
+        case SWG_ERR_ADMISSION: return "admission denied";
+        case SWG_ERR_TIMEOUT: return "device retry limit";
+        case SWG_ERR_CUDA: return "CUDA error";
+        case SWG_ERR_NO_DEVICE: return "no CUDA device";
+        case SWG_ERR_BAD_STATE: return "bad state";
+        case SWG_ERR_IO: return "I/O error";
+        case SWG_ERR_NOT_READY: return "not ready";
+    }
+    return "unknown status";
+}
+
+const char *swg_last_error(void) { return swg::g_last_error.c_str(); }
+
+const char *swg_version(void) { return "swapgb 0.1 (sm_103a)"; }
+
+swg_status swg_graph_create(swg_graph **out) {
+    if (!out) return SWG_ERR_BAD_INPUT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        swg::set_error("no CUDA device visible");
+        return SWG_ERR_NO_DEVICE;
+    }
+    swg_graph *g = new (std::nothrow) swg_graph;
+    if (!g) return SWG_ERR_OOM;
+    cudaError_t e = cudaGetDevice(&g->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->own, cudaStreamNonBlocking);
+    for (int i = 0; e == cudaSuccess && i < 5; i++) e = cudaEventCreate(&g->ev[i]);
+    if (e == cudaSuccess) e = cudaMalloc(&g->d_hll, sizeof(unsigned) << swg::kHllBits);
+    if (e == cudaSuccess) e = cudaMalloc(&g->d_ctl, sizeof(Control));
+    if (e == cudaSuccess) e = cudaMallocHost(&g->h_ctl, sizeof(Control));
+    if (e == cudaSuccess) e = cudaMallocHost(&g->h_hll, sizeof(unsigned) << swg::kHllBits);
+    if (e != cudaSuccess) {
+        swg_status st = cuda_fail(e, "graph create");
+        swg_graph_free(g);
+        return st;
+    }
+    *out = g;
+    return SWG_OK;
+}
+
+void swg_graph_free(swg_graph *g) {
+    if (!g) return;
+    cudaSetDevice(g->device);
+    if (g->own) cudaStreamSynchronize(g->own);
+    cudaFree(g->d_packed);
+    cudaFree(g->d_off);
+    cudaFree(g->d_len);
+    cudaFree(g->d_prefix);
+    cudaFree(g->d_scan);
+    cudaFree(g->d_tiles);
+    cudaFree(g->d_table);
+    cudaFree(g->d_out_keys);
+    cudaFree(g->d_out_mult);
+    cudaFree(g->d_hll);
+    cudaFree(g->d_ctl);
+    if (g->h_ctl) cudaFreeHost(g->h_ctl);
+    if (g->h_hll) cudaFreeHost(g->h_hll);
+    for (auto &e : g->ev)
+        if (e) cudaEventDestroy(e);
+    if (g->own) cudaStreamDestroy(g->own);
+    delete g;
+}
+
+swg_status swg_graph_build_device(swg_graph *g, const swg_opts *o, const uint32_t *d_packed,
+                                  uint64_t n_words, const uint64_t *d_read_off,
+                                  const uint32_t *d_read_len, uint64_t n_reads) {
+    if (!g) return SWG_ERR_BAD_INPUT;
+    return build_impl(g, o, d_packed, n_words, d_read_off, d_read_len, n_reads);
+}
+
+swg_status swg_graph_build(swg_graph *g, const swg_opts *o, const uint32_t *packed,
+                           uint64_t n_words, const uint64_t *read_off, const uint32_t *read_len,
+                           uint64_t n_reads) {
+    if (!g) return SWG_ERR_BAD_INPUT;
+    swg_status st = check_opts(o);
+    if (st) return st;
+    if (n_reads && (!packed || !read_off || !read_len)) {
+        swg::set_error("NULL read buffer");
+        return SWG_ERR_BAD_INPUT;
+    }
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    cudaStream_t s = stream_of(g, o);
+    if ((st = ensure(&g->d_packed, &g->packed_cap, n_words, "packed reads"))) return st;
+    if (g->reads_cap < n_reads || !g->d_off || !g->d_len) {
+        cudaFree(g->d_off);
+        cudaFree(g->d_len);
+        g->d_off = nullptr;
+        g->d_len = nullptr;
+        g->reads_cap = 0;
+        SWG_CUDA(cudaMalloc(&g->d_off, std::max<uint64_t>(n_reads, 1) * 8), "read offsets");
+        SWG_CUDA(cudaMalloc(&g->d_len, std::max<uint64_t>(n_reads, 1) * 4), "read lengths");
+        g->reads_cap = std::max<uint64_t>(n_reads, 1);
+    }
+    if (n_words)
+        SWG_CUDA(cudaMemcpyAsync(g->d_packed, packed, n_words * 4, cudaMemcpyHostToDevice, s),
+                 "copy packed reads");
+    if (n_reads) {
+        SWG_CUDA(cudaMemcpyAsync(g->d_off, read_off, n_reads * 8, cudaMemcpyHostToDevice, s),
+                 "copy read offsets");
+        SWG_CUDA(cudaMemcpyAsync(g->d_len, read_len, n_reads * 4, cudaMemcpyHostToDevice, s),
+                 "copy read lengths");
+    }
+    return build_impl(g, o, g->d_packed, n_words, g->d_off, g->d_len, n_reads);
+}
+
+swg_status swg_build(const swg_opts *o, const uint32_t *packed, uint64_t n_words,
+                     const uint64_t *read_off, const uint32_t *read_len, uint64_t n_reads,
+                     swg_graph **out) {
+    if (!out) return SWG_ERR_BAD_INPUT;
+    *out = nullptr;
+    swg_graph *g = nullptr;
+    swg_status st = swg_graph_create(&g);
+    if (st) return st;
+    st = swg_graph_build(g, o, packed, n_words, read_off, read_len, n_reads);
+    if (st) {
+        swg_graph_free(g);
+        return st;
+    }
+    *out = g;
+    return SWG_OK;
+}
+
+swg_status swg_build_fasta(const swg_opts *o, const char *text, uint64_t len, swg_graph **out) {
+    if (!out) return SWG_ERR_BAD_INPUT;
+    *out = nullptr;
+    swg_status st = check_opts(o);
+    if (st) return st;
+    swg_reads *r = nullptr;
+    st = swg_reads_from_fasta(text, len, o->k, &r);
+    if (st) return st;
+    const uint32_t *p;
+    const uint64_t *off;
+    const uint32_t *ln;
+    uint64_t nw, nr, nb;
+    swg_reads_view(r, &p, &nw, &off, &ln, &nr, &nb);
+    st = swg_build(o, p, nw, off, ln, nr, out);
+    swg_reads_free(r);
+    return st;
+}
+
+swg_status swg_graph_size(const swg_graph *g, uint64_t *n) {
+    if (!g || !n) return SWG_ERR_BAD_INPUT;
+    if (!g->built) return SWG_ERR_BAD_STATE;
+    *n = g->n_out;
+    return SWG_OK;
+}
+
+swg_status swg_graph_distinct(const swg_graph *g, uint64_t *n) {
+    if (!g || !n) return SWG_ERR_BAD_INPUT;
+    if (!g->built) return SWG_ERR_BAD_STATE;
+    *n = g->n_distinct;
+    return SWG_OK;
+}
+
+swg_status swg_graph_device_view(const swg_graph *g, const uint64_t **d_keys,
+                                 const uint64_t **d_mult, uint64_t *n) {
+    if (!g) return SWG_ERR_BAD_INPUT;
+    if (!g->built) return SWG_ERR_BAD_STATE;
+    if (d_keys) *d_keys = reinterpret_cast<const uint64_t *>(g->d_out_keys);
+    if (d_mult) *d_mult = reinterpret_cast<const uint64_t *>(g->d_out_mult);
+    if (n) *n = g->n_out;
+    return SWG_OK;
+}
+
+swg_status swg_graph_copy_out(const swg_graph *g, uint64_t *keys, uint8_t *mult, uint64_t cap,
+                              int sorted, uint64_t *n) {
+    if (!g) return SWG_ERR_BAD_INPUT;
+    if (!g->built) return SWG_ERR_BAD_STATE;
+    if (n) *n = g->n_out;
+    if (cap < g->n_out) {
+        swg::set_error("output capacity smaller than the survivor count");
+        return SWG_ERR_BAD_INPUT;
+    }
+    if (g->n_out == 0) return SWG_OK;
+    if (!sorted) {
+        SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+        if (keys)
+            SWG_CUDA(cudaMemcpy(keys, g->d_out_keys, g->n_out * 8, cudaMemcpyDeviceToHost),
+                     "copy keys");
+        if (mult)
+            SWG_CUDA(cudaMemcpy(mult, g->d_out_mult, g->n_out * 8, cudaMemcpyDeviceToHost),
+                     "copy multiplicities");
+        return SWG_OK;
+    }
+    std::vector<uint64_t> k, m;
+    swg_status st = fetch_sorted(g, k, m);
+    if (st) return st;
+    if (keys) std::memcpy(keys, k.data(), g->n_out * 8);
+    if (mult) std::memcpy(mult, m.data(), g->n_out * 8);
+    return SWG_OK;
+}
+
+swg_status swg_graph_stats(const swg_graph *g, int64_t out[5]) {
+    if (!g || !out) return SWG_ERR_BAD_INPUT;
+    std::vector<uint64_t> k, m;
+    swg_status st = fetch_sorted(g, k, m);
+    if (st) return st;
+    swg::graph_stats(reinterpret_cast<const uint8_t *>(m.data()), g->n_out, g->k, out);
+    return SWG_OK;
+}
+
+swg_status swg_graph_write_kmer_graph(const swg_graph *g, const char *path) {
+    if (!g || !path) return SWG_ERR_BAD_INPUT;
+    std::vector<uint64_t> k, m;
+    swg_status st = fetch_sorted(g, k, m);
+    if (st) return st;
+    return swg::write_kmer_graph(k.data(), reinterpret_cast<const uint8_t *>(m.data()), g->n_out,
+                                 g->k, path);
+}
+
+swg_status swg_graph_write_node_lines(const swg_graph *g, const char *path) {
+    if (!g || !path) return SWG_ERR_BAD_INPUT;
+    std::vector<uint64_t> k, m;
+    swg_status st = fetch_sorted(g, k, m);
+    if (st) return st;
+    return swg::write_node_lines(k.data(), reinterpret_cast<const uint8_t *>(m.data()), g->n_out,
+                                 path);
+}
+
+static swg_status sorted_copy(const uint64_t *keys, const uint8_t *mult, uint64_t n,
+                              std::vector<uint64_t> &k, std::vector<uint64_t> &m) {
+    if (n && (!keys || !mult)) return SWG_ERR_BAD_INPUT;
+    k.assign(keys, keys + n);
+    m.resize(n);
+    if (n) std::memcpy(m.data(), mult, n * 8);
+    swg::sort_records(k.data(), m.data(), n);
+    return SWG_OK;
+}
+
+swg_status swg_records_write_kmer_graph(const uint64_t *keys, const uint8_t *mult, uint64_t n,
+                                        int k, const char *path) {
+    if (!path) return SWG_ERR_BAD_INPUT;
+    std::vector<uint64_t> kk, mm;
+    swg_status st = sorted_copy(keys, mult, n, kk, mm);
+    if (st) return st;
+    return swg::write_kmer_graph(kk.data(), reinterpret_cast<const uint8_t *>(mm.data()), n, k, path);
+}
+
+swg_status swg_records_write_node_lines(const uint64_t *keys, const uint8_t *mult, uint64_t n,
+                                        const char *path) {
+    if (!path) return SWG_ERR_BAD_INPUT;
+    std::vector<uint64_t> kk, mm;
+    swg_status st = sorted_copy(keys, mult, n, kk, mm);
+    if (st) return st;
+    return swg::write_node_lines(kk.data(), reinterpret_cast<const uint8_t *>(mm.data()), n, path);
+}
+
+swg_status swg_graph_last_timings(const swg_graph *g, float ms[5], int *launches) {
+    if (!g) return SWG_ERR_BAD_INPUT;
+    if (!g->built) return SWG_ERR_BAD_STATE;
+    if (ms) std::memcpy(ms, g->ms, sizeof(g->ms));
+    if (launches) *launches = g->launches;
+    return SWG_OK;
+}
+
+swg_status swg_probe_random_access(int kind, uint64_t table_bytes, uint64_t n_ops, void *stream,
+                                   double *ops_per_s) {
+    if (!ops_per_s || kind < 0 || kind > 4 || n_ops == 0 || table_bytes < 4096)
+        return SWG_ERR_BAD_INPUT;
+    float ms = 0;
+    cudaError_t e = swg::run_probe(kind, table_bytes, n_ops, (cudaStream_t)stream, &ms);
+    if (e != cudaSuccess) return cuda_fail(e, "random-access probe");
+    *ops_per_s = ms > 0 ? (double)n_ops / (ms * 1e-3) : 0;
+    return SWG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,609 @@
+// sm_103a kernels of the k-mer graph build.
+//
+//   k_scan_*      exclusive prefix of k-mer occurrences per read
+//   k_tiles       first read of every tile of kTileOcc occurrences
+//   k_hll         HyperLogLog sketch of the distinct canonical k-molecules
+//                 (sizes the table before the count)
+//   k_count       K1: fused extraction + counting. Every thread takes one
+//                 k-mer occurrence of the tile, builds its canonical
+//                 k-molecule and arc slots (kmerGraph.cpp:240-296), equal
+//                 keys inside a warp are merged (match.any), and one lane per
+//                 key inserts or updates the open-addressing table in HBM with
+//                 a 128-bit CAS on {key, 8 x uint8 counts} (saturating adds,
+//                 graph.cpp:1058-1080)
+//   k_compact     K2: the -c cutoff (graph.cpp:1092-1114) as one streaming
+//                 pass over the table with block-level stream compaction
+//   k_probe       random-access roofline probe
+//
+// Every device-side retry loop is bounded; on exhaustion the kernel sets a
+// status bit that the host reads after the build.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "swg_internal.h"
+
+namespace swg {
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kSmemReads = 512;
+constexpr int kMaxProbe = 1 << 14;
+constexpr int kMaxCas = 1 << 20;
+constexpr int kScanBlock = 256;
+constexpr int kScanItems = 8;
+constexpr uint64_t kScanChunk = (uint64_t)kScanBlock * kScanItems;
+constexpr int kCBlock = 256;
+constexpr int kCItems = 8;
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdull;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ull;
+    x ^= x >> 33;
+    return x;
+}
+
+// Reverse complement of a k-mer held in the low 2k bits (k <= 31): complement
+// every base (b -> 3-b, i.e. bitwise NOT), reverse the 2-bit groups. Same
+// value as the reference's O(k) loop (kmerGraph.cpp:5-14).
+__device__ __forceinline__ uint64_t revcomp_dev(uint64_t x, int k) {
+    uint64_t y = __brevll(~x);
+    y = ((y >> 1) & 0x5555555555555555ull) | ((y & 0x5555555555555555ull) << 1);
+    return y >> (64 - 2 * k);
+}
+
+__device__ __forceinline__ uint32_t ldw(const uint32_t *__restrict__ p, uint64_t i, uint64_t n) {
+    return i < n ? __ldg(p + i) : 0u;
+}
+
+// 32 bases starting at base g, first base in bits 63..62.
+__device__ __forceinline__ uint64_t window32(const uint32_t *__restrict__ p, uint64_t n,
+                                             uint64_t g) {
+    const uint64_t w = g >> 4;
+    const int sh = (int)(g & 15) * 2;
+    const uint64_t hi = ((uint64_t)ldw(p, w, n) << 32) | ldw(p, w + 1, n);
+    if (sh == 0) return hi;
+    return (hi << sh) | (uint64_t)(ldw(p, w + 2, n) >> (32 - sh));
+}
+
+__device__ __forceinline__ uint32_t base_at(const uint32_t *__restrict__ p, uint64_t n,
+                                            uint64_t g) {
+    return (ldw(p, g >> 4, n) >> (30 - 2 * (int)(g & 15))) & 3u;
+}
+
+__device__ __forceinline__ uint64_t umin64(uint64_t a, uint64_t b) { return a < b ? a : b; }
+
+__device__ __forceinline__ uint64_t occ_of(uint32_t len, int k) {
+    return len >= (uint32_t)k ? (uint64_t)(len - (uint32_t)k + 1) : 0ull;
+}
+
+__device__ __forceinline__ ulonglong2 ld_relaxed16(const Entry *e) {
+    ulonglong2 v;
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];"
+                 : "=l"(v.x), "=l"(v.y)
+                 : "l"(e)
+                 : "memory");
+    return v;
+}
+
+// 128-bit compare-and-swap on {key, cnt}; returns the previous contents.
+__device__ __forceinline__ ulonglong2 cas128(Entry *e, uint64_t cmp_key, uint64_t cmp_cnt,
+                                             uint64_t new_key, uint64_t new_cnt) {
+    ulonglong2 old;
+    asm volatile(
+        "{\n\t"
+        ".reg .b128 cmpv, newv, oldv;\n\t"
+        "mov.b128 cmpv, {%2, %3};\n\t"
+        "mov.b128 newv, {%4, %5};\n\t"
+        "atom.relaxed.gpu.global.cas.b128 oldv, [%6], cmpv, newv;\n\t"
+        "mov.b128 {%0, %1}, oldv;\n\t"
+        "}"
+        : "=l"(old.x), "=l"(old.y)
+        : "l"(cmp_key), "l"(cmp_cnt), "l"(new_key), "l"(new_cnt), "l"(e)
+        : "memory");
+    return old;
+}
+
+// Per-byte saturating add of 8 uint8 counts (min(a+b, 255) in each byte).
+__device__ __forceinline__ uint64_t satadd8(uint64_t a, uint64_t b) {
+    const uint32_t lo = __vaddus4((uint32_t)a, (uint32_t)b);
+    const uint32_t hi = __vaddus4((uint32_t)(a >> 32), (uint32_t)(b >> 32));
+    return ((uint64_t)hi << 32) | lo;
+}
+
+// Add `inc` to the counts of `key` (present at e, last seen counts `cur`).
+__device__ __forceinline__ void update_counts(Entry *e, uint64_t key, uint64_t cur, uint64_t inc,
+                                              unsigned *status) {
+    for (int tries = 0; tries < kMaxCas; ++tries) {
+        const uint64_t nxt = satadd8(cur, inc);
+        if (nxt == cur) return;  // every touched slot already at 255
+        const ulonglong2 old = cas128(e, key, cur, key, nxt);
+        if (old.y == cur) return;
+        cur = old.y;
+    }
+    atomicOr(status, kStatusCasLimit);
+}
+
+// Insert `key` with counts `inc`, or add `inc` to its counts. Returns 1 when
+// this call inserted the key.
+__device__ __forceinline__ unsigned insert_or_update(Entry *__restrict__ table, uint64_t cap,
+                                                     uint64_t key, uint64_t inc,
+                                                     unsigned *status) {
+    uint64_t h = __umul64hi(mix64(key), cap);
+    for (int step = 0; step < kMaxProbe; ++step) {
+        Entry *e = table + h;
+        const ulonglong2 v = ld_relaxed16(e);
+        if (v.x == key) {
+            update_counts(e, key, v.y, inc, status);
+            return 0;
+        }
+        if (v.x == 0) {
+            const ulonglong2 old = cas128(e, 0, 0, key, inc);
+            if (old.x == 0) return 1;  // empty entries always hold zero counts
+            if (old.x == key) {
+                update_counts(e, key, old.y, inc, status);
+                return 0;
+            }
+        }
+        h = (h + 1 == cap) ? 0 : h + 1;
+    }
+    atomicOr(status, kStatusTableFull);
+    return 0;
+}
+
+// ---------------------------------------------------------------------
+// Block-wide exclusive scan of one uint64 per thread (blockDim = NT).
+template <int NT>
+__device__ __forceinline__ uint64_t block_exclusive_scan(uint64_t v, uint64_t *warp_buf,
+                                                         uint64_t *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint64_t y = __shfl_up_sync(kFull, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) warp_buf[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint64_t w = lane < NT / 32 ? warp_buf[lane] : 0;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint64_t y = __shfl_up_sync(kFull, w, d);
+            if (lane >= d) w += y;
+        }
+        if (lane < NT / 32) warp_buf[lane] = w;
+    }
+    __syncthreads();
+    const uint64_t warp_prefix = warp ? warp_buf[warp - 1] : 0;
+    if (total) *total = warp_buf[NT / 32 - 1];
+    __syncthreads();
+    return warp_prefix + x - v;
+}
+
+// ---------------------------------------------------------------------
+// Occurrence prefix: occ_prefix[r] = sum_{q<r} max(0, len[q]-k+1).
+__global__ void __launch_bounds__(kScanBlock) k_scan_reduce(const uint32_t *__restrict__ len,
+                                                            uint64_t n, int k,
+                                                            uint64_t *__restrict__ block_sums) {
+    __shared__ uint64_t wb[kScanBlock / 32];
+    const uint64_t base = (uint64_t)blockIdx.x * kScanChunk;
+    uint64_t s = 0;
+    for (int it = 0; it < kScanItems; ++it) {
+        const uint64_t r = base + (uint64_t)it * kScanBlock + threadIdx.x;
+        if (r < n) s += occ_of(len[r], k);
+    }
+    uint64_t total;
+    block_exclusive_scan<kScanBlock>(s, wb, &total);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_blocks(uint64_t *block_sums, uint64_t nb,
+                                                      uint64_t *occ_total) {
+    __shared__ uint64_t wb[32];
+    __shared__ uint64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint64_t base = 0; base < nb; base += 1024) {
+        const uint64_t i = base + threadIdx.x;
+        const uint64_t v = i < nb ? block_sums[i] : 0;
+        uint64_t total;
+        const uint64_t ex = block_exclusive_scan<1024>(v, wb, &total);
+        const uint64_t c = carry;
+        if (i < nb) block_sums[i] = c + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) carry = c + total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *occ_total = carry;
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_write(const uint32_t *__restrict__ len,
+                                                           uint64_t n, int k,
+                                                           const uint64_t *__restrict__ block_sums,
+                                                           uint64_t *__restrict__ prefix) {
+    __shared__ uint64_t wb[kScanBlock / 32];
+    const uint64_t base = (uint64_t)blockIdx.x * kScanChunk + (uint64_t)threadIdx.x * kScanItems;
+    uint64_t v[kScanItems];
+    uint64_t s = 0;
+#pragma unroll
+    for (int it = 0; it < kScanItems; ++it) {
+        const uint64_t r = base + it;
+        v[it] = r < n ? occ_of(len[r], k) : 0;
+        s += v[it];
+    }
+    uint64_t run = block_sums[blockIdx.x] + block_exclusive_scan<kScanBlock>(s, wb, nullptr);
+#pragma unroll
+    for (int it = 0; it < kScanItems; ++it) {
+        const uint64_t r = base + it;
+        if (r < n) prefix[r] = run;
+        run += v[it];
+    }
+}
+
+// First read of every tile: the read holding occurrence t*kTileOcc.
+__global__ void k_tiles(const uint64_t *__restrict__ prefix, uint64_t n_reads, uint64_t n_tiles,
+                        uint32_t *__restrict__ first) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tiles) return;
+    const uint64_t target = t * kTileOcc;
+    uint64_t lo = 0, hi = n_reads + 1;  // upper_bound over prefix[0..n_reads]
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (prefix[mid] <= target) lo = mid + 1;
+        else hi = mid;
+    }
+    first[t] = (uint32_t)(lo - 1);
+}
+
+// ---------------------------------------------------------------------
+// Tile mapping shared by the HLL and count kernels.
+struct TileSmem {
+    uint64_t pre[kSmemReads + 1];
+    uint64_t off[kSmemReads];
+    uint32_t len[kSmemReads];
+};
+
+struct TileView {
+    uint64_t r0, nr;  // first read, reads overlapping the tile
+    bool in_smem;
+};
+
+__device__ __forceinline__ TileView load_tile(const BuildArgs &a, uint64_t t, TileSmem &s) {
+    TileView v;
+    v.r0 = a.tile_first_read[t];
+    const uint64_t r1 = (t + 1 < a.n_tiles) ? a.tile_first_read[t + 1] : a.n_reads - 1;
+    v.nr = r1 - v.r0 + 1;
+    v.in_smem = v.nr <= (uint64_t)kSmemReads;
+    if (v.in_smem) {
+        for (uint64_t j = threadIdx.x; j <= v.nr; j += blockDim.x) {
+            s.pre[j] = a.occ_prefix[v.r0 + j];
+            if (j < v.nr) {
+                s.off[j] = a.read_off[v.r0 + j];
+                s.len[j] = a.read_len[v.r0 + j];
+            }
+        }
+    }
+    return v;
+}
+
+// Read holding occurrence i, with its prefix, offset and length.
+__device__ __forceinline__ void find_read(const BuildArgs &a, const TileView &v,
+                                          const TileSmem &s, uint64_t i, uint64_t &pre,
+                                          uint64_t &off, uint32_t &len) {
+    if (v.in_smem) {
+        uint64_t lo = 0, hi = v.nr;  // last j with pre[j] <= i
+        while (hi - lo > 1) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if (s.pre[mid] <= i) lo = mid;
+            else hi = mid;
+        }
+        pre = s.pre[lo];
+        off = s.off[lo];
+        len = s.len[lo];
+    } else {
+        uint64_t lo = v.r0, hi = v.r0 + v.nr;
+        while (hi - lo > 1) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if (a.occ_prefix[mid] <= i) lo = mid;
+            else hi = mid;
+        }
+        pre = a.occ_prefix[lo];
+        off = a.read_off[lo];
+        len = a.read_len[lo];
+    }
+}
+
+// Canonical k-molecule of occurrence i and its arc increments (one byte per
+// slot). kmerGraph.cpp:240-296 restated per occurrence j of a read:
+// K = max(C, rc(C)), f = (C == K); right arc (j+k < L) -> slot
+// (f ? 0 : 4) + base[j+k]; left arc (j >= 1) -> slot (f ? 4 : 0) + 3 - base[j-1].
+__device__ __forceinline__ void make_occ(const BuildArgs &a, const TileView &v, const TileSmem &s,
+                                         uint64_t i, uint64_t &key, uint64_t &inc) {
+    uint64_t pre, off;
+    uint32_t len;
+    find_read(a, v, s, i, pre, off, len);
+    const int k = a.k;
+    const uint64_t p = i - pre, g = off + p;
+    const uint64_t win = window32(a.packed, a.n_words, g);
+    const uint64_t fwd = win >> (64 - 2 * k);
+    const uint64_t rc = revcomp_dev(fwd, k);
+    const bool f = fwd >= rc;
+    key = f ? fwd : rc;
+    inc = 0;
+    if (p + (uint64_t)k < len) {
+        const uint32_t rb = (uint32_t)(win >> (62 - 2 * k)) & 3u;
+        inc += 1ull << (8 * ((f ? 0u : 4u) + rb));
+    }
+    if (p >= 1) {
+        const uint32_t lb = base_at(a.packed, a.n_words, g - 1);
+        inc += 1ull << (8 * ((f ? 4u : 0u) + 3u - lb));
+    }
+}
+
+// ---------------------------------------------------------------------
+// HyperLogLog over the canonical keys (persistent over tiles).
+__global__ void __launch_bounds__(kK1Block) k_hll(BuildArgs a) {
+    __shared__ TileSmem s;
+    __shared__ unsigned regs[1 << kHllBits];
+    for (int j = threadIdx.x; j < (1 << kHllBits); j += blockDim.x) regs[j] = 0;
+    for (uint64_t t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
+        __syncthreads();
+        const TileView v = load_tile(a, t, s);
+        __syncthreads();
+        const uint64_t A = t * kTileOcc;
+        const uint64_t B = umin64(A + kTileOcc, a.total_occ);
+        for (uint64_t i = A + threadIdx.x; i < B; i += blockDim.x) {
+            uint64_t key, inc;
+            make_occ(a, v, s, i, key, inc);
+            const uint64_t h = mix64(key ^ 0x9e3779b97f4a7c15ull);
+            const unsigned idx = (unsigned)(h >> (64 - kHllBits));
+            const uint64_t rest = (h << kHllBits) | (1ull << (kHllBits - 1));
+            const unsigned rank = (unsigned)__clzll(rest) + 1;
+            if (rank > regs[idx]) atomicMax(&regs[idx], rank);
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < (1 << kHllBits); j += blockDim.x)
+        if (regs[j]) atomicMax(&a.hll[j], regs[j]);
+}
+
+// ---------------------------------------------------------------------
+// K1: fused extraction + counting, one tile per block.
+__global__ void __launch_bounds__(kK1Block) k_count(BuildArgs a) {
+    __shared__ TileSmem s;
+    __shared__ unsigned s_stop;
+    __shared__ unsigned long long s_ins;
+    const uint64_t t = blockIdx.x;
+    if (threadIdx.x == 0) {
+        s_ins = 0;
+        s_stop = (*(volatile unsigned *)a.status) & kStatusTableFull;
+    }
+    const TileView v = load_tile(a, t, s);
+    __syncthreads();
+    if (s_stop) return;
+    const int lane = threadIdx.x & 31;
+    unsigned my_ins = 0;
+    const uint64_t A = t * kTileOcc;
+    const uint64_t B = umin64(A + kTileOcc, a.total_occ);
+    for (uint64_t base = A; base < B; base += kK1Block) {
+        const uint64_t i = base + threadIdx.x;
+        const bool valid = i < B;
+        const unsigned vmask = __ballot_sync(kFull, valid);
+        if (!valid) continue;
+        uint64_t key, inc;
+        make_occ(a, v, s, i, key, inc);
+        // merge equal keys of this warp (tandem repeats, duplicated reads)
+        const unsigned peers = __match_any_sync(vmask, key);
+        if (__any_sync(vmask, peers != (1u << lane))) {
+            uint64_t tot = 0;
+#pragma unroll
+            for (int sl = 0; sl < 8; ++sl) {
+                const unsigned b = __ballot_sync(vmask, (unsigned)(inc >> (8 * sl)) & 1u);
+                tot |= (uint64_t)__popc(b & peers) << (8 * sl);
+            }
+            inc = tot;
+        }
+        if (lane == __ffs(peers) - 1) my_ins += insert_or_update(a.table, a.cap, key, inc, a.status);
+    }
+    if (my_ins) atomicAdd(&s_ins, (unsigned long long)my_ins);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_ins) {
+        const unsigned long long before = atomicAdd(&a.counters[0], s_ins);
+        // stop the build early once the table is nearly full; the host retries
+        if ((before + s_ins) * 20 > (unsigned long long)a.cap * 19) atomicOr(a.status, kStatusTableFull);
+    }
+}
+
+// ---------------------------------------------------------------------
+// K2: cutoff + compaction. multiplicity < c -> 0 (graph.cpp:1105); a key
+// survives iff one of its 8 slots is nonzero (graph.cpp:1106-1108).
+__global__ void __launch_bounds__(kCBlock) k_compact(BuildArgs a) {
+    __shared__ uint64_t wb[kCBlock / 32];
+    __shared__ unsigned long long s_base;
+    const uint64_t chunk = (uint64_t)blockIdx.x * kCBlock * kCItems;
+    const int c = a.cutoff;
+    const uint32_t thr = c <= 0 ? 0u : (c >= 256 ? 0u : (uint32_t)c * 0x01010101u);
+    const bool all_cut = c >= 256;
+    uint64_t keys[kCItems], cnts[kCItems];
+    unsigned keep = 0;
+    int nkeep = 0;
+#pragma unroll
+    for (int it = 0; it < kCItems; ++it) {
+        const uint64_t idx = chunk + (uint64_t)it * kCBlock + threadIdx.x;
+        keys[it] = 0;
+        cnts[it] = 0;
+        if (idx < a.cap) {
+            const ulonglong2 e = *reinterpret_cast<const ulonglong2 *>(a.table + idx);
+            uint64_t v = e.y;
+            if (thr) {
+                const uint32_t lo = (uint32_t)v & __vcmpgeu4((uint32_t)v, thr);
+                const uint32_t hi = (uint32_t)(v >> 32) & __vcmpgeu4((uint32_t)(v >> 32), thr);
+                v = ((uint64_t)hi << 32) | lo;
+            }
+            if (all_cut) v = 0;
+            keys[it] = e.x;
+            cnts[it] = v;
+            if (e.x != 0 && v != 0) {
+                keep |= 1u << it;
+                nkeep++;
+            }
+        }
+    }
+    uint64_t total;
+    const uint64_t ex = block_exclusive_scan<kCBlock>((uint64_t)nkeep, wb, &total);
+    if (threadIdx.x == 0) s_base = total ? atomicAdd(&a.counters[1], (unsigned long long)total) : 0;
+    __syncthreads();
+    uint64_t pos = s_base + ex;
+#pragma unroll
+    for (int it = 0; it < kCItems; ++it) {
+        if (keep & (1u << it)) {
+            if (pos < a.out_cap) {
+                a.out_keys[pos] = keys[it];
+                a.out_mult[pos] = cnts[it];
+            }
+            pos++;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// Random-access probe (roofline denominator).
+__global__ void __launch_bounds__(256) k_probe(int kind, Entry *table, uint64_t n16,
+                                               uint64_t ops_per_thread, uint64_t seed,
+                                               unsigned long long *sink) {
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint64_t x = mix64(seed ^ (tid * 0x9e3779b97f4a7c15ull)) | 1ull;
+    unsigned long long acc = 0;
+    for (uint64_t op = 0; op < ops_per_thread; ++op) {
+        x ^= x >> 12;
+        x ^= x << 25;
+        x ^= x >> 27;
+        const uint64_t r = x * 0x2545f4914f6cdd1dull;
+        Entry *e = table + __umul64hi(r, n16);
+        switch (kind) {
+            case 0: atomicAdd(reinterpret_cast<unsigned *>(e), 1u); break;
+            case 1: acc += atomicAdd(reinterpret_cast<unsigned long long *>(e), 1ull); break;
+            case 2: acc += cas128(e, 0, 0, 0, 0).y; break;
+            case 3: {
+                const ulonglong2 v = ld_relaxed16(e);
+                acc += v.x ^ v.y;
+                break;
+            }
+            default: {
+                const ulonglong2 v = ld_relaxed16(e);
+                acc += cas128(e, v.x, v.y, v.x, v.y + 1).y;
+                break;
+            }
+        }
+    }
+    if (acc == 0x123456789ull) *sink = acc;  // keeps the loads live
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------
+// Host launchers.
+
+int device_sm_count() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+uint64_t scan_block_count(uint64_t n_reads) { return (n_reads + kScanChunk - 1) / kScanChunk; }
+
+int launch_occ_scan(const BuildArgs &a, cudaStream_t s) {
+    const uint64_t nb = scan_block_count(a.n_reads);
+    if (nb == 0) return 0;
+    k_scan_reduce<<<(unsigned)nb, kScanBlock, 0, s>>>(a.read_len, a.n_reads, a.k, a.scan_blocks);
+    k_scan_blocks<<<1, 1024, 0, s>>>(a.scan_blocks, nb, a.occ_prefix + a.n_reads);
+    k_scan_write<<<(unsigned)nb, kScanBlock, 0, s>>>(a.read_len, a.n_reads, a.k, a.scan_blocks,
+                                                     a.occ_prefix);
+    return 3;
+}
+
+int launch_tiles(const BuildArgs &a, cudaStream_t s) {
+    if (a.n_tiles == 0) return 0;
+    const unsigned grid = (unsigned)((a.n_tiles + 255) / 256);
+    k_tiles<<<grid, 256, 0, s>>>(a.occ_prefix, a.n_reads, a.n_tiles, a.tile_first_read);
+    return 1;
+}
+
+int launch_hll(const BuildArgs &a, cudaStream_t s) {
+    if (a.n_tiles == 0) return 0;
+    const uint64_t grid = std::min<uint64_t>(a.n_tiles, (uint64_t)device_sm_count() * 4);
+    k_hll<<<(unsigned)grid, kK1Block, 0, s>>>(a);
+    return 1;
+}
+
+// Standard HyperLogLog estimate with the small-range (linear counting) correction.
+double hll_estimate(const unsigned *regs) {
+    const int m = 1 << kHllBits;
+    double sum = 0;
+    int zeros = 0;
+    for (int j = 0; j < m; j++) {
+        sum += ldexp(1.0, -(int)regs[j]);
+        zeros += regs[j] == 0;
+    }
+    const double alpha = 0.7213 / (1.0 + 1.079 / m);
+    double e = alpha * (double)m * (double)m / sum;
+    if (e <= 2.5 * m && zeros > 0) e = m * log((double)m / zeros);
+    return e;
+}
+
+int launch_count(const BuildArgs &a, cudaStream_t s) {
+    if (a.n_tiles == 0) return 0;
+    k_count<<<(unsigned)a.n_tiles, kK1Block, 0, s>>>(a);
+    return 1;
+}
+
+int launch_compact(const BuildArgs &a, cudaStream_t s) {
+    const uint64_t per = (uint64_t)kCBlock * kCItems;
+    const uint64_t grid = (a.cap + per - 1) / per;
+    if (grid == 0) return 0;
+    k_compact<<<(unsigned)grid, kCBlock, 0, s>>>(a);
+    return 1;
+}
+
+cudaError_t run_probe(int kind, uint64_t table_bytes, uint64_t n_ops, cudaStream_t s, float *ms) {
+    Entry *table = nullptr;
+    unsigned long long *sink = nullptr;
+    const uint64_t n16 = table_bytes / sizeof(Entry);
+    if (n16 == 0) return cudaErrorInvalidValue;
+    cudaError_t err = cudaMalloc(&table, n16 * sizeof(Entry));
+    if (err != cudaSuccess) return err;
+    err = cudaMalloc(&sink, sizeof(unsigned long long));
+    if (err != cudaSuccess) {
+        cudaFree(table);
+        return err;
+    }
+    cudaMemsetAsync(table, 0, n16 * sizeof(Entry), s);
+    const unsigned grid = (unsigned)device_sm_count() * 8;
+    const uint64_t threads = (uint64_t)grid * 256;
+    const uint64_t per = (n_ops + threads - 1) / threads;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    // warm-up launch, then the timed one
+    k_probe<<<grid, 256, 0, s>>>(kind, table, n16, per / 4 + 1, 7, sink);
+    cudaEventRecord(e0, s);
+    k_probe<<<grid, 256, 0, s>>>(kind, table, n16, per, 11, sink);
+    cudaEventRecord(e1, s);
+    err = cudaEventSynchronize(e1);
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    *ms = t * (float)((double)n_ops / (double)(per * threads));  // scale to exactly n_ops
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    cudaFree(table);
+    if (err == cudaSuccess) err = cudaGetLastError();
+    return err;
+}
+
+}  // namespace swg

@@ -1,0 +1,85 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "swapgb.h"
+
+namespace swg {
+
+// Hash-table entry: one canonical k-molecule and its 8 saturating uint8 edge
+// multiplicities (byte t = slot t, the reference's arc::multiplicity[t],
+// graph.cpp:36-40). Key 0 marks an empty entry: a canonical key is
+// max(kmer, revcomp(kmer)) and revcomp(0) = 4^k-1 > 0, so 0 is never a key.
+struct __align__(16) Entry {
+    unsigned long long key;
+    unsigned long long cnt;
+};
+
+// Device status bits (set by kernels, read by the host after a build).
+enum : unsigned {
+    kStatusTableFull = 1u,  // probe limit reached or table nearly full
+    kStatusCasLimit = 2u,   // a bounded CAS retry loop gave up
+};
+
+constexpr int kK1Block = 256;
+constexpr int kK1Items = 16;
+constexpr uint64_t kTileOcc = (uint64_t)kK1Block * kK1Items;  // occurrences per tile
+constexpr int kHllBits = 12;                                  // 4096 registers
+
+// Per-build launch parameters.
+struct BuildArgs {
+    const uint32_t *packed;
+    uint64_t n_words;
+    const uint64_t *read_off;
+    const uint32_t *read_len;
+    uint64_t n_reads;
+    int k;
+    int cutoff;
+    // workspace
+    uint64_t *occ_prefix;      // n_reads + 1
+    uint64_t *scan_blocks;     // scratch for the scan
+    uint32_t *tile_first_read; // n_tiles
+    uint64_t n_tiles;
+    uint64_t total_occ;
+    Entry *table;
+    uint64_t cap;
+    unsigned *hll;             // 1 << kHllBits registers
+    unsigned *status;
+    unsigned long long *counters;  // [0] inserted, [1] survivors
+    unsigned long long *out_keys;
+    unsigned long long *out_mult;
+    uint64_t out_cap;
+};
+
+// Kernel launchers (kernels.cu). Each returns the number of launches made.
+int launch_occ_scan(const BuildArgs &a, cudaStream_t s);
+uint64_t scan_block_count(uint64_t n_reads);
+int launch_tiles(const BuildArgs &a, cudaStream_t s);
+int launch_hll(const BuildArgs &a, cudaStream_t s);
+double hll_estimate(const unsigned *regs_host);
+int launch_count(const BuildArgs &a, cudaStream_t s);
+int launch_compact(const BuildArgs &a, cudaStream_t s);
+cudaError_t run_probe(int kind, uint64_t table_bytes, uint64_t n_ops, cudaStream_t s, float *ms);
+int device_sm_count();
+
+// Thread-local error message (api.cpp).
+void set_error(const std::string &msg);
+
+// Host framing / packing (reads.cpp).
+swg_status pack_fasta(const char *text, uint64_t len, int k, swg_reads **out);
+
+// Host writers (writers.cpp): records sorted by key.
+swg_status write_kmer_graph(const uint64_t *keys, const uint8_t *mult, uint64_t n, int k,
+                            const char *path);
+swg_status write_node_lines(const uint64_t *keys, const uint8_t *mult, uint64_t n,
+                            const char *path);
+void graph_stats(const uint8_t *mult, uint64_t n, int k, int64_t out[5]);
+void sort_records(uint64_t *keys, uint64_t *mult8, uint64_t n);
+uint64_t revcomp_host(uint64_t x, int k);
+uint64_t kmer_graph_neighbour(uint64_t key, int slot, int k);
+
+}  // namespace swg

@@ -1,0 +1,325 @@
+"""ctypes binding of the GB300 k-mer graph builder (C ABI in include/swapgb.h).
+
+This is a thin host-side mirror of the library: it loads the in-tree
+libswapgb.so (built by build.py) and raises if it is missing. There is no
+Python or CPU implementation of the build behind it.
+
+    reads = reads_from_fasta(text, k=31)
+    g = Graph()
+    g.build(Opts(k=31, cutoff=5), reads.packed, reads.off, reads.len)
+    keys, mult = g.copy_out(sorted=True)   # uint64[n], uint8[n, 8]
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libswapgb.so"
+SYNTH_PATH = PKG / "libswgsynth.so"
+SWAP_BIN = PKG / "bin" / "swap"
+
+STATUS = {
+    0: "SWG_OK", 1: "SWG_ERR_BAD_INPUT", 2: "SWG_ERR_TABLE_FULL", 3: "SWG_ERR_OOM",
+    4: "SWG_ERR_ADMISSION", 5: "SWG_ERR_TIMEOUT", 6: "SWG_ERR_CUDA", 7: "SWG_ERR_NO_DEVICE",
+    8: "SWG_ERR_BAD_STATE", 9: "SWG_ERR_IO", 10: "SWG_ERR_NOT_READY",
+}
+
+
+class SwgError(RuntimeError):
+    def __init__(self, status: int, what: str, msg: str):
+        super().__init__("%s: %s (%s)" % (what, STATUS.get(status, status), msg))
+        self.status = status
+
+
+class Opts(C.Structure):
+    _fields_ = [("k", C.c_int), ("cutoff", C.c_int), ("load_factor", C.c_double),
+                ("expected_distinct", C.c_uint64), ("stream", C.c_void_p)]
+
+    def __init__(self, k: int = 23, cutoff: int = 5, load_factor: float = 0.0,
+                 expected_distinct: int = 0, stream: int | None = None):
+        super().__init__(k, cutoff, load_factor, expected_distinct, stream)
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded libswapgb.so; raises if the native library has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError("native library %s is missing: run build()" % LIB_PATH)
+        L = C.CDLL(str(LIB_PATH))
+        P, u64, i32 = C.c_void_p, C.c_uint64, C.c_int
+        pu64 = C.POINTER(C.c_uint64)
+        sigs = {
+            "swg_status_string": (C.c_char_p, [i32]),
+            "swg_last_error": (C.c_char_p, []),
+            "swg_version": (C.c_char_p, []),
+            "swg_reads_from_fasta": (i32, [C.c_char_p, u64, i32, C.POINTER(P)]),
+            "swg_reads_from_fasta_file": (i32, [C.c_char_p, i32, C.POINTER(P)]),
+            "swg_reads_view": (i32, [P, C.POINTER(P), pu64, C.POINTER(P), C.POINTER(P), pu64, pu64]),
+            "swg_reads_records": (u64, [P]),
+            "swg_reads_free": (None, [P]),
+            "swg_graph_create": (i32, [C.POINTER(P)]),
+            "swg_graph_free": (None, [P]),
+            "swg_graph_build": (i32, [P, C.POINTER(Opts), P, u64, P, P, u64]),
+            "swg_graph_build_device": (i32, [P, C.POINTER(Opts), P, u64, P, P, u64]),
+            "swg_build": (i32, [C.POINTER(Opts), P, u64, P, P, u64, C.POINTER(P)]),
+            "swg_build_fasta": (i32, [C.POINTER(Opts), C.c_char_p, u64, C.POINTER(P)]),
+            "swg_graph_size": (i32, [P, pu64]),
+            "swg_graph_distinct": (i32, [P, pu64]),
+            "swg_graph_device_view": (i32, [P, C.POINTER(P), C.POINTER(P), pu64]),
+            "swg_graph_copy_out": (i32, [P, P, P, u64, i32, pu64]),
+            "swg_graph_stats": (i32, [P, C.POINTER(C.c_int64)]),
+            "swg_graph_write_kmer_graph": (i32, [P, C.c_char_p]),
+            "swg_graph_write_node_lines": (i32, [P, C.c_char_p]),
+            "swg_records_write_kmer_graph": (i32, [P, P, u64, i32, C.c_char_p]),
+            "swg_records_write_node_lines": (i32, [P, P, u64, C.c_char_p]),
+            "swg_graph_last_timings": (i32, [P, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
+            "swg_probe_random_access": (i32, [i32, u64, u64, P, C.POINTER(C.c_double)]),
+        }
+        for name, (res, args) in sigs.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int, what: str) -> None:
+    if status != 0:
+        raise SwgError(status, what, lib().swg_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data if a.size else 0
+
+
+class Reads:
+    """Packed reads on the host (swg_reads), with numpy views of its arrays."""
+
+    def __init__(self, handle: int):
+        self._h = C.c_void_p(handle)
+        p, off, ln = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        nw, nr, nb = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(lib().swg_reads_view(self._h, C.byref(p), C.byref(nw), C.byref(off), C.byref(ln),
+                                    C.byref(nr), C.byref(nb)), "swg_reads_view")
+        self.n_words, self.n_reads, self.n_bases = nw.value, nr.value, nb.value
+        self.records = lib().swg_reads_records(self._h)
+        self.packed = _view(p.value, nw.value, np.uint32)
+        self.off = _view(off.value, nr.value, np.uint64)
+        self.len = _view(ln.value, nr.value, np.uint32)
+
+    def close(self) -> None:
+        if self._h:
+            lib().swg_reads_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _view(addr: int | None, n: int, dtype) -> np.ndarray:
+    if not n or not addr:
+        return np.zeros(0, dtype=dtype)
+    buf = (C.c_char * (n * np.dtype(dtype).itemsize)).from_address(addr)
+    return np.frombuffer(buf, dtype=dtype, count=n)
+
+
+def reads_from_fasta(text: bytes, k: int) -> Reads:
+    h = C.c_void_p()
+    _check(lib().swg_reads_from_fasta(text, len(text), k, C.byref(h)), "swg_reads_from_fasta")
+    return Reads(h.value)
+
+
+def reads_from_fasta_file(path: str, k: int) -> Reads:
+    h = C.c_void_p()
+    _check(lib().swg_reads_from_fasta_file(str(path).encode(), k, C.byref(h)),
+           "swg_reads_from_fasta_file")
+    return Reads(h.value)
+
+
+class Graph:
+    """A device-resident filtered k-mer graph (swg_graph) and its workspace."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        _check(lib().swg_graph_create(C.byref(h)), "swg_graph_create")
+        self._h = h
+
+    def close(self) -> None:
+        if self._h:
+            lib().swg_graph_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def build(self, opts: Opts, packed: np.ndarray, off: np.ndarray, ln: np.ndarray) -> "Graph":
+        packed = np.ascontiguousarray(packed, dtype=np.uint32)
+        off = np.ascontiguousarray(off, dtype=np.uint64)
+        ln = np.ascontiguousarray(ln, dtype=np.uint32)
+        _check(lib().swg_graph_build(self._h, C.byref(opts), _ptr(packed), packed.size, _ptr(off),
+                                     _ptr(ln), off.size), "swg_graph_build")
+        return self
+
+    def build_reads(self, opts: Opts, reads: Reads) -> "Graph":
+        return self.build(opts, reads.packed, reads.off, reads.len)
+
+    def build_device(self, opts: Opts, d_packed: int, n_words: int, d_off: int, d_len: int,
+                     n_reads: int) -> "Graph":
+        _check(lib().swg_graph_build_device(self._h, C.byref(opts), d_packed, n_words, d_off,
+                                            d_len, n_reads), "swg_graph_build_device")
+        return self
+
+    def size(self) -> int:
+        n = C.c_uint64()
+        _check(lib().swg_graph_size(self._h, C.byref(n)), "swg_graph_size")
+        return n.value
+
+    def distinct(self) -> int:
+        n = C.c_uint64()
+        _check(lib().swg_graph_distinct(self._h, C.byref(n)), "swg_graph_distinct")
+        return n.value
+
+    def device_view(self) -> tuple[int, int, int]:
+        k, m, n = C.c_void_p(), C.c_void_p(), C.c_uint64()
+        _check(lib().swg_graph_device_view(self._h, C.byref(k), C.byref(m), C.byref(n)),
+               "swg_graph_device_view")
+        return k.value or 0, m.value or 0, n.value
+
+    def copy_out(self, sorted: bool = True) -> tuple[np.ndarray, np.ndarray]:
+        n = self.size()
+        keys = np.zeros(n, dtype=np.uint64)
+        mult = np.zeros((n, 8), dtype=np.uint8)
+        got = C.c_uint64()
+        _check(lib().swg_graph_copy_out(self._h, _ptr(keys), _ptr(mult), n, int(sorted),
+                                        C.byref(got)), "swg_graph_copy_out")
+        return keys, mult
+
+    def stats(self) -> list[int]:
+        out = (C.c_int64 * 5)()
+        _check(lib().swg_graph_stats(self._h, out), "swg_graph_stats")
+        return list(out)
+
+    def write_kmer_graph(self, path: str) -> None:
+        _check(lib().swg_graph_write_kmer_graph(self._h, str(path).encode()),
+               "swg_graph_write_kmer_graph")
+
+    def write_node_lines(self, path: str) -> None:
+        _check(lib().swg_graph_write_node_lines(self._h, str(path).encode()),
+               "swg_graph_write_node_lines")
+
+    def timings(self) -> tuple[list[float], int]:
+        ms = (C.c_float * 5)()
+        n = C.c_int()
+        _check(lib().swg_graph_last_timings(self._h, ms, C.byref(n)), "swg_graph_last_timings")
+        return list(ms), n.value
+
+
+def build_fasta(opts: Opts, text: bytes) -> Graph:
+    g = Graph.__new__(Graph)
+    h = C.c_void_p()
+    _check(lib().swg_build_fasta(C.byref(opts), text, len(text), C.byref(h)), "swg_build_fasta")
+    g._h = h
+    return g
+
+
+def records_write_kmer_graph(keys: np.ndarray, mult: np.ndarray, k: int, path: str) -> None:
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    mult = np.ascontiguousarray(mult, dtype=np.uint8).reshape(-1, 8)
+    _check(lib().swg_records_write_kmer_graph(_ptr(keys), _ptr(mult), keys.size, k,
+                                              str(path).encode()), "swg_records_write_kmer_graph")
+
+
+def records_write_node_lines(keys: np.ndarray, mult: np.ndarray, path: str) -> None:
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    mult = np.ascontiguousarray(mult, dtype=np.uint8).reshape(-1, 8)
+    _check(lib().swg_records_write_node_lines(_ptr(keys), _ptr(mult), keys.size,
+                                              str(path).encode()), "swg_records_write_node_lines")
+
+
+PROBE_KINDS = {"red_add_u32": 0, "atom_add_u64": 1, "cas128": 2, "load16": 3, "load16_cas128": 4}
+
+
+def probe_random_access(kind: str, table_bytes: int, n_ops: int, stream: int | None = None) -> float:
+    """Random-access operations per second on this GPU (device time)."""
+    out = C.c_double()
+    _check(lib().swg_probe_random_access(PROBE_KINDS[kind], table_bytes, n_ops, stream,
+                                         C.byref(out)), "swg_probe_random_access")
+    return out.value
+
+
+# ---- synthetic reads ------------------------------------------------------
+
+class SynthParams(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("genome_len", C.c_uint64), ("gc", C.c_double),
+                ("repeat_frac", C.c_double), ("repeat_unit_min", C.c_uint32),
+                ("repeat_unit_max", C.c_uint32), ("repeat_copies_min", C.c_uint32),
+                ("repeat_copies_max", C.c_uint32), ("repeat_divergence", C.c_double),
+                ("tandem_frac", C.c_double), ("tandem_unit_min", C.c_uint32),
+                ("tandem_unit_max", C.c_uint32), ("tandem_len_min", C.c_uint32),
+                ("tandem_len_max", C.c_uint32), ("n_reads", C.c_uint64), ("read_len", C.c_uint32),
+                ("sub_rate", C.c_double), ("indel_rate", C.c_double), ("threads", C.c_int)]
+
+
+_synth = None
+
+
+def _synth_lib() -> C.CDLL:
+    global _synth
+    if _synth is None:
+        if not SYNTH_PATH.exists():
+            raise RuntimeError("%s is missing: run build()" % SYNTH_PATH)
+        L = C.CDLL(str(SYNTH_PATH))
+        L.swg_synth_defaults.argtypes = [C.POINTER(SynthParams)]
+        L.swg_synth_defaults.restype = None
+        L.swg_synth_fasta.argtypes = [C.POINTER(SynthParams), C.POINTER(C.c_void_p)]
+        L.swg_synth_fasta.restype = C.c_int64
+        L.swg_synth_fasta_file.argtypes = [C.POINTER(SynthParams), C.c_char_p]
+        L.swg_synth_fasta_file.restype = C.c_int64
+        L.swg_synth_free.argtypes = [C.c_void_p]
+        L.swg_synth_free.restype = None
+        _synth = L
+    return _synth
+
+
+def synth_params(**kw) -> SynthParams:
+    p = SynthParams()
+    _synth_lib().swg_synth_defaults(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def synth_fasta(**kw) -> bytes:
+    """Seeded synthetic FASTA (see csrc/synth.h for the parameters)."""
+    p = synth_params(**kw)
+    buf = C.c_void_p()
+    n = _synth_lib().swg_synth_fasta(C.byref(p), C.byref(buf))
+    if n < 0:
+        raise RuntimeError("synthetic read generation failed")
+    try:
+        return C.string_at(buf.value, n)
+    finally:
+        _synth_lib().swg_synth_free(buf)
+
+
+def synth_fasta_file(path: str, **kw) -> int:
+    p = synth_params(**kw)
+    n = _synth_lib().swg_synth_fasta_file(C.byref(p), str(path).encode())
+    if n < 0:
+        raise RuntimeError("synthetic read generation failed")
+    return n

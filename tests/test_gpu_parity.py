@@ -1,0 +1,151 @@
+"""GPU parity: the sm_103a build through the C ABI against the reference's
+own outputs (golden fixtures) and the CPU restatement. Integer work, so the
+bar is bit-exact equality of every key and every multiplicity."""
+import numpy as np
+import pytest
+
+import oracle
+import swapgb
+from common import golden, kat, kat_text, sha_lines, sorted_lines, synth_case, synth_case_text
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_build(text: bytes, k: int, c: int, **kw) -> swapgb.Graph:
+    reads = swapgb.reads_from_fasta(text, k)
+    g = swapgb.Graph()
+    g.build_reads(swapgb.Opts(k=k, cutoff=c, **kw), reads)
+    return g
+
+
+def assert_same_records(g: swapgb.Graph, text: bytes, k: int, c: int) -> None:
+    keys, mult = g.copy_out(sorted=True)
+    okeys, omult = oracle.records(text, k, c)
+    assert keys.size == okeys.size, (keys.size, okeys.size)
+    assert np.array_equal(keys, okeys)
+    bad = np.nonzero((mult != omult).any(axis=1))[0]
+    assert bad.size == 0, "first mismatch key=%d gpu=%s oracle=%s" % (
+        keys[bad[0]], mult[bad[0]].tolist(), omult[bad[0]].tolist())
+
+
+@pytest.mark.parametrize("case", [c["name"] for c in golden()["kat"]])
+def test_kat_matches_reference(case, tmp_path):
+    c = kat(case)
+    g = gpu_build(kat_text(case), c["k"], c["c"])
+    g.write_kmer_graph(tmp_path / "kg.txt")
+    g.write_node_lines(tmp_path / "nodes.txt")
+    assert sha_lines(sorted_lines(tmp_path / "kg.txt")) == c["kmer_graph_sha256"]
+    assert sha_lines(sorted_lines(tmp_path / "nodes.txt")) == c["nodes_sha256"]
+    assert g.size() == c["n_nodes"]
+    if c["totals"]:
+        st = g.stats()
+        assert st[0] == c["totals"]["recvNodeNum"] and st[1] == c["totals"]["recvEdgeNum"]
+
+
+@pytest.mark.parametrize("case", [c["name"] for c in golden()["synth"]])
+def test_synthetic_matches_reference(case, tmp_path):
+    c = synth_case(case)
+    text = synth_case_text(case)
+    g = gpu_build(text, c["k"], c["c"])
+    assert g.size() == c["n_nodes"]
+    g.write_node_lines(tmp_path / "nodes.txt")
+    assert sha_lines(sorted_lines(tmp_path / "nodes.txt")) == c["nodes_sha256"]
+    g.write_kmer_graph(tmp_path / "kg.txt")
+    assert sha_lines(sorted_lines(tmp_path / "kg.txt")) == c["kmer_graph_sha256"]
+
+
+@pytest.mark.parametrize("k,c", [(19, 0), (21, 1), (23, 2), (27, 3), (29, 4), (31, 5), (31, -3),
+                                 (9, 2), (15, 1), (20, 2), (1, 1), (2, 0)])
+def test_k_and_cutoff_sweep(k, c):
+    text = synth_case_text("c2_small")
+    g = gpu_build(text, k, c)
+    assert_same_records(g, text, k, c)
+
+
+def test_repeats_and_tandems():
+    text = swapgb.synth_fasta(seed=21, genome_len=300000, repeat_frac=0.05, tandem_frac=0.02,
+                              n_reads=60000, read_len=150, sub_rate=0.005)
+    g = gpu_build(text, 31, 3)
+    assert_same_records(g, text, 31, 3)
+
+
+def test_hot_keys_saturate():
+    # one k-mer hit millions of times inside single warps: poly-A and short
+    # tandem units; counts must saturate at exactly 255
+    reads = ["A" * 250, "AC" * 125, "ACG" * 83, "T" * 200, "ACGTT" * 50] * 4000
+    text = "".join(">h%d\n%s\n" % (i, r) for i, r in enumerate(reads)).encode()
+    for c in (0, 2, 255):
+        g = gpu_build(text, 21, c)
+        assert_same_records(g, text, 21, c)
+        _, mult = g.copy_out()
+        assert mult.max() == 255
+
+
+def test_table_full_retry():
+    # a sizing hint far too small forces the device-side full detection and
+    # the host's rebuild with a larger table
+    text = synth_case_text("c1_small")
+    g = gpu_build(text, 21, 2, expected_distinct=10)
+    assert_same_records(g, text, 21, 2)
+
+
+def test_high_load_factor():
+    text = synth_case_text("c2_small")
+    g = gpu_build(text, 31, 5, load_factor=0.9)
+    assert_same_records(g, text, 31, 5)
+
+
+def test_empty_and_short_inputs():
+    text = b">a\nACGT\n>b\nAC\n"  # every read shorter than k
+    g = gpu_build(text, 19, 0)
+    assert g.size() == 0 and g.distinct() == 0
+    text = b">a\nACGTACGTACGTACGTACGTA\n"  # L == k: one key, all-zero mask, dropped
+    g = gpu_build(text, 21, 0)
+    assert g.size() == 0 and g.distinct() == 1
+
+
+def test_device_input_path_and_handle_reuse():
+    import torch
+    text1 = synth_case_text("c2_small")
+    text2 = synth_case_text("c4_ragged")
+    g = swapgb.Graph()
+    for text, k, c in ((text1, 31, 5), (text2, 27, 3), (text1, 31, 5)):
+        r = swapgb.reads_from_fasta(text, k)
+        p = torch.from_numpy(r.packed.view(np.int32).copy()).cuda()
+        o = torch.from_numpy(r.off.view(np.int64).copy()).cuda()
+        ln = torch.from_numpy(r.len.view(np.int32).copy()).cuda()
+        torch.cuda.synchronize()
+        g.build_device(swapgb.Opts(k=k, cutoff=c), p.data_ptr(), p.numel(), o.data_ptr(),
+                       ln.data_ptr(), o.numel())
+        assert_same_records(g, text, k, c)
+        ms, launches = g.timings()
+        assert launches >= 6 and ms[4] > 0
+
+
+def test_unsorted_copy_is_a_permutation():
+    text = synth_case_text("k25_c1")
+    g = gpu_build(text, 25, 1)
+    k1, m1 = g.copy_out(sorted=False)
+    order = np.argsort(k1, kind="stable")
+    k2, m2 = g.copy_out(sorted=True)
+    assert np.array_equal(k1[order], k2) and np.array_equal(m1[order], m2)
+
+
+def test_build_fasta_entry_point():
+    text = kat_text("orient_k19")
+    g = swapgb.build_fasta(swapgb.Opts(k=19, cutoff=1), text)
+    assert_same_records(g, text, 19, 1)
+
+
+def test_cli_matches_reference(tmp_path):
+    import subprocess
+    c = kat("orient_k31_c3")
+    fa = tmp_path / "in.fa"
+    fa.write_bytes(kat_text("orient_k31_c3"))
+    out = tmp_path / "out"
+    r = subprocess.run([str(swapgb.SWAP_BIN), "-k", "31", "-c", "3", "-i", str(fa), "-o", str(out),
+                        "-s"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout
+    assert sha_lines(sorted_lines(out / "kmerGraph.txt")) == c["kmer_graph_sha256"]
+    assert sha_lines(sorted_lines(out / "nodes.txt")) == c["nodes_sha256"]
+    assert "recvNodeNum = %d" % c["totals"]["recvNodeNum"] in r.stdout

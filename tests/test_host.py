@@ -1,0 +1,132 @@
+"""Host-side parts of the library that need no GPU: FASTA framing and 2-bit
+packing, the output writers, the C-ABI surface and the command line."""
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+import swapgb
+from common import golden, kat, kat_text, sha_lines, sorted_lines, synth_case_text
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def unpack(reads: swapgb.Reads) -> np.ndarray:
+    idx = np.arange(reads.n_bases, dtype=np.uint64)
+    w = reads.packed[(idx >> np.uint64(4)).astype(np.int64)]
+    sh = (np.uint64(30) - np.uint64(2) * (idx & np.uint64(15))).astype(np.uint32)
+    return ((w >> sh) & 3).astype(np.uint8)
+
+
+def same_framing(text: bytes, k: int) -> None:
+    r = swapgb.reads_from_fasta(text, k)
+    o = oracle.parse(text, k)
+    assert r.n_reads == o["n_reads"] and r.n_bases == o["n_bases"]
+    assert r.records == o["n_records"]
+    assert np.array_equal(r.off, o["off"]) and np.array_equal(r.len, o["len"])
+    assert np.array_equal(unpack(r), o["codes"])
+
+
+@pytest.mark.parametrize("case", [c["name"] for c in golden()["kat"]])
+def test_framing_matches_oracle_kat(case):
+    same_framing(kat_text(case), kat(case)["k"])
+
+
+def test_framing_large_parallel():
+    # > 4 MiB per chunk: exercises the multi-threaded two-pass framing and the
+    # words shared between chunks
+    text = synth_case_text("c1_full")
+    same_framing(text, 21)
+
+
+def test_framing_leading_bytes_skipped():
+    # bytes before the first '>' are skipped, as kmerGraph.cpp:113 does (the
+    # reference then never finishes; this library does not hang on them)
+    body = b">a\nACGTACGTACGTACGTACGTACGT\n>b\nTTTTGGGGCCCCAAAATTTTGGGG\n"
+    r1 = swapgb.reads_from_fasta(b"junk\n\nmore junk\n" + body, 19)
+    r2 = swapgb.reads_from_fasta(body, 19)
+    assert np.array_equal(r1.packed, r2.packed) and np.array_equal(r1.len, r2.len)
+
+
+@pytest.mark.parametrize("text,why", [
+    (b">r1\nACGTACGTACGTACGTACGTAC", "last record without newline"),
+    (b">r1\nACGTACGTACGTACGTACGTAC\n>r2\n", "header without sequence line"),
+    (b"ACGTACGTACGTACGTACGTAC\n", "no record start"),
+    (b">r1\nACGTACGT\x00ACGTACGTACGTAC\n", "NUL byte"),
+    (b"", "empty input"),
+])
+def test_framing_rejects_what_the_reference_never_finishes(text, why):
+    with pytest.raises(swapgb.SwgError) as e:
+        swapgb.reads_from_fasta(text, 19)
+    assert e.value.status == 1, why
+
+
+def test_framing_bad_k():
+    with pytest.raises(swapgb.SwgError):
+        swapgb.reads_from_fasta(b">r\nACGT\n", 32)
+
+
+@pytest.mark.parametrize("case", [c["name"] for c in golden()["kat"]])
+def test_record_writers_match_reference(case, tmp_path):
+    c = kat(case)
+    keys, mult = oracle.records(kat_text(case), c["k"], c["c"])
+    # writers take records in any order
+    perm = np.random.default_rng(0).permutation(keys.size)
+    swapgb.records_write_kmer_graph(keys[perm], mult[perm], c["k"], tmp_path / "kg.txt")
+    swapgb.records_write_node_lines(keys[perm], mult[perm], tmp_path / "nodes.txt")
+    assert sha_lines(sorted_lines(tmp_path / "kg.txt")) == c["kmer_graph_sha256"]
+    assert sha_lines(sorted_lines(tmp_path / "nodes.txt")) == c["nodes_sha256"]
+    # the library writes its lines already sorted by first token
+    assert (tmp_path / "kg.txt").read_text().splitlines() == sorted_lines(tmp_path / "kg.txt")
+
+
+def test_abi_exports_every_declared_symbol():
+    header = (ROOT / "include" / "swapgb.h").read_text()
+    header = re.sub(r"/\*.*?\*/", "", header, flags=re.S)  # declarations only
+    declared = set(re.findall(r"\b(swg_\w+)\s*\(", header))
+    out = subprocess.run(["nm", "-D", "--defined-only", str(swapgb.LIB_PATH)],
+                         stdout=subprocess.PIPE, text=True, check=True).stdout
+    exported = {l.split()[-1] for l in out.splitlines() if " T " in l}
+    assert declared, "no declarations parsed"
+    assert declared <= exported, sorted(declared - exported)
+    lib = swapgb.lib()
+    for name in declared:
+        assert hasattr(lib, name)
+
+
+def test_status_strings():
+    lib = swapgb.lib()
+    for s in range(11):
+        assert lib.swg_status_string(s)
+    assert lib.swg_version().startswith(b"swapgb")
+
+
+def test_cli_argument_checks(tmp_path):
+    swap = str(swapgb.SWAP_BIN)
+    r = subprocess.run([swap, "-k", "20", "-i", "x.fa", "-o", str(tmp_path / "o")],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 2 and "odd number" in r.stdout
+    r = subprocess.run([swap, "-k", "33", "-i", "x.fa", "-o", str(tmp_path / "o")],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 2
+    r = subprocess.run([swap, "-k", "21"], stdout=subprocess.PIPE, text=True)
+    assert r.returncode == 2 and "Usage" in r.stdout
+    (tmp_path / "exists").mkdir()
+    r = subprocess.run([swap, "-i", "x.fa", "-o", str(tmp_path / "exists")],
+                       stdout=subprocess.PIPE, text=True)
+    assert r.returncode == 1 and "Creating directory" in r.stdout
+    r = subprocess.run([swap, "-v"], stdout=subprocess.PIPE, text=True)
+    assert r.returncode == 0 and "version" in r.stdout
+
+
+def test_synthetic_generator_is_deterministic():
+    a = swapgb.synth_fasta(seed=5, genome_len=50000, n_reads=5000, read_len=150, sub_rate=0.01,
+                           indel_rate=0.001, repeat_frac=0.05, tandem_frac=0.02, threads=1)
+    b = swapgb.synth_fasta(seed=5, genome_len=50000, n_reads=5000, read_len=150, sub_rate=0.01,
+                           indel_rate=0.001, repeat_frac=0.05, tandem_frac=0.02, threads=5)
+    assert a == b
+    lines = a.split(b"\n")
+    assert lines[0] == b">r0" and all(len(x) == 150 for x in lines[1:-1:2])
