@@ -46,6 +46,8 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-probe", action="store_true", help="skip the random-access probe")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--reads", type=int, default=0,
+                    help="smaller case for profiling: this many reads, genome scaled to keep 50x")
     return ap.parse_args()
 
 
@@ -209,7 +211,11 @@ def main() -> int:
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    text = swapgb.synth_fasta(**WORKLOAD)
+    work = dict(WORKLOAD)
+    if args.reads:
+        work["genome_len"] = max(10_000, WORKLOAD["genome_len"] * args.reads // WORKLOAD["n_reads"])
+        work["n_reads"] = args.reads
+    text = swapgb.synth_fasta(**work)
     reads = swapgb.reads_from_fasta(text, K)
     n_bases = reads.n_bases
     n_occ = int((reads.len.astype(np.int64) - K + 1).clip(min=0).sum())

@@ -230,8 +230,11 @@ swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, u
             return SWG_ERR_TIMEOUT;
         }
         if (status & swg::kStatusTableFull) {
-            const double inserted = (double)g->h_ctl->counters[0];
-            cap = (uint64_t)std::ceil(std::max(2.0 * (double)cap, inserted * 2.0 / load)) + 64;
+            // the distinct count never exceeds the occurrence count: retry at
+            // that bound first, then double (only a probe-length pathology
+            // can fill a table sized by the bound)
+            const uint64_t bound = (uint64_t)std::ceil((double)a.total_occ / load) + 64;
+            cap = cap < bound ? bound : cap * 2;
             continue;
         }
         g->n_distinct = g->h_ctl->counters[0];
