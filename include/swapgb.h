@@ -150,6 +150,23 @@ swg_status swg_records_write_node_lines(const uint64_t *keys, const uint8_t *mul
  * [4] whole build. Also the launch count of the last build. */
 swg_status swg_graph_last_timings(const swg_graph *g, float ms[5], int *launches);
 
+/* ---- build without device allocation ------------------------------------ */
+/* No counterpart in the reference. For callers that must not have the library
+ * allocate device memory (their memory is reserved by another allocator or a
+ * fixed budget, or they cannot accept cudaMalloc's device-wide synchronisation
+ * mid-run): the whole build runs in one file-scope device array of about
+ * 72 MiB that every GPU loading the library holds until exit. The reads and the
+ * output arrays (keys[out_cap], mult[out_cap] as in swg_graph_device_view) are
+ * the caller's device memory. At most 1048576 reads and 2516505 k-mer
+ * occurrences per call, else SWG_ERR_BAD_INPUT; more than out_cap survivors
+ * gives SWG_ERR_BAD_INPUT with *n_out set to the count needed. The first call
+ * on a device resolves the array's address (make it before any stream capture).
+ * Calls share the array: calls whose device work overlaps race. */
+swg_status swg_build_device_noalloc(const swg_opts *o, const uint32_t *d_packed, uint64_t n_words,
+                                    const uint64_t *d_read_off, const uint32_t *d_read_len,
+                                    uint64_t n_reads, uint64_t *d_keys_out, uint64_t *d_mult_out,
+                                    uint64_t out_cap, uint64_t *n_out);
+
 /* ---- roofline probe ----------------------------------------------------- */
 /* Random-access throughput on this GPU: n_ops operations at uniformly random
  * 16-byte-aligned addresses of a table of table_bytes bytes (allocated and

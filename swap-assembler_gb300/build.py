@@ -63,6 +63,10 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict[str, Path]:
     if ptxas_info:
         cu_cmd.insert(1, "-Xptxas=-v")
     jobs.append((OBJ / "kernels.o", [cu, *headers], cu_cmd))
+    na = CSRC / "noalloc.cu"
+    jobs.append((OBJ / "noalloc.o", [na, *headers],
+                 [nvcc, *ARCH, "-lineinfo", "-Xcompiler", "-fPIC", *common, "-c", str(na), "-o",
+                  str(OBJ / "noalloc.o")]))
     for name in ("api.cpp", "reads.cpp", "writers.cpp"):
         src = CSRC / name
         o = OBJ / (name[:-4] + ".o")
@@ -81,7 +85,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict[str, Path]:
         list(ex.map(lambda j: _run(j[2]), todo))
 
     lib = PKG / "libswapgb.so"
-    lib_objs = [OBJ / n for n in ("kernels.o", "api.o", "reads.o", "writers.o")]
+    lib_objs = [OBJ / n for n in ("kernels.o", "noalloc.o", "api.o", "reads.o", "writers.o")]
     if _stale(lib, lib_objs):
         _run([nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, lib_objs), "-lpthread"])
     synth = PKG / "libswgsynth.so"
