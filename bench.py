@@ -46,13 +46,16 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-probe", action="store_true", help="skip the random-access probe")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--algo", default="direct", choices=["direct", "partitioned"])
+    ap.add_argument("--order", default="input", choices=["input", "minimizer"],
+                    help="read order of the direct algorithm")
     ap.add_argument("--reads", type=int, default=0,
                     help="smaller case for profiling: this many reads, genome scaled to keep 50x")
     return ap.parse_args()
 
 
-def config_dict() -> dict:
-    return {"workload": "plain single-sample build: 5 Mbp genome (GC 50%), 2.5M x 100 bp reads "
+def config_dict(algo: str = "direct", order: str = "input") -> dict:
+    return {"algorithm": algo, "read_order": order, "workload": "plain single-sample build: 5 Mbp genome (GC 50%), 2.5M x 100 bp reads "
                         "at 50x from both strands, 1% subs + 0.1% indels, k=31, c=5",
             "genome_bp": WORKLOAD["genome_len"], "reads": WORKLOAD["n_reads"],
             "read_len": WORKLOAD["read_len"], "k": K, "c": CUTOFF,
@@ -236,7 +239,10 @@ def main() -> int:
     n_bases = reads.n_bases
     n_occ = int((reads.len.astype(np.int64) - K + 1).clip(min=0).sum())
     stream = torch.cuda.current_stream(dev)
-    opts = swapgb.Opts(k=K, cutoff=CUTOFF, stream=stream.cuda_stream)
+    algo = swapgb.ALGO_PARTITIONED if args.algo == "partitioned" else swapgb.ALGO_DIRECT
+    order = swapgb.ORDER_MINIMIZER if args.order == "minimizer" else swapgb.ORDER_INPUT
+    opts = swapgb.Opts(k=K, cutoff=CUTOFF, stream=stream.cuda_stream, algorithm=algo,
+                       read_order=order)
 
     d_packed = torch.from_numpy(reads.packed.view(np.int32).copy()).to(dev)
     d_off = torch.from_numpy(reads.off.view(np.int64).copy()).to(dev)
@@ -256,7 +262,7 @@ def main() -> int:
         dist.barrier()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(args.steps)]
-    count_ms, launches = [], 0
+    phase_ms, launches = [], 0
     with ClockSampler(local) as clocks:
         torch.cuda.synchronize()
         t_wall0 = time.perf_counter()
@@ -266,7 +272,7 @@ def main() -> int:
             step()
             evs[i][1].record(stream)
             ms, nl = g.timings()
-            count_ms.append(ms[2])
+            phase_ms.append(ms)
             launches += nl
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall0
@@ -305,35 +311,49 @@ def main() -> int:
     h2d = h_packed.numel() * 4 + h_off.numel() * 8 + h_len.numel() * 4
     d2h = n_e2e * 16
 
-    # ---- roofline of the dominant kernel (K1 extract+count) ----
+    # ---- rooflines ----
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
     peak_src = "of measured" if hbm else "of fallback"
     hbm = hbm or 6800.0
-    k1_ms = statistics.mean(count_ms)
-    algo_bytes = n_occ * 64 + n_bases / 4 + reads.n_reads * 12
-    achieved = algo_bytes / (k1_ms * 1e-3) / 1e9
-    tpo, tsrc = k_count_traffic_per_occ()
-    roofline = {"kernel": "k_count", "bound": "hbm", "achieved": achieved, "peak": hbm,
+    info = g.info()
+    mean_ms = [statistics.mean(m[i] for m in phase_ms) for i in range(5)]
+    n_with_occ = int((reads.len >= K).sum())
+    if algo == swapgb.ALGO_DIRECT:
+        kname, k_ms = "k_count", mean_ms[2]
+        algo_bytes = n_occ * 64 + n_bases / 4 + reads.n_reads * 12
+        model = ("64 B per k-mer occurrence (one 32 B sector of the hash-table entry read + "
+                 "written back) + 0.25 B per base + 12 B per read")
+    else:
+        # the whole partitioned build: every kernel, DRAM bytes it cannot avoid
+        kname, k_ms = "partitioned build (all kernels)", mean_ms[4]
+        algo_bytes = (n_occ * 16 + 2 * (n_bases / 4 + reads.n_reads * 12) + survivors * 16)
+        model = ("8 B record written + read per k-mer occurrence, packed input read twice "
+                 "(0.25 B/base + 12 B/read each), 16 B per surviving k-molecule written; "
+                 "partition slices stay in L2")
+    achieved = algo_bytes / (k_ms * 1e-3) / 1e9
+    tpo, tsrc = k_count_traffic_per_occ() if algo == swapgb.ALGO_DIRECT else (None, None)
+    roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hbm,
                 "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src,
                 "traffic": (tpo * n_occ) if tpo else None, "traffic_source": tsrc,
-                "algorithmic_bytes": algo_bytes,
-                "bytes_model": "64 B per k-mer occurrence (one 32 B sector of the hash-table "
-                               "entry read + written back) + 0.25 B per base + 12 B per read",
-                "k_count_ms": k1_ms}
+                "algorithmic_bytes": algo_bytes, "bytes_model": model, "kernel_ms": k_ms}
     atomic = None
     if not args.no_probe and rank == 0:
         table_bytes = 16 << 30
         r_red = swapgb.probe_random_access("red_add_u32", table_bytes, 1 << 31, stream.cuda_stream)
         r_pat = swapgb.probe_random_access("load16_cas128", table_bytes, 1 << 30, stream.cuda_stream)
+        r_l2 = swapgb.probe_random_access("load16_cas128", 48 << 20, 1 << 30, stream.cuda_stream)
         # per read of length L: (L-k+1) key probes + 2(L-k) slot increments
-        ops = n_occ + 2 * (n_occ - int((reads.len >= K).sum()))
-        achieved_ops = ops / (k1_ms * 1e-3)
-        atomic = {"R_red_add_u32_per_s": r_red, "load16_cas128_per_s": r_pat,
-                  "table_bytes": table_bytes, "ops_per_step": ops,
-                  "achieved_ops_per_s": achieved_ops, "frac_of_R": achieved_ops / r_red,
-                  "occurrences_per_s": n_occ / (k1_ms * 1e-3),
-                  "frac_occ_vs_load16_cas128": (n_occ / (k1_ms * 1e-3)) / r_pat}
+        ops = n_occ + 2 * (n_occ - n_with_occ)
+        count_ms = mean_ms[2]
+        atomic = {"R_red_add_u32_per_s": r_red, "dram_load16_cas128_per_s": r_pat,
+                  "l2_load16_cas128_per_s": r_l2, "table_bytes": table_bytes,
+                  "ops_per_step": ops, "achieved_ops_per_s": ops / (mean_ms[4] * 1e-3),
+                  "frac_of_R": ops / (mean_ms[4] * 1e-3) / r_red,
+                  "occurrences_per_s_counting_phase": n_occ / (count_ms * 1e-3),
+                  "frac_counting_phase_vs_" + ("dram" if algo == swapgb.ALGO_DIRECT else "l2")
+                  + "_load16_cas128": (n_occ / (count_ms * 1e-3))
+                  / (r_pat if algo == swapgb.ALGO_DIRECT else r_l2)}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(text, n_bases)
@@ -343,11 +363,12 @@ def main() -> int:
             "metric": METRIC, "value": value, "unit": "bases/s", "n_gpus": world,
             "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-            "data": "synthetic (seeded generator, no dataset)", "config": config_dict(),
+            "data": "synthetic (seeded generator, no dataset)", "config": config_dict(args.algo, args.order),
             "e2e": {"value": aggregate_value(n_bases, world, e2e_s * 1e3), "unit": "bases/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": "swg_graph_build on pinned host packed reads + swg_graph_copy_out"},
             "gpu_launches": launches,
+            "build": dict(info, phase_ms_mean=mean_ms),
             "roofline": roofline,
             "random_access": atomic,
             "cpu_baseline": cpu,

@@ -62,13 +62,41 @@ typedef enum swg_status {
     SWG_ERR_NOT_READY = 10  /* server: result not finished yet */
 } swg_status;
 
+/* Counting algorithms (same results, different memory traffic). */
+#define SWG_ALGO_DEFAULT 0     /* direct */
+#define SWG_ALGO_DIRECT 1      /* one pass into a device-wide table in HBM */
+#define SWG_ALGO_PARTITIONED 2 /* hash-partitioned records, each partition counted in L2 */
+
+/* Order in which the direct algorithm counts the reads (same results). */
+#define SWG_ORDER_INPUT 0     /* input order (default) */
+#define SWG_ORDER_MINIMIZER 1 /* reads sharing a minimizer k-molecule counted together:
+                                 fewer DRAM misses, more CAS contention; slower on GB300 */
+
 typedef struct swg_opts {
     int k;                      /* 1..31; the CLI enforces the reference's odd 19..31 */
     int cutoff;                 /* -c: slot kept iff multiplicity >= cutoff */
     double load_factor;         /* target hash-table load, (0,0.9]; 0 selects 0.6 */
-    uint64_t expected_distinct; /* table sizing hint; 0 = estimate on the device */
+    uint64_t expected_distinct; /* direct algorithm: table sizing hint; 0 = estimate on the device */
     void *stream;               /* cudaStream_t; NULL = the library's own stream */
+    int algorithm;              /* SWG_ALGO_*; 0 = default */
+    int read_order;             /* direct: SWG_ORDER_*; 0 = input order */
 } swg_opts;
+
+/* What the last build did (for measurement and tests). */
+typedef struct swg_build_info {
+    int algorithm;        /* SWG_ALGO_DIRECT or SWG_ALGO_PARTITIONED */
+    int launches;         /* kernel launches of the build */
+    uint64_t occurrences; /* k-mer occurrences counted */
+    uint64_t distinct;    /* distinct k-molecules before the cutoff */
+    uint64_t survivors;   /* after the cutoff */
+    uint64_t table_entries; /* direct: table capacity; partitioned: entries per slice slot */
+    uint32_t partitions;  /* partitioned: number of partitions */
+    uint32_t slots;       /* partitioned: partitions counted at once (one wave) */
+    uint32_t waves;       /* partitioned: waves */
+    uint32_t retries;     /* rebuilds after a full table */
+    double estimate;      /* direct: distinct-count estimate used for sizing */
+    float ms[5];          /* as swg_graph_last_timings */
+} swg_build_info;
 
 typedef struct swg_reads swg_reads; /* host-side packed reads */
 typedef struct swg_graph swg_graph; /* device-resident filtered k-mer graph + workspace */
@@ -146,9 +174,12 @@ swg_status swg_records_write_kmer_graph(const uint64_t *keys, const uint8_t *mul
 swg_status swg_records_write_node_lines(const uint64_t *keys, const uint8_t *mult, uint64_t n,
                                         const char *path);
 /* Device times (ms) of the last build's phases, from CUDA events on the build
- * stream: [0] estimate, [1] table clear, [2] extract+count, [3] cutoff+compaction,
- * [4] whole build. Also the launch count of the last build. */
+ * stream: [0] sizing (occurrence prefix, tiles, distinct estimate or partition
+ * histogram), [1] preparation (table clear, or record scatter), [2] counting
+ * (K1, or every wave's partition count + compaction), [3] cutoff+compaction
+ * (direct only), [4] whole build. Also the launch count of the last build. */
 swg_status swg_graph_last_timings(const swg_graph *g, float ms[5], int *launches);
+swg_status swg_graph_build_info(const swg_graph *g, swg_build_info *info);
 
 /* ---- build without device allocation ------------------------------------ */
 /* No counterpart in the reference. For callers that must not have the library

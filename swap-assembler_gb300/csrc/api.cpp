@@ -68,6 +68,29 @@ struct swg_graph {
     uint64_t cap_used = 0;
     float ms[5] = {0, 0, 0, 0, 0};
     int launches = 0;
+    int algorithm = 0;
+    uint64_t occurrences = 0;
+    double estimate = 0;
+    uint32_t retries = 0;
+    // partitioned workspace
+    unsigned long long *d_part = nullptr;  // count[P] | start[P+1] | cursor[P]
+    uint64_t part_cap = 0;
+    unsigned long long *h_part = nullptr;  // pinned copy of start[P+1]
+    unsigned long long *d_records = nullptr;
+    uint64_t records_cap = 0;
+    Entry *d_slices = nullptr;
+    uint64_t slices_cap = 0;
+    uint32_t parts = 0, slots = 0, waves = 0;
+    uint64_t slot_cap = 0;
+    // read-order workspace
+    unsigned *d_minhash = nullptr;
+    uint64_t minhash_cap = 0;
+    unsigned *d_bucket = nullptr;
+    uint64_t bucket_cap = 0;
+    uint64_t *d_poff = nullptr;
+    uint64_t poff_cap = 0;
+    uint32_t *d_plen = nullptr;
+    uint64_t plen_cap = 0;
 };
 
 namespace {
@@ -108,6 +131,11 @@ swg_status check_opts(const swg_opts *o) {
         swg::set_error("k must be in 1..31");
         return SWG_ERR_BAD_INPUT;
     }
+    if (o->algorithm < 0 || o->algorithm > SWG_ALGO_PARTITIONED || o->read_order < 0 ||
+        o->read_order > SWG_ORDER_MINIMIZER) {
+        swg::set_error("unknown algorithm or read order");
+        return SWG_ERR_BAD_INPUT;
+    }
     if (o->load_factor < 0 || o->load_factor > 0.9) {
         swg::set_error("load_factor must be in (0, 0.9] (0 = default)");
         return SWG_ERR_BAD_INPUT;
@@ -118,6 +146,10 @@ swg_status check_opts(const swg_opts *o) {
 cudaStream_t stream_of(swg_graph *g, const swg_opts *o) {
     return o->stream ? (cudaStream_t)o->stream : g->own;
 }
+
+swg_status build_direct(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s, double load);
+swg_status build_partitioned(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s,
+                             double load);
 
 swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, uint64_t n_words,
                       const uint64_t *off, const uint32_t *len, uint64_t n_reads) {
@@ -168,12 +200,24 @@ swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, u
              "read occurrence total");
     SWG_CUDA(cudaStreamSynchronize(s), "occurrence scan");
     a.total_occ = g->h_ctl->occ_total;
+    g->occurrences = a.total_occ;
+    g->retries = 0;
+    g->estimate = 0;
     a.n_tiles = (a.total_occ + swg::kTileOcc - 1) / swg::kTileOcc;
     if ((st = ensure(&g->d_tiles, &g->tiles_cap, a.n_tiles, "tile table"))) return st;
     a.tile_first_read = g->d_tiles;
     g->launches += swg::launch_tiles(a, s);
     SWG_CUDA(cudaGetLastError(), "tile launch");
 
+    if (o->algorithm == SWG_ALGO_PARTITIONED) return build_partitioned(g, o, a, s, load);
+    return build_direct(g, o, a, s, load);
+}
+
+// One pass into a device-wide table in HBM: HyperLogLog sizing, clear, K1, K2.
+swg_status build_direct(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s,
+                        double load) {
+    swg_status st;
+    g->algorithm = SWG_ALGO_DIRECT;
     // table sizing: caller's hint, else a HyperLogLog estimate on the device
     double est;
     if (o->expected_distinct) {
@@ -181,9 +225,35 @@ swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, u
     } else if (a.total_occ == 0) {
         est = 0;
     } else {
+        est = -1;  // from the sketch below
+    }
+    // One pass computes the HyperLogLog registers and every read's minimizer;
+    // the reads are then counted in minimizer order (reads sharing a
+    // minimizer overlap, so their shared k-molecules hit entries already in L2).
+    const bool reorder = o->read_order == SWG_ORDER_MINIMIZER && a.total_occ > 0;
+    if (reorder) {
+        if ((st = ensure(&g->d_minhash, &g->minhash_cap, a.n_reads, "read minimizers"))) return st;
+        SWG_CUDA(cudaMemsetAsync(g->d_minhash, 0xff, a.n_reads * sizeof(unsigned), s), "clear minimizers");
+        SWG_CUDA(cudaMemsetAsync(g->d_hll, 0, sizeof(unsigned) << swg::kHllBits, s), "memset hll");
+        g->launches += swg::launch_sketch(a, g->d_minhash, s);
+        SWG_CUDA(cudaGetLastError(), "sketch launch");
+    } else if (est < 0) {
         SWG_CUDA(cudaMemsetAsync(g->d_hll, 0, sizeof(unsigned) << swg::kHllBits, s), "memset hll");
         g->launches += swg::launch_hll(a, s);
         SWG_CUDA(cudaGetLastError(), "hll launch");
+    }
+    if (reorder) {
+        if ((st = ensure(&g->d_bucket, &g->bucket_cap, swg::bucket_count(), "read buckets"))) return st;
+        if ((st = ensure(&g->d_poff, &g->poff_cap, a.n_reads, "ordered offsets"))) return st;
+        if ((st = ensure(&g->d_plen, &g->plen_cap, a.n_reads, "ordered lengths"))) return st;
+        g->launches += swg::launch_read_order(a, g->d_minhash, g->d_bucket, g->d_poff, g->d_plen, s);
+        a.read_off = g->d_poff;
+        a.read_len = g->d_plen;
+        g->launches += swg::launch_occ_scan(a, s);
+        g->launches += swg::launch_tiles(a, s);
+        SWG_CUDA(cudaGetLastError(), "read order launch");
+    }
+    if (est < 0) {
         SWG_CUDA(cudaMemcpyAsync(g->h_hll, g->d_hll, sizeof(unsigned) << swg::kHllBits,
                                  cudaMemcpyDeviceToHost, s),
                  "read hll");
@@ -191,6 +261,7 @@ swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, u
         est = swg::hll_estimate(g->h_hll) * 1.06;  // ~3.7 standard errors of margin
     }
     est = std::min(est, (double)a.total_occ);
+    g->estimate = est;
     uint64_t cap = (uint64_t)std::ceil(std::max(est, 1.0) / load) + 64;
     for (int attempt = 0; attempt < 6; ++attempt) {
         if ((st = ensure(&g->d_table, &g->table_cap, cap, "hash table"))) return st;
@@ -235,6 +306,7 @@ swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, u
             // can fill a table sized by the bound)
             const uint64_t bound = (uint64_t)std::ceil((double)a.total_occ / load) + 64;
             cap = cap < bound ? bound : cap * 2;
+            g->retries++;
             continue;
         }
         g->n_distinct = g->h_ctl->counters[0];
@@ -252,6 +324,118 @@ swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, u
     }
     swg::set_error("hash table still full after 6 enlargements");
     return SWG_ERR_TABLE_FULL;
+}
+
+// Hash-partitioned counting: every occurrence becomes an 8-byte record
+// {low bits of mix64(key), arc code}, scattered to the partition named by the
+// top bits; each partition is then counted in a table slice sized by its
+// record count (an upper bound on its distinct keys) that stays resident in
+// L2, several partitions (a wave) at a time, and compacted straight from L2.
+swg_status build_partitioned(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s,
+                             double load) {
+    swg_status st;
+    g->algorithm = SWG_ALGO_PARTITIONED;
+    // about 1M slice entries (16 MiB) per partition, 2^8..2^10 partitions
+    const double want = (double)a.total_occ / load / (double)(1u << 20);
+    int bits = swg::kPartBitsMin;
+    while (bits < swg::kPartBitsMax && (double)(1u << bits) < want) bits++;
+    swg::PartArgs pa;
+    std::memset(&pa, 0, sizeof(pa));
+    pa.bits = bits;
+    pa.n_parts = 1u << bits;
+    pa.load_num = 3;  // slice capacity = count / 0.6 + 16
+    pa.load_den = 5;
+    if (load != 0.6) {
+        pa.load_num = (int)std::lround(load * 1000.0);
+        pa.load_den = 1000;
+    }
+    const uint64_t P = pa.n_parts;
+    if ((st = ensure(&g->d_part, &g->part_cap, 3 * P + 1, "partition table"))) return st;
+    pa.part_count = g->d_part;
+    pa.part_start = g->d_part + P;
+    pa.part_cursor = g->d_part + 2 * P + 1;
+    SWG_CUDA(cudaMemsetAsync(pa.part_count, 0, P * sizeof(unsigned long long), s), "clear partitions");
+    g->launches += swg::launch_part_count(a, pa, s);
+    g->launches += swg::launch_part_prefix(pa, s);
+    SWG_CUDA(cudaGetLastError(), "partition count launch");
+    SWG_CUDA(cudaMemcpyAsync(g->h_part, pa.part_start, (P + 1) * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, s),
+             "read partition offsets");
+    SWG_CUDA(cudaEventRecord(g->ev[1], s), "event");
+    SWG_CUDA(cudaStreamSynchronize(s), "partition count");
+    const unsigned long long *start = g->h_part;
+    uint64_t max_count = 0;
+    for (uint64_t p = 0; p < P; p++) max_count = std::max<uint64_t>(max_count, start[p + 1] - start[p]);
+    const uint64_t chunk = 256 * 8;  // k_part_compact block chunk
+    uint64_t slot_cap = max_count * (uint64_t)pa.load_den / (uint64_t)pa.load_num + 16;
+    slot_cap = (slot_cap + chunk - 1) / chunk * chunk;
+    int dev = g->device, l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev);
+    const double budget = 0.55 * (double)(l2 > 0 ? l2 : (126 << 20));
+    uint64_t slots = (uint64_t)(budget / (double)(slot_cap * sizeof(Entry)));
+    slots = std::max<uint64_t>(1, std::min<uint64_t>(slots, std::min<uint64_t>(P, 64)));
+    pa.slot_cap = slot_cap;
+    pa.n_slots = (uint32_t)slots;
+    if ((st = ensure(&g->d_slices, &g->slices_cap, slots * slot_cap, "partition slices"))) return st;
+    if ((st = ensure(&g->d_records, &g->records_cap, std::max<uint64_t>(a.total_occ, 1),
+                     "partition records")))
+        return st;
+    const uint64_t out_want = std::max<uint64_t>(a.total_occ, 1);
+    if (g->out_cap < out_want || !g->d_out_keys || !g->d_out_mult) {
+        cudaFree(g->d_out_keys);
+        cudaFree(g->d_out_mult);
+        g->d_out_keys = g->d_out_mult = nullptr;
+        g->out_cap = 0;
+        SWG_CUDA(cudaMalloc(&g->d_out_keys, out_want * 8), "output keys");
+        SWG_CUDA(cudaMalloc(&g->d_out_mult, out_want * 8), "output multiplicities");
+        g->out_cap = out_want;
+    }
+    pa.slices = g->d_slices;
+    pa.records = g->d_records;
+    a.out_keys = g->d_out_keys;
+    a.out_mult = g->d_out_mult;
+    a.out_cap = out_want;
+    SWG_CUDA(cudaMemsetAsync(g->d_slices, 0, slots * slot_cap * sizeof(Entry), s), "clear slices");
+    g->launches += swg::launch_part_scatter(a, pa, s);
+    SWG_CUDA(cudaGetLastError(), "scatter launch");
+    SWG_CUDA(cudaEventRecord(g->ev[2], s), "event");
+    uint32_t waves = 0;
+    for (uint64_t p0 = 0; p0 < P; p0 += slots) {
+        const uint32_t n = (uint32_t)std::min<uint64_t>(slots, P - p0);
+        g->launches += swg::launch_part_wave(a, pa, (uint32_t)p0, n, start[p0], start[p0 + n], s);
+        waves++;
+    }
+    SWG_CUDA(cudaGetLastError(), "wave launch");
+    SWG_CUDA(cudaEventRecord(g->ev[3], s), "event");
+    SWG_CUDA(cudaEventRecord(g->ev[4], s), "event");
+    SWG_CUDA(cudaMemcpyAsync(g->h_ctl, g->d_ctl, sizeof(Control) - sizeof(uint64_t),
+                             cudaMemcpyDeviceToHost, s),
+             "read status");
+    SWG_CUDA(cudaStreamSynchronize(s), "build");
+    const unsigned status = g->h_ctl->status;
+    if (status & swg::kStatusCasLimit) {
+        swg::set_error("a bounded CAS retry loop gave up on the device");
+        return SWG_ERR_TIMEOUT;
+    }
+    if (status & swg::kStatusTableFull) {
+        swg::set_error("a partition slice reached the probe limit");
+        return SWG_ERR_TABLE_FULL;
+    }
+    g->parts = (uint32_t)P;
+    g->slots = (uint32_t)slots;
+    g->waves = waves;
+    g->slot_cap = slot_cap;
+    g->cap_used = slot_cap;
+    g->n_distinct = g->h_ctl->counters[0];
+    g->n_out = g->h_ctl->counters[1];
+    g->built = true;
+    float t[5] = {0, 0, 0, 0, 0};
+    cudaEventElapsedTime(&t[0], g->ev[0], g->ev[1]);
+    cudaEventElapsedTime(&t[1], g->ev[1], g->ev[2]);
+    cudaEventElapsedTime(&t[2], g->ev[2], g->ev[3]);
+    cudaEventElapsedTime(&t[4], g->ev[0], g->ev[4]);
+    std::memcpy(g->ms, t, sizeof(t));
+    return SWG_OK;
 }
 
 swg_status fetch_sorted(const swg_graph *g, std::vector<uint64_t> &keys,
@@ -316,6 +500,8 @@ swg_status swg_graph_create(swg_graph **out) {
     if (e == cudaSuccess) e = cudaMalloc(&g->d_ctl, sizeof(Control));
     if (e == cudaSuccess) e = cudaMallocHost(&g->h_ctl, sizeof(Control));
     if (e == cudaSuccess) e = cudaMallocHost(&g->h_hll, sizeof(unsigned) << swg::kHllBits);
+    if (e == cudaSuccess)
+        e = cudaMallocHost(&g->h_part, sizeof(unsigned long long) * ((1u << swg::kPartBitsMax) + 1));
     if (e != cudaSuccess) {
         swg_status st = cuda_fail(e, "graph create");
         swg_graph_free(g);
@@ -340,6 +526,14 @@ void swg_graph_free(swg_graph *g) {
     cudaFree(g->d_out_mult);
     cudaFree(g->d_hll);
     cudaFree(g->d_ctl);
+    cudaFree(g->d_part);
+    cudaFree(g->d_minhash);
+    cudaFree(g->d_bucket);
+    cudaFree(g->d_poff);
+    cudaFree(g->d_plen);
+    cudaFree(g->d_records);
+    cudaFree(g->d_slices);
+    if (g->h_part) cudaFreeHost(g->h_part);
     if (g->h_ctl) cudaFreeHost(g->h_ctl);
     if (g->h_hll) cudaFreeHost(g->h_hll);
     for (auto &e : g->ev)
@@ -537,6 +731,25 @@ swg_status swg_graph_last_timings(const swg_graph *g, float ms[5], int *launches
     if (!g->built) return SWG_ERR_BAD_STATE;
     if (ms) std::memcpy(ms, g->ms, sizeof(g->ms));
     if (launches) *launches = g->launches;
+    return SWG_OK;
+}
+
+swg_status swg_graph_build_info(const swg_graph *g, swg_build_info *info) {
+    if (!g || !info) return SWG_ERR_BAD_INPUT;
+    if (!g->built) return SWG_ERR_BAD_STATE;
+    std::memset(info, 0, sizeof(*info));
+    info->algorithm = g->algorithm;
+    info->launches = g->launches;
+    info->occurrences = g->occurrences;
+    info->distinct = g->n_distinct;
+    info->survivors = g->n_out;
+    info->table_entries = g->cap_used;
+    info->partitions = g->algorithm == SWG_ALGO_PARTITIONED ? g->parts : 0;
+    info->slots = g->algorithm == SWG_ALGO_PARTITIONED ? g->slots : 0;
+    info->waves = g->algorithm == SWG_ALGO_PARTITIONED ? g->waves : 0;
+    info->retries = g->retries;
+    info->estimate = g->estimate;
+    std::memcpy(info->ms, g->ms, sizeof(g->ms));
     return SWG_OK;
 }
 

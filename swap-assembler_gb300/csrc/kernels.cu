@@ -293,7 +293,7 @@ __device__ __forceinline__ TileView load_tile(const BuildArgs &a, uint64_t t, Ti
 // Read holding occurrence i, with its prefix, offset and length.
 __device__ __forceinline__ void find_read(const BuildArgs &a, const TileView &v,
                                           const TileSmem &s, uint64_t i, uint64_t &pre,
-                                          uint64_t &off, uint32_t &len) {
+                                          uint64_t &off, uint32_t &len, uint64_t &ridx) {
     if (v.in_smem) {
         uint64_t lo = 0, hi = v.nr;  // last j with pre[j] <= i
         while (hi - lo > 1) {
@@ -304,6 +304,7 @@ __device__ __forceinline__ void find_read(const BuildArgs &a, const TileView &v,
         pre = s.pre[lo];
         off = s.off[lo];
         len = s.len[lo];
+        ridx = v.r0 + lo;
     } else {
         uint64_t lo = v.r0, hi = v.r0 + v.nr;
         while (hi - lo > 1) {
@@ -314,6 +315,7 @@ __device__ __forceinline__ void find_read(const BuildArgs &a, const TileView &v,
         pre = a.occ_prefix[lo];
         off = a.read_off[lo];
         len = a.read_len[lo];
+        ridx = lo;
     }
 }
 
@@ -323,9 +325,9 @@ __device__ __forceinline__ void find_read(const BuildArgs &a, const TileView &v,
 // (f ? 0 : 4) + base[j+k]; left arc (j >= 1) -> slot (f ? 4 : 0) + 3 - base[j-1].
 __device__ __forceinline__ void make_occ(const BuildArgs &a, const TileView &v, const TileSmem &s,
                                          uint64_t i, uint64_t &key, uint64_t &inc) {
-    uint64_t pre, off;
+    uint64_t pre, off, ridx;
     uint32_t len;
-    find_read(a, v, s, i, pre, off, len);
+    find_read(a, v, s, i, pre, off, len, ridx);
     const int k = a.k;
     const uint64_t p = i - pre, g = off + p;
     const uint64_t win = window32(a.packed, a.n_words, g);
@@ -344,8 +346,76 @@ __device__ __forceinline__ void make_occ(const BuildArgs &a, const TileView &v, 
     }
 }
 
+// Rolling walk over the occurrences [i0, i1) of a tile: one read lookup and
+// one window extraction where a read starts, then one base rolled in per
+// occurrence. Calls fn(key, code) with the canonical k-molecule and its arc
+// code: bits 0-2 right slot, bit 3 right arc present, bits 4-6 left slot,
+// bit 7 left arc present (slots as in make_occ), and the read's index.
+template <typename F>
+__device__ __forceinline__ void walk_run(const BuildArgs &a, const TileView &v, const TileSmem &s,
+                                         uint64_t i0, uint64_t i1, F &&fn) {
+    const int k = a.k;
+    const uint64_t kmask = (1ull << (2 * k)) - 1;
+    const int top = 2 * (k - 1);
+    uint64_t fwd = 0, rc = 0, last = 0, g = 0, p = 0, ridx = 0;
+    uint32_t len = 0, rb = 0;
+    for (uint64_t i = i0; i < i1; ++i) {
+        uint32_t lb;
+        bool has_l;
+        if (i == i0 || i > last) {
+            uint64_t pre, off;
+            find_read(a, v, s, i, pre, off, len, ridx);
+            p = i - pre;
+            g = off + p;
+            last = pre + (len - (uint32_t)k);
+            const uint64_t win = window32(a.packed, a.n_words, g);
+            fwd = win >> (64 - 2 * k);
+            rc = revcomp_dev(fwd, k);
+            rb = (uint32_t)(win >> (62 - 2 * k)) & 3u;  // base g+k (used only if inside the read)
+            has_l = p >= 1;
+            lb = has_l ? base_at(a.packed, a.n_words, g - 1) : 0u;
+        } else {
+            lb = (uint32_t)(fwd >> top) & 3u;  // first base of the previous k-mer
+            has_l = true;
+            ++g;
+            ++p;
+            fwd = ((fwd << 2) | rb) & kmask;
+            rc = (rc >> 2) | ((uint64_t)(3u - rb) << top);
+            rb = (p + (uint64_t)k < len) ? base_at(a.packed, a.n_words, g + (uint64_t)k) : 0u;
+        }
+        const bool has_r = p + (uint64_t)k < len;
+        const bool f = fwd >= rc;
+        unsigned code = 0;
+        if (has_r) code |= 0x08u | ((f ? 0u : 4u) + rb);
+        if (has_l) code |= 0x80u | (((f ? 4u : 0u) + 3u - lb) << 4);
+        fn(f ? fwd : rc, code, ridx);
+    }
+}
+
+__device__ __forceinline__ uint64_t code_inc(unsigned code) {
+    uint64_t inc = 0;
+    if (code & 0x08u) inc += 1ull << (8 * (code & 7u));
+    if (code & 0x80u) inc += 1ull << (8 * ((code >> 4) & 7u));
+    return inc;
+}
+
+// Inverse of mix64 (each xor-shift by 33 is its own inverse on 64 bits; the
+// multipliers are the inverses of mix64's modulo 2^64).
+__device__ __forceinline__ uint64_t unmix64(uint64_t x) {
+    x ^= x >> 33;
+    x *= 0x9cb4b2f8129337dbull;
+    x ^= x >> 33;
+    x *= 0x4f74430c22a54005ull;
+    x ^= x >> 33;
+    return x;
+}
+
 // ---------------------------------------------------------------------
-// HyperLogLog over the canonical keys (persistent over tiles).
+// HyperLogLog over the canonical keys (persistent over tiles). Each thread
+// takes a run of kK1Items consecutive occurrences of the tile: one read lookup
+// and one window extraction at the start of the run (and at every read
+// boundary inside it), then the k-mer and its reverse complement are rolled
+// one base at a time.
 __global__ void __launch_bounds__(kK1Block) k_hll(BuildArgs a) {
     __shared__ TileSmem s;
     __shared__ unsigned regs[1 << kHllBits];
@@ -356,19 +426,97 @@ __global__ void __launch_bounds__(kK1Block) k_hll(BuildArgs a) {
         __syncthreads();
         const uint64_t A = t * kTileOcc;
         const uint64_t B = umin64(A + kTileOcc, a.total_occ);
-        for (uint64_t i = A + threadIdx.x; i < B; i += blockDim.x) {
-            uint64_t key, inc;
-            make_occ(a, v, s, i, key, inc);
+        const uint64_t i0 = A + (uint64_t)threadIdx.x * kK1Items;
+        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B), [&](uint64_t key, unsigned, uint64_t) {
             const uint64_t h = mix64(key ^ 0x9e3779b97f4a7c15ull);
             const unsigned idx = (unsigned)(h >> (64 - kHllBits));
             const uint64_t rest = (h << kHllBits) | (1ull << (kHllBits - 1));
             const unsigned rank = (unsigned)__clzll(rest) + 1;
             if (rank > regs[idx]) atomicMax(&regs[idx], rank);
-        }
+        });
     }
     __syncthreads();
     for (int j = threadIdx.x; j < (1 << kHllBits); j += blockDim.x)
         if (regs[j]) atomicMax(&a.hll[j], regs[j]);
+}
+
+// HyperLogLog of the canonical keys fused with each read's minimizer: the
+// smallest 32-bit hash over the read's canonical k-molecules. Reads that share
+// a minimizer overlap in the genome, so counting them one after another keeps
+// their common k-molecules' table entries in L2.
+__global__ void __launch_bounds__(kK1Block) k_sketch(BuildArgs a, unsigned *minhash) {
+    __shared__ TileSmem s;
+    __shared__ unsigned regs[1 << kHllBits];
+    for (int j = threadIdx.x; j < (1 << kHllBits); j += blockDim.x) regs[j] = 0;
+    for (uint64_t t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
+        __syncthreads();
+        const TileView v = load_tile(a, t, s);
+        __syncthreads();
+        const uint64_t A = t * kTileOcc;
+        const uint64_t B = umin64(A + kTileOcc, a.total_occ);
+        const uint64_t i0 = A + (uint64_t)threadIdx.x * kK1Items;
+        uint64_t cur = ~0ull;
+        unsigned best = 0xffffffffu;
+        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B), [&](uint64_t key, unsigned, uint64_t r) {
+            const uint64_t h = mix64(key ^ 0x9e3779b97f4a7c15ull);
+            const unsigned idx = (unsigned)(h >> (64 - kHllBits));
+            const uint64_t rest = (h << kHllBits) | (1ull << (kHllBits - 1));
+            const unsigned rank = (unsigned)__clzll(rest) + 1;
+            if (rank > regs[idx]) atomicMax(&regs[idx], rank);
+            if (r != cur) {
+                if (cur != ~0ull) atomicMin(&minhash[cur], best);
+                cur = r;
+                best = 0xffffffffu;
+            }
+            const unsigned mh = (unsigned)(mix64(key) >> 32);
+            best = mh < best ? mh : best;
+        });
+        if (cur != ~0ull) atomicMin(&minhash[cur], best);
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < (1 << kHllBits); j += blockDim.x)
+        if (regs[j]) atomicMax(&a.hll[j], regs[j]);
+}
+
+// Counting sort of the reads into 2^16 buckets by the top bits of their
+// minimizer (reads with equal minimizers end up next to each other).
+constexpr int kBucketBits = 16;
+
+__global__ void k_bucket_hist(const unsigned *__restrict__ minhash, uint64_t n,
+                              unsigned *__restrict__ hist) {
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+         r += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(&hist[minhash[r] >> (32 - kBucketBits)], 1u);
+}
+
+__global__ void __launch_bounds__(1024) k_bucket_scan(unsigned *hist) {
+    __shared__ uint64_t wb[32];
+    constexpr int per = (1 << kBucketBits) / 1024;
+    unsigned v[per];
+    uint64_t sum = 0;
+#pragma unroll
+    for (int x = 0; x < per; ++x) {
+        v[x] = hist[threadIdx.x * per + x];
+        sum += v[x];
+    }
+    uint64_t run = block_exclusive_scan<1024>(sum, wb, nullptr);
+#pragma unroll
+    for (int x = 0; x < per; ++x) {
+        hist[threadIdx.x * per + x] = (unsigned)run;
+        run += v[x];
+    }
+}
+
+__global__ void k_bucket_scatter(const unsigned *__restrict__ minhash, uint64_t n,
+                                 unsigned *__restrict__ cursor, const uint64_t *__restrict__ off,
+                                 const uint32_t *__restrict__ len, uint64_t *__restrict__ out_off,
+                                 uint32_t *__restrict__ out_len) {
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
+         r += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned pos = atomicAdd(&cursor[minhash[r] >> (32 - kBucketBits)], 1u);
+        out_off[pos] = off[r];
+        out_len[pos] = len[r];
+    }
 }
 
 // ---------------------------------------------------------------------
@@ -471,6 +619,225 @@ __global__ void __launch_bounds__(kCBlock) k_compact(BuildArgs a) {
 }
 
 // ---------------------------------------------------------------------
+// Partitioned build. A record is {the low 64-bits bits of h = mix64(key),
+// shifted left by 8 | arc code}; the partition is the top `bits` bits of h,
+// so h (a bijection of the key) is whole again in the partition's pass.
+constexpr int kMaxSlots = 64;
+constexpr int kPartChunk = kCBlock * kCItems;  // slot capacities are multiples of this
+
+__device__ __forceinline__ uint64_t slice_cap_of(const PartArgs &pa, unsigned long long count) {
+    const uint64_t c = count * (uint64_t)pa.load_den / (uint64_t)pa.load_num + 16;
+    return c < pa.slot_cap ? c : pa.slot_cap;
+}
+
+// Phase A: records per partition.
+__global__ void __launch_bounds__(kK1Block) k_part_count(BuildArgs a, PartArgs pa) {
+    __shared__ TileSmem s;
+    __shared__ unsigned hist[1 << kPartBitsMax];
+    for (uint32_t j = threadIdx.x; j < pa.n_parts; j += blockDim.x) hist[j] = 0;
+    const int shift = 64 - pa.bits;
+    for (uint64_t t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
+        __syncthreads();
+        const TileView v = load_tile(a, t, s);
+        __syncthreads();
+        const uint64_t A = t * kTileOcc;
+        const uint64_t B = umin64(A + kTileOcc, a.total_occ);
+        const uint64_t i0 = A + (uint64_t)threadIdx.x * kK1Items;
+        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B), [&](uint64_t key, unsigned, uint64_t) {
+            atomicAdd(&hist[mix64(key) >> shift], 1u);
+        });
+    }
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < pa.n_parts; j += blockDim.x)
+        if (hist[j]) atomicAdd(&pa.part_count[j], (unsigned long long)hist[j]);
+}
+
+// Exclusive prefix over the partitions (n_parts <= 1024, one block).
+__global__ void __launch_bounds__(1024) k_part_prefix(PartArgs pa) {
+    __shared__ uint64_t wb[32];
+    const uint32_t j = threadIdx.x;
+    const uint64_t c = j < pa.n_parts ? pa.part_count[j] : 0;
+    uint64_t total;
+    const uint64_t ex = block_exclusive_scan<1024>(c, wb, &total);
+    if (j < pa.n_parts) {
+        pa.part_start[j] = ex;
+        pa.part_cursor[j] = ex;
+    }
+    if (j == 0) pa.part_start[pa.n_parts] = total;
+}
+
+// Phase B: scatter the records, grouped by partition inside each tile so
+// that every warp writes runs of consecutive records.
+constexpr size_t kScatterDynSmem = kTileOcc * (sizeof(unsigned long long) + 2 * sizeof(unsigned short));
+
+__global__ void __launch_bounds__(kK1Block) k_part_scatter(BuildArgs a, PartArgs pa) {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    unsigned long long *rec = reinterpret_cast<unsigned long long *>(dyn);
+    unsigned short *pid = reinterpret_cast<unsigned short *>(rec + kTileOcc);
+    unsigned short *perm = pid + kTileOcc;
+    __shared__ TileSmem s;
+    __shared__ unsigned hist[1 << kPartBitsMax];
+    __shared__ unsigned loff[1 << kPartBitsMax];
+    __shared__ unsigned long long gbase[1 << kPartBitsMax];
+    __shared__ uint64_t wb[kK1Block / 32];
+    const int shift = 64 - pa.bits;
+    const uint64_t lowmask = (1ull << shift) - 1;
+    const uint32_t per = (pa.n_parts + kK1Block - 1) / kK1Block;  // partitions per thread
+    for (uint64_t t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < pa.n_parts; j += blockDim.x) hist[j] = 0;
+        const TileView v = load_tile(a, t, s);
+        __syncthreads();
+        const uint64_t A = t * kTileOcc;
+        const uint64_t B = umin64(A + kTileOcc, a.total_occ);
+        const uint32_t n = (uint32_t)(B - A);
+        uint32_t q = threadIdx.x * kK1Items;
+        const uint64_t i0 = A + q;
+        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B), [&](uint64_t key, unsigned code, uint64_t) {
+            const uint64_t h = mix64(key);
+            const unsigned part = (unsigned)(h >> shift);
+            rec[q] = ((h & lowmask) << 8) | code;
+            pid[q] = (unsigned short)part;
+            atomicAdd(&hist[part], 1u);
+            ++q;
+        });
+        __syncthreads();
+        // local offsets of the partitions inside the tile, and their global runs
+        uint64_t mine = 0;
+        for (uint32_t x = 0; x < per; ++x) {
+            const uint32_t j = threadIdx.x * per + x;
+            if (j < pa.n_parts) mine += hist[j];
+        }
+        uint64_t run = block_exclusive_scan<kK1Block>(mine, wb, nullptr);
+        for (uint32_t x = 0; x < per; ++x) {
+            const uint32_t j = threadIdx.x * per + x;
+            if (j < pa.n_parts) {
+                const unsigned c = hist[j];
+                loff[j] = (unsigned)run;
+                run += c;
+                gbase[j] = c ? atomicAdd(&pa.part_cursor[j], (unsigned long long)c) : 0;
+                hist[j] = 0;
+            }
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            const unsigned part = pid[i];
+            perm[loff[part] + atomicAdd(&hist[part], 1u)] = (unsigned short)i;
+        }
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+            const unsigned i = perm[j];
+            const unsigned part = pid[i];
+            pa.records[gbase[part] + (j - loff[part])] = rec[i];
+        }
+    }
+}
+
+// Phase C: count the records of partitions [p0, p0+n) into their slices.
+__global__ void __launch_bounds__(kK1Block) k_part_insert(BuildArgs a, PartArgs pa, uint32_t p0,
+                                                          uint32_t n, uint64_t rb, uint64_t re) {
+    __shared__ unsigned long long st[kMaxSlots + 1];
+    for (uint32_t j = threadIdx.x; j <= n; j += blockDim.x) st[j] = pa.part_start[p0 + j];
+    __syncthreads();
+    const int shift = 64 - pa.bits;
+    const int lane = threadIdx.x & 31;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = rb + (uint64_t)blockIdx.x * blockDim.x; base < re; base += stride) {
+        const uint64_t r = base + threadIdx.x;
+        const bool valid = r < re;
+        const unsigned vmask = __ballot_sync(kFull, valid);
+        if (!valid) continue;
+        uint32_t lo = 0, hi = n;  // last slot j with st[j] <= r
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (st[mid] <= r) lo = mid;
+            else hi = mid;
+        }
+        const unsigned long long rec = pa.records[r];
+        const uint64_t h = ((uint64_t)(p0 + lo) << shift) | (rec >> 8);
+        uint64_t inc = code_inc((unsigned)rec & 0xffu);
+        const unsigned peers = __match_any_sync(vmask, h);
+        if (__any_sync(vmask, peers != (1u << lane))) {
+            uint64_t tot = 0;
+#pragma unroll
+            for (int sl = 0; sl < 8; ++sl) {
+                const unsigned b = __ballot_sync(vmask, (unsigned)(inc >> (8 * sl)) & 1u);
+                tot |= (uint64_t)__popc(b & peers) << (8 * sl);
+            }
+            inc = tot;
+        }
+        if (lane == __ffs(peers) - 1)
+            insert_or_update(pa.slices + (uint64_t)lo * pa.slot_cap,
+                             slice_cap_of(pa, st[lo + 1] - st[lo]), h, inc, a.status);
+    }
+}
+
+// Phase D: cutoff + compaction of the slices of partitions [p0, p0+n); every
+// used entry is zeroed for the next wave. One block per chunk of a slot.
+__global__ void __launch_bounds__(kCBlock) k_part_compact(BuildArgs a, PartArgs pa, uint32_t p0) {
+    __shared__ uint64_t wb[kCBlock / 32];
+    __shared__ unsigned long long s_base;
+    const uint64_t chunks_per_slot = pa.slot_cap / kPartChunk;
+    const uint32_t j = (uint32_t)(blockIdx.x / chunks_per_slot);
+    const uint64_t chunk = (blockIdx.x % chunks_per_slot) * (uint64_t)kPartChunk;
+    const uint64_t cap = slice_cap_of(pa, pa.part_count[p0 + j]);
+    Entry *slice = pa.slices + (uint64_t)j * pa.slot_cap;
+    const int c = a.cutoff;
+    const uint32_t thr = c <= 0 ? 0u : (c >= 256 ? 0u : (uint32_t)c * 0x01010101u);
+    const bool all_cut = c >= 256;
+    uint64_t keys[kCItems], cnts[kCItems];
+    unsigned keep = 0;
+    int nkeep = 0, nused = 0;
+#pragma unroll
+    for (int it = 0; it < kCItems; ++it) {
+        const uint64_t idx = chunk + (uint64_t)it * kCBlock + threadIdx.x;
+        keys[it] = 0;
+        cnts[it] = 0;
+        if (idx < cap) {
+            Entry *e = slice + idx;
+            const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(e);
+            if (v.x != 0) {
+                uint64_t w = v.y;
+                if (thr) {
+                    const uint32_t lo = (uint32_t)w & __vcmpgeu4((uint32_t)w, thr);
+                    const uint32_t hi = (uint32_t)(w >> 32) & __vcmpgeu4((uint32_t)(w >> 32), thr);
+                    w = ((uint64_t)hi << 32) | lo;
+                }
+                if (all_cut) w = 0;
+                *reinterpret_cast<ulonglong2 *>(e) = make_ulonglong2(0ull, 0ull);
+                nused++;
+                if (w != 0) {
+                    keys[it] = unmix64(v.x);
+                    cnts[it] = w;
+                    keep |= 1u << it;
+                    nkeep++;
+                }
+            }
+        }
+    }
+    uint64_t total;
+    const uint64_t ex = block_exclusive_scan<kCBlock>((uint64_t)nkeep, wb, &total);
+    uint64_t used;
+    block_exclusive_scan<kCBlock>((uint64_t)nused, wb, &used);
+    if (threadIdx.x == 0) {
+        s_base = total ? atomicAdd(&a.counters[1], (unsigned long long)total) : 0;
+        if (used) atomicAdd(&a.counters[0], (unsigned long long)used);
+    }
+    __syncthreads();
+    uint64_t pos = s_base + ex;
+#pragma unroll
+    for (int it = 0; it < kCItems; ++it) {
+        if (keep & (1u << it)) {
+            if (pos < a.out_cap) {
+                a.out_keys[pos] = keys[it];
+                a.out_mult[pos] = cnts[it];
+            }
+            pos++;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
 // Random-access probe (roofline denominator).
 __global__ void __launch_bounds__(256) k_probe(int kind, Entry *table, uint64_t n16,
                                                uint64_t ops_per_thread, uint64_t seed,
@@ -536,7 +903,7 @@ int launch_tiles(const BuildArgs &a, cudaStream_t s) {
 
 int launch_hll(const BuildArgs &a, cudaStream_t s) {
     if (a.n_tiles == 0) return 0;
-    const uint64_t grid = std::min<uint64_t>(a.n_tiles, (uint64_t)device_sm_count() * 4);
+    const uint64_t grid = std::min<uint64_t>(a.n_tiles, (uint64_t)device_sm_count() * 8);
     k_hll<<<(unsigned)grid, kK1Block, 0, s>>>(a);
     return 1;
 }
@@ -556,6 +923,27 @@ double hll_estimate(const unsigned *regs) {
     return e;
 }
 
+int launch_sketch(const BuildArgs &a, unsigned *minhash, cudaStream_t s) {
+    if (a.n_tiles == 0) return 0;
+    const uint64_t grid = std::min<uint64_t>(a.n_tiles, (uint64_t)device_sm_count() * 8);
+    k_sketch<<<(unsigned)grid, kK1Block, 0, s>>>(a, minhash);
+    return 1;
+}
+
+uint64_t bucket_count() { return 1ull << kBucketBits; }
+
+int launch_read_order(const BuildArgs &a, const unsigned *minhash, unsigned *hist,
+                      uint64_t *out_off, uint32_t *out_len, cudaStream_t s) {
+    if (a.n_reads == 0) return 0;
+    const uint64_t grid = std::min<uint64_t>((a.n_reads + 255) / 256, (uint64_t)device_sm_count() * 8);
+    cudaMemsetAsync(hist, 0, sizeof(unsigned) << kBucketBits, s);
+    k_bucket_hist<<<(unsigned)grid, 256, 0, s>>>(minhash, a.n_reads, hist);
+    k_bucket_scan<<<1, 1024, 0, s>>>(hist);
+    k_bucket_scatter<<<(unsigned)grid, 256, 0, s>>>(minhash, a.n_reads, hist, a.read_off,
+                                                    a.read_len, out_off, out_len);
+    return 3;
+}
+
 int launch_count(const BuildArgs &a, cudaStream_t s) {
     if (a.n_tiles == 0) return 0;
     k_count<<<(unsigned)a.n_tiles, kK1Block, 0, s>>>(a);
@@ -568,6 +956,44 @@ int launch_compact(const BuildArgs &a, cudaStream_t s) {
     if (grid == 0) return 0;
     k_compact<<<(unsigned)grid, kCBlock, 0, s>>>(a);
     return 1;
+}
+
+int launch_part_count(const BuildArgs &a, const PartArgs &p, cudaStream_t s) {
+    if (a.n_tiles == 0) return 0;
+    const uint64_t grid = std::min<uint64_t>(a.n_tiles, (uint64_t)device_sm_count() * 8);
+    k_part_count<<<(unsigned)grid, kK1Block, 0, s>>>(a, p);
+    return 1;
+}
+
+int launch_part_prefix(const PartArgs &p, cudaStream_t s) {
+    k_part_prefix<<<1, 1024, 0, s>>>(p);
+    return 1;
+}
+
+int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s) {
+    if (a.n_tiles == 0) return 0;
+    cudaFuncSetAttribute(k_part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kScatterDynSmem);
+    const uint64_t grid = std::min<uint64_t>(a.n_tiles, (uint64_t)device_sm_count() * 3);
+    k_part_scatter<<<(unsigned)grid, kK1Block, kScatterDynSmem, s>>>(a, p);
+    return 1;
+}
+
+int launch_part_wave(const BuildArgs &a, const PartArgs &p, uint32_t p0, uint32_t n, uint64_t rb,
+                     uint64_t re, cudaStream_t s) {
+    int launches = 0;
+    if (re > rb) {
+        const uint64_t blocks = (re - rb + kK1Block - 1) / kK1Block;
+        const uint64_t grid = std::min<uint64_t>(blocks, (uint64_t)device_sm_count() * 8);
+        k_part_insert<<<(unsigned)grid, kK1Block, 0, s>>>(a, p, p0, n, rb, re);
+        launches++;
+    }
+    const uint64_t grid = (uint64_t)n * (p.slot_cap / kPartChunk);
+    if (grid) {
+        k_part_compact<<<(unsigned)grid, kCBlock, 0, s>>>(a, p, p0);
+        launches++;
+    }
+    return launches;
 }
 
 cudaError_t run_probe(int kind, uint64_t table_bytes, uint64_t n_ops, cudaStream_t s, float *ms) {

@@ -55,14 +55,42 @@ struct BuildArgs {
     uint64_t out_cap;
 };
 
+// Partitioned build: records {hash low bits, arc code} scattered by the top
+// bits of mix64(key) into n_parts partitions, each counted in a table slice
+// small enough to stay in L2, a wave of n_slots partitions at a time.
+constexpr int kPartBitsMin = 8;
+constexpr int kPartBitsMax = 10;
+
+struct PartArgs {
+    int bits;                          // log2(n_parts)
+    uint32_t n_parts;
+    unsigned long long *part_count;    // [n_parts] records per partition
+    unsigned long long *part_start;    // [n_parts + 1] exclusive prefix
+    unsigned long long *part_cursor;   // [n_parts] scatter cursors
+    unsigned long long *records;       // [total_occ]
+    Entry *slices;                     // [n_slots * slot_cap]
+    uint64_t slot_cap;
+    uint32_t n_slots;
+    int load_num, load_den;            // slice capacity = count * den / num + 16
+};
+
 // Kernel launchers (kernels.cu). Each returns the number of launches made.
 int launch_occ_scan(const BuildArgs &a, cudaStream_t s);
 uint64_t scan_block_count(uint64_t n_reads);
 int launch_tiles(const BuildArgs &a, cudaStream_t s);
 int launch_hll(const BuildArgs &a, cudaStream_t s);
 double hll_estimate(const unsigned *regs_host);
+int launch_sketch(const BuildArgs &a, unsigned *minhash, cudaStream_t s);
+uint64_t bucket_count();
+int launch_read_order(const BuildArgs &a, const unsigned *minhash, unsigned *hist,
+                      uint64_t *out_off, uint32_t *out_len, cudaStream_t s);
 int launch_count(const BuildArgs &a, cudaStream_t s);
 int launch_compact(const BuildArgs &a, cudaStream_t s);
+int launch_part_count(const BuildArgs &a, const PartArgs &p, cudaStream_t s);
+int launch_part_prefix(const PartArgs &p, cudaStream_t s);
+int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s);
+int launch_part_wave(const BuildArgs &a, const PartArgs &p, uint32_t p0, uint32_t n,
+                     uint64_t rec_begin, uint64_t rec_end, cudaStream_t s);
 cudaError_t run_probe(int kind, uint64_t table_bytes, uint64_t n_ops, cudaStream_t s, float *ms);
 int device_sm_count();
 

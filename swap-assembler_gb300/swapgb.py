@@ -34,13 +34,33 @@ class SwgError(RuntimeError):
         self.status = status
 
 
+ALGO_DEFAULT, ALGO_DIRECT, ALGO_PARTITIONED = 0, 1, 2
+ORDER_INPUT, ORDER_MINIMIZER = 0, 1
+
+
 class Opts(C.Structure):
     _fields_ = [("k", C.c_int), ("cutoff", C.c_int), ("load_factor", C.c_double),
-                ("expected_distinct", C.c_uint64), ("stream", C.c_void_p)]
+                ("expected_distinct", C.c_uint64), ("stream", C.c_void_p),
+                ("algorithm", C.c_int), ("read_order", C.c_int)]
 
     def __init__(self, k: int = 23, cutoff: int = 5, load_factor: float = 0.0,
-                 expected_distinct: int = 0, stream: int | None = None):
-        super().__init__(k, cutoff, load_factor, expected_distinct, stream)
+                 expected_distinct: int = 0, stream: int | None = None, algorithm: int = 0,
+                 read_order: int = 0):
+        super().__init__(k, cutoff, load_factor, expected_distinct, stream, algorithm,
+                         read_order)
+
+
+class BuildInfo(C.Structure):
+    _fields_ = [("algorithm", C.c_int), ("launches", C.c_int), ("occurrences", C.c_uint64),
+                ("distinct", C.c_uint64), ("survivors", C.c_uint64),
+                ("table_entries", C.c_uint64), ("partitions", C.c_uint32),
+                ("slots", C.c_uint32), ("waves", C.c_uint32), ("retries", C.c_uint32),
+                ("estimate", C.c_double), ("ms", C.c_float * 5)]
+
+    def as_dict(self) -> dict:
+        d = {name: getattr(self, name) for name, _ in self._fields_ if name != "ms"}
+        d["ms"] = list(self.ms)
+        return d
 
 
 _lib = None
@@ -80,6 +100,7 @@ def lib() -> C.CDLL:
             "swg_records_write_kmer_graph": (i32, [P, P, u64, i32, C.c_char_p]),
             "swg_records_write_node_lines": (i32, [P, P, u64, C.c_char_p]),
             "swg_graph_last_timings": (i32, [P, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
+            "swg_graph_build_info": (i32, [P, C.POINTER(BuildInfo)]),
             "swg_probe_random_access": (i32, [i32, u64, u64, P, C.POINTER(C.c_double)]),
         }
         for name, (res, args) in sigs.items():
@@ -219,6 +240,11 @@ class Graph:
     def write_node_lines(self, path: str) -> None:
         _check(lib().swg_graph_write_node_lines(self._h, str(path).encode()),
                "swg_graph_write_node_lines")
+
+    def info(self) -> dict:
+        bi = BuildInfo()
+        _check(lib().swg_graph_build_info(self._h, C.byref(bi)), "swg_graph_build_info")
+        return bi.as_dict()
 
     def timings(self) -> tuple[list[float], int]:
         ms = (C.c_float * 5)()

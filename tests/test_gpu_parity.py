@@ -28,10 +28,20 @@ def assert_same_records(g: swapgb.Graph, text: bytes, k: int, c: int) -> None:
         keys[bad[0]], mult[bad[0]].tolist(), omult[bad[0]].tolist())
 
 
+# (algorithm, read order): direct in input order (the default), direct in
+# minimizer order, partitioned
+ALGOS = [pytest.param(dict(algorithm=swapgb.ALGO_DIRECT), id="direct"),
+         pytest.param(dict(algorithm=swapgb.ALGO_DIRECT, read_order=swapgb.ORDER_MINIMIZER),
+                      id="direct-minimizer-order"),
+         pytest.param(dict(algorithm=swapgb.ALGO_PARTITIONED), id="partitioned")]
+
+
+@pytest.mark.parametrize("algo", ALGOS)
 @pytest.mark.parametrize("case", [c["name"] for c in golden()["kat"]])
-def test_kat_matches_reference(case, tmp_path):
+def test_kat_matches_reference(case, algo, tmp_path):
     c = kat(case)
-    g = gpu_build(kat_text(case), c["k"], c["c"])
+    g = gpu_build(kat_text(case), c["k"], c["c"], **algo)
+    assert g.info()["algorithm"] == algo["algorithm"]
     g.write_kmer_graph(tmp_path / "kg.txt")
     g.write_node_lines(tmp_path / "nodes.txt")
     assert sha_lines(sorted_lines(tmp_path / "kg.txt")) == c["kmer_graph_sha256"]
@@ -42,11 +52,12 @@ def test_kat_matches_reference(case, tmp_path):
         assert st[0] == c["totals"]["recvNodeNum"] and st[1] == c["totals"]["recvEdgeNum"]
 
 
+@pytest.mark.parametrize("algo", ALGOS)
 @pytest.mark.parametrize("case", [c["name"] for c in golden()["synth"]])
-def test_synthetic_matches_reference(case, tmp_path):
+def test_synthetic_matches_reference(case, algo, tmp_path):
     c = synth_case(case)
     text = synth_case_text(case)
-    g = gpu_build(text, c["k"], c["c"])
+    g = gpu_build(text, c["k"], c["c"], **algo)
     assert g.size() == c["n_nodes"]
     g.write_node_lines(tmp_path / "nodes.txt")
     assert sha_lines(sorted_lines(tmp_path / "nodes.txt")) == c["nodes_sha256"]
@@ -56,51 +67,68 @@ def test_synthetic_matches_reference(case, tmp_path):
 
 @pytest.mark.parametrize("k,c", [(19, 0), (21, 1), (23, 2), (27, 3), (29, 4), (31, 5), (31, -3),
                                  (9, 2), (15, 1), (20, 2), (1, 1), (2, 0)])
-def test_k_and_cutoff_sweep(k, c):
+@pytest.mark.parametrize("algo", ALGOS)
+def test_k_and_cutoff_sweep(k, c, algo):
     text = synth_case_text("c2_small")
-    g = gpu_build(text, k, c)
+    g = gpu_build(text, k, c, **algo)
     assert_same_records(g, text, k, c)
 
 
-def test_repeats_and_tandems():
+@pytest.mark.parametrize("algo", ALGOS)
+def test_repeats_and_tandems(algo):
     text = swapgb.synth_fasta(seed=21, genome_len=300000, repeat_frac=0.05, tandem_frac=0.02,
                               n_reads=60000, read_len=150, sub_rate=0.005)
-    g = gpu_build(text, 31, 3)
+    g = gpu_build(text, 31, 3, **algo)
     assert_same_records(g, text, 31, 3)
 
 
-def test_hot_keys_saturate():
+@pytest.mark.parametrize("algo", ALGOS)
+def test_hot_keys_saturate(algo):
     # one k-mer hit millions of times inside single warps: poly-A and short
     # tandem units; counts must saturate at exactly 255
     reads = ["A" * 250, "AC" * 125, "ACG" * 83, "T" * 200, "ACGTT" * 50] * 4000
     text = "".join(">h%d\n%s\n" % (i, r) for i, r in enumerate(reads)).encode()
     for c in (0, 2, 255):
-        g = gpu_build(text, 21, c)
+        g = gpu_build(text, 21, c, **algo)
         assert_same_records(g, text, 21, c)
         _, mult = g.copy_out()
         assert mult.max() == 255
 
 
+def test_partitioned_multi_wave_and_larger_input():
+    # enough occurrences for more partitions than one wave holds
+    text = swapgb.synth_fasta(seed=23, genome_len=2_000_000, n_reads=1_000_000, read_len=100,
+                              sub_rate=0.01, indel_rate=0.001)
+    g = gpu_build(text, 31, 5, algorithm=swapgb.ALGO_PARTITIONED)
+    info = g.info()
+    assert info["waves"] > 1 and info["partitions"] >= 256
+    assert_same_records(g, text, 31, 5)
+    assert info["occurrences"] == 70_000_000
+
+
 def test_table_full_retry():
     # a sizing hint far too small forces the device-side full detection and
-    # the host's rebuild with a larger table
+    # the host's rebuild with a larger table (direct algorithm)
     text = synth_case_text("c1_small")
-    g = gpu_build(text, 21, 2, expected_distinct=10)
+    g = gpu_build(text, 21, 2, expected_distinct=10, algorithm=swapgb.ALGO_DIRECT)
     assert_same_records(g, text, 21, 2)
+    assert g.info()["retries"] >= 1
 
 
-def test_high_load_factor():
+@pytest.mark.parametrize("algo", ALGOS)
+def test_high_load_factor(algo):
     text = synth_case_text("c2_small")
-    g = gpu_build(text, 31, 5, load_factor=0.9)
+    g = gpu_build(text, 31, 5, load_factor=0.9, **algo)
     assert_same_records(g, text, 31, 5)
 
 
-def test_empty_and_short_inputs():
+@pytest.mark.parametrize("algo", ALGOS)
+def test_empty_and_short_inputs(algo):
     text = b">a\nACGT\n>b\nAC\n"  # every read shorter than k
-    g = gpu_build(text, 19, 0)
+    g = gpu_build(text, 19, 0, **algo)
     assert g.size() == 0 and g.distinct() == 0
     text = b">a\nACGTACGTACGTACGTACGTA\n"  # L == k: one key, all-zero mask, dropped
-    g = gpu_build(text, 21, 0)
+    g = gpu_build(text, 21, 0, **algo)
     assert g.size() == 0 and g.distinct() == 1
 
 
@@ -109,13 +137,16 @@ def test_device_input_path_and_handle_reuse():
     text1 = synth_case_text("c2_small")
     text2 = synth_case_text("c4_ragged")
     g = swapgb.Graph()
-    for text, k, c in ((text1, 31, 5), (text2, 27, 3), (text1, 31, 5)):
+    for text, k, c, algo, order in ((text1, 31, 5, 2, 0), (text2, 27, 3, 1, 1),
+                                    (text1, 31, 5, 1, 0), (text2, 27, 3, 2, 0),
+                                    (text1, 31, 5, 1, 1)):
         r = swapgb.reads_from_fasta(text, k)
         p = torch.from_numpy(r.packed.view(np.int32).copy()).cuda()
         o = torch.from_numpy(r.off.view(np.int64).copy()).cuda()
         ln = torch.from_numpy(r.len.view(np.int32).copy()).cuda()
         torch.cuda.synchronize()
-        g.build_device(swapgb.Opts(k=k, cutoff=c), p.data_ptr(), p.numel(), o.data_ptr(),
+        g.build_device(swapgb.Opts(k=k, cutoff=c, algorithm=algo, read_order=order),
+                       p.data_ptr(), p.numel(), o.data_ptr(),
                        ln.data_ptr(), o.numel())
         assert_same_records(g, text, k, c)
         ms, launches = g.timings()
