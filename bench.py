@@ -46,6 +46,7 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-probe", action="store_true", help="skip the random-access probe")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-samples measurement")
     ap.add_argument("--algo", default="direct", choices=["direct", "partitioned"])
     ap.add_argument("--order", default="input", choices=["input", "minimizer"],
                     help="read order of the direct algorithm")
@@ -156,6 +157,66 @@ def cpu_baseline(text: bytes, n_bases: int, budget_s: float = 20.0) -> dict:
     return {"value": nb / dt, "unit": "bases/s", "cores": threads, "kind": "port",
             "sample": "first %d of %d bases (framing + count + cutoff, sorted records), %.1f s"
                       % (nb, n_bases, dt)}
+
+
+def batched_samples(n: int = 256, seed: int = 4) -> list[dict]:
+    """The batched workload: genome sizes log-uniform 50 kbp-2 Mbp, read length
+    from {75, 100, 150, 250}, coverage uniform 10-60x, substitutions uniform
+    0.1-1%, k=27, c=3 for every sample."""
+    import math
+    import random
+    rng = random.Random(seed)
+    out = []
+    for i in range(n):
+        g = int(math.exp(rng.uniform(math.log(50_000), math.log(2_000_000))))
+        L = rng.choice([75, 100, 150, 250])
+        cov = rng.uniform(10, 60)
+        out.append(dict(seed=10_000 + i, genome_len=g, n_reads=int(cov * g / L), read_len=L,
+                        sub_rate=rng.uniform(0.001, 0.01)))
+    return out
+
+
+def batched_metrics(stream_ptr: int, repeats: int = 3) -> dict:
+    """Samples/s of one batched build over all samples vs one plain build per
+    sample, both from host packed reads to device-resident results."""
+    import numpy as np
+    import torch
+    import swapgb
+    specs = batched_samples()
+    reads = [swapgb.reads_from_fasta(swapgb.synth_fasta(**p), 27) for p in specs]
+    bases = sum(r.n_bases for r in reads)
+    opts = swapgb.Opts(k=27, cutoff=3, stream=stream_ptr)
+    plain, batch = swapgb.Graph(), swapgb.Graph()
+    samples = [(r, 27, 3) for r in reads]
+    batch.build_batch(opts, samples)  # warm-up (allocations)
+    for r in reads:
+        plain.build_reads(opts, r)
+    torch.cuda.synchronize()
+    t_plain, t_batch = [], []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        for r in reads:
+            plain.build_reads(opts, r)
+        torch.cuda.synchronize()
+        t_plain.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        batch.build_batch(opts, samples)
+        torch.cuda.synchronize()
+        t_batch.append(time.perf_counter() - t0)
+    # spot check: the last sample of the batch equals its plain build
+    kp, mp = plain.copy_out(sorted=True)
+    kb, mb = batch.batch_copy_out(len(reads) - 1)
+    same = bool(np.array_equal(kp, kb) and np.array_equal(mp, mb))
+    tp, tb = min(t_plain), min(t_batch)
+    return {"workload": "256 samples, genome log-uniform 50 kbp-2 Mbp, reads 75/100/150/250 bp, "
+                        "10-60x, 0.1-1% subs, k=27 c=3 (seeded synthetic)",
+            "samples": len(reads), "bases": bases,
+            "plain_s": tp, "batched_s": tb,
+            "plain_samples_per_s": len(reads) / tp, "batched_samples_per_s": len(reads) / tb,
+            "batched_bases_per_s": bases / tb, "speedup": tp / tb,
+            "last_sample_identical": same,
+            "path": "host packed reads -> device-resident graphs; plain = swg_graph_build per "
+                    "sample, batched = one swg_batch_build"}
 
 
 def run_reference_arm(args) -> int:
@@ -354,6 +415,9 @@ def main() -> int:
                   "frac_counting_phase_vs_" + ("dram" if algo == swapgb.ALGO_DIRECT else "l2")
                   + "_load16_cas128": (n_occ / (count_ms * 1e-3))
                   / (r_pat if algo == swapgb.ALGO_DIRECT else r_l2)}
+    batched = None
+    if rank == 0 and not args.no_batch and not args.reads:
+        batched = batched_metrics(stream.cuda_stream)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(text, n_bases)
@@ -371,6 +435,7 @@ def main() -> int:
             "build": dict(info, phase_ms_mean=mean_ms),
             "roofline": roofline,
             "random_access": atomic,
+            "batched": batched,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "kmers_per_s": world * n_occ / (ms_per_step * 1e-3),

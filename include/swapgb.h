@@ -146,7 +146,38 @@ swg_status swg_build(const swg_opts *o, const uint32_t *packed, uint64_t n_words
 /* Convenience: frame + pack a FASTA held in host memory, then build. */
 swg_status swg_build_fasta(const swg_opts *o, const char *text, uint64_t len, swg_graph **out);
 
+/* ---- batched build ---------------------------------------------------- */
+/* One sample of a batch: its packed reads in HOST memory (layout as above,
+ * offsets relative to its own packed words) and its own k and cutoff. */
+typedef struct swg_sample {
+    const uint32_t *packed;
+    uint64_t n_words;
+    const uint64_t *read_off;
+    const uint32_t *read_len;
+    uint64_t n_reads;
+    int k;
+    int cutoff;
+} swg_sample;
+
+/* Build many independent samples at once: their reads are copied into one
+ * device stream, every kernel runs once over all samples, each sample counts
+ * into its own partition of one shared table and gets its own output region.
+ * Each sample's result equals a plain build of that sample alone. Uses the
+ * direct algorithm; opts->k and opts->cutoff are ignored (per sample). */
+swg_status swg_batch_build(swg_graph *g, const swg_opts *o, const swg_sample *samples,
+                           uint32_t n_samples);
+swg_status swg_batch_samples(const swg_graph *g, uint32_t *n_samples);
+/* Per-sample results of the last batched build (sample s < n_samples). */
+swg_status swg_batch_sample_info(const swg_graph *g, uint32_t s, uint64_t *occurrences,
+                                 uint64_t *distinct, uint64_t *survivors);
+swg_status swg_batch_device_view(const swg_graph *g, uint32_t s, const uint64_t **d_keys,
+                                 const uint64_t **d_mult, uint64_t *n);
+swg_status swg_batch_copy_out(const swg_graph *g, uint32_t s, uint64_t *keys, uint8_t *mult,
+                              uint64_t cap, int sorted, uint64_t *n);
+
 /* ---- results ---------------------------------------------------------- */
+/* The swg_graph_* result calls below refer to a single-sample build
+ * (SWG_ERR_BAD_STATE after a batched build; use swg_batch_* there). */
 /* Number of surviving k-molecules (after the cutoff). */
 swg_status swg_graph_size(const swg_graph *g, uint64_t *n);
 /* Distinct k-molecules before the cutoff (all keys ever inserted). */

@@ -91,6 +91,23 @@ struct swg_graph {
     uint64_t poff_cap = 0;
     uint32_t *d_plen = nullptr;
     uint64_t plen_cap = 0;
+    // batched build (n_samples == 0 after a single-sample build)
+    uint32_t n_samples = 0;
+    std::vector<uint64_t> s_tbase, s_tcap, s_out, s_distinct, s_occ;
+    swg::SegParams *d_segs = nullptr;
+    uint64_t segs_cap = 0;
+    uint32_t *d_read_seg = nullptr;
+    uint64_t read_seg_cap = 0;
+    unsigned long long *d_seg_counts = nullptr;
+    uint64_t seg_counts_cap = 0;
+    unsigned *d_seg_status = nullptr;
+    uint64_t seg_status_cap = 0;
+    uint64_t *d_seg_meta = nullptr;  // read start [S+1] | offset shift [S] | occurrence prefix [S+1]
+    uint64_t seg_meta_cap = 0;
+    double *d_est = nullptr;
+    uint64_t est_cap = 0;
+    unsigned *d_hll_seg = nullptr;
+    uint64_t hll_seg_cap = 0;
 };
 
 namespace {
@@ -119,6 +136,20 @@ swg_status ensure(T **p, uint64_t *cap, uint64_t want, const char *what) {
         return cuda_fail(e, what);
     }
     *cap = n;
+    return SWG_OK;
+}
+
+// Device read offsets and lengths (host-input builds), grown together.
+swg_status ensure_reads(swg_graph *g, uint64_t n_reads) {
+    if (g->reads_cap >= n_reads && g->d_off && g->d_len) return SWG_OK;
+    cudaFree(g->d_off);
+    cudaFree(g->d_len);
+    g->d_off = nullptr;
+    g->d_len = nullptr;
+    g->reads_cap = 0;
+    SWG_CUDA(cudaMalloc(&g->d_off, std::max<uint64_t>(n_reads, 1) * 8), "read offsets");
+    SWG_CUDA(cudaMalloc(&g->d_len, std::max<uint64_t>(n_reads, 1) * 4), "read lengths");
+    g->reads_cap = std::max<uint64_t>(n_reads, 1);
     return SWG_OK;
 }
 
@@ -166,6 +197,7 @@ swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, u
     SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
     cudaStream_t s = stream_of(g, o);
     g->built = false;
+    g->n_samples = 0;
     g->k = o->k;
     g->cutoff = o->cutoff;
     g->launches = 0;
@@ -438,10 +470,234 @@ swg_status build_partitioned(swg_graph *g, const swg_opts *o, BuildArgs &a, cuda
     return SWG_OK;
 }
 
+// ---------------------------------------------------------------------
+// Batched build: all samples are segments of one build (direct algorithm).
+swg_status batch_impl(swg_graph *g, const swg_opts *o, const swg_sample *sm, uint32_t S) {
+    if (!o || !sm || S == 0) {
+        swg::set_error("batch: no samples");
+        return SWG_ERR_BAD_INPUT;
+    }
+    if (o->load_factor < 0 || o->load_factor > 0.9) {
+        swg::set_error("load_factor must be in (0, 0.9] (0 = default)");
+        return SWG_ERR_BAD_INPUT;
+    }
+    uint64_t W = 0, R = 0;
+    std::vector<uint64_t> meta(3 * (uint64_t)S + 2, 0);  // read start [S+1] | shift [S] | prefix [S+1]
+    for (uint32_t i = 0; i < S; i++) {
+        if (sm[i].k < 1 || sm[i].k > 31) {
+            swg::set_error("batch: sample k must be in 1..31");
+            return SWG_ERR_BAD_INPUT;
+        }
+        if (sm[i].n_reads && (!sm[i].packed || !sm[i].read_off || !sm[i].read_len)) {
+            swg::set_error("batch: NULL read buffer");
+            return SWG_ERR_BAD_INPUT;
+        }
+        meta[i] = R;
+        meta[S + 1 + i] = W * 16;  // base offset of the sample's words in the stream
+        R += sm[i].n_reads;
+        W += sm[i].n_words;
+    }
+    meta[S] = R;
+    if (R >= 0xffffffffull) {
+        swg::set_error("at most 2^32-2 reads per build");
+        return SWG_ERR_BAD_INPUT;
+    }
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    cudaStream_t s = stream_of(g, o);
+    const double load = o->load_factor > 0 ? o->load_factor : 0.6;
+    g->built = false;
+    g->launches = 0;
+    g->retries = 0;
+    g->algorithm = SWG_ALGO_DIRECT;
+    swg_status st;
+    if ((st = ensure(&g->d_packed, &g->packed_cap, std::max<uint64_t>(W, 1), "packed reads"))) return st;
+    if ((st = ensure_reads(g, R))) return st;
+    if ((st = ensure(&g->d_read_seg, &g->read_seg_cap, std::max<uint64_t>(R, 1), "read samples")))
+        return st;
+    if ((st = ensure(&g->d_segs, &g->segs_cap, S, "sample table"))) return st;
+    if ((st = ensure(&g->d_seg_counts, &g->seg_counts_cap, 2ull * S, "sample counters"))) return st;
+    if ((st = ensure(&g->d_seg_status, &g->seg_status_cap, S, "sample status"))) return st;
+    if ((st = ensure(&g->d_seg_meta, &g->seg_meta_cap, meta.size(), "sample metadata"))) return st;
+    if ((st = ensure(&g->d_est, &g->est_cap, S, "sample estimates"))) return st;
+    if ((st = ensure(&g->d_hll_seg, &g->hll_seg_cap, (uint64_t)S << swg::kHllBits, "sample sketches")))
+        return st;
+    if ((st = ensure(&g->d_prefix, &g->prefix_cap, R + 1, "occurrence prefix"))) return st;
+    if ((st = ensure(&g->d_scan, &g->scan_cap, swg::scan_block_count(R) + 1, "scan scratch"))) return st;
+
+    SWG_CUDA(cudaEventRecord(g->ev[0], s), "event");
+    uint64_t wofs = 0, rofs = 0;
+    for (uint32_t i = 0; i < S; i++) {
+        if (sm[i].n_words)
+            SWG_CUDA(cudaMemcpyAsync(g->d_packed + wofs, sm[i].packed, sm[i].n_words * 4,
+                                     cudaMemcpyHostToDevice, s), "copy packed reads");
+        if (sm[i].n_reads) {
+            SWG_CUDA(cudaMemcpyAsync(g->d_off + rofs, sm[i].read_off, sm[i].n_reads * 8,
+                                     cudaMemcpyHostToDevice, s), "copy read offsets");
+            SWG_CUDA(cudaMemcpyAsync(g->d_len + rofs, sm[i].read_len, sm[i].n_reads * 4,
+                                     cudaMemcpyHostToDevice, s), "copy read lengths");
+        }
+        wofs += sm[i].n_words;
+        rofs += sm[i].n_reads;
+    }
+    std::vector<swg::SegParams> segs(S);
+    for (uint32_t i = 0; i < S; i++) {
+        segs[i].k = sm[i].k;
+        segs[i].cutoff = sm[i].cutoff;
+        segs[i].tbase = 0;
+        segs[i].tcap = 0;
+    }
+    SWG_CUDA(cudaMemcpyAsync(g->d_seg_meta, meta.data(), (2 * (uint64_t)S + 1) * 8,
+                             cudaMemcpyHostToDevice, s), "copy sample metadata");
+    SWG_CUDA(cudaMemcpyAsync(g->d_segs, segs.data(), S * sizeof(swg::SegParams),
+                             cudaMemcpyHostToDevice, s), "copy sample table");
+    BuildArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.packed = g->d_packed;
+    a.n_words = W;
+    a.read_off = g->d_off;
+    a.read_len = g->d_len;
+    a.n_reads = R;
+    a.k = sm[0].k;
+    a.occ_prefix = g->d_prefix;
+    a.scan_blocks = g->d_scan;
+    a.status = &g->d_ctl->status;
+    a.counters = g->d_ctl->counters;
+    a.read_seg = g->d_read_seg;
+    a.segs = g->d_segs;
+    a.n_segs = S;
+    a.seg_counts = g->d_seg_counts;
+    a.seg_status = g->d_seg_status;
+    a.hll = g->d_hll_seg;
+    g->launches += swg::launch_seg_setup(a, g->d_seg_meta, g->d_seg_meta + S + 1, g->d_read_seg,
+                                         g->d_off, s);
+    SWG_CUDA(cudaMemsetAsync(g->d_prefix, 0, sizeof(uint64_t), s), "memset prefix");
+    g->launches += swg::launch_occ_scan(a, s);
+    g->launches += swg::launch_gather_prefix(g->d_prefix, g->d_seg_meta, S + 1,
+                                             g->d_seg_meta + 2 * (uint64_t)S + 1, s);
+    SWG_CUDA(cudaGetLastError(), "batch setup launch");
+    SWG_CUDA(cudaMemcpyAsync(meta.data() + 2 * S + 1, g->d_seg_meta + 2 * (uint64_t)S + 1,
+                             (S + 1) * 8, cudaMemcpyDeviceToHost, s), "read sample occurrences");
+    SWG_CUDA(cudaStreamSynchronize(s), "batch occurrence scan");
+    const uint64_t *occ_pre = meta.data() + 2 * S + 1;
+    a.total_occ = occ_pre[S];
+    g->occurrences = a.total_occ;
+    a.n_tiles = (a.total_occ + swg::kTileOcc - 1) / swg::kTileOcc;
+    if ((st = ensure(&g->d_tiles, &g->tiles_cap, a.n_tiles, "tile table"))) return st;
+    a.tile_first_read = g->d_tiles;
+    g->launches += swg::launch_tiles(a, s);
+    std::vector<double> est(S, 0.0);
+    if (a.total_occ) {
+        SWG_CUDA(cudaMemsetAsync(g->d_hll_seg, 0, ((uint64_t)S << swg::kHllBits) * 4, s), "memset sketches");
+        g->launches += swg::launch_hll(a, s);
+        g->launches += swg::launch_hll_estimates(g->d_hll_seg, S, g->d_est, s);
+        SWG_CUDA(cudaGetLastError(), "sketch launch");
+        SWG_CUDA(cudaMemcpyAsync(est.data(), g->d_est, S * sizeof(double), cudaMemcpyDeviceToHost, s),
+                 "read estimates");
+        SWG_CUDA(cudaStreamSynchronize(s), "batch sketch");
+    }
+    SWG_CUDA(cudaEventRecord(g->ev[1], s), "event");
+    std::vector<uint64_t> cap(S);
+    for (uint32_t i = 0; i < S; i++) {
+        const double occ = (double)(occ_pre[i + 1] - occ_pre[i]);
+        const double e = std::min(est[i] * 1.06, occ);
+        cap[i] = (uint64_t)std::ceil(std::max(e, 1.0) / load) + 64;
+    }
+    const uint64_t chunk = 256 * 8;  // k_compact chunk: sample regions start on it
+    g->s_occ.assign(S, 0);
+    for (uint32_t i = 0; i < S; i++) g->s_occ[i] = occ_pre[i + 1] - occ_pre[i];
+    for (int attempt = 0; attempt < 6; ++attempt) {
+        uint64_t total = 0;
+        for (uint32_t i = 0; i < S; i++) {
+            segs[i].tbase = total;
+            segs[i].tcap = cap[i];
+            total += (cap[i] + chunk - 1) / chunk * chunk;
+        }
+        if ((st = ensure(&g->d_table, &g->table_cap, total, "hash table"))) return st;
+        if (g->out_cap < total || !g->d_out_keys || !g->d_out_mult) {
+            cudaFree(g->d_out_keys);
+            cudaFree(g->d_out_mult);
+            g->d_out_keys = g->d_out_mult = nullptr;
+            g->out_cap = 0;
+            SWG_CUDA(cudaMalloc(&g->d_out_keys, total * 8), "output keys");
+            SWG_CUDA(cudaMalloc(&g->d_out_mult, total * 8), "output multiplicities");
+            g->out_cap = total;
+        }
+        SWG_CUDA(cudaMemcpyAsync(g->d_segs, segs.data(), S * sizeof(swg::SegParams),
+                                 cudaMemcpyHostToDevice, s), "copy sample table");
+        a.table = g->d_table;
+        a.cap = total;
+        a.out_keys = g->d_out_keys;
+        a.out_mult = g->d_out_mult;
+        a.out_cap = total;
+        SWG_CUDA(cudaMemsetAsync(g->d_table, 0, total * sizeof(Entry), s), "clear table");
+        SWG_CUDA(cudaMemsetAsync(g->d_seg_counts, 0, 2ull * S * 8, s), "clear counters");
+        SWG_CUDA(cudaMemsetAsync(g->d_seg_status, 0, S * 4, s), "clear status");
+        SWG_CUDA(cudaEventRecord(g->ev[2], s), "event");
+        g->launches += swg::launch_count(a, s);
+        SWG_CUDA(cudaEventRecord(g->ev[3], s), "event");
+        g->launches += swg::launch_compact(a, s);
+        SWG_CUDA(cudaGetLastError(), "batch count launch");
+        SWG_CUDA(cudaEventRecord(g->ev[4], s), "event");
+        std::vector<unsigned long long> counts(2 * (uint64_t)S);
+        std::vector<unsigned> status(S);
+        SWG_CUDA(cudaMemcpyAsync(counts.data(), g->d_seg_counts, counts.size() * 8,
+                                 cudaMemcpyDeviceToHost, s), "read counters");
+        SWG_CUDA(cudaMemcpyAsync(status.data(), g->d_seg_status, S * 4, cudaMemcpyDeviceToHost, s),
+                 "read status");
+        SWG_CUDA(cudaStreamSynchronize(s), "batch build");
+        bool again = false;
+        for (uint32_t i = 0; i < S; i++) {
+            if (status[i] & swg::kStatusCasLimit) {
+                swg::set_error("a bounded CAS retry loop gave up on the device");
+                return SWG_ERR_TIMEOUT;
+            }
+            if (status[i] & swg::kStatusTableFull) {
+                const uint64_t bound = (uint64_t)std::ceil((double)g->s_occ[i] / load) + 64;
+                cap[i] = cap[i] < bound ? bound : cap[i] * 2;
+                again = true;
+            }
+        }
+        if (again) {
+            g->retries++;
+            continue;
+        }
+        g->n_samples = S;
+        g->s_tbase.resize(S);
+        g->s_tcap.resize(S);
+        g->s_out.resize(S);
+        g->s_distinct.resize(S);
+        for (uint32_t i = 0; i < S; i++) {
+            g->s_tbase[i] = segs[i].tbase;
+            g->s_tcap[i] = segs[i].tcap;
+            g->s_distinct[i] = counts[2 * i];
+            g->s_out[i] = counts[2 * i + 1];
+        }
+        g->n_distinct = 0;
+        g->n_out = 0;
+        for (uint32_t i = 0; i < S; i++) {
+            g->n_distinct += g->s_distinct[i];
+            g->n_out += g->s_out[i];
+        }
+        g->cap_used = total;
+        g->built = true;
+        float t[5] = {0, 0, 0, 0, 0};
+        cudaEventElapsedTime(&t[0], g->ev[0], g->ev[1]);
+        cudaEventElapsedTime(&t[1], g->ev[1], g->ev[2]);
+        cudaEventElapsedTime(&t[2], g->ev[2], g->ev[3]);
+        cudaEventElapsedTime(&t[3], g->ev[3], g->ev[4]);
+        cudaEventElapsedTime(&t[4], g->ev[0], g->ev[4]);
+        std::memcpy(g->ms, t, sizeof(t));
+        return SWG_OK;
+    }
+    swg::set_error("hash table still full after 6 enlargements");
+    return SWG_ERR_TABLE_FULL;
+}
+
 swg_status fetch_sorted(const swg_graph *g, std::vector<uint64_t> &keys,
                         std::vector<uint64_t> &mult) {
-    if (!g || !g->built) {
-        swg::set_error("graph has not been built");
+    if (!g || !g->built || g->n_samples) {
+        swg::set_error(g && g->n_samples ? "batched build: use the swg_batch_* calls"
+                                         : "graph has not been built");
         return SWG_ERR_BAD_STATE;
     }
     keys.resize(g->n_out);
@@ -528,6 +784,13 @@ void swg_graph_free(swg_graph *g) {
     cudaFree(g->d_ctl);
     cudaFree(g->d_part);
     cudaFree(g->d_minhash);
+    cudaFree(g->d_segs);
+    cudaFree(g->d_read_seg);
+    cudaFree(g->d_seg_counts);
+    cudaFree(g->d_seg_status);
+    cudaFree(g->d_seg_meta);
+    cudaFree(g->d_est);
+    cudaFree(g->d_hll_seg);
     cudaFree(g->d_bucket);
     cudaFree(g->d_poff);
     cudaFree(g->d_plen);
@@ -562,16 +825,7 @@ swg_status swg_graph_build(swg_graph *g, const swg_opts *o, const uint32_t *pack
     SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
     cudaStream_t s = stream_of(g, o);
     if ((st = ensure(&g->d_packed, &g->packed_cap, n_words, "packed reads"))) return st;
-    if (g->reads_cap < n_reads || !g->d_off || !g->d_len) {
-        cudaFree(g->d_off);
-        cudaFree(g->d_len);
-        g->d_off = nullptr;
-        g->d_len = nullptr;
-        g->reads_cap = 0;
-        SWG_CUDA(cudaMalloc(&g->d_off, std::max<uint64_t>(n_reads, 1) * 8), "read offsets");
-        SWG_CUDA(cudaMalloc(&g->d_len, std::max<uint64_t>(n_reads, 1) * 4), "read lengths");
-        g->reads_cap = std::max<uint64_t>(n_reads, 1);
-    }
+    if ((st = ensure_reads(g, n_reads))) return st;
     if (n_words)
         SWG_CUDA(cudaMemcpyAsync(g->d_packed, packed, n_words * 4, cudaMemcpyHostToDevice, s),
                  "copy packed reads");
@@ -621,14 +875,14 @@ swg_status swg_build_fasta(const swg_opts *o, const char *text, uint64_t len, sw
 
 swg_status swg_graph_size(const swg_graph *g, uint64_t *n) {
     if (!g || !n) return SWG_ERR_BAD_INPUT;
-    if (!g->built) return SWG_ERR_BAD_STATE;
+    if (!g->built || g->n_samples) return SWG_ERR_BAD_STATE;
     *n = g->n_out;
     return SWG_OK;
 }
 
 swg_status swg_graph_distinct(const swg_graph *g, uint64_t *n) {
     if (!g || !n) return SWG_ERR_BAD_INPUT;
-    if (!g->built) return SWG_ERR_BAD_STATE;
+    if (!g->built || g->n_samples) return SWG_ERR_BAD_STATE;
     *n = g->n_distinct;
     return SWG_OK;
 }
@@ -636,7 +890,7 @@ swg_status swg_graph_distinct(const swg_graph *g, uint64_t *n) {
 swg_status swg_graph_device_view(const swg_graph *g, const uint64_t **d_keys,
                                  const uint64_t **d_mult, uint64_t *n) {
     if (!g) return SWG_ERR_BAD_INPUT;
-    if (!g->built) return SWG_ERR_BAD_STATE;
+    if (!g->built || g->n_samples) return SWG_ERR_BAD_STATE;
     if (d_keys) *d_keys = reinterpret_cast<const uint64_t *>(g->d_out_keys);
     if (d_mult) *d_mult = reinterpret_cast<const uint64_t *>(g->d_out_mult);
     if (n) *n = g->n_out;
@@ -646,7 +900,7 @@ swg_status swg_graph_device_view(const swg_graph *g, const uint64_t **d_keys,
 swg_status swg_graph_copy_out(const swg_graph *g, uint64_t *keys, uint8_t *mult, uint64_t cap,
                               int sorted, uint64_t *n) {
     if (!g) return SWG_ERR_BAD_INPUT;
-    if (!g->built) return SWG_ERR_BAD_STATE;
+    if (!g->built || g->n_samples) return SWG_ERR_BAD_STATE;
     if (n) *n = g->n_out;
     if (cap < g->n_out) {
         swg::set_error("output capacity smaller than the survivor count");
@@ -731,6 +985,65 @@ swg_status swg_graph_last_timings(const swg_graph *g, float ms[5], int *launches
     if (!g->built) return SWG_ERR_BAD_STATE;
     if (ms) std::memcpy(ms, g->ms, sizeof(g->ms));
     if (launches) *launches = g->launches;
+    return SWG_OK;
+}
+
+swg_status swg_batch_build(swg_graph *g, const swg_opts *o, const swg_sample *samples,
+                           uint32_t n_samples) {
+    if (!g) return SWG_ERR_BAD_INPUT;
+    return batch_impl(g, o, samples, n_samples);
+}
+
+swg_status swg_batch_samples(const swg_graph *g, uint32_t *n_samples) {
+    if (!g || !n_samples) return SWG_ERR_BAD_INPUT;
+    if (!g->built || !g->n_samples) return SWG_ERR_BAD_STATE;
+    *n_samples = g->n_samples;
+    return SWG_OK;
+}
+
+swg_status swg_batch_sample_info(const swg_graph *g, uint32_t s, uint64_t *occurrences,
+                                 uint64_t *distinct, uint64_t *survivors) {
+    if (!g) return SWG_ERR_BAD_INPUT;
+    if (!g->built || !g->n_samples) return SWG_ERR_BAD_STATE;
+    if (s >= g->n_samples) return SWG_ERR_BAD_INPUT;
+    if (occurrences) *occurrences = g->s_occ[s];
+    if (distinct) *distinct = g->s_distinct[s];
+    if (survivors) *survivors = g->s_out[s];
+    return SWG_OK;
+}
+
+swg_status swg_batch_device_view(const swg_graph *g, uint32_t s, const uint64_t **d_keys,
+                                 const uint64_t **d_mult, uint64_t *n) {
+    if (!g) return SWG_ERR_BAD_INPUT;
+    if (!g->built || !g->n_samples) return SWG_ERR_BAD_STATE;
+    if (s >= g->n_samples) return SWG_ERR_BAD_INPUT;
+    if (d_keys) *d_keys = reinterpret_cast<const uint64_t *>(g->d_out_keys + g->s_tbase[s]);
+    if (d_mult) *d_mult = reinterpret_cast<const uint64_t *>(g->d_out_mult + g->s_tbase[s]);
+    if (n) *n = g->s_out[s];
+    return SWG_OK;
+}
+
+swg_status swg_batch_copy_out(const swg_graph *g, uint32_t s, uint64_t *keys, uint8_t *mult,
+                              uint64_t cap, int sorted, uint64_t *n) {
+    if (!g) return SWG_ERR_BAD_INPUT;
+    if (!g->built || !g->n_samples) return SWG_ERR_BAD_STATE;
+    if (s >= g->n_samples) return SWG_ERR_BAD_INPUT;
+    const uint64_t cnt = g->s_out[s];
+    if (n) *n = cnt;
+    if (cap < cnt) {
+        swg::set_error("output capacity smaller than the survivor count");
+        return SWG_ERR_BAD_INPUT;
+    }
+    if (!cnt) return SWG_OK;
+    std::vector<uint64_t> k(cnt), m(cnt);
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    SWG_CUDA(cudaMemcpy(k.data(), g->d_out_keys + g->s_tbase[s], cnt * 8, cudaMemcpyDeviceToHost),
+             "copy keys");
+    SWG_CUDA(cudaMemcpy(m.data(), g->d_out_mult + g->s_tbase[s], cnt * 8, cudaMemcpyDeviceToHost),
+             "copy multiplicities");
+    if (sorted) swg::sort_records(k.data(), m.data(), cnt);
+    if (keys) std::memcpy(keys, k.data(), cnt * 8);
+    if (mult) std::memcpy(mult, m.data(), cnt * 8);
     return SWG_OK;
 }
 

@@ -80,6 +80,16 @@ __device__ __forceinline__ uint64_t occ_of(uint32_t len, int k) {
     return len >= (uint32_t)k ? (uint64_t)(len - (uint32_t)k + 1) : 0ull;
 }
 
+// Sample (segment) of read r and its parameters; a single-sample build has no
+// segment arrays and takes k, cutoff, table and counters from BuildArgs.
+__device__ __forceinline__ uint32_t seg_of(const BuildArgs &a, uint64_t r) {
+    return a.read_seg ? a.read_seg[r] : 0u;
+}
+
+__device__ __forceinline__ int k_of(const BuildArgs &a, uint32_t seg) {
+    return a.segs ? a.segs[seg].k : a.k;
+}
+
 __device__ __forceinline__ ulonglong2 ld_relaxed16(const Entry *e) {
     ulonglong2 v;
     asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];"
@@ -186,19 +196,17 @@ __device__ __forceinline__ uint64_t block_exclusive_scan(uint64_t v, uint64_t *w
 
 // ---------------------------------------------------------------------
 // Occurrence prefix: occ_prefix[r] = sum_{q<r} max(0, len[q]-k+1).
-__global__ void __launch_bounds__(kScanBlock) k_scan_reduce(const uint32_t *__restrict__ len,
-                                                            uint64_t n, int k,
-                                                            uint64_t *__restrict__ block_sums) {
+__global__ void __launch_bounds__(kScanBlock) k_scan_reduce(BuildArgs a) {
     __shared__ uint64_t wb[kScanBlock / 32];
     const uint64_t base = (uint64_t)blockIdx.x * kScanChunk;
     uint64_t s = 0;
     for (int it = 0; it < kScanItems; ++it) {
         const uint64_t r = base + (uint64_t)it * kScanBlock + threadIdx.x;
-        if (r < n) s += occ_of(len[r], k);
+        if (r < a.n_reads) s += occ_of(a.read_len[r], k_of(a, seg_of(a, r)));
     }
     uint64_t total;
     block_exclusive_scan<kScanBlock>(s, wb, &total);
-    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+    if (threadIdx.x == 0) a.scan_blocks[blockIdx.x] = total;
 }
 
 __global__ void __launch_bounds__(1024) k_scan_blocks(uint64_t *block_sums, uint64_t nb,
@@ -221,10 +229,7 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(uint64_t *block_sums, uint
     if (threadIdx.x == 0) *occ_total = carry;
 }
 
-__global__ void __launch_bounds__(kScanBlock) k_scan_write(const uint32_t *__restrict__ len,
-                                                           uint64_t n, int k,
-                                                           const uint64_t *__restrict__ block_sums,
-                                                           uint64_t *__restrict__ prefix) {
+__global__ void __launch_bounds__(kScanBlock) k_scan_write(BuildArgs a) {
     __shared__ uint64_t wb[kScanBlock / 32];
     const uint64_t base = (uint64_t)blockIdx.x * kScanChunk + (uint64_t)threadIdx.x * kScanItems;
     uint64_t v[kScanItems];
@@ -232,14 +237,14 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_write(const uint32_t *__res
 #pragma unroll
     for (int it = 0; it < kScanItems; ++it) {
         const uint64_t r = base + it;
-        v[it] = r < n ? occ_of(len[r], k) : 0;
+        v[it] = r < a.n_reads ? occ_of(a.read_len[r], k_of(a, seg_of(a, r))) : 0;
         s += v[it];
     }
-    uint64_t run = block_sums[blockIdx.x] + block_exclusive_scan<kScanBlock>(s, wb, nullptr);
+    uint64_t run = a.scan_blocks[blockIdx.x] + block_exclusive_scan<kScanBlock>(s, wb, nullptr);
 #pragma unroll
     for (int it = 0; it < kScanItems; ++it) {
         const uint64_t r = base + it;
-        if (r < n) prefix[r] = run;
+        if (r < a.n_reads) a.occ_prefix[r] = run;
         run += v[it];
     }
 }
@@ -265,6 +270,7 @@ struct TileSmem {
     uint64_t pre[kSmemReads + 1];
     uint64_t off[kSmemReads];
     uint32_t len[kSmemReads];
+    uint32_t seg[kSmemReads];
 };
 
 struct TileView {
@@ -284,6 +290,7 @@ __device__ __forceinline__ TileView load_tile(const BuildArgs &a, uint64_t t, Ti
             if (j < v.nr) {
                 s.off[j] = a.read_off[v.r0 + j];
                 s.len[j] = a.read_len[v.r0 + j];
+                s.seg[j] = seg_of(a, v.r0 + j);
             }
         }
     }
@@ -293,7 +300,8 @@ __device__ __forceinline__ TileView load_tile(const BuildArgs &a, uint64_t t, Ti
 // Read holding occurrence i, with its prefix, offset and length.
 __device__ __forceinline__ void find_read(const BuildArgs &a, const TileView &v,
                                           const TileSmem &s, uint64_t i, uint64_t &pre,
-                                          uint64_t &off, uint32_t &len, uint64_t &ridx) {
+                                          uint64_t &off, uint32_t &len, uint64_t &ridx,
+                                          uint32_t &seg) {
     if (v.in_smem) {
         uint64_t lo = 0, hi = v.nr;  // last j with pre[j] <= i
         while (hi - lo > 1) {
@@ -305,6 +313,7 @@ __device__ __forceinline__ void find_read(const BuildArgs &a, const TileView &v,
         off = s.off[lo];
         len = s.len[lo];
         ridx = v.r0 + lo;
+        seg = s.seg[lo];
     } else {
         uint64_t lo = v.r0, hi = v.r0 + v.nr;
         while (hi - lo > 1) {
@@ -316,6 +325,7 @@ __device__ __forceinline__ void find_read(const BuildArgs &a, const TileView &v,
         off = a.read_off[lo];
         len = a.read_len[lo];
         ridx = lo;
+        seg = seg_of(a, lo);
     }
 }
 
@@ -324,11 +334,11 @@ __device__ __forceinline__ void find_read(const BuildArgs &a, const TileView &v,
 // K = max(C, rc(C)), f = (C == K); right arc (j+k < L) -> slot
 // (f ? 0 : 4) + base[j+k]; left arc (j >= 1) -> slot (f ? 4 : 0) + 3 - base[j-1].
 __device__ __forceinline__ void make_occ(const BuildArgs &a, const TileView &v, const TileSmem &s,
-                                         uint64_t i, uint64_t &key, uint64_t &inc) {
+                                         uint64_t i, uint64_t &key, uint64_t &inc, uint32_t &seg) {
     uint64_t pre, off, ridx;
     uint32_t len;
-    find_read(a, v, s, i, pre, off, len, ridx);
-    const int k = a.k;
+    find_read(a, v, s, i, pre, off, len, ridx, seg);
+    const int k = k_of(a, seg);
     const uint64_t p = i - pre, g = off + p;
     const uint64_t win = window32(a.packed, a.n_words, g);
     const uint64_t fwd = win >> (64 - 2 * k);
@@ -354,17 +364,20 @@ __device__ __forceinline__ void make_occ(const BuildArgs &a, const TileView &v, 
 template <typename F>
 __device__ __forceinline__ void walk_run(const BuildArgs &a, const TileView &v, const TileSmem &s,
                                          uint64_t i0, uint64_t i1, F &&fn) {
-    const int k = a.k;
-    const uint64_t kmask = (1ull << (2 * k)) - 1;
-    const int top = 2 * (k - 1);
+    int k = a.k;
+    uint64_t kmask = 0;
+    int top = 0;
     uint64_t fwd = 0, rc = 0, last = 0, g = 0, p = 0, ridx = 0;
-    uint32_t len = 0, rb = 0;
+    uint32_t len = 0, rb = 0, seg = 0;
     for (uint64_t i = i0; i < i1; ++i) {
         uint32_t lb;
         bool has_l;
         if (i == i0 || i > last) {
             uint64_t pre, off;
-            find_read(a, v, s, i, pre, off, len, ridx);
+            find_read(a, v, s, i, pre, off, len, ridx, seg);
+            k = k_of(a, seg);
+            kmask = (1ull << (2 * k)) - 1;
+            top = 2 * (k - 1);
             p = i - pre;
             g = off + p;
             last = pre + (len - (uint32_t)k);
@@ -388,7 +401,7 @@ __device__ __forceinline__ void walk_run(const BuildArgs &a, const TileView &v, 
         unsigned code = 0;
         if (has_r) code |= 0x08u | ((f ? 0u : 4u) + rb);
         if (has_l) code |= 0x80u | (((f ? 4u : 0u) + 3u - lb) << 4);
-        fn(f ? fwd : rc, code, ridx);
+        fn(f ? fwd : rc, code, ridx, seg);
     }
 }
 
@@ -419,25 +432,103 @@ __device__ __forceinline__ uint64_t unmix64(uint64_t x) {
 __global__ void __launch_bounds__(kK1Block) k_hll(BuildArgs a) {
     __shared__ TileSmem s;
     __shared__ unsigned regs[1 << kHllBits];
+    __shared__ uint32_t s_cur;
     for (int j = threadIdx.x; j < (1 << kHllBits); j += blockDim.x) regs[j] = 0;
-    for (uint64_t t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
+    if (threadIdx.x == 0) s_cur = 0xffffffffu;
+    // a contiguous range of tiles per block: the sample changes only at its
+    // boundaries, and the block keeps the current sample's registers in smem
+    const uint64_t t0 = a.n_tiles * blockIdx.x / gridDim.x;
+    const uint64_t t1 = a.n_tiles * (blockIdx.x + 1) / gridDim.x;
+    auto flush = [&](uint32_t seg) {
+        for (int j = threadIdx.x; j < (1 << kHllBits); j += blockDim.x)
+            if (regs[j]) {
+                atomicMax(&a.hll[((uint64_t)seg << kHllBits) + j], regs[j]);
+                regs[j] = 0;
+            }
+    };
+    for (uint64_t t = t0; t < t1; ++t) {
         __syncthreads();
         const TileView v = load_tile(a, t, s);
         __syncthreads();
+        const uint32_t first = v.in_smem ? s.seg[0] : seg_of(a, v.r0);
+        if (first != s_cur) {
+            if (s_cur != 0xffffffffu) flush(s_cur);
+            __syncthreads();
+            if (threadIdx.x == 0) s_cur = first;
+            __syncthreads();
+        }
+        const uint32_t cur = s_cur;
         const uint64_t A = t * kTileOcc;
         const uint64_t B = umin64(A + kTileOcc, a.total_occ);
         const uint64_t i0 = A + (uint64_t)threadIdx.x * kK1Items;
-        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B), [&](uint64_t key, unsigned, uint64_t) {
+        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B),
+                 [&](uint64_t key, unsigned, uint64_t, uint32_t seg) {
             const uint64_t h = mix64(key ^ 0x9e3779b97f4a7c15ull);
             const unsigned idx = (unsigned)(h >> (64 - kHllBits));
             const uint64_t rest = (h << kHllBits) | (1ull << (kHllBits - 1));
             const unsigned rank = (unsigned)__clzll(rest) + 1;
-            if (rank > regs[idx]) atomicMax(&regs[idx], rank);
+            if (seg == cur) {
+                if (rank > regs[idx]) atomicMax(&regs[idx], rank);
+            } else {
+                atomicMax(&a.hll[((uint64_t)seg << kHllBits) + idx], rank);
+            }
         });
     }
     __syncthreads();
-    for (int j = threadIdx.x; j < (1 << kHllBits); j += blockDim.x)
-        if (regs[j]) atomicMax(&a.hll[j], regs[j]);
+    if (s_cur != 0xffffffffu) flush(s_cur);
+}
+
+// HyperLogLog estimate per sample (the same formula as hll_estimate).
+__global__ void __launch_bounds__(256) k_hll_est(const unsigned *regs, double *est) {
+    __shared__ double ssum[256];
+    __shared__ int szero[256];
+    const unsigned *r = regs + ((uint64_t)blockIdx.x << kHllBits);
+    double sum = 0;
+    int zeros = 0;
+    for (int j = threadIdx.x; j < (1 << kHllBits); j += blockDim.x) {
+        sum += ldexp(1.0, -(int)r[j]);
+        zeros += r[j] == 0;
+    }
+    ssum[threadIdx.x] = sum;
+    szero[threadIdx.x] = zeros;
+    __syncthreads();
+    for (int d = 128; d > 0; d >>= 1) {
+        if (threadIdx.x < d) {
+            ssum[threadIdx.x] += ssum[threadIdx.x + d];
+            szero[threadIdx.x] += szero[threadIdx.x + d];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double m = (double)(1 << kHllBits);
+        const double alpha = 0.7213 / (1.0 + 1.079 / m);
+        double e = alpha * m * m / ssum[0];
+        if (e <= 2.5 * m && szero[0] > 0) e = m * log(m / (double)szero[0]);
+        est[blockIdx.x] = e;
+    }
+}
+
+// Batched builds: the sample of every read and the shift of its offset into
+// the concatenated packed stream.
+__global__ void k_seg_setup(uint32_t n_segs, const uint64_t *__restrict__ seg_read_start,
+                            const uint64_t *__restrict__ seg_base_shift,
+                            uint32_t *__restrict__ read_seg, uint64_t *__restrict__ read_off) {
+    const uint32_t sg = blockIdx.x % n_segs;
+    const uint32_t part = blockIdx.x / n_segs, parts = gridDim.x / n_segs;
+    const uint64_t rs = seg_read_start[sg], re = seg_read_start[sg + 1];
+    const uint64_t shift = seg_base_shift[sg];
+    for (uint64_t r = rs + (uint64_t)part * blockDim.x + threadIdx.x; r < re;
+         r += (uint64_t)parts * blockDim.x) {
+        read_seg[r] = sg;
+        read_off[r] += shift;
+    }
+}
+
+__global__ void k_gather_prefix(const uint64_t *__restrict__ prefix,
+                                const uint64_t *__restrict__ idx, uint32_t n,
+                                uint64_t *__restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = prefix[idx[i]];
 }
 
 // HyperLogLog of the canonical keys fused with each read's minimizer: the
@@ -457,7 +548,7 @@ __global__ void __launch_bounds__(kK1Block) k_sketch(BuildArgs a, unsigned *minh
         const uint64_t i0 = A + (uint64_t)threadIdx.x * kK1Items;
         uint64_t cur = ~0ull;
         unsigned best = 0xffffffffu;
-        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B), [&](uint64_t key, unsigned, uint64_t r) {
+        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B), [&](uint64_t key, unsigned, uint64_t r, uint32_t) {
             const uint64_t h = mix64(key ^ 0x9e3779b97f4a7c15ull);
             const unsigned idx = (unsigned)(h >> (64 - kHllBits));
             const uint64_t rest = (h << kHllBits) | (1ull << (kHllBits - 1));
@@ -521,18 +612,26 @@ __global__ void k_bucket_scatter(const unsigned *__restrict__ minhash, uint64_t 
 
 // ---------------------------------------------------------------------
 // K1: fused extraction + counting, one tile per block.
+// kSeg: batched build (per-sample tables, status and counters).
+template <bool kSeg>
 __global__ void __launch_bounds__(kK1Block) k_count(BuildArgs a) {
     __shared__ TileSmem s;
     __shared__ unsigned s_stop;
+    __shared__ uint32_t s_seg0;
     __shared__ unsigned long long s_ins;
     const uint64_t t = blockIdx.x;
-    if (threadIdx.x == 0) {
-        s_ins = 0;
-        s_stop = (*(volatile unsigned *)a.status) & kStatusTableFull;
-    }
+    if (threadIdx.x == 0) s_ins = 0;
     const TileView v = load_tile(a, t, s);
     __syncthreads();
-    if (s_stop) return;
+    if (threadIdx.x == 0) {
+        s_seg0 = v.in_smem ? s.seg[0] : seg_of(a, v.r0);
+        const unsigned *st0 = kSeg ? a.seg_status + s_seg0 : a.status;
+        s_stop = (*(volatile const unsigned *)st0) & kStatusTableFull;
+    }
+    __syncthreads();
+    const uint32_t seg0 = s_seg0;
+    const bool stop0 = s_stop != 0;
+    if (stop0 && !kSeg) return;  // the table is being rebuilt larger
     const int lane = threadIdx.x & 31;
     unsigned my_ins = 0;
     const uint64_t A = t * kTileOcc;
@@ -543,9 +642,11 @@ __global__ void __launch_bounds__(kK1Block) k_count(BuildArgs a) {
         const unsigned vmask = __ballot_sync(kFull, valid);
         if (!valid) continue;
         uint64_t key, inc;
-        make_occ(a, v, s, i, key, inc);
+        uint32_t seg;
+        make_occ(a, v, s, i, key, inc, seg);
         // merge equal keys of this warp (tandem repeats, duplicated reads)
-        const unsigned peers = __match_any_sync(vmask, key);
+        unsigned peers = __match_any_sync(vmask, key);
+        if (kSeg) peers &= __match_any_sync(vmask, seg);
         if (__any_sync(vmask, peers != (1u << lane))) {
             uint64_t tot = 0;
 #pragma unroll
@@ -555,14 +656,31 @@ __global__ void __launch_bounds__(kK1Block) k_count(BuildArgs a) {
             }
             inc = tot;
         }
-        if (lane == __ffs(peers) - 1) my_ins += insert_or_update(a.table, a.cap, key, inc, a.status);
+        if (lane != __ffs(peers) - 1) continue;
+        if (!kSeg) {
+            my_ins += insert_or_update(a.table, a.cap, key, inc, a.status);
+            continue;
+        }
+        const SegParams &p = a.segs[seg];
+        unsigned *st = a.seg_status + seg;
+        if (seg == seg0) {
+            if (!stop0) my_ins += insert_or_update(a.table + p.tbase, p.tcap, key, inc, st);
+        } else if (!((*(volatile const unsigned *)st) & kStatusTableFull)) {
+            if (insert_or_update(a.table + p.tbase, p.tcap, key, inc, st)) {
+                const unsigned long long before = atomicAdd(&a.seg_counts[2 * seg], 1ull);
+                if ((before + 1) * 20 > p.tcap * 19) atomicOr(st, kStatusTableFull);
+            }
+        }
     }
     if (my_ins) atomicAdd(&s_ins, (unsigned long long)my_ins);
     __syncthreads();
     if (threadIdx.x == 0 && s_ins) {
-        const unsigned long long before = atomicAdd(&a.counters[0], s_ins);
-        // stop the build early once the table is nearly full; the host retries
-        if ((before + s_ins) * 20 > (unsigned long long)a.cap * 19) atomicOr(a.status, kStatusTableFull);
+        unsigned long long *ctr = kSeg ? a.seg_counts + 2 * seg0 : a.counters;
+        unsigned *st = kSeg ? a.seg_status + seg0 : a.status;
+        const unsigned long long cap = kSeg ? a.segs[seg0].tcap : a.cap;
+        const unsigned long long before = atomicAdd(ctr, s_ins);
+        // stop early once the table is nearly full; the host retries larger
+        if ((before + s_ins) * 20 > cap * 19) atomicOr(st, kStatusTableFull);
     }
 }
 
@@ -573,7 +691,21 @@ __global__ void __launch_bounds__(kCBlock) k_compact(BuildArgs a) {
     __shared__ uint64_t wb[kCBlock / 32];
     __shared__ unsigned long long s_base;
     const uint64_t chunk = (uint64_t)blockIdx.x * kCBlock * kCItems;
-    const int c = a.cutoff;
+    int c = a.cutoff;
+    unsigned long long *ctr = a.counters;
+    uint64_t obase = 0, ocap = a.out_cap;
+    if (a.segs) {  // sample regions start at multiples of the chunk
+        uint32_t lo = 0, hi = a.n_segs;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (a.segs[mid].tbase <= chunk) lo = mid;
+            else hi = mid;
+        }
+        c = a.segs[lo].cutoff;
+        ctr = a.seg_counts + 2 * lo;
+        obase = a.segs[lo].tbase;
+        ocap = a.segs[lo].tcap;
+    }
     const uint32_t thr = c <= 0 ? 0u : (c >= 256 ? 0u : (uint32_t)c * 0x01010101u);
     const bool all_cut = c >= 256;
     uint64_t keys[kCItems], cnts[kCItems];
@@ -603,15 +735,15 @@ __global__ void __launch_bounds__(kCBlock) k_compact(BuildArgs a) {
     }
     uint64_t total;
     const uint64_t ex = block_exclusive_scan<kCBlock>((uint64_t)nkeep, wb, &total);
-    if (threadIdx.x == 0) s_base = total ? atomicAdd(&a.counters[1], (unsigned long long)total) : 0;
+    if (threadIdx.x == 0) s_base = total ? atomicAdd(&ctr[1], (unsigned long long)total) : 0;
     __syncthreads();
     uint64_t pos = s_base + ex;
 #pragma unroll
     for (int it = 0; it < kCItems; ++it) {
         if (keep & (1u << it)) {
-            if (pos < a.out_cap) {
-                a.out_keys[pos] = keys[it];
-                a.out_mult[pos] = cnts[it];
+            if (pos < ocap) {
+                a.out_keys[obase + pos] = keys[it];
+                a.out_mult[obase + pos] = cnts[it];
             }
             pos++;
         }
@@ -643,7 +775,7 @@ __global__ void __launch_bounds__(kK1Block) k_part_count(BuildArgs a, PartArgs p
         const uint64_t A = t * kTileOcc;
         const uint64_t B = umin64(A + kTileOcc, a.total_occ);
         const uint64_t i0 = A + (uint64_t)threadIdx.x * kK1Items;
-        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B), [&](uint64_t key, unsigned, uint64_t) {
+        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B), [&](uint64_t key, unsigned, uint64_t, uint32_t) {
             atomicAdd(&hist[mix64(key) >> shift], 1u);
         });
     }
@@ -693,7 +825,7 @@ __global__ void __launch_bounds__(kK1Block) k_part_scatter(BuildArgs a, PartArgs
         const uint32_t n = (uint32_t)(B - A);
         uint32_t q = threadIdx.x * kK1Items;
         const uint64_t i0 = A + q;
-        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B), [&](uint64_t key, unsigned code, uint64_t) {
+        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B), [&](uint64_t key, unsigned code, uint64_t, uint32_t) {
             const uint64_t h = mix64(key);
             const unsigned part = (unsigned)(h >> shift);
             rec[q] = ((h & lowmask) << 8) | code;
@@ -887,10 +1019,9 @@ uint64_t scan_block_count(uint64_t n_reads) { return (n_reads + kScanChunk - 1) 
 int launch_occ_scan(const BuildArgs &a, cudaStream_t s) {
     const uint64_t nb = scan_block_count(a.n_reads);
     if (nb == 0) return 0;
-    k_scan_reduce<<<(unsigned)nb, kScanBlock, 0, s>>>(a.read_len, a.n_reads, a.k, a.scan_blocks);
+    k_scan_reduce<<<(unsigned)nb, kScanBlock, 0, s>>>(a);
     k_scan_blocks<<<1, 1024, 0, s>>>(a.scan_blocks, nb, a.occ_prefix + a.n_reads);
-    k_scan_write<<<(unsigned)nb, kScanBlock, 0, s>>>(a.read_len, a.n_reads, a.k, a.scan_blocks,
-                                                     a.occ_prefix);
+    k_scan_write<<<(unsigned)nb, kScanBlock, 0, s>>>(a);
     return 3;
 }
 
@@ -944,9 +1075,33 @@ int launch_read_order(const BuildArgs &a, const unsigned *minhash, unsigned *his
     return 3;
 }
 
+int launch_seg_setup(const BuildArgs &a, const uint64_t *seg_read_start,
+                     const uint64_t *seg_base_shift, uint32_t *read_seg, uint64_t *read_off,
+                     cudaStream_t s) {
+    if (a.n_segs == 0) return 0;
+    const uint32_t parts = (uint32_t)std::max<uint64_t>(1, (uint64_t)device_sm_count() * 8 / a.n_segs);
+    k_seg_setup<<<a.n_segs * parts, 256, 0, s>>>(a.n_segs, seg_read_start, seg_base_shift,
+                                                 read_seg, read_off);
+    return 1;
+}
+
+int launch_hll_estimates(const unsigned *regs, uint32_t n_segs, double *est, cudaStream_t s) {
+    if (n_segs == 0) return 0;
+    k_hll_est<<<n_segs, 256, 0, s>>>(regs, est);
+    return 1;
+}
+
+int launch_gather_prefix(const uint64_t *prefix, const uint64_t *idx, uint32_t n, uint64_t *out,
+                         cudaStream_t s) {
+    if (n == 0) return 0;
+    k_gather_prefix<<<(n + 255) / 256, 256, 0, s>>>(prefix, idx, n, out);
+    return 1;
+}
+
 int launch_count(const BuildArgs &a, cudaStream_t s) {
     if (a.n_tiles == 0) return 0;
-    k_count<<<(unsigned)a.n_tiles, kK1Block, 0, s>>>(a);
+    if (a.segs) k_count<true><<<(unsigned)a.n_tiles, kK1Block, 0, s>>>(a);
+    else k_count<false><<<(unsigned)a.n_tiles, kK1Block, 0, s>>>(a);
     return 1;
 }
 

@@ -30,6 +30,16 @@ constexpr int kK1Items = 16;
 constexpr uint64_t kTileOcc = (uint64_t)kK1Block * kK1Items;  // occurrences per tile
 constexpr int kHllBits = 12;                                  // 4096 registers
 
+// Per-sample parameters of a batched build (samples = segments of one
+// build): the sample's table region (its output uses the same offsets), its
+// k and its cutoff.
+struct SegParams {
+    unsigned long long tbase;
+    unsigned long long tcap;
+    int k;
+    int cutoff;
+};
+
 // Per-build launch parameters.
 struct BuildArgs {
     const uint32_t *packed;
@@ -53,6 +63,12 @@ struct BuildArgs {
     unsigned long long *out_keys;
     unsigned long long *out_mult;
     uint64_t out_cap;
+    // batched builds only (all null / 0 for a single sample)
+    const uint32_t *read_seg;          // [n_reads] sample of each read
+    const SegParams *segs;             // [n_segs]
+    uint32_t n_segs;
+    unsigned long long *seg_counts;    // [2 * n_segs]: inserted, survivors
+    unsigned *seg_status;              // [n_segs]
 };
 
 // Partitioned build: records {hash low bits, arc code} scattered by the top
@@ -85,6 +101,12 @@ uint64_t bucket_count();
 int launch_read_order(const BuildArgs &a, const unsigned *minhash, unsigned *hist,
                       uint64_t *out_off, uint32_t *out_len, cudaStream_t s);
 int launch_count(const BuildArgs &a, cudaStream_t s);
+int launch_seg_setup(const BuildArgs &a, const uint64_t *seg_read_start,
+                     const uint64_t *seg_base_shift, uint32_t *read_seg, uint64_t *read_off,
+                     cudaStream_t s);
+int launch_hll_estimates(const unsigned *regs, uint32_t n_segs, double *est, cudaStream_t s);
+int launch_gather_prefix(const uint64_t *prefix, const uint64_t *idx, uint32_t n, uint64_t *out,
+                         cudaStream_t s);
 int launch_compact(const BuildArgs &a, cudaStream_t s);
 int launch_part_count(const BuildArgs &a, const PartArgs &p, cudaStream_t s);
 int launch_part_prefix(const PartArgs &p, cudaStream_t s);

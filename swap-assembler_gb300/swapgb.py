@@ -63,6 +63,12 @@ class BuildInfo(C.Structure):
         return d
 
 
+class Sample(C.Structure):
+    _fields_ = [("packed", C.c_void_p), ("n_words", C.c_uint64), ("read_off", C.c_void_p),
+                ("read_len", C.c_void_p), ("n_reads", C.c_uint64), ("k", C.c_int),
+                ("cutoff", C.c_int)]
+
+
 _lib = None
 
 
@@ -102,6 +108,11 @@ def lib() -> C.CDLL:
             "swg_graph_last_timings": (i32, [P, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
             "swg_graph_build_info": (i32, [P, C.POINTER(BuildInfo)]),
             "swg_probe_random_access": (i32, [i32, u64, u64, P, C.POINTER(C.c_double)]),
+            "swg_batch_build": (i32, [P, C.POINTER(Opts), C.POINTER(Sample), C.c_uint32]),
+            "swg_batch_samples": (i32, [P, C.POINTER(C.c_uint32)]),
+            "swg_batch_sample_info": (i32, [P, C.c_uint32, pu64, pu64, pu64]),
+            "swg_batch_device_view": (i32, [P, C.c_uint32, C.POINTER(P), C.POINTER(P), pu64]),
+            "swg_batch_copy_out": (i32, [P, C.c_uint32, P, P, u64, i32, pu64]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -240,6 +251,35 @@ class Graph:
     def write_node_lines(self, path: str) -> None:
         _check(lib().swg_graph_write_node_lines(self._h, str(path).encode()),
                "swg_graph_write_node_lines")
+
+    def build_batch(self, opts: Opts, samples: list) -> "Graph":
+        """samples: list of (Reads, k, cutoff). Each sample gets its own result."""
+        arr = (Sample * len(samples))()
+        for i, (r, k, c) in enumerate(samples):
+            arr[i] = Sample(_ptr(r.packed), r.n_words, _ptr(r.off), _ptr(r.len), r.n_reads, k, c)
+        self._batch_keepalive = samples
+        _check(lib().swg_batch_build(self._h, C.byref(opts), arr, len(samples)), "swg_batch_build")
+        return self
+
+    def batch_size(self) -> int:
+        n = C.c_uint32()
+        _check(lib().swg_batch_samples(self._h, C.byref(n)), "swg_batch_samples")
+        return n.value
+
+    def batch_info(self, s: int) -> tuple[int, int, int]:
+        o, d, v = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        _check(lib().swg_batch_sample_info(self._h, s, C.byref(o), C.byref(d), C.byref(v)),
+               "swg_batch_sample_info")
+        return o.value, d.value, v.value
+
+    def batch_copy_out(self, s: int, sorted: bool = True) -> tuple[np.ndarray, np.ndarray]:
+        n = self.batch_info(s)[2]
+        keys = np.zeros(n, dtype=np.uint64)
+        mult = np.zeros((n, 8), dtype=np.uint8)
+        got = C.c_uint64()
+        _check(lib().swg_batch_copy_out(self._h, s, _ptr(keys), _ptr(mult), n, int(sorted),
+                                        C.byref(got)), "swg_batch_copy_out")
+        return keys, mult
 
     def info(self) -> dict:
         bi = BuildInfo()
