@@ -47,6 +47,7 @@ def parse_args():
     ap.add_argument("--no-probe", action="store_true", help="skip the random-access probe")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-samples measurement")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served-requests measurement")
     ap.add_argument("--algo", default="direct", choices=["direct", "partitioned"])
     ap.add_argument("--order", default="input", choices=["input", "minimizer"],
                     help="read order of the direct algorithm")
@@ -217,6 +218,85 @@ def batched_metrics(stream_ptr: int, repeats: int = 3) -> dict:
             "last_sample_identical": same,
             "path": "host packed reads -> device-resident graphs; plain = swg_graph_build per "
                     "sample, batched = one swg_batch_build"}
+
+
+def served_metrics(duration_s: float = 10.0, rate: float = 50.0, seed: int = 5) -> dict:
+    """Poisson request stream (mean `rate` req/s) through the request server.
+    Request sizes follow the batched workload's per-sample distribution, plus
+    2% large requests (10 Mbp genome, 40x, 150 bp reads); k from
+    {21, 25, 27, 31} and c from {2, 3, 5} per request; 150 GiB admission budget.
+    A pool of distinct request inputs is generated once and drawn from."""
+    import random
+    import threading
+    import swapgb
+    rng = random.Random(seed)
+    specs = batched_samples(n=40, seed=seed)
+    pool = [swapgb.reads_from_fasta(swapgb.synth_fasta(**p), 21) for p in specs]
+    large = swapgb.reads_from_fasta(swapgb.synth_fasta(seed=77, genome_len=10_000_000,
+                                                       n_reads=2_666_667, read_len=150,
+                                                       sub_rate=0.005), 21)
+    srv = swapgb.Server(memory_budget=150 << 30, workers=2)
+    # warm-up: one request of each kind
+    for r in (pool[0], large):
+        t = srv.submit(r, 27, 3)
+        srv.wait(t, 120.0)
+        srv.release(t)
+    tickets, sizes, kinds = [], [], []
+    lock = threading.Lock()
+    done = threading.Event()
+    lat = {}
+
+    def collector():
+        i = 0
+        while True:
+            with lock:
+                have = i < len(tickets)
+                t = tickets[i] if have else None
+            if not have:
+                if done.is_set():
+                    with lock:
+                        if i >= len(tickets):
+                            return
+                    continue
+                time.sleep(0.0005)
+                continue
+            srv.wait(t, 300.0)
+            lat[t] = srv.poll(t)[1]
+            srv.release(t)
+            i += 1
+
+    th = threading.Thread(target=collector)
+    th.start()
+    t0 = time.perf_counter()
+    t_next = 0.0
+    while t_next < duration_s:
+        now = time.perf_counter() - t0
+        if now < t_next:
+            time.sleep(t_next - now)
+        is_large = rng.random() < 0.02
+        r = large if is_large else pool[rng.randrange(len(pool))]
+        k, c = rng.choice([21, 25, 27, 31]), rng.choice([2, 3, 5])
+        t = srv.submit(r, k, c)
+        with lock:
+            tickets.append(t)
+            sizes.append(r.n_bases)
+            kinds.append(is_large)
+        t_next += rng.expovariate(rate)
+    done.set()
+    th.join()
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    ls = sorted(lat[t] for t in tickets)
+    q = lambda f: ls[min(len(ls) - 1, int(f * len(ls)))]
+    return {"workload": "Poisson %.0f req/s for %.0f s; sizes from the batched workload's per-sample "
+                        "distribution + 2%% large (10 Mbp, 40x, 150 bp); k in {21,25,27,31}, c in "
+                        "{2,3,5}; 150 GiB budget; 2 workers" % (rate, duration_s),
+            "requests": len(tickets), "large_requests": sum(kinds),
+            "p50_ms": 1e3 * q(0.50), "p99_ms": 1e3 * q(0.99), "max_ms": 1e3 * ls[-1],
+            "aggregate_bases_per_s": sum(sizes) / wall, "offered_bases_per_s": sum(sizes) / duration_s,
+            "batches": st["batches"], "max_batch_requests": st["max_batch_requests"],
+            "latency": "submit (including the server's copy of the reads) to the result resident on the device"}
 
 
 def run_reference_arm(args) -> int:
@@ -418,6 +498,9 @@ def main() -> int:
     batched = None
     if rank == 0 and not args.no_batch and not args.reads:
         batched = batched_metrics(stream.cuda_stream)
+    served = None
+    if rank == 0 and not args.no_serve and not args.reads:
+        served = served_metrics()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(text, n_bases)
@@ -436,6 +519,7 @@ def main() -> int:
             "roofline": roofline,
             "random_access": atomic,
             "batched": batched,
+            "served": served,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "kmers_per_s": world * n_occ / (ms_per_step * 1e-3),

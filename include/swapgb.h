@@ -175,6 +175,53 @@ swg_status swg_batch_device_view(const swg_graph *g, uint32_t s, const uint64_t 
 swg_status swg_batch_copy_out(const swg_graph *g, uint32_t s, uint64_t *keys, uint8_t *mult,
                               uint64_t cap, int sorted, uint64_t *n);
 
+/* ---- request server (continuous batching) ------------------------------ */
+/* Graph-build requests arrive at any time; worker threads batch every queued
+ * request that fits the memory budget into one batched build (several batches
+ * overlap on the device, one per worker) and keep each result on the device
+ * until it is fetched or released. Admission charges a request an estimate of
+ * its footprint (sized by its k-mer occurrence count, an upper bound on its
+ * distinct k-molecules) while its batch runs and its exact result size while
+ * resident; a request larger than the whole budget is refused
+ * (SWG_ERR_ADMISSION). Each result equals the plain build of that request. */
+typedef struct swg_server swg_server;
+
+typedef struct swg_server_opts {
+    uint64_t memory_budget; /* device bytes for in-flight batches + resident results; 0 = 150 GiB */
+    uint32_t workers;       /* batches in flight at once; 0 = 2 */
+    uint32_t max_batch;     /* requests per batch; 0 = no limit */
+    double load_factor;     /* 0 = 0.6 */
+} swg_server_opts;
+
+typedef struct swg_server_stats {
+    uint64_t submitted, completed, failed, rejected, batches, max_batch_requests;
+    uint64_t queued, bytes_reserved, bytes_resident;
+} swg_server_stats;
+
+#define SWG_REQ_QUEUED 0
+#define SWG_REQ_RUNNING 1
+#define SWG_REQ_DONE 2
+#define SWG_REQ_FAILED 3
+
+swg_status swg_server_create(const swg_server_opts *o, swg_server **out);
+/* Copies the request's reads; the caller may free them on return. */
+swg_status swg_server_submit(swg_server *srv, const swg_sample *req, uint64_t *ticket);
+/* Non-blocking: state (SWG_REQ_*) and latency so far (submit to completion). */
+swg_status swg_server_poll(swg_server *srv, uint64_t ticket, int *state, double *latency_s);
+/* Blocks at most timeout_s seconds; SWG_ERR_NOT_READY on timeout. */
+swg_status swg_server_wait(swg_server *srv, uint64_t ticket, double timeout_s);
+swg_status swg_server_result_info(swg_server *srv, uint64_t ticket, uint64_t *survivors,
+                                  uint64_t *distinct);
+/* Copies the result to host memory (sorted by key when sorted != 0) and frees
+ * it on the device; the ticket is then gone. */
+swg_status swg_server_fetch(swg_server *srv, uint64_t ticket, uint64_t *keys, uint8_t *mult,
+                            uint64_t cap, int sorted, uint64_t *n);
+/* Drops a finished result without copying it. */
+swg_status swg_server_release(swg_server *srv, uint64_t ticket);
+swg_status swg_server_get_stats(swg_server *srv, swg_server_stats *out);
+/* Finishes the batches in flight, drops queued requests and results, frees. */
+void swg_server_free(swg_server *srv);
+
 /* ---- results ---------------------------------------------------------- */
 /* The swg_graph_* result calls below refer to a single-sample build
  * (SWG_ERR_BAD_STATE after a batched build; use swg_batch_* there). */

@@ -67,7 +67,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict[str, Path]:
     jobs.append((OBJ / "noalloc.o", [na, *headers],
                  [nvcc, *ARCH, "-lineinfo", "-Xcompiler", "-fPIC", *common, "-c", str(na), "-o",
                   str(OBJ / "noalloc.o")]))
-    for name in ("api.cpp", "reads.cpp", "writers.cpp"):
+    for name in ("api.cpp", "reads.cpp", "writers.cpp", "server.cpp"):
         src = CSRC / name
         o = OBJ / (name[:-4] + ".o")
         jobs.append((o, [src, *headers], ["g++", "-fPIC", "-pthread", "-Wall", *common,
@@ -85,7 +85,8 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict[str, Path]:
         list(ex.map(lambda j: _run(j[2]), todo))
 
     lib = PKG / "libswapgb.so"
-    lib_objs = [OBJ / n for n in ("kernels.o", "noalloc.o", "api.o", "reads.o", "writers.o")]
+    lib_objs = [OBJ / n for n in ("kernels.o", "noalloc.o", "api.o", "reads.o", "writers.o",
+                                  "server.o")]
     if _stale(lib, lib_objs):
         _run([nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, lib_objs), "-lpthread"])
     synth = PKG / "libswgsynth.so"

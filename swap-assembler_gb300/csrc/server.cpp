@@ -1,0 +1,405 @@
+// Request server: continuous batching of graph builds on one GPU.
+//
+// Clients submit single-sample requests (packed reads in host memory, their
+// own k and cutoff) at any time. Worker threads, each with its own graph
+// handle and CUDA stream, repeatedly take every queued request that fits the
+// device-memory budget (in arrival order) and build them as one batch
+// (swg_batch_build); with two or more workers, batches overlap on the device.
+// Each request's filtered graph is then copied to its own device buffer and
+// stays resident until the client fetches or releases it. Admission: a
+// request is charged an estimated footprint while its batch runs (inputs,
+// table and outputs sized by its k-mer occurrence count, an upper bound on its
+// distinct k-molecules) and its exact result size while resident; a request
+// larger than the whole budget is refused at submission.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "swg_internal.h"
+
+namespace {
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Request {
+    uint64_t ticket = 0;
+    std::vector<uint32_t> packed;
+    std::vector<uint64_t> off;
+    std::vector<uint32_t> len;
+    int k = 0, cutoff = 0;
+    uint64_t occ = 0;
+    uint64_t footprint = 0;
+    int state = SWG_REQ_QUEUED;
+    swg_status status = SWG_OK;
+    std::string error;
+    uint64_t n_out = 0, distinct = 0;
+    unsigned long long *d_keys = nullptr, *d_mult = nullptr;
+    uint64_t resident = 0;
+    double t_submit = 0, t_done = 0;
+};
+
+}  // namespace
+
+struct swg_server {
+    swg_server_opts opts;
+    int device = 0;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Request *> queue;
+    std::unordered_map<uint64_t, Request *> reqs;
+    uint64_t next_ticket = 1;
+    uint64_t reserved = 0;  // in-flight footprints
+    uint64_t resident = 0;  // results waiting to be fetched
+    swg_server_stats st;
+    bool stop = false;
+    std::vector<std::thread> workers;
+    cudaStream_t fetch_stream = nullptr;
+};
+
+namespace {
+
+uint64_t footprint_of(uint64_t reads, uint64_t words, uint64_t occ, double load) {
+    const uint64_t cap = (uint64_t)((double)occ / load) + 2048;
+    return words * 4 + reads * (8 + 4 + 8 + 4) + cap * 16 * 2;
+}
+
+void worker_main(swg_server *srv) {
+    cudaSetDevice(srv->device);
+    swg_graph *g = nullptr;
+    if (swg_graph_create(&g) != SWG_OK) return;
+    cudaStream_t stream = nullptr;
+    cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+    swg_opts o;
+    std::memset(&o, 0, sizeof(o));
+    o.load_factor = srv->opts.load_factor;
+    o.stream = stream;
+    for (;;) {
+        std::vector<Request *> batch;
+        {
+            std::unique_lock<std::mutex> lock(srv->mu);
+            for (;;) {
+                if (srv->stop) break;
+                while (!srv->queue.empty()) {
+                    Request *r = srv->queue.front();
+                    if (srv->reserved + srv->resident + r->footprint > srv->opts.memory_budget)
+                        break;  // waits until memory frees up (arrival order is kept)
+                    srv->queue.pop_front();
+                    srv->reserved += r->footprint;
+                    r->state = SWG_REQ_RUNNING;
+                    batch.push_back(r);
+                    if (srv->opts.max_batch && batch.size() >= srv->opts.max_batch) break;
+                }
+                if (!batch.empty()) break;
+                srv->cv_work.wait(lock);
+            }
+            if (batch.empty()) break;  // stopping
+            srv->st.batches++;
+            srv->st.max_batch_requests = std::max<uint64_t>(srv->st.max_batch_requests, batch.size());
+        }
+        std::vector<swg_sample> samples(batch.size());
+        for (size_t i = 0; i < batch.size(); i++) {
+            Request *r = batch[i];
+            samples[i].packed = r->packed.data();
+            samples[i].n_words = r->packed.size();
+            samples[i].read_off = r->off.data();
+            samples[i].read_len = r->len.data();
+            samples[i].n_reads = r->off.size();
+            samples[i].k = r->k;
+            samples[i].cutoff = r->cutoff;
+        }
+        swg_status bs = swg_batch_build(g, &o, samples.data(), (uint32_t)samples.size());
+        std::string berr = bs ? swg_last_error() : "";
+        std::vector<swg_status> rs(batch.size(), bs);
+        for (size_t i = 0; bs == SWG_OK && i < batch.size(); i++) {
+            Request *r = batch[i];
+            const uint64_t *dk = nullptr, *dm = nullptr;
+            uint64_t n = 0, occ = 0, distinct = 0;
+            swg_batch_device_view(g, (uint32_t)i, &dk, &dm, &n);
+            swg_batch_sample_info(g, (uint32_t)i, &occ, &distinct, nullptr);
+            r->n_out = n;
+            r->distinct = distinct;
+            if (n) {
+                cudaError_t e = cudaMallocAsync(&r->d_keys, n * 8, stream);
+                if (e == cudaSuccess) e = cudaMallocAsync(&r->d_mult, n * 8, stream);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(r->d_keys, dk, n * 8, cudaMemcpyDeviceToDevice, stream);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(r->d_mult, dm, n * 8, cudaMemcpyDeviceToDevice, stream);
+                if (e != cudaSuccess) {
+                    cudaGetLastError();
+                    rs[i] = e == cudaErrorMemoryAllocation ? SWG_ERR_OOM : SWG_ERR_CUDA;
+                    r->error = cudaGetErrorString(e);
+                }
+            }
+        }
+        cudaStreamSynchronize(stream);
+        {
+            std::lock_guard<std::mutex> lock(srv->mu);
+            const double t = now_s();
+            for (size_t i = 0; i < batch.size(); i++) {
+                Request *r = batch[i];
+                srv->reserved -= r->footprint;
+                r->t_done = t;
+                r->status = rs[i];
+                // the inputs are no longer needed
+                std::vector<uint32_t>().swap(r->packed);
+                std::vector<uint64_t>().swap(r->off);
+                std::vector<uint32_t>().swap(r->len);
+                if (rs[i] == SWG_OK) {
+                    r->state = SWG_REQ_DONE;
+                    r->resident = r->n_out * 16;
+                    srv->resident += r->resident;
+                    srv->st.completed++;
+                } else {
+                    r->state = SWG_REQ_FAILED;
+                    if (r->error.empty()) r->error = berr;
+                    srv->st.failed++;
+                }
+            }
+        }
+        srv->cv_done.notify_all();
+        srv->cv_work.notify_all();
+    }
+    cudaStreamSynchronize(stream);
+    cudaStreamDestroy(stream);
+    swg_graph_free(g);
+}
+
+void free_result(swg_server *srv, Request *r) {
+    if (r->d_keys) cudaFreeAsync(r->d_keys, srv->fetch_stream);
+    if (r->d_mult) cudaFreeAsync(r->d_mult, srv->fetch_stream);
+    r->d_keys = r->d_mult = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+swg_status swg_server_create(const swg_server_opts *o, swg_server **out) {
+    if (!out) return SWG_ERR_BAD_INPUT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        swg::set_error("no CUDA device visible");
+        return SWG_ERR_NO_DEVICE;
+    }
+    swg_server *srv = new (std::nothrow) swg_server;
+    if (!srv) return SWG_ERR_OOM;
+    std::memset(&srv->opts, 0, sizeof(srv->opts));
+    if (o) srv->opts = *o;
+    if (!srv->opts.memory_budget) srv->opts.memory_budget = 150ull << 30;
+    if (!srv->opts.workers) srv->opts.workers = 2;
+    if (srv->opts.load_factor <= 0 || srv->opts.load_factor > 0.9) srv->opts.load_factor = 0.6;
+    std::memset(&srv->st, 0, sizeof(srv->st));
+    cudaGetDevice(&srv->device);
+    if (cudaStreamCreateWithFlags(&srv->fetch_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete srv;
+        swg::set_error("stream creation failed");
+        return SWG_ERR_CUDA;
+    }
+    for (uint32_t i = 0; i < srv->opts.workers; i++) srv->workers.emplace_back(worker_main, srv);
+    *out = srv;
+    return SWG_OK;
+}
+
+swg_status swg_server_submit(swg_server *srv, const swg_sample *req, uint64_t *ticket) {
+    if (!srv || !req || !ticket) return SWG_ERR_BAD_INPUT;
+    if (req->k < 1 || req->k > 31) {
+        swg::set_error("k must be in 1..31");
+        return SWG_ERR_BAD_INPUT;
+    }
+    if (req->n_reads && (!req->packed || !req->read_off || !req->read_len)) {
+        swg::set_error("NULL read buffer");
+        return SWG_ERR_BAD_INPUT;
+    }
+    const double t0 = now_s();
+    Request *r = new (std::nothrow) Request;
+    if (!r) return SWG_ERR_OOM;
+    try {
+        r->packed.assign(req->packed, req->packed + req->n_words);
+        r->off.assign(req->read_off, req->read_off + req->n_reads);
+        r->len.assign(req->read_len, req->read_len + req->n_reads);
+    } catch (...) {
+        delete r;
+        return SWG_ERR_OOM;
+    }
+    r->k = req->k;
+    r->cutoff = req->cutoff;
+    for (uint64_t i = 0; i < req->n_reads; i++)
+        if (req->read_len[i] >= (uint32_t)req->k) r->occ += req->read_len[i] - req->k + 1;
+    r->footprint = footprint_of(req->n_reads, req->n_words, r->occ, srv->opts.load_factor);
+    r->t_submit = t0;
+    std::lock_guard<std::mutex> lock(srv->mu);
+    if (r->footprint > srv->opts.memory_budget) {
+        srv->st.rejected++;
+        delete r;
+        swg::set_error("request footprint exceeds the server's memory budget");
+        return SWG_ERR_ADMISSION;
+    }
+    if (srv->stop) {
+        delete r;
+        return SWG_ERR_BAD_STATE;
+    }
+    r->ticket = srv->next_ticket++;
+    srv->reqs[r->ticket] = r;
+    srv->queue.push_back(r);
+    srv->st.submitted++;
+    *ticket = r->ticket;
+    srv->cv_work.notify_one();
+    return SWG_OK;
+}
+
+swg_status swg_server_poll(swg_server *srv, uint64_t ticket, int *state, double *latency_s) {
+    if (!srv) return SWG_ERR_BAD_INPUT;
+    std::lock_guard<std::mutex> lock(srv->mu);
+    auto it = srv->reqs.find(ticket);
+    if (it == srv->reqs.end()) return SWG_ERR_BAD_INPUT;
+    Request *r = it->second;
+    if (state) *state = r->state;
+    if (latency_s) *latency_s = r->t_done > 0 ? r->t_done - r->t_submit : now_s() - r->t_submit;
+    return SWG_OK;
+}
+
+swg_status swg_server_wait(swg_server *srv, uint64_t ticket, double timeout_s) {
+    if (!srv) return SWG_ERR_BAD_INPUT;
+    std::unique_lock<std::mutex> lock(srv->mu);
+    auto it = srv->reqs.find(ticket);
+    if (it == srv->reqs.end()) return SWG_ERR_BAD_INPUT;
+    Request *r = it->second;
+    const auto until = std::chrono::steady_clock::now() +
+                       std::chrono::duration_cast<std::chrono::steady_clock::duration>(
+                           std::chrono::duration<double>(timeout_s));
+    while (r->state == SWG_REQ_QUEUED || r->state == SWG_REQ_RUNNING) {
+        if (srv->cv_done.wait_until(lock, until) == std::cv_status::timeout &&
+            (r->state == SWG_REQ_QUEUED || r->state == SWG_REQ_RUNNING))
+            return SWG_ERR_NOT_READY;
+    }
+    if (r->state == SWG_REQ_FAILED) {
+        swg::set_error(r->error);
+        return r->status;
+    }
+    return SWG_OK;
+}
+
+swg_status swg_server_result_info(swg_server *srv, uint64_t ticket, uint64_t *survivors,
+                                  uint64_t *distinct) {
+    if (!srv) return SWG_ERR_BAD_INPUT;
+    std::lock_guard<std::mutex> lock(srv->mu);
+    auto it = srv->reqs.find(ticket);
+    if (it == srv->reqs.end()) return SWG_ERR_BAD_INPUT;
+    Request *r = it->second;
+    if (r->state == SWG_REQ_FAILED) return r->status;
+    if (r->state != SWG_REQ_DONE) return SWG_ERR_NOT_READY;
+    if (survivors) *survivors = r->n_out;
+    if (distinct) *distinct = r->distinct;
+    return SWG_OK;
+}
+
+swg_status swg_server_fetch(swg_server *srv, uint64_t ticket, uint64_t *keys, uint8_t *mult,
+                            uint64_t cap, int sorted, uint64_t *n) {
+    if (!srv) return SWG_ERR_BAD_INPUT;
+    Request *r = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(srv->mu);
+        auto it = srv->reqs.find(ticket);
+        if (it == srv->reqs.end()) return SWG_ERR_BAD_INPUT;
+        r = it->second;
+        if (r->state == SWG_REQ_FAILED) {
+            swg::set_error(r->error);
+            return r->status;
+        }
+        if (r->state != SWG_REQ_DONE) return SWG_ERR_NOT_READY;
+        if (n) *n = r->n_out;
+        if (cap < r->n_out) {
+            swg::set_error("output capacity smaller than the survivor count");
+            return SWG_ERR_BAD_INPUT;
+        }
+        srv->reqs.erase(it);  // the caller owns the result from here
+    }
+    swg_status st = SWG_OK;
+    cudaSetDevice(srv->device);
+    if (r->n_out) {
+        std::vector<uint64_t> k(r->n_out), m(r->n_out);
+        cudaError_t e = cudaMemcpyAsync(k.data(), r->d_keys, r->n_out * 8, cudaMemcpyDeviceToHost,
+                                        srv->fetch_stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(m.data(), r->d_mult, r->n_out * 8, cudaMemcpyDeviceToHost,
+                                srv->fetch_stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(srv->fetch_stream);
+        if (e != cudaSuccess) {
+            swg::set_error(std::string("fetch: ") + cudaGetErrorString(e));
+            st = SWG_ERR_CUDA;
+        } else {
+            if (sorted) swg::sort_records(k.data(), m.data(), r->n_out);
+            if (keys) std::memcpy(keys, k.data(), r->n_out * 8);
+            if (mult) std::memcpy(mult, m.data(), r->n_out * 8);
+        }
+    }
+    free_result(srv, r);
+    {
+        std::lock_guard<std::mutex> lock(srv->mu);
+        srv->resident -= r->resident;
+    }
+    srv->cv_work.notify_all();
+    delete r;
+    return st;
+}
+
+swg_status swg_server_release(swg_server *srv, uint64_t ticket) {
+    if (!srv) return SWG_ERR_BAD_INPUT;
+    Request *r = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(srv->mu);
+        auto it = srv->reqs.find(ticket);
+        if (it == srv->reqs.end()) return SWG_ERR_BAD_INPUT;
+        r = it->second;
+        if (r->state == SWG_REQ_QUEUED || r->state == SWG_REQ_RUNNING) return SWG_ERR_NOT_READY;
+        srv->reqs.erase(it);
+        srv->resident -= r->resident;
+    }
+    cudaSetDevice(srv->device);
+    free_result(srv, r);
+    srv->cv_work.notify_all();
+    delete r;
+    return SWG_OK;
+}
+
+swg_status swg_server_get_stats(swg_server *srv, swg_server_stats *out) {
+    if (!srv || !out) return SWG_ERR_BAD_INPUT;
+    std::lock_guard<std::mutex> lock(srv->mu);
+    *out = srv->st;
+    out->queued = srv->queue.size();
+    out->bytes_reserved = srv->reserved;
+    out->bytes_resident = srv->resident;
+    return SWG_OK;
+}
+
+void swg_server_free(swg_server *srv) {
+    if (!srv) return;
+    {
+        std::lock_guard<std::mutex> lock(srv->mu);
+        srv->stop = true;
+    }
+    srv->cv_work.notify_all();
+    for (auto &t : srv->workers) t.join();
+    cudaSetDevice(srv->device);
+    for (auto &kv : srv->reqs) {
+        free_result(srv, kv.second);
+        delete kv.second;
+    }
+    cudaStreamSynchronize(srv->fetch_stream);
+    cudaStreamDestroy(srv->fetch_stream);
+    delete srv;
+}
+
+}  // extern "C"

@@ -69,6 +69,22 @@ class Sample(C.Structure):
                 ("cutoff", C.c_int)]
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("memory_budget", C.c_uint64), ("workers", C.c_uint32), ("max_batch", C.c_uint32),
+                ("load_factor", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("submitted", "completed", "failed", "rejected", "batches",
+                                          "max_batch_requests", "queued", "bytes_reserved",
+                                          "bytes_resident")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
 _lib = None
 
 
@@ -113,6 +129,15 @@ def lib() -> C.CDLL:
             "swg_batch_sample_info": (i32, [P, C.c_uint32, pu64, pu64, pu64]),
             "swg_batch_device_view": (i32, [P, C.c_uint32, C.POINTER(P), C.POINTER(P), pu64]),
             "swg_batch_copy_out": (i32, [P, C.c_uint32, P, P, u64, i32, pu64]),
+            "swg_server_create": (i32, [C.POINTER(ServerOpts), C.POINTER(P)]),
+            "swg_server_submit": (i32, [P, C.POINTER(Sample), pu64]),
+            "swg_server_poll": (i32, [P, u64, C.POINTER(i32), C.POINTER(C.c_double)]),
+            "swg_server_wait": (i32, [P, u64, C.c_double]),
+            "swg_server_result_info": (i32, [P, u64, pu64, pu64]),
+            "swg_server_fetch": (i32, [P, u64, P, P, u64, i32, pu64]),
+            "swg_server_release": (i32, [P, u64]),
+            "swg_server_get_stats": (i32, [P, C.POINTER(ServerStats)]),
+            "swg_server_free": (None, [P]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -389,3 +414,60 @@ def synth_fasta_file(path: str, **kw) -> int:
     if n < 0:
         raise RuntimeError("synthetic read generation failed")
     return n
+
+
+class Server:
+    """Request server (continuous batching); results stay on the device until
+    fetched or released."""
+
+    def __init__(self, memory_budget: int = 0, workers: int = 0, max_batch: int = 0,
+                 load_factor: float = 0.0):
+        h = C.c_void_p()
+        o = ServerOpts(memory_budget, workers, max_batch, load_factor)
+        _check(lib().swg_server_create(C.byref(o), C.byref(h)), "swg_server_create")
+        self._h = h
+
+    def close(self) -> None:
+        if self._h:
+            lib().swg_server_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, reads: Reads, k: int, cutoff: int) -> int:
+        smp = Sample(_ptr(reads.packed), reads.n_words, _ptr(reads.off), _ptr(reads.len),
+                     reads.n_reads, k, cutoff)
+        t = C.c_uint64()
+        _check(lib().swg_server_submit(self._h, C.byref(smp), C.byref(t)), "swg_server_submit")
+        return t.value
+
+    def poll(self, ticket: int) -> tuple[int, float]:
+        st, lat = C.c_int(), C.c_double()
+        _check(lib().swg_server_poll(self._h, ticket, C.byref(st), C.byref(lat)), "swg_server_poll")
+        return st.value, lat.value
+
+    def wait(self, ticket: int, timeout_s: float = 60.0) -> None:
+        _check(lib().swg_server_wait(self._h, ticket, timeout_s), "swg_server_wait")
+
+    def fetch(self, ticket: int, sorted: bool = True) -> tuple[np.ndarray, np.ndarray]:
+        n, d = C.c_uint64(), C.c_uint64()
+        _check(lib().swg_server_result_info(self._h, ticket, C.byref(n), C.byref(d)),
+               "swg_server_result_info")
+        keys = np.zeros(n.value, dtype=np.uint64)
+        mult = np.zeros((n.value, 8), dtype=np.uint8)
+        got = C.c_uint64()
+        _check(lib().swg_server_fetch(self._h, ticket, _ptr(keys), _ptr(mult), n.value, int(sorted),
+                                      C.byref(got)), "swg_server_fetch")
+        return keys, mult
+
+    def release(self, ticket: int) -> None:
+        _check(lib().swg_server_release(self._h, ticket), "swg_server_release")
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(lib().swg_server_get_stats(self._h, C.byref(st)), "swg_server_get_stats")
+        return st.as_dict()
