@@ -423,33 +423,52 @@ def main() -> int:
     survivors, distinct = g.size(), g.distinct()
 
     # ---- end to end through the C ABI on pinned host buffers ----
-    h_packed = torch.from_numpy(reads.packed.view(np.int32).copy()).pin_memory()
-    h_off = torch.from_numpy(reads.off.view(np.int64).copy()).pin_memory()
-    h_len = torch.from_numpy(reads.len.view(np.int32).copy()).pin_memory()
+    lib = swapgb.lib()
     h_keys = torch.empty(max(survivors, 1) + (1 << 20), dtype=torch.int64).pin_memory()
     h_mult = torch.empty_like(h_keys)
     g2 = swapgb.Graph()
-    lib = swapgb.lib()
 
-    def e2e_step() -> int:
-        swapgb._check(lib.swg_graph_build(g2._h, swapgb.C.byref(opts), h_packed.data_ptr(),
-                                          h_packed.numel(), h_off.data_ptr(), h_len.data_ptr(),
-                                          h_off.numel()), "swg_graph_build")
+    def copy_out_e2e() -> int:
         n = swapgb.C.c_uint64()
         swapgb._check(lib.swg_graph_copy_out(g2._h, h_keys.data_ptr(), h_mult.data_ptr(),
                                              h_keys.numel(), 0, swapgb.C.byref(n)), "copy_out")
         return n.value
 
-    for _ in range(2):
-        e2e_step()
-    torch.cuda.synchronize()
-    e2e_t = []
-    for _ in range(max(3, min(args.steps, 10))):
-        t0 = time.perf_counter()
-        n_e2e = e2e_step()
-        e2e_t.append(time.perf_counter() - t0)
-    e2e_s = max_over_ranks(statistics.mean(e2e_t), world, dev)
-    h2d = h_packed.numel() * 4 + h_off.numel() * 8 + h_len.numel() * 4
+    # (1) the FASTA text as a user has it: copied to the device, framed and
+    # packed there, built, filtered graph copied back
+    h_text = torch.from_numpy(np.frombuffer(text, dtype=np.uint8).copy()).pin_memory()
+
+    def e2e_fasta() -> int:
+        swapgb._check(lib.swg_graph_build_fasta(g2._h, swapgb.C.byref(opts), h_text.data_ptr(),
+                                                h_text.numel()), "swg_graph_build_fasta")
+        return copy_out_e2e()
+
+    # (2) host packed reads (swg_graph_build)
+    h_packed = torch.from_numpy(reads.packed.view(np.int32).copy()).pin_memory()
+    h_off = torch.from_numpy(reads.off.view(np.int64).copy()).pin_memory()
+    h_len = torch.from_numpy(reads.len.view(np.int32).copy()).pin_memory()
+
+    def e2e_packed() -> int:
+        swapgb._check(lib.swg_graph_build(g2._h, swapgb.C.byref(opts), h_packed.data_ptr(),
+                                          h_packed.numel(), h_off.data_ptr(), h_len.data_ptr(),
+                                          h_off.numel()), "swg_graph_build")
+        return copy_out_e2e()
+
+    def timed(fn) -> tuple[float, int]:
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(max(3, min(args.steps, 10))):
+            t0 = time.perf_counter()
+            n = fn()
+            ts.append(time.perf_counter() - t0)
+        return max_over_ranks(statistics.mean(ts), world, dev), n
+
+    e2e_s, n_e2e = timed(e2e_fasta)
+    e2e_p_s, _ = timed(e2e_packed)
+    h2d = h_text.numel()
+    h2d_p = h_packed.numel() * 4 + h_off.numel() * 8 + h_len.numel() * 4
     d2h = n_e2e * 16
 
     # ---- rooflines ----
@@ -513,7 +532,12 @@ def main() -> int:
             "data": "synthetic (seeded generator, no dataset)", "config": config_dict(args.algo, args.order),
             "e2e": {"value": aggregate_value(n_bases, world, e2e_s * 1e3), "unit": "bases/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "path": "swg_graph_build on pinned host packed reads + swg_graph_copy_out"},
+                    "path": "swg_graph_build_fasta on the pinned FASTA text (framing + packing on "
+                            "the device) + swg_graph_copy_out"},
+            "e2e_packed": {"value": aggregate_value(n_bases, world, e2e_p_s * 1e3),
+                           "unit": "bases/s", "h2d_bytes_per_step": h2d_p,
+                           "d2h_bytes_per_step": d2h,
+                           "path": "swg_graph_build on pinned host packed reads + swg_graph_copy_out"},
             "gpu_launches": launches,
             "build": dict(info, phase_ms_mean=mean_ms),
             "roofline": roofline,

@@ -139,6 +139,11 @@ swg_status swg_graph_build(swg_graph *g, const swg_opts *o, const uint32_t *pack
 swg_status swg_graph_build_device(swg_graph *g, const swg_opts *o, const uint32_t *d_packed,
                                   uint64_t n_words, const uint64_t *d_read_off,
                                   const uint32_t *d_read_len, uint64_t n_reads);
+/* Build from a FASTA held in HOST memory, framed and packed ON THE DEVICE: the
+ * text is copied to the GPU, lines are found and paired there with the same
+ * framing as swg_reads_from_fasta (same errors), reads are 2-bit packed, then
+ * built as swg_graph_build_device. */
+swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *text, uint64_t len);
 /* Convenience: create + build from host packed reads. */
 swg_status swg_build(const swg_opts *o, const uint32_t *packed, uint64_t n_words,
                      const uint64_t *read_off, const uint32_t *read_len, uint64_t n_reads,
@@ -276,12 +281,34 @@ swg_status swg_build_device_noalloc(const swg_opts *o, const uint32_t *d_packed,
                                     uint64_t n_reads, uint64_t *d_keys_out, uint64_t *d_mult_out,
                                     uint64_t out_cap, uint64_t *n_out);
 
+/* ---- autotuner ---------------------------------------------------------- */
+/* Times trial builds of a sample (device packed reads, as for
+ * swg_graph_build_device) for each candidate table load factor and counting
+ * scheme (direct table in input order, direct table in minimizer order,
+ * hash-partitioned slices) and appends the fastest to a cache file as one
+ * JSON line keyed by (k, read-length band of read_len_hint). */
+typedef struct swg_tuning {
+    double load_factor;
+    int algorithm;
+    int read_order;
+    float ms;
+} swg_tuning;
+
+swg_status swg_autotune(const swg_opts *base, const uint32_t *d_packed, uint64_t n_words,
+                        const uint64_t *d_read_off, const uint32_t *d_read_len, uint64_t n_reads,
+                        uint32_t read_len_hint, const char *cache_path, swg_tuning *best);
+/* Sets o's load factor, algorithm and read order from the cache entry for
+ * (k, band of read_len); SWG_ERR_NOT_READY when the cache has none. */
+swg_status swg_autotune_apply(const char *cache_path, int k, uint32_t read_len, swg_opts *o);
+
 /* ---- roofline probe ----------------------------------------------------- */
 /* Random-access throughput on this GPU: n_ops operations at uniformly random
  * 16-byte-aligned addresses of a table of table_bytes bytes (allocated and
  * freed inside). kind: 0 = 32-bit atomicAdd (no return), 1 = 64-bit CAS,
  * 2 = 128-bit CAS, 3 = 16-byte load, 4 = 16-byte load + 128-bit CAS on the
- * same address. Writes operations per second (device time). */
+ * same address, 5 = as 3 with four independent loads in flight per thread,
+ * 6 = as 4 with two independent chains per thread. Writes accesses (kinds
+ * 5/6: loads, load+CAS pairs) per second (device time). */
 swg_status swg_probe_random_access(int kind, uint64_t table_bytes, uint64_t n_ops, void *stream,
                                    double *ops_per_s);
 

@@ -54,7 +54,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict[str, Path]:
     nvcc = str(cuda / "bin" / "nvcc")
     OBJ.mkdir(parents=True, exist_ok=True)
     (PKG / "bin").mkdir(exist_ok=True)
-    headers = [INCLUDE / "swapgb.h", CSRC / "swg_internal.h"]
+    headers = [INCLUDE / "swapgb.h", CSRC / "swg_internal.h", CSRC / "dev_util.cuh"]
     common = ["-O3", "-std=c++17", "-I" + str(INCLUDE), "-I" + str(CSRC)]
     jobs = []
     cu = CSRC / "kernels.cu"
@@ -63,11 +63,15 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict[str, Path]:
     if ptxas_info:
         cu_cmd.insert(1, "-Xptxas=-v")
     jobs.append((OBJ / "kernels.o", [cu, *headers], cu_cmd))
+    fr = CSRC / "framing.cu"
+    jobs.append((OBJ / "framing.o", [fr, *headers],
+                 [nvcc, *ARCH, "-lineinfo", "-Xcompiler", "-fPIC", *common, "-c", str(fr), "-o",
+                  str(OBJ / "framing.o")]))
     na = CSRC / "noalloc.cu"
     jobs.append((OBJ / "noalloc.o", [na, *headers],
                  [nvcc, *ARCH, "-lineinfo", "-Xcompiler", "-fPIC", *common, "-c", str(na), "-o",
                   str(OBJ / "noalloc.o")]))
-    for name in ("api.cpp", "reads.cpp", "writers.cpp", "server.cpp"):
+    for name in ("api.cpp", "reads.cpp", "writers.cpp", "server.cpp", "autotune.cpp"):
         src = CSRC / name
         o = OBJ / (name[:-4] + ".o")
         jobs.append((o, [src, *headers], ["g++", "-fPIC", "-pthread", "-Wall", *common,
@@ -85,8 +89,8 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict[str, Path]:
         list(ex.map(lambda j: _run(j[2]), todo))
 
     lib = PKG / "libswapgb.so"
-    lib_objs = [OBJ / n for n in ("kernels.o", "noalloc.o", "api.o", "reads.o", "writers.o",
-                                  "server.o")]
+    lib_objs = [OBJ / n for n in ("kernels.o", "framing.o", "noalloc.o", "api.o", "reads.o",
+                                  "writers.o", "server.o", "autotune.o")]
     if _stale(lib, lib_objs):
         _run([nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, lib_objs), "-lpthread"])
     synth = PKG / "libswgsynth.so"

@@ -91,6 +91,11 @@ struct swg_graph {
     uint64_t poff_cap = 0;
     uint32_t *d_plen = nullptr;
     uint64_t plen_cap = 0;
+    // device framing workspace
+    unsigned char *d_text = nullptr;
+    uint64_t text_cap = 0;
+    uint64_t *d_fw = nullptr;  // chunk counts | scan scratch | newline positions | records x3
+    uint64_t fw_cap = 0;
     // batched build (n_samples == 0 after a single-sample build)
     uint32_t n_samples = 0;
     std::vector<uint64_t> s_tbase, s_tcap, s_out, s_distinct, s_occ;
@@ -784,6 +789,8 @@ void swg_graph_free(swg_graph *g) {
     cudaFree(g->d_ctl);
     cudaFree(g->d_part);
     cudaFree(g->d_minhash);
+    cudaFree(g->d_text);
+    cudaFree(g->d_fw);
     cudaFree(g->d_segs);
     cudaFree(g->d_read_seg);
     cudaFree(g->d_seg_counts);
@@ -836,6 +843,85 @@ swg_status swg_graph_build(swg_graph *g, const swg_opts *o, const uint32_t *pack
                  "copy read lengths");
     }
     return build_impl(g, o, g->d_packed, n_words, g->d_off, g->d_len, n_reads);
+}
+
+swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *text, uint64_t len) {
+    if (!g) return SWG_ERR_BAD_INPUT;
+    swg_status st = check_opts(o);
+    if (st) return st;
+    if (!text || len == 0) {
+        swg::set_error("empty FASTA input");
+        return SWG_ERR_BAD_INPUT;
+    }
+    const char *first = (const char *)std::memchr(text, '>', len);
+    if (!first) {
+        swg::set_error("no '>' record start in the input");
+        return SWG_ERR_BAD_INPUT;
+    }
+    if (text[len - 1] != '\n') {
+        swg::set_error("the last record is not terminated by a newline");
+        return SWG_ERR_BAD_INPUT;
+    }
+    const uint64_t n = len - (uint64_t)(first - text);
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    cudaStream_t s = stream_of(g, o);
+    if ((st = ensure(&g->d_text, &g->text_cap, n + 16, "FASTA text"))) return st;
+    SWG_CUDA(cudaMemcpyAsync(g->d_text, first, n, cudaMemcpyHostToDevice, s), "copy FASTA text");
+    const uint64_t nc = swg::framing_chunks(n);
+    // workspace: counts [nc] | scratch [S] | total [2] | newline positions [nl] | records x3
+    const uint64_t S = std::max(swg::gscan_scratch(nc), swg::gscan_scratch(n / 2 + 1));
+    uint64_t want = nc + S + 2;
+    if ((st = ensure(&g->d_fw, &g->fw_cap, want, "framing workspace"))) return st;
+    uint64_t *counts = g->d_fw, *scratch = counts + nc, *tot = scratch + S;
+    SWG_CUDA(cudaMemsetAsync(g->d_ctl, 0, sizeof(unsigned), s), "clear flag");
+    int launches = swg::launch_nl_count(g->d_text, n, counts, &g->d_ctl->status, s);
+    launches += swg::launch_gscan(counts, counts, nc, scratch, tot, s);
+    uint64_t h[2] = {0, 0};
+    unsigned nul = 0;
+    SWG_CUDA(cudaMemcpyAsync(h, tot, 8, cudaMemcpyDeviceToHost, s), "read newline count");
+    SWG_CUDA(cudaMemcpyAsync(&nul, &g->d_ctl->status, 4, cudaMemcpyDeviceToHost, s), "read flag");
+    SWG_CUDA(cudaStreamSynchronize(s), "framing count");
+    if (nul) {
+        swg::set_error("NUL byte in the FASTA input");
+        return SWG_ERR_BAD_INPUT;
+    }
+    const uint64_t NL = h[0];
+    if (NL & 1) {
+        swg::set_error("the last record has a header line but no sequence line");
+        return SWG_ERR_BAD_INPUT;
+    }
+    const uint64_t R = NL / 2;
+    want = nc + S + 2 + NL + 3 * std::max<uint64_t>(R, 1);
+    if (want > g->fw_cap) {  // grow, keeping the chunk bases computed above
+        uint64_t *nw = nullptr;
+        SWG_CUDA(cudaMalloc(&nw, want * 8), "framing workspace");
+        SWG_CUDA(cudaMemcpyAsync(nw, g->d_fw, (nc + S + 2) * 8, cudaMemcpyDeviceToDevice, s),
+                 "copy framing workspace");
+        SWG_CUDA(cudaStreamSynchronize(s), "framing workspace");
+        cudaFree(g->d_fw);
+        g->d_fw = nw;
+        g->fw_cap = want;
+        counts = g->d_fw;
+        scratch = counts + nc;
+        tot = scratch + S;
+    }
+    uint64_t *nl = tot + 2, *keep = nl + NL, *words = keep + R, *idx = words + R;
+    launches += swg::launch_nl_pos(g->d_text, n, counts, nl, s);
+    launches += swg::launch_rec_len(nl, R, o->k, keep, words, s);
+    launches += swg::launch_gscan(keep, idx, R, scratch, tot, s);
+    launches += swg::launch_gscan(words, words, R, scratch, tot + 1, s);
+    SWG_CUDA(cudaGetLastError(), "framing launch");
+    SWG_CUDA(cudaMemcpyAsync(h, tot, 16, cudaMemcpyDeviceToHost, s), "read framing totals");
+    SWG_CUDA(cudaStreamSynchronize(s), "framing scan");
+    const uint64_t n_reads = h[0], n_words = h[1];
+    if ((st = ensure(&g->d_packed, &g->packed_cap, n_words + 4, "packed reads"))) return st;
+    if ((st = ensure_reads(g, n_reads))) return st;
+    launches += swg::launch_rec_pack(g->d_text, nl, R, o->k, idx, words, g->d_off, g->d_len,
+                                     g->d_packed, s);
+    SWG_CUDA(cudaGetLastError(), "pack launch");
+    st = build_impl(g, o, g->d_packed, n_words, g->d_off, g->d_len, n_reads);
+    if (st == SWG_OK) g->launches += launches;
+    return st;
 }
 
 swg_status swg_build(const swg_opts *o, const uint32_t *packed, uint64_t n_words,
@@ -1068,12 +1154,13 @@ swg_status swg_graph_build_info(const swg_graph *g, swg_build_info *info) {
 
 swg_status swg_probe_random_access(int kind, uint64_t table_bytes, uint64_t n_ops, void *stream,
                                    double *ops_per_s) {
-    if (!ops_per_s || kind < 0 || kind > 4 || n_ops == 0 || table_bytes < 4096)
+    if (!ops_per_s || kind < 0 || kind > 6 || n_ops == 0 || table_bytes < 4096)
         return SWG_ERR_BAD_INPUT;
     float ms = 0;
     cudaError_t e = swg::run_probe(kind, table_bytes, n_ops, (cudaStream_t)stream, &ms);
     if (e != cudaSuccess) return cuda_fail(e, "random-access probe");
-    *ops_per_s = ms > 0 ? (double)n_ops / (ms * 1e-3) : 0;
+    const double per = kind == 5 ? 4.0 : (kind == 6 ? 2.0 : 1.0);  // accesses per operation
+    *ops_per_s = ms > 0 ? per * (double)n_ops / (ms * 1e-3) : 0;
     return SWG_OK;
 }
 

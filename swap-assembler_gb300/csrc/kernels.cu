@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "dev_util.cuh"
 #include "swg_internal.h"
 
 namespace swg {
@@ -165,35 +166,6 @@ __device__ __forceinline__ unsigned insert_or_update(Entry *__restrict__ table, 
 }
 
 // ---------------------------------------------------------------------
-// Block-wide exclusive scan of one uint64 per thread (blockDim = NT).
-template <int NT>
-__device__ __forceinline__ uint64_t block_exclusive_scan(uint64_t v, uint64_t *warp_buf,
-                                                         uint64_t *total) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint64_t x = v;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const uint64_t y = __shfl_up_sync(kFull, x, d);
-        if (lane >= d) x += y;
-    }
-    if (lane == 31) warp_buf[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        uint64_t w = lane < NT / 32 ? warp_buf[lane] : 0;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint64_t y = __shfl_up_sync(kFull, w, d);
-            if (lane >= d) w += y;
-        }
-        if (lane < NT / 32) warp_buf[lane] = w;
-    }
-    __syncthreads();
-    const uint64_t warp_prefix = warp ? warp_buf[warp - 1] : 0;
-    if (total) *total = warp_buf[NT / 32 - 1];
-    __syncthreads();
-    return warp_prefix + x - v;
-}
-
 // ---------------------------------------------------------------------
 // Occurrence prefix: occ_prefix[r] = sum_{q<r} max(0, len[q]-k+1).
 __global__ void __launch_bounds__(kScanBlock) k_scan_reduce(BuildArgs a) {
@@ -992,9 +964,27 @@ __global__ void __launch_bounds__(256) k_probe(int kind, Entry *table, uint64_t 
                 acc += v.x ^ v.y;
                 break;
             }
-            default: {
+            case 4: {
                 const ulonglong2 v = ld_relaxed16(e);
                 acc += cas128(e, v.x, v.y, v.x, v.y + 1).y;
+                break;
+            }
+            case 5: {  // four independent 16-byte loads in flight
+                const uint64_t r2 = r * 0x9e3779b97f4a7c15ull, r3 = r2 * 0x9e3779b97f4a7c15ull,
+                               r4 = r3 * 0x9e3779b97f4a7c15ull;
+                const ulonglong2 a0 = ld_relaxed16(e);
+                const ulonglong2 a1 = ld_relaxed16(table + __umul64hi(r2, n16));
+                const ulonglong2 a2 = ld_relaxed16(table + __umul64hi(r3, n16));
+                const ulonglong2 a3 = ld_relaxed16(table + __umul64hi(r4, n16));
+                acc += a0.x ^ a1.y ^ a2.x ^ a3.y;
+                break;
+            }
+            default: {  // two independent load + CAS chains in flight
+                Entry *e2 = table + __umul64hi(r * 0x9e3779b97f4a7c15ull, n16);
+                const ulonglong2 v = ld_relaxed16(e);
+                const ulonglong2 w = ld_relaxed16(e2);
+                acc += cas128(e, v.x, v.y, v.x, v.y + 1).y;
+                acc += cas128(e2, w.x, w.y, w.x, w.y + 1).y;
                 break;
             }
         }

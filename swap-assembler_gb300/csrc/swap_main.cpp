@@ -15,6 +15,7 @@
 #include <sys/stat.h>
 #include <sys/types.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -101,22 +102,35 @@ int main(int argc, char **argv) {
     std::printf("Runing command: %s -k %d -c %d -i %s -o %s\n", argv[0], k, c, in.c_str(), out.c_str());
 
     const double t0 = now_s();
-    swg_reads *reads = nullptr;
-    swg_status st = swg_reads_from_fasta_file(in.c_str(), k, &reads);
-    if (st) return fail(st, "reading the FASTA input");
+    std::string text;
+    {
+        FILE *fp = std::fopen(in.c_str(), "rb");
+        if (!fp) {
+            std::printf("Error: cannot open %s\n", in.c_str());
+            return 1;
+        }
+        std::fseek(fp, 0, SEEK_END);
+        const long long sz = ftello(fp);
+        std::fseek(fp, 0, SEEK_SET);
+        text.resize((size_t)std::max(0LL, sz));
+        const size_t got = sz > 0 ? std::fread(&text[0], 1, (size_t)sz, fp) : 0;
+        std::fclose(fp);
+        if ((long long)got != sz) {
+            std::printf("Error: short read from %s\n", in.c_str());
+            return 1;
+        }
+    }
     const double t1 = now_s();
-    const uint32_t *packed;
-    const uint64_t *off;
-    const uint32_t *len;
-    uint64_t nw, nr, nb;
-    swg_reads_view(reads, &packed, &nw, &off, &len, &nr, &nb);
     swg_opts o;
     std::memset(&o, 0, sizeof(o));
     o.k = k;
     o.cutoff = c;
     swg_graph *g = nullptr;
-    st = swg_build(&o, packed, nw, off, len, nr, &g);
-    swg_reads_free(reads);
+    swg_status st = swg_graph_create(&g);
+    if (st) return fail(st, "creating the graph");
+    // framing, packing and counting all run on the GPU
+    st = swg_graph_build_fasta(g, &o, text.data(), text.size());
+    std::string().swap(text);
     if (st) return fail(st, "building the k-mer graph");
     const double t2 = now_s();
     int64_t stats[5];
@@ -136,8 +150,8 @@ int main(int argc, char **argv) {
     swg_graph_last_timings(g, ms, &launches);
     FILE *lf = std::fopen((out + "/logtime.txt").c_str(), "w");
     if (lf) {
-        std::fprintf(lf, "Time spend in Geting Reads %.5f\n", t1 - t0);
-        std::fprintf(lf, "Time spend in Constructing Graph %.5f (device %.5f: estimate %.5f, clear %.5f, count %.5f, cutoff %.5f)\n",
+        std::fprintf(lf, "Time spend in Geting Reads (file read) %.5f\n", t1 - t0);
+        std::fprintf(lf, "Time spend in Constructing Graph %.5f (framing on the device; build %.5f: sizing %.5f, clear %.5f, count %.5f, cutoff %.5f)\n",
                      t2 - t1, ms[4] * 1e-3, ms[0] * 1e-3, ms[1] * 1e-3, ms[2] * 1e-3, ms[3] * 1e-3);
         std::fprintf(lf, "Time spend in writing output %.5f\n", t3 - t2);
         std::fprintf(lf, "Time spend in All step %.5f\n", t3 - t0);

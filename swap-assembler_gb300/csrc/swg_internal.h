@@ -113,6 +113,20 @@ int launch_part_prefix(const PartArgs &p, cudaStream_t s);
 int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s);
 int launch_part_wave(const BuildArgs &a, const PartArgs &p, uint32_t p0, uint32_t n,
                      uint64_t rec_begin, uint64_t rec_end, cudaStream_t s);
+// Device FASTA framing (framing.cu).
+uint64_t framing_chunks(uint64_t n);
+uint64_t gscan_scratch(uint64_t n);
+int launch_gscan(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t *scratch, uint64_t *total,
+                 cudaStream_t s);
+int launch_nl_count(const unsigned char *t, uint64_t n, uint64_t *counts, unsigned *flag,
+                    cudaStream_t s);
+int launch_nl_pos(const unsigned char *t, uint64_t n, const uint64_t *chunk_base, uint64_t *nl,
+                  cudaStream_t s);
+int launch_rec_len(const uint64_t *nl, uint64_t n_rec, int k, uint64_t *keep, uint64_t *words,
+                   cudaStream_t s);
+int launch_rec_pack(const unsigned char *t, const uint64_t *nl, uint64_t n_rec, int k,
+                    const uint64_t *read_idx, const uint64_t *word_off, uint64_t *off,
+                    uint32_t *len, uint32_t *packed, cudaStream_t s);
 cudaError_t run_probe(int kind, uint64_t table_bytes, uint64_t n_ops, cudaStream_t s, float *ms);
 int device_sm_count();
 

@@ -85,6 +85,11 @@ class ServerStats(C.Structure):
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
+class Tuning(C.Structure):
+    _fields_ = [("load_factor", C.c_double), ("algorithm", C.c_int), ("read_order", C.c_int),
+                ("ms", C.c_float)]
+
+
 _lib = None
 
 
@@ -112,6 +117,7 @@ def lib() -> C.CDLL:
             "swg_graph_build_device": (i32, [P, C.POINTER(Opts), P, u64, P, P, u64]),
             "swg_build": (i32, [C.POINTER(Opts), P, u64, P, P, u64, C.POINTER(P)]),
             "swg_build_fasta": (i32, [C.POINTER(Opts), C.c_char_p, u64, C.POINTER(P)]),
+            "swg_graph_build_fasta": (i32, [P, C.POINTER(Opts), P, u64]),
             "swg_graph_size": (i32, [P, pu64]),
             "swg_graph_distinct": (i32, [P, pu64]),
             "swg_graph_device_view": (i32, [P, C.POINTER(P), C.POINTER(P), pu64]),
@@ -138,6 +144,9 @@ def lib() -> C.CDLL:
             "swg_server_release": (i32, [P, u64]),
             "swg_server_get_stats": (i32, [P, C.POINTER(ServerStats)]),
             "swg_server_free": (None, [P]),
+            "swg_autotune": (i32, [C.POINTER(Opts), P, u64, P, P, u64, C.c_uint32, C.c_char_p,
+                                   C.POINTER(Tuning)]),
+            "swg_autotune_apply": (i32, [C.c_char_p, i32, C.c_uint32, C.POINTER(Opts)]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -277,6 +286,17 @@ class Graph:
         _check(lib().swg_graph_write_node_lines(self._h, str(path).encode()),
                "swg_graph_write_node_lines")
 
+    def build_fasta(self, opts: Opts, text) -> "Graph":
+        """Frame and pack the FASTA on the device, then build. `text` is bytes
+        or a host buffer address with its length as (addr, n)."""
+        if isinstance(text, tuple):
+            addr, n = text
+        else:
+            buf = C.create_string_buffer(text, len(text))
+            addr, n = C.addressof(buf), len(text)
+        _check(lib().swg_graph_build_fasta(self._h, C.byref(opts), addr, n), "swg_graph_build_fasta")
+        return self
+
     def build_batch(self, opts: Opts, samples: list) -> "Graph":
         """samples: list of (Reads, k, cutoff). Each sample gets its own result."""
         arr = (Sample * len(samples))()
@@ -340,7 +360,8 @@ def records_write_node_lines(keys: np.ndarray, mult: np.ndarray, path: str) -> N
                                               str(path).encode()), "swg_records_write_node_lines")
 
 
-PROBE_KINDS = {"red_add_u32": 0, "atom_add_u64": 1, "cas128": 2, "load16": 3, "load16_cas128": 4}
+PROBE_KINDS = {"red_add_u32": 0, "atom_add_u64": 1, "cas128": 2, "load16": 3, "load16_cas128": 4,
+               "load16_x4": 5, "load16_cas128_x2": 6}
 
 
 def probe_random_access(kind: str, table_bytes: int, n_ops: int, stream: int | None = None) -> float:
@@ -471,3 +492,21 @@ class Server:
         st = ServerStats()
         _check(lib().swg_server_get_stats(self._h, C.byref(st)), "swg_server_get_stats")
         return st.as_dict()
+
+
+def autotune(opts: Opts, d_packed: int, n_words: int, d_off: int, d_len: int, n_reads: int,
+             read_len: int, cache_path: str) -> dict:
+    t = Tuning()
+    _check(lib().swg_autotune(C.byref(opts), d_packed, n_words, d_off, d_len, n_reads, read_len,
+                              str(cache_path).encode(), C.byref(t)), "swg_autotune")
+    return {"load_factor": t.load_factor, "algorithm": t.algorithm, "read_order": t.read_order,
+            "ms": t.ms}
+
+
+def autotune_apply(cache_path: str, k: int, read_len: int, opts: Opts) -> bool:
+    """Fill opts from the cache; False when the cache has no entry."""
+    st = lib().swg_autotune_apply(str(cache_path).encode(), k, read_len, C.byref(opts))
+    if st == 10:
+        return False
+    _check(st, "swg_autotune_apply")
+    return True

@@ -180,3 +180,54 @@ def test_cli_matches_reference(tmp_path):
     assert sha_lines(sorted_lines(out / "kmerGraph.txt")) == c["kmer_graph_sha256"]
     assert sha_lines(sorted_lines(out / "nodes.txt")) == c["nodes_sha256"]
     assert "recvNodeNum = %d" % c["totals"]["recvNodeNum"] in r.stdout
+
+
+@pytest.mark.parametrize("case", [c["name"] for c in golden()["kat"]])
+def test_device_framing_matches_reference(case, tmp_path):
+    c = kat(case)
+    g = swapgb.Graph().build_fasta(swapgb.Opts(k=c["k"], cutoff=c["c"]), kat_text(case))
+    g.write_kmer_graph(tmp_path / "kg.txt")
+    g.write_node_lines(tmp_path / "nodes.txt")
+    assert sha_lines(sorted_lines(tmp_path / "kg.txt")) == c["kmer_graph_sha256"]
+    assert sha_lines(sorted_lines(tmp_path / "nodes.txt")) == c["nodes_sha256"]
+
+
+@pytest.mark.parametrize("case", ["c1_full", "c4_ragged", "c3_small"])
+def test_device_framing_synthetic(case):
+    c = synth_case(case)
+    text = synth_case_text(case)
+    g = swapgb.Graph().build_fasta(swapgb.Opts(k=c["k"], cutoff=c["c"]), text)
+    assert g.size() == c["n_nodes"]
+    assert_same_records(g, text, c["k"], c["c"])
+
+
+def test_device_framing_odd_inputs():
+    # leading bytes before the first '>', records shorter than k, CRLF
+    text = b"junk\n\n>a\nACGTACGTACGTACGTACGTACGTTTGCA\r\n>b\nAC\n>c\n" + b"ACGT" * 40 + b"\n"
+    g = swapgb.Graph().build_fasta(swapgb.Opts(k=19, cutoff=0), text)
+    k1, m1 = g.copy_out()
+    g2 = gpu_build(text, 19, 0)
+    k2, m2 = g2.copy_out()
+    assert np.array_equal(k1, k2) and np.array_equal(m1, m2)
+    for bad in (b">r1\nACGTACGTACGTACGTACGTAC", b">r1\nACGTACGTACGTACGTACGTAC\n>r2\n",
+                b"ACGTACGTACGTACGTACGTAC\n", b">r1\nACGTACGT\x00ACGTACGTACGTAC\n"):
+        with pytest.raises(swapgb.SwgError) as e:
+            swapgb.Graph().build_fasta(swapgb.Opts(k=19, cutoff=0), bad)
+        assert e.value.status == 1
+
+
+def test_autotune_then_build(tmp_path):
+    import torch
+    text = synth_case_text("c2_small")
+    r = swapgb.reads_from_fasta(text, 31)
+    p = torch.from_numpy(r.packed.view(np.int32).copy()).cuda()
+    o = torch.from_numpy(r.off.view(np.int64).copy()).cuda()
+    ln = torch.from_numpy(r.len.view(np.int32).copy()).cuda()
+    cache = tmp_path / "tune.jsonl"
+    best = swapgb.autotune(swapgb.Opts(k=31, cutoff=5), p.data_ptr(), p.numel(), o.data_ptr(),
+                           ln.data_ptr(), o.numel(), 100, cache)
+    assert best["algorithm"] in (1, 2) and 0.5 <= best["load_factor"] <= 0.8 and best["ms"] > 0
+    opts = swapgb.Opts(k=31, cutoff=5)
+    assert swapgb.autotune_apply(cache, 31, 100, opts)
+    g = swapgb.Graph().build_reads(opts, r)
+    assert_same_records(g, text, 31, 5)

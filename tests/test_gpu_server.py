@@ -56,8 +56,29 @@ def test_mixed_requests_equal_plain_builds():
         assert np.array_equal(keys, pk) and np.array_equal(mult, pm), "request %d" % i
     st = srv.stats()
     assert st["completed"] == len(reqs) and st["failed"] == 0
-    assert st["batches"] < len(reqs)  # some requests were batched together
     assert st["bytes_resident"] == 0 and st["bytes_reserved"] == 0
+    srv.close()
+
+
+def test_requests_arriving_during_a_build_join_the_next_batch():
+    # one worker busy with a large request; the small requests submitted
+    # meanwhile queue up and are built together as the next batch
+    big = swapgb.reads_from_fasta(swapgb.synth_fasta(seed=9, genome_len=2_000_000, n_reads=1_500_000,
+                                                     read_len=150, sub_rate=0.01), 31)
+    reqs = _requests()[:8]
+    small = [swapgb.reads_from_fasta(t, k) for t, k, _ in reqs]
+    srv = swapgb.Server(workers=1)
+    tb = srv.submit(big, 31, 5)
+    ts = [srv.submit(r, k, c) for r, (_, k, c) in zip(small, reqs)]
+    for t in [tb] + ts:
+        srv.wait(t, 120.0)
+    st = srv.stats()
+    assert st["max_batch_requests"] >= 2 and st["batches"] < 1 + len(ts)
+    for t, (text, k, c) in zip(ts, reqs):
+        keys, mult = srv.fetch(t)
+        pk, pm = _plain(text, k, c)
+        assert np.array_equal(keys, pk) and np.array_equal(mult, pm)
+    srv.release(tb)
     srv.close()
 
 

@@ -130,3 +130,17 @@ def test_synthetic_generator_is_deterministic():
     assert a == b
     lines = a.split(b"\n")
     assert lines[0] == b">r0" and all(len(x) == 150 for x in lines[1:-1:2])
+
+
+def test_autotune_cache_lookup(tmp_path):
+    cache = tmp_path / "tune.jsonl"
+    opts = swapgb.Opts(k=31, cutoff=5)
+    assert not swapgb.autotune_apply(cache, 31, 100, opts)  # no file yet
+    cache.write_text(
+        '{"k": 31, "band": 1, "load": 0.700, "algorithm": 1, "read_order": 0, "ms": 9.1}\n'
+        '{"k": 27, "band": 2, "load": 0.500, "algorithm": 2, "read_order": 0, "ms": 1.0}\n'
+        '{"k": 31, "band": 1, "load": 0.800, "algorithm": 1, "read_order": 1, "ms": 8.0}\n')
+    assert swapgb.autotune_apply(cache, 31, 100, opts)  # 100 bp -> band 1; last entry wins
+    assert abs(opts.load_factor - 0.8) < 1e-9 and opts.algorithm == 1 and opts.read_order == 1
+    assert swapgb.autotune_apply(cache, 27, 150, opts) and opts.algorithm == 2
+    assert not swapgb.autotune_apply(cache, 27, 250, opts)
