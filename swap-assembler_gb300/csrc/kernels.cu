@@ -401,40 +401,49 @@ __device__ __forceinline__ uint64_t unmix64(uint64_t x) {
 // and one window extraction at the start of the run (and at every read
 // boundary inside it), then the k-mer and its reverse complement are rolled
 // one base at a time.
-__global__ void __launch_bounds__(kK1Block) k_hll(BuildArgs a) {
-    __shared__ TileSmem s;
+// HyperLogLog, one thread per read: the k-mer and its reverse complement
+// are rolled base by base (one packed word loaded every 16 bases), so the
+// lanes of a warp advance in lockstep over reads of equal length. Blocks take
+// contiguous read ranges; the current sample's registers live in smem.
+__global__ void __launch_bounds__(256) k_hll_reads(BuildArgs a) {
     __shared__ unsigned regs[1 << kHllBits];
     __shared__ uint32_t s_cur;
     for (int j = threadIdx.x; j < (1 << kHllBits); j += blockDim.x) regs[j] = 0;
     if (threadIdx.x == 0) s_cur = 0xffffffffu;
-    // a contiguous range of tiles per block: the sample changes only at its
-    // boundaries, and the block keeps the current sample's registers in smem
-    const uint64_t t0 = a.n_tiles * blockIdx.x / gridDim.x;
-    const uint64_t t1 = a.n_tiles * (blockIdx.x + 1) / gridDim.x;
-    auto flush = [&](uint32_t seg) {
-        for (int j = threadIdx.x; j < (1 << kHllBits); j += blockDim.x)
-            if (regs[j]) {
-                atomicMax(&a.hll[((uint64_t)seg << kHllBits) + j], regs[j]);
-                regs[j] = 0;
-            }
-    };
-    for (uint64_t t = t0; t < t1; ++t) {
+    const uint64_t r0 = a.n_reads * blockIdx.x / gridDim.x;
+    const uint64_t r1 = a.n_reads * (blockIdx.x + 1) / gridDim.x;
+    for (uint64_t base = r0; base < r1; base += blockDim.x) {
         __syncthreads();
-        const TileView v = load_tile(a, t, s);
-        __syncthreads();
-        const uint32_t first = v.in_smem ? s.seg[0] : seg_of(a, v.r0);
+        const uint32_t first = seg_of(a, base);
         if (first != s_cur) {
-            if (s_cur != 0xffffffffu) flush(s_cur);
+            if (s_cur != 0xffffffffu)
+                for (int j = threadIdx.x; j < (1 << kHllBits); j += blockDim.x)
+                    if (regs[j]) {
+                        atomicMax(&a.hll[((uint64_t)s_cur << kHllBits) + j], regs[j]);
+                        regs[j] = 0;
+                    }
             __syncthreads();
             if (threadIdx.x == 0) s_cur = first;
             __syncthreads();
         }
         const uint32_t cur = s_cur;
-        const uint64_t A = t * kTileOcc;
-        const uint64_t B = umin64(A + kTileOcc, a.total_occ);
-        const uint64_t i0 = A + (uint64_t)threadIdx.x * kK1Items;
-        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B),
-                 [&](uint64_t key, unsigned, uint64_t, uint32_t seg) {
+        const uint64_t r = base + threadIdx.x;
+        if (r >= r1) continue;
+        const uint32_t seg = seg_of(a, r);
+        const int k = k_of(a, seg);
+        const uint32_t L = a.read_len[r];
+        if (L < (uint32_t)k) continue;
+        const uint64_t kmask = (1ull << (2 * k)) - 1;
+        const int top = 2 * (k - 1);
+        uint64_t g = a.read_off[r], fwd = 0, rc = 0;
+        uint32_t w = ldw(a.packed, g >> 4, a.n_words);
+        for (uint32_t p = 0; p < L; ++p, ++g) {
+            if (p && (g & 15) == 0) w = ldw(a.packed, g >> 4, a.n_words);
+            const uint32_t b = (w >> (30 - 2 * (int)(g & 15))) & 3u;
+            fwd = ((fwd << 2) | b) & kmask;
+            rc = (rc >> 2) | ((uint64_t)(3u - b) << top);
+            if (p + 1 < (uint32_t)k) continue;
+            const uint64_t key = fwd >= rc ? fwd : rc;
             const uint64_t h = mix64(key ^ 0x9e3779b97f4a7c15ull);
             const unsigned idx = (unsigned)(h >> (64 - kHllBits));
             const uint64_t rest = (h << kHllBits) | (1ull << (kHllBits - 1));
@@ -444,10 +453,12 @@ __global__ void __launch_bounds__(kK1Block) k_hll(BuildArgs a) {
             } else {
                 atomicMax(&a.hll[((uint64_t)seg << kHllBits) + idx], rank);
             }
-        });
+        }
     }
     __syncthreads();
-    if (s_cur != 0xffffffffu) flush(s_cur);
+    if (s_cur != 0xffffffffu)
+        for (int j = threadIdx.x; j < (1 << kHllBits); j += blockDim.x)
+            if (regs[j]) atomicMax(&a.hll[((uint64_t)s_cur << kHllBits) + j], regs[j]);
 }
 
 // HyperLogLog estimate per sample (the same formula as hll_estimate).
@@ -1023,9 +1034,9 @@ int launch_tiles(const BuildArgs &a, cudaStream_t s) {
 }
 
 int launch_hll(const BuildArgs &a, cudaStream_t s) {
-    if (a.n_tiles == 0) return 0;
-    const uint64_t grid = std::min<uint64_t>(a.n_tiles, (uint64_t)device_sm_count() * 8);
-    k_hll<<<(unsigned)grid, kK1Block, 0, s>>>(a);
+    if (a.n_tiles == 0 || a.n_reads == 0) return 0;
+    const uint64_t grid = std::min<uint64_t>((a.n_reads + 255) / 256, (uint64_t)device_sm_count() * 8);
+    k_hll_reads<<<(unsigned)grid, 256, 0, s>>>(a);
     return 1;
 }
 
