@@ -48,7 +48,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-samples measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-requests measurement")
-    ap.add_argument("--algo", default="direct", choices=["direct", "partitioned"])
+    ap.add_argument("--algo", default="direct", choices=["direct", "partitioned", "bucketed"])
     ap.add_argument("--order", default="input", choices=["input", "minimizer"],
                     help="read order of the direct algorithm")
     ap.add_argument("--reads", type=int, default=0,
@@ -380,7 +380,8 @@ def main() -> int:
     n_bases = reads.n_bases
     n_occ = int((reads.len.astype(np.int64) - K + 1).clip(min=0).sum())
     stream = torch.cuda.current_stream(dev)
-    algo = swapgb.ALGO_PARTITIONED if args.algo == "partitioned" else swapgb.ALGO_DIRECT
+    algo = {"direct": swapgb.ALGO_DIRECT, "partitioned": swapgb.ALGO_PARTITIONED,
+            "bucketed": swapgb.ALGO_BUCKETED}[args.algo]
     order = swapgb.ORDER_MINIMIZER if args.order == "minimizer" else swapgb.ORDER_INPUT
     opts = swapgb.Opts(k=K, cutoff=CUTOFF, stream=stream.cuda_stream, algorithm=algo,
                        read_order=order)

@@ -66,6 +66,7 @@ typedef enum swg_status {
 #define SWG_ALGO_DEFAULT 0     /* direct */
 #define SWG_ALGO_DIRECT 1      /* one pass into a device-wide table in HBM */
 #define SWG_ALGO_PARTITIONED 2 /* hash-partitioned records, each partition counted in L2 */
+#define SWG_ALGO_BUCKETED 3    /* records split into buckets counted in shared memory */
 
 /* Order in which the direct algorithm counts the reads (same results). */
 #define SWG_ORDER_INPUT 0     /* input order (default) */

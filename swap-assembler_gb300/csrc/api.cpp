@@ -96,6 +96,14 @@ struct swg_graph {
     uint64_t text_cap = 0;
     uint64_t *d_fw = nullptr;  // chunk counts | scan scratch | newline positions | records x3
     uint64_t fw_cap = 0;
+    // bucketed workspace
+    unsigned long long *d_rec2 = nullptr;
+    uint64_t rec2_cap = 0;
+    unsigned long long *d_bk = nullptr;  // cursor2 [nb] | off2 [nb+1] | big [nb] | scratch
+    uint64_t bk_cap = 0;
+    Entry *d_arena = nullptr;
+    uint64_t arena_cap = 0;
+    uint32_t big_buckets = 0;
     // batched build (n_samples == 0 after a single-sample build)
     uint32_t n_samples = 0;
     std::vector<uint64_t> s_tbase, s_tcap, s_out, s_distinct, s_occ;
@@ -167,7 +175,7 @@ swg_status check_opts(const swg_opts *o) {
         swg::set_error("k must be in 1..31");
         return SWG_ERR_BAD_INPUT;
     }
-    if (o->algorithm < 0 || o->algorithm > SWG_ALGO_PARTITIONED || o->read_order < 0 ||
+    if (o->algorithm < 0 || o->algorithm > SWG_ALGO_BUCKETED || o->read_order < 0 ||
         o->read_order > SWG_ORDER_MINIMIZER) {
         swg::set_error("unknown algorithm or read order");
         return SWG_ERR_BAD_INPUT;
@@ -186,6 +194,8 @@ cudaStream_t stream_of(swg_graph *g, const swg_opts *o) {
 swg_status build_direct(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s, double load);
 swg_status build_partitioned(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s,
                              double load);
+swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s,
+                          double load);
 
 swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, uint64_t n_words,
                       const uint64_t *off, const uint32_t *len, uint64_t n_reads) {
@@ -247,6 +257,7 @@ swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, u
     SWG_CUDA(cudaGetLastError(), "tile launch");
 
     if (o->algorithm == SWG_ALGO_PARTITIONED) return build_partitioned(g, o, a, s, load);
+    if (o->algorithm == SWG_ALGO_BUCKETED) return build_bucketed(g, o, a, s, load);
     return build_direct(g, o, a, s, load);
 }
 
@@ -698,6 +709,134 @@ swg_status batch_impl(swg_graph *g, const swg_opts *o, const swg_sample *sm, uin
     return SWG_ERR_TABLE_FULL;
 }
 
+// Bucketed counting: the records of the hash partitions (as in the
+// partitioned build) are split again into buckets of a few hundred records by
+// the next hash bits, and every bucket is counted by one CTA in a
+// shared-memory hash table and compacted from there. Buckets too large for
+// shared memory (hot k-molecules) are counted in a global-memory table.
+swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s,
+                          double load) {
+    swg_status st;
+    g->algorithm = SWG_ALGO_BUCKETED;
+    const uint64_t N = a.total_occ;
+    int b1 = N <= (400ull << 20) ? 8 : (N <= (1600ull << 20) ? 9 : 10);
+    const uint64_t P = 1ull << b1;
+    int b2 = 0;
+    while (b2 < 11 && (double)N / (double)(P << b2) > 700.0) b2++;
+    swg::PartArgs pa;
+    std::memset(&pa, 0, sizeof(pa));
+    pa.bits = b1;
+    pa.n_parts = (uint32_t)P;
+    pa.load_num = 3;
+    pa.load_den = 5;
+    if ((st = ensure(&g->d_part, &g->part_cap, 3 * P + 1, "partition table"))) return st;
+    pa.part_count = g->d_part;
+    pa.part_start = g->d_part + P;
+    pa.part_cursor = g->d_part + 2 * P + 1;
+    if ((st = ensure(&g->d_records, &g->records_cap, std::max<uint64_t>(N, 1), "records"))) return st;
+    if ((st = ensure(&g->d_rec2, &g->rec2_cap, std::max<uint64_t>(N, 1), "bucket records"))) return st;
+    const uint64_t NB = P << b2;
+    const uint64_t scratch = swg::gscan_scratch(NB);
+    if ((st = ensure(&g->d_bk, &g->bk_cap, 3 * NB + 1 + scratch + 2, "bucket table"))) return st;
+    const uint64_t out_want = std::max<uint64_t>(N, 1);
+    if (g->out_cap < out_want || !g->d_out_keys || !g->d_out_mult) {
+        cudaFree(g->d_out_keys);
+        cudaFree(g->d_out_mult);
+        g->d_out_keys = g->d_out_mult = nullptr;
+        g->out_cap = 0;
+        SWG_CUDA(cudaMalloc(&g->d_out_keys, out_want * 8), "output keys");
+        SWG_CUDA(cudaMalloc(&g->d_out_mult, out_want * 8), "output multiplicities");
+        g->out_cap = out_want;
+    }
+    pa.records = g->d_records;
+    a.out_keys = g->d_out_keys;
+    a.out_mult = g->d_out_mult;
+    a.out_cap = out_want;
+    swg::BucketArgs bk;
+    std::memset(&bk, 0, sizeof(bk));
+    bk.b1 = b1;
+    bk.b2 = b2;
+    bk.n_parts = (uint32_t)P;
+    bk.part_start = pa.part_start;
+    bk.rec1 = g->d_records;
+    bk.rec2 = g->d_rec2;
+    bk.cursor2 = g->d_bk;
+    bk.off2 = g->d_bk + NB;
+    bk.big = g->d_bk + 2 * NB + 1;
+    bk.big_cap = (uint32_t)std::min<uint64_t>(NB, 0xffffffffu);
+    bk.big_count = &g->d_ctl->pad;
+    bk.n_rec = N;
+    unsigned long long *scr = g->d_bk + 3 * NB + 1;
+    unsigned long long *tot = scr + scratch;
+
+    SWG_CUDA(cudaMemsetAsync(pa.part_count, 0, P * 8, s), "clear partitions");
+    g->launches += swg::launch_part_count(a, pa, s);
+    g->launches += swg::launch_part_prefix(pa, s);
+    SWG_CUDA(cudaEventRecord(g->ev[1], s), "event");
+    g->launches += swg::launch_part_scatter(a, pa, s);
+    SWG_CUDA(cudaMemsetAsync(bk.cursor2, 0, NB * 8, s), "clear bucket counts");
+    g->launches += swg::launch_sub_hist(bk, s);
+    g->launches += swg::launch_gscan(reinterpret_cast<const uint64_t *>(bk.cursor2),
+                                     reinterpret_cast<uint64_t *>(bk.off2), NB,
+                                     reinterpret_cast<uint64_t *>(scr),
+                                     reinterpret_cast<uint64_t *>(bk.off2 + NB), s);
+    SWG_CUDA(cudaMemcpyAsync(bk.cursor2, bk.off2, NB * 8, cudaMemcpyDeviceToDevice, s), "bucket cursors");
+    g->launches += swg::launch_sub_scatter(bk, s);
+    SWG_CUDA(cudaGetLastError(), "bucket scatter launch");
+    SWG_CUDA(cudaEventRecord(g->ev[2], s), "event");
+    g->launches += swg::launch_bucket_count(a, bk, s);
+    SWG_CUDA(cudaGetLastError(), "bucket count launch");
+    SWG_CUDA(cudaMemcpyAsync(g->h_ctl, g->d_ctl, sizeof(Control) - sizeof(uint64_t),
+                             cudaMemcpyDeviceToHost, s), "read status");
+    SWG_CUDA(cudaStreamSynchronize(s), "bucket count");
+    (void)tot;
+    const unsigned nbig = g->h_ctl->pad;
+    g->big_buckets = nbig;
+    if (nbig) {  // hot buckets: count them in a global-memory table, one after another
+        std::vector<unsigned long long> big(nbig), offs(NB + 1);
+        SWG_CUDA(cudaMemcpyAsync(big.data(), bk.big, nbig * 8, cudaMemcpyDeviceToHost, s), "read big buckets");
+        SWG_CUDA(cudaMemcpyAsync(offs.data(), bk.off2, (NB + 1) * 8, cudaMemcpyDeviceToHost, s),
+                 "read bucket offsets");
+        SWG_CUDA(cudaStreamSynchronize(s), "big buckets");
+        for (unsigned i = 0; i < nbig; i++) {
+            const uint64_t bb = big[i], rb = offs[bb], re = offs[bb + 1];
+            const uint64_t cap = (uint64_t)std::ceil((double)(re - rb) / load) + 64;
+            if ((st = ensure(&g->d_arena, &g->arena_cap, cap, "big-bucket table"))) return st;
+            SWG_CUDA(cudaMemsetAsync(g->d_arena, 0, cap * sizeof(Entry), s), "clear big-bucket table");
+            g->launches += swg::launch_big_bucket(a, bk, bb, rb, re, g->d_arena, cap, s);
+        }
+        SWG_CUDA(cudaGetLastError(), "big bucket launch");
+        SWG_CUDA(cudaMemcpyAsync(g->h_ctl, g->d_ctl, sizeof(Control) - sizeof(uint64_t),
+                                 cudaMemcpyDeviceToHost, s), "read status");
+    }
+    SWG_CUDA(cudaEventRecord(g->ev[3], s), "event");
+    SWG_CUDA(cudaEventRecord(g->ev[4], s), "event");
+    SWG_CUDA(cudaStreamSynchronize(s), "build");
+    const unsigned status = g->h_ctl->status;
+    if (status & swg::kStatusCasLimit) {
+        swg::set_error("a bounded CAS retry loop gave up on the device");
+        return SWG_ERR_TIMEOUT;
+    }
+    if (status & swg::kStatusTableFull) {
+        swg::set_error("a big-bucket table reached the probe limit");
+        return SWG_ERR_TABLE_FULL;
+    }
+    g->parts = (uint32_t)P;
+    g->slots = (uint32_t)(1u << b2);
+    g->waves = nbig;
+    g->cap_used = NB;
+    g->n_distinct = g->h_ctl->counters[0];
+    g->n_out = g->h_ctl->counters[1];
+    g->built = true;
+    float t[5] = {0, 0, 0, 0, 0};
+    cudaEventElapsedTime(&t[0], g->ev[0], g->ev[1]);
+    cudaEventElapsedTime(&t[1], g->ev[1], g->ev[2]);
+    cudaEventElapsedTime(&t[2], g->ev[2], g->ev[3]);
+    cudaEventElapsedTime(&t[4], g->ev[0], g->ev[4]);
+    std::memcpy(g->ms, t, sizeof(t));
+    return SWG_OK;
+}
+
 swg_status fetch_sorted(const swg_graph *g, std::vector<uint64_t> &keys,
                         std::vector<uint64_t> &mult) {
     if (!g || !g->built || g->n_samples) {
@@ -790,6 +929,9 @@ void swg_graph_free(swg_graph *g) {
     cudaFree(g->d_part);
     cudaFree(g->d_minhash);
     cudaFree(g->d_text);
+    cudaFree(g->d_rec2);
+    cudaFree(g->d_bk);
+    cudaFree(g->d_arena);
     cudaFree(g->d_fw);
     cudaFree(g->d_segs);
     cudaFree(g->d_read_seg);
@@ -1143,9 +1285,10 @@ swg_status swg_graph_build_info(const swg_graph *g, swg_build_info *info) {
     info->distinct = g->n_distinct;
     info->survivors = g->n_out;
     info->table_entries = g->cap_used;
-    info->partitions = g->algorithm == SWG_ALGO_PARTITIONED ? g->parts : 0;
-    info->slots = g->algorithm == SWG_ALGO_PARTITIONED ? g->slots : 0;
-    info->waves = g->algorithm == SWG_ALGO_PARTITIONED ? g->waves : 0;
+    const bool parted = g->algorithm == SWG_ALGO_PARTITIONED || g->algorithm == SWG_ALGO_BUCKETED;
+    info->partitions = parted ? g->parts : 0;
+    info->slots = parted ? g->slots : 0;
+    info->waves = parted ? g->waves : 0;
     info->retries = g->retries;
     info->estimate = g->estimate;
     std::memcpy(info->ms, g->ms, sizeof(g->ms));

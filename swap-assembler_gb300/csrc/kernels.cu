@@ -953,6 +953,309 @@ __global__ void __launch_bounds__(kCBlock) k_part_compact(BuildArgs a, PartArgs 
 }
 
 // ---------------------------------------------------------------------
+// Bucketed build. Level-1 records come from k_part_scatter (2^b1 partitions,
+// record = low 64-b1 bits of h shifted left by 8 | arc code); the next b2
+// bits of h name the sub-bucket. Each bucket is then counted by one CTA in a
+// shared-memory hash table and compacted from there.
+constexpr int kBkChunk = 4096;    // records per block in the sub-bucket passes
+constexpr int kBkTable = 2048;    // shared-memory table entries per bucket
+constexpr int kBkSmemMax = 1400;  // larger buckets take the global-memory path
+constexpr int kBkBinsMax = 2 << 11;  // local bins of a chunk: two partitions x 2^b2 (b2 <= 11)
+constexpr int kBkPartsMax = 1 << kPartBitsMax;
+
+__device__ __forceinline__ uint32_t sub_of(const BucketArgs &b, unsigned long long rec) {
+    return b.b2 ? (uint32_t)((rec >> 8) >> (64 - b.b1 - b.b2)) : 0u;
+}
+
+// Level-1 partition of record index r (last p with part_start[p] <= r).
+__device__ __forceinline__ uint32_t part_of_rec(const unsigned long long *st, uint32_t n_parts,
+                                                uint64_t r) {
+    uint32_t lo = 0, hi = n_parts;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (st[mid] <= r) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) k_sub_hist(BucketArgs b) {
+    __shared__ unsigned long long st[kBkPartsMax + 1];
+    __shared__ unsigned hist[kBkBinsMax];
+    const uint32_t P2 = 1u << b.b2;
+    for (uint32_t j = threadIdx.x; j <= b.n_parts; j += blockDim.x) st[j] = b.part_start[j];
+    for (uint32_t j = threadIdx.x; j < 2 * P2; j += blockDim.x) hist[j] = 0;
+    __syncthreads();
+    const uint64_t r0 = (uint64_t)blockIdx.x * kBkChunk;
+    const uint64_t r1 = umin64(r0 + kBkChunk, b.n_rec);
+    const uint32_t p0 = part_of_rec(st, b.n_parts, r0);
+    for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        const unsigned long long rec = b.rec1[r];
+        uint32_t p = p0;
+        while (p + 1 < b.n_parts && st[p + 1] <= r) ++p;
+        const uint32_t sub = sub_of(b, rec);
+        if (p - p0 < 2) atomicAdd(&hist[(p - p0) * P2 + sub], 1u);
+        else atomicAdd(&b.cursor2[(uint64_t)p * P2 + sub], 1ull);  // rare: tiny partitions
+    }
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < 2 * P2; j += blockDim.x) {
+        const uint32_t p = p0 + j / P2;
+        if (hist[j] && p < b.n_parts) atomicAdd(&b.cursor2[(uint64_t)p * P2 + (j % P2)], (unsigned long long)hist[j]);
+    }
+}
+
+constexpr size_t kSubScatterDyn = kBkChunk * sizeof(unsigned long long) +
+                                  2 * kBkChunk * sizeof(unsigned short) +
+                                  kBkBinsMax * (2 * sizeof(unsigned) + sizeof(unsigned long long));
+
+__global__ void __launch_bounds__(256) k_sub_scatter(BucketArgs b) {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    unsigned long long *rec = reinterpret_cast<unsigned long long *>(dyn);
+    unsigned long long *gbase = rec + kBkChunk;
+    unsigned *hist = reinterpret_cast<unsigned *>(gbase + kBkBinsMax);
+    unsigned *loff = hist + kBkBinsMax;
+    unsigned short *bin = reinterpret_cast<unsigned short *>(loff + kBkBinsMax);
+    unsigned short *perm = bin + kBkChunk;
+    __shared__ unsigned long long st[kBkPartsMax + 1];
+    __shared__ uint64_t wb[8];
+    const uint32_t P2 = 1u << b.b2, nb = 2 * P2;
+    for (uint32_t j = threadIdx.x; j <= b.n_parts; j += blockDim.x) st[j] = b.part_start[j];
+    for (uint32_t j = threadIdx.x; j < nb; j += blockDim.x) hist[j] = 0;
+    __syncthreads();
+    const uint64_t r0 = (uint64_t)blockIdx.x * kBkChunk;
+    const uint32_t n = (uint32_t)(umin64(r0 + kBkChunk, b.n_rec) - r0);
+    const uint32_t p0 = part_of_rec(st, b.n_parts, r0);
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint64_t r = r0 + i;
+        const unsigned long long v = b.rec1[r];
+        uint32_t p = p0;
+        while (p + 1 < b.n_parts && st[p + 1] <= r) ++p;
+        const uint32_t sub = sub_of(b, v);
+        if (p - p0 < 2) {
+            const uint32_t bn = (p - p0) * P2 + sub;
+            rec[i] = v;
+            bin[i] = (unsigned short)bn;
+            atomicAdd(&hist[bn], 1u);
+        } else {  // rare: a chunk spanning more than two partitions
+            const unsigned long long pos = atomicAdd(&b.cursor2[(uint64_t)p * P2 + sub], 1ull);
+            b.rec2[pos] = v;
+            bin[i] = 0xffff;
+        }
+    }
+    __syncthreads();
+    // local offsets of the bins, global runs for each
+    const uint32_t per = (nb + blockDim.x - 1) / blockDim.x;
+    uint64_t mine = 0;
+    for (uint32_t x = 0; x < per; ++x) {
+        const uint32_t j = threadIdx.x * per + x;
+        if (j < nb) mine += hist[j];
+    }
+    uint64_t run = block_exclusive_scan<256>(mine, wb, nullptr);
+    for (uint32_t x = 0; x < per; ++x) {
+        const uint32_t j = threadIdx.x * per + x;
+        if (j < nb) {
+            const unsigned c = hist[j];
+            loff[j] = (unsigned)run;
+            run += c;
+            const uint32_t p = p0 + j / P2;
+            gbase[j] = (c && p < b.n_parts) ? atomicAdd(&b.cursor2[(uint64_t)p * P2 + (j % P2)], (unsigned long long)c) : 0;
+            hist[j] = 0;
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const unsigned bn = bin[i];
+        if (bn != 0xffff) perm[loff[bn] + atomicAdd(&hist[bn], 1u)] = (unsigned short)i;
+    }
+    __syncthreads();
+    const unsigned kept = loff[nb - 1] + hist[nb - 1];
+    for (uint32_t j = threadIdx.x; j < kept; j += blockDim.x) {
+        const unsigned i = perm[j];
+        const unsigned bn = bin[i];
+        b.rec2[gbase[bn] + (j - loff[bn])] = rec[i];
+    }
+}
+
+constexpr size_t kBucketDyn = kBkTable * (sizeof(unsigned long long) + 4 * sizeof(unsigned));
+
+// One CTA per bucket: count in shared memory, cutoff, compact.
+__global__ void __launch_bounds__(256) k_bucket_count(BuildArgs a, BucketArgs b) {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    unsigned long long *keys = reinterpret_cast<unsigned long long *>(dyn);
+    unsigned *cnt = reinterpret_cast<unsigned *>(keys + kBkTable);  // 8 x uint16 per entry
+    __shared__ uint64_t wb[8];
+    __shared__ unsigned long long s_base;
+    const uint64_t bk = blockIdx.x;
+    const uint64_t rb = b.off2[bk], re = b.off2[bk + 1];
+    const uint64_t nrec = re - rb;
+    if (nrec == 0) return;
+    if (nrec > (uint64_t)kBkSmemMax) {
+        if (threadIdx.x == 0) {
+            const unsigned i = atomicAdd(b.big_count, 1u);
+            if (i < b.big_cap) b.big[i] = bk;
+        }
+        return;
+    }
+    for (int j = threadIdx.x; j < kBkTable; j += blockDim.x) {
+        keys[j] = 0;
+        cnt[4 * j] = cnt[4 * j + 1] = cnt[4 * j + 2] = cnt[4 * j + 3] = 0;
+    }
+    __syncthreads();
+    const uint64_t hp = (uint64_t)(bk >> b.b2) << (64 - b.b1);
+    for (uint64_t r = rb + threadIdx.x; r < re; r += blockDim.x) {
+        const unsigned long long rec = b.rec2[r];
+        const unsigned long long h = hp | (rec >> 8);
+        uint32_t slot = (uint32_t)h & (kBkTable - 1);
+        for (int step = 0; step < kBkTable; ++step) {
+            const unsigned long long old = atomicCAS(&keys[slot], 0ull, h);
+            if (old == 0 || old == h) break;
+            slot = (slot + 1) & (kBkTable - 1);
+        }
+        const unsigned code = (unsigned)rec & 0xffu;
+        if (code & 0x08u) {
+            const unsigned t = code & 7u;
+            atomicAdd(&cnt[4 * slot + (t >> 1)], 1u << (16 * (t & 1)));
+        }
+        if (code & 0x80u) {
+            const unsigned t = (code >> 4) & 7u;
+            atomicAdd(&cnt[4 * slot + (t >> 1)], 1u << (16 * (t & 1)));
+        }
+    }
+    __syncthreads();
+    const int c = a.cutoff;
+    const uint32_t thr = c <= 0 ? 0u : (c >= 256 ? 0u : (uint32_t)c * 0x01010101u);
+    constexpr int per = kBkTable / 256;
+    uint64_t ok[per], om[per];
+    unsigned keep = 0;
+    int nkeep = 0, nused = 0;
+#pragma unroll
+    for (int it = 0; it < per; ++it) {
+        const int s = it * 256 + threadIdx.x;
+        const unsigned long long h = keys[s];
+        ok[it] = om[it] = 0;
+        if (!h) continue;
+        nused++;
+        uint64_t m = 0;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const unsigned v = (cnt[4 * s + (t >> 1)] >> (16 * (t & 1))) & 0xffffu;
+            m |= (uint64_t)(v > 255u ? 255u : v) << (8 * t);
+        }
+        if (thr) {
+            const uint32_t lo = (uint32_t)m & __vcmpgeu4((uint32_t)m, thr);
+            const uint32_t hi = (uint32_t)(m >> 32) & __vcmpgeu4((uint32_t)(m >> 32), thr);
+            m = ((uint64_t)hi << 32) | lo;
+        }
+        if (c >= 256) m = 0;
+        if (m) {
+            ok[it] = unmix64(h);
+            om[it] = m;
+            keep |= 1u << it;
+            nkeep++;
+        }
+    }
+    uint64_t total, used;
+    const uint64_t ex = block_exclusive_scan<256>((uint64_t)nkeep, wb, &total);
+    block_exclusive_scan<256>((uint64_t)nused, wb, &used);
+    if (threadIdx.x == 0) {
+        s_base = total ? atomicAdd(&a.counters[1], (unsigned long long)total) : 0;
+        if (used) atomicAdd(&a.counters[0], (unsigned long long)used);
+    }
+    __syncthreads();
+    uint64_t pos = s_base + ex;
+#pragma unroll
+    for (int it = 0; it < per; ++it) {
+        if (keep & (1u << it)) {
+            if (pos < a.out_cap) {
+                a.out_keys[pos] = ok[it];
+                a.out_mult[pos] = om[it];
+            }
+            pos++;
+        }
+    }
+}
+
+// Buckets too large for shared memory: count in a global-memory table.
+__global__ void __launch_bounds__(kK1Block) k_big_insert(BuildArgs a, uint64_t hp, const unsigned long long *rec2,
+                                                         uint64_t rb, uint64_t re, Entry *table,
+                                                         uint64_t cap) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t base = rb + (uint64_t)blockIdx.x * blockDim.x; base < re; base += stride) {
+        const uint64_t r = base + threadIdx.x;
+        const bool valid = r < re;
+        const unsigned vmask = __ballot_sync(kFull, valid);
+        if (!valid) continue;
+        const unsigned long long rec = rec2[r];
+        const uint64_t h = hp | (rec >> 8);
+        uint64_t inc = code_inc((unsigned)rec & 0xffu);
+        const unsigned peers = __match_any_sync(vmask, h);
+        if (__any_sync(vmask, peers != (1u << lane))) {
+            uint64_t tot = 0;
+#pragma unroll
+            for (int sl = 0; sl < 8; ++sl) {
+                const unsigned bb = __ballot_sync(vmask, (unsigned)(inc >> (8 * sl)) & 1u);
+                tot |= (uint64_t)__popc(bb & peers) << (8 * sl);
+            }
+            inc = tot;
+        }
+        if (lane == __ffs(peers) - 1) insert_or_update(table, cap, h, inc, a.status);
+    }
+}
+
+__global__ void __launch_bounds__(kCBlock) k_big_compact(BuildArgs a, const Entry *table, uint64_t cap) {
+    __shared__ uint64_t wb[kCBlock / 32];
+    __shared__ unsigned long long s_base;
+    const uint64_t chunk = (uint64_t)blockIdx.x * kCBlock * kCItems;
+    const int c = a.cutoff;
+    const uint32_t thr = c <= 0 ? 0u : (c >= 256 ? 0u : (uint32_t)c * 0x01010101u);
+    uint64_t keys[kCItems], cnts[kCItems];
+    unsigned keep = 0;
+    int nkeep = 0, nused = 0;
+#pragma unroll
+    for (int it = 0; it < kCItems; ++it) {
+        const uint64_t idx = chunk + (uint64_t)it * kCBlock + threadIdx.x;
+        keys[it] = cnts[it] = 0;
+        if (idx >= cap) continue;
+        const ulonglong2 e = *reinterpret_cast<const ulonglong2 *>(table + idx);
+        if (!e.x) continue;
+        nused++;
+        uint64_t v = e.y;
+        if (thr) {
+            const uint32_t lo = (uint32_t)v & __vcmpgeu4((uint32_t)v, thr);
+            const uint32_t hi = (uint32_t)(v >> 32) & __vcmpgeu4((uint32_t)(v >> 32), thr);
+            v = ((uint64_t)hi << 32) | lo;
+        }
+        if (c >= 256) v = 0;
+        if (v) {
+            keys[it] = unmix64(e.x);
+            cnts[it] = v;
+            keep |= 1u << it;
+            nkeep++;
+        }
+    }
+    uint64_t total, used;
+    const uint64_t ex = block_exclusive_scan<kCBlock>((uint64_t)nkeep, wb, &total);
+    block_exclusive_scan<kCBlock>((uint64_t)nused, wb, &used);
+    if (threadIdx.x == 0) {
+        s_base = total ? atomicAdd(&a.counters[1], (unsigned long long)total) : 0;
+        if (used) atomicAdd(&a.counters[0], (unsigned long long)used);
+    }
+    __syncthreads();
+    uint64_t pos = s_base + ex;
+#pragma unroll
+    for (int it = 0; it < kCItems; ++it) {
+        if (keep & (1u << it)) {
+            if (pos < a.out_cap) {
+                a.out_keys[pos] = keys[it];
+                a.out_mult[pos] = cnts[it];
+            }
+            pos++;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
 // Random-access probe (roofline denominator).
 __global__ void __launch_bounds__(256) k_probe(int kind, Entry *table, uint64_t n16,
                                                uint64_t ops_per_thread, uint64_t seed,
@@ -1150,6 +1453,42 @@ int launch_part_wave(const BuildArgs &a, const PartArgs &p, uint32_t p0, uint32_
         launches++;
     }
     return launches;
+}
+
+int launch_sub_hist(const BucketArgs &b, cudaStream_t s) {
+    const uint64_t grid = (b.n_rec + kBkChunk - 1) / kBkChunk;
+    if (!grid) return 0;
+    k_sub_hist<<<(unsigned)grid, 256, 0, s>>>(b);
+    return 1;
+}
+
+int launch_sub_scatter(const BucketArgs &b, cudaStream_t s) {
+    const uint64_t grid = (b.n_rec + kBkChunk - 1) / kBkChunk;
+    if (!grid) return 0;
+    cudaFuncSetAttribute(k_sub_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSubScatterDyn);
+    k_sub_scatter<<<(unsigned)grid, 256, kSubScatterDyn, s>>>(b);
+    return 1;
+}
+
+int launch_bucket_count(const BuildArgs &a, const BucketArgs &b, cudaStream_t s) {
+    const uint64_t grid = (uint64_t)b.n_parts << b.b2;
+    cudaFuncSetAttribute(k_bucket_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kBucketDyn);
+    k_bucket_count<<<(unsigned)grid, 256, kBucketDyn, s>>>(a, b);
+    return 1;
+}
+
+int launch_big_bucket(const BuildArgs &a, const BucketArgs &b, uint64_t bucket, uint64_t rb,
+                      uint64_t re, Entry *table, uint64_t cap, cudaStream_t s) {
+    const uint64_t hp = (uint64_t)(bucket >> b.b2) << (64 - b.b1);
+    const uint64_t blocks = std::min<uint64_t>((re - rb + kK1Block - 1) / kK1Block,
+                                               (uint64_t)device_sm_count() * 8);
+    k_big_insert<<<(unsigned)std::max<uint64_t>(blocks, 1), kK1Block, 0, s>>>(a, hp, b.rec2, rb, re,
+                                                                              table, cap);
+    const uint64_t per = (uint64_t)kCBlock * kCItems;
+    k_big_compact<<<(unsigned)((cap + per - 1) / per), kCBlock, 0, s>>>(a, table, cap);
+    return 2;
 }
 
 cudaError_t run_probe(int kind, uint64_t table_bytes, uint64_t n_ops, cudaStream_t s, float *ms) {

@@ -90,6 +90,22 @@ struct PartArgs {
     int load_num, load_den;            // slice capacity = count * den / num + 16
 };
 
+// Bucketed build: the level-1 partition records are split again by the next
+// b2 bits of the hash into sub-buckets small enough for a shared-memory table.
+struct BucketArgs {
+    int b1, b2;                            // partition bits, sub-bucket bits
+    uint32_t n_parts;                      // 1 << b1
+    const unsigned long long *part_start;  // [n_parts + 1] level-1 offsets
+    const unsigned long long *rec1;        // level-1 records
+    unsigned long long *rec2;              // records grouped by bucket
+    unsigned long long *off2;              // [n_buckets + 1] bucket offsets
+    unsigned long long *cursor2;           // [n_buckets] scatter cursors
+    uint64_t n_rec;
+    unsigned long long *big;               // buckets too large for shared memory
+    unsigned *big_count;
+    uint32_t big_cap;
+};
+
 // Kernel launchers (kernels.cu). Each returns the number of launches made.
 int launch_occ_scan(const BuildArgs &a, cudaStream_t s);
 uint64_t scan_block_count(uint64_t n_reads);
@@ -127,6 +143,11 @@ int launch_rec_len(const uint64_t *nl, uint64_t n_rec, int k, uint64_t *keep, ui
 int launch_rec_pack(const unsigned char *t, const uint64_t *nl, uint64_t n_rec, int k,
                     const uint64_t *read_idx, const uint64_t *word_off, uint64_t *off,
                     uint32_t *len, uint32_t *packed, cudaStream_t s);
+int launch_sub_hist(const BucketArgs &b, cudaStream_t s);
+int launch_sub_scatter(const BucketArgs &b, cudaStream_t s);
+int launch_bucket_count(const BuildArgs &a, const BucketArgs &b, cudaStream_t s);
+int launch_big_bucket(const BuildArgs &a, const BucketArgs &b, uint64_t bucket, uint64_t rb,
+                      uint64_t re, Entry *table, uint64_t cap, cudaStream_t s);
 cudaError_t run_probe(int kind, uint64_t table_bytes, uint64_t n_ops, cudaStream_t s, float *ms);
 int device_sm_count();
 

@@ -34,7 +34,7 @@ class SwgError(RuntimeError):
         self.status = status
 
 
-ALGO_DEFAULT, ALGO_DIRECT, ALGO_PARTITIONED = 0, 1, 2
+ALGO_DEFAULT, ALGO_DIRECT, ALGO_PARTITIONED, ALGO_BUCKETED = 0, 1, 2, 3
 ORDER_INPUT, ORDER_MINIMIZER = 0, 1
 
 

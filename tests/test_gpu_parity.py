@@ -29,11 +29,12 @@ def assert_same_records(g: swapgb.Graph, text: bytes, k: int, c: int) -> None:
 
 
 # (algorithm, read order): direct in input order (the default), direct in
-# minimizer order, partitioned
+# minimizer order, partitioned, bucketed
 ALGOS = [pytest.param(dict(algorithm=swapgb.ALGO_DIRECT), id="direct"),
          pytest.param(dict(algorithm=swapgb.ALGO_DIRECT, read_order=swapgb.ORDER_MINIMIZER),
                       id="direct-minimizer-order"),
-         pytest.param(dict(algorithm=swapgb.ALGO_PARTITIONED), id="partitioned")]
+         pytest.param(dict(algorithm=swapgb.ALGO_PARTITIONED), id="partitioned"),
+         pytest.param(dict(algorithm=swapgb.ALGO_BUCKETED), id="bucketed")]
 
 
 @pytest.mark.parametrize("algo", ALGOS)
@@ -231,3 +232,16 @@ def test_autotune_then_build(tmp_path):
     assert swapgb.autotune_apply(cache, 31, 100, opts)
     g = swapgb.Graph().build_reads(opts, r)
     assert_same_records(g, text, 31, 5)
+
+
+def test_bucketed_large_input_and_hot_buckets():
+    text = swapgb.synth_fasta(seed=23, genome_len=2_000_000, n_reads=1_000_000, read_len=100,
+                              sub_rate=0.01, indel_rate=0.001)
+    g = gpu_build(text, 31, 5, algorithm=swapgb.ALGO_BUCKETED)
+    assert_same_records(g, text, 31, 5)
+    # one k-mer repeated far more often than a shared-memory bucket holds
+    reads = ["A" * 250, "AC" * 125] * 30000 + ["ACGTTGCA" * 20] * 500
+    text = "".join(">h%d\n%s\n" % (i, r) for i, r in enumerate(reads)).encode()
+    g = gpu_build(text, 21, 2, algorithm=swapgb.ALGO_BUCKETED)
+    assert g.info()["waves"] >= 1  # global-memory path taken
+    assert_same_records(g, text, 21, 2)
