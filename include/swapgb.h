@@ -85,16 +85,20 @@ typedef struct swg_opts {
 
 /* What the last build did (for measurement and tests). */
 typedef struct swg_build_info {
-    int algorithm;        /* SWG_ALGO_DIRECT or SWG_ALGO_PARTITIONED */
+    int algorithm;        /* SWG_ALGO_DIRECT, _PARTITIONED or _BUCKETED */
     int launches;         /* kernel launches of the build */
     uint64_t occurrences; /* k-mer occurrences counted */
     uint64_t distinct;    /* distinct k-molecules before the cutoff */
     uint64_t survivors;   /* after the cutoff */
-    uint64_t table_entries; /* direct: table capacity; partitioned: entries per slice slot */
-    uint32_t partitions;  /* partitioned: number of partitions */
-    uint32_t slots;       /* partitioned: partitions counted at once (one wave) */
-    uint32_t waves;       /* partitioned: waves */
-    uint32_t retries;     /* rebuilds after a full table */
+    uint64_t table_entries; /* direct: table capacity; partitioned: entries per slice slot;
+                               bucketed: number of buckets */
+    uint32_t partitions;  /* partitioned, bucketed: number of (level-1) partitions */
+    uint32_t slots;       /* partitioned: partitions counted at once (one wave);
+                             bucketed: sub-buckets per partition */
+    uint32_t waves;       /* partitioned: waves; bucketed: buckets counted in a
+                             global-memory table */
+    uint32_t retries;     /* direct: rebuilds after a full table; bucketed: buckets
+                             recounted in the larger (tier-2) shared-memory table */
     double estimate;      /* direct: distinct-count estimate used for sizing */
     float ms[5];          /* as swg_graph_last_timings */
 } swg_build_info;

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -28,9 +29,11 @@ using swg::Entry;
 
 struct Control {  // device-side control block
     unsigned status;
-    unsigned pad;
+    unsigned pad;                    // bucketed build: tier-1 overflow count
     unsigned long long counters[2];  // inserted keys, survivors
-    uint64_t occ_total;
+    unsigned pad2;                   // bucketed build: tier-2 overflow count
+    unsigned pad3;
+    uint64_t occ_total;              // last: the memsets of the control block stop before it
 };
 
 struct swg_graph {
@@ -721,8 +724,11 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     const uint64_t N = a.total_occ;
     int b1 = N <= (400ull << 20) ? 8 : (N <= (1600ull << 20) ? 9 : 10);
     const uint64_t P = 1ull << b1;
+    // sub-buckets of about kBucketRecords records (SWG_BUCKET_RECORDS overrides)
+    double target = 6144.0;
+    if (const char *e = std::getenv("SWG_BUCKET_RECORDS")) target = std::max(64.0, std::atof(e));
     int b2 = 0;
-    while (b2 < 11 && (double)N / (double)(P << b2) > 700.0) b2++;
+    while (b2 < 10 && (double)N / (double)(P << b2) > target) b2++;
     swg::PartArgs pa;
     std::memset(&pa, 0, sizeof(pa));
     pa.bits = b1;
@@ -737,7 +743,10 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     if ((st = ensure(&g->d_rec2, &g->rec2_cap, std::max<uint64_t>(N, 1), "bucket records"))) return st;
     const uint64_t NB = P << b2;
     const uint64_t scratch = swg::gscan_scratch(NB);
-    if ((st = ensure(&g->d_bk, &g->bk_cap, 3 * NB + 1 + scratch + 2, "bucket table"))) return st;
+    // d_bk: cursors / survivor counts [NB] | offsets [NB+1] | big list [NB] |
+    // survivor prefix [NB+1] | scan scratch | totals [2] | chunk prefix [P+1] |
+    // second big list [NB]
+    if ((st = ensure(&g->d_bk, &g->bk_cap, 5 * NB + 2 + scratch + 2 + P + 1, "bucket table"))) return st;
     const uint64_t out_want = std::max<uint64_t>(N, 1);
     if (g->out_cap < out_want || !g->d_out_keys || !g->d_out_mult) {
         cudaFree(g->d_out_keys);
@@ -766,14 +775,21 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     bk.big_cap = (uint32_t)std::min<uint64_t>(NB, 0xffffffffu);
     bk.big_count = &g->d_ctl->pad;
     bk.n_rec = N;
-    unsigned long long *scr = g->d_bk + 3 * NB + 1;
+    bk.surv = bk.cursor2;  // the cursors are spent once the records are grouped
+    bk.surv_off = g->d_bk + 3 * NB + 1;
+    bk.stage_keys = g->d_records;  // level-1 records are spent too
+    unsigned long long *scr = bk.surv_off + NB + 1;
     unsigned long long *tot = scr + scratch;
+    bk.chunk_start = tot + 2;
+    bk.big2 = bk.chunk_start + P + 1;
+    bk.big2_count = &g->d_ctl->pad2;
 
     SWG_CUDA(cudaMemsetAsync(pa.part_count, 0, P * 8, s), "clear partitions");
     g->launches += swg::launch_part_count(a, pa, s);
     g->launches += swg::launch_part_prefix(pa, s);
     SWG_CUDA(cudaEventRecord(g->ev[1], s), "event");
     g->launches += swg::launch_part_scatter(a, pa, s);
+    g->launches += swg::launch_chunk_prefix(bk, s);
     SWG_CUDA(cudaMemsetAsync(bk.cursor2, 0, NB * 8, s), "clear bucket counts");
     g->launches += swg::launch_sub_hist(bk, s);
     g->launches += swg::launch_gscan(reinterpret_cast<const uint64_t *>(bk.cursor2),
@@ -785,16 +801,22 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     SWG_CUDA(cudaGetLastError(), "bucket scatter launch");
     SWG_CUDA(cudaEventRecord(g->ev[2], s), "event");
     g->launches += swg::launch_bucket_count(a, bk, s);
+    g->launches += swg::launch_gscan(reinterpret_cast<const uint64_t *>(bk.surv),
+                                     reinterpret_cast<uint64_t *>(bk.surv_off), NB,
+                                     reinterpret_cast<uint64_t *>(scr),
+                                     reinterpret_cast<uint64_t *>(bk.surv_off + NB), s);
+    g->launches += swg::launch_bucket_gather(a, bk, NB, s);
     SWG_CUDA(cudaGetLastError(), "bucket count launch");
     SWG_CUDA(cudaMemcpyAsync(g->h_ctl, g->d_ctl, sizeof(Control) - sizeof(uint64_t),
                              cudaMemcpyDeviceToHost, s), "read status");
     SWG_CUDA(cudaStreamSynchronize(s), "bucket count");
     (void)tot;
-    const unsigned nbig = g->h_ctl->pad;
-    g->big_buckets = nbig;
+    const unsigned nbig = g->h_ctl->pad2;  // buckets no shared-memory table held
+    g->big_buckets = g->h_ctl->pad;
+    g->retries = g->h_ctl->pad;
     if (nbig) {  // hot buckets: count them in a global-memory table, one after another
         std::vector<unsigned long long> big(nbig), offs(NB + 1);
-        SWG_CUDA(cudaMemcpyAsync(big.data(), bk.big, nbig * 8, cudaMemcpyDeviceToHost, s), "read big buckets");
+        SWG_CUDA(cudaMemcpyAsync(big.data(), bk.big2, nbig * 8, cudaMemcpyDeviceToHost, s), "read big buckets");
         SWG_CUDA(cudaMemcpyAsync(offs.data(), bk.off2, (NB + 1) * 8, cudaMemcpyDeviceToHost, s),
                  "read bucket offsets");
         SWG_CUDA(cudaStreamSynchronize(s), "big buckets");

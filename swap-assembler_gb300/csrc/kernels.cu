@@ -13,6 +13,10 @@
 //                 graph.cpp:1058-1080)
 //   k_compact     K2: the -c cutoff (graph.cpp:1092-1114) as one streaming
 //                 pass over the table with block-level stream compaction
+//   k_p1_*, k_sub_*, k_bucket_*
+//                 bucketed build: two hash-partition scatters group the
+//                 occurrence records by bucket, then one CTA per bucket
+//                 counts it in a shared-memory table
 //   k_probe       random-access roofline probe
 //
 // Every device-side retry loop is bounded; on exhaustion the kernel sets a
@@ -745,26 +749,181 @@ __device__ __forceinline__ uint64_t slice_cap_of(const PartArgs &pa, unsigned lo
     return c < pa.slot_cap ? c : pa.slot_cap;
 }
 
-// Phase A: records per partition.
-__global__ void __launch_bounds__(kK1Block) k_part_count(BuildArgs a, PartArgs pa) {
-    __shared__ TileSmem s;
+// Shared memory of k_p1_scatter: a round's records, their partitions and
+// order, and per partition its count, local offset and global run base.
+size_t p1_scatter_smem(uint32_t n_parts) {
+    return kTileOcc * (sizeof(unsigned long long) + sizeof(unsigned short)) +
+           (size_t)n_parts * (sizeof(unsigned long long) + 2 * sizeof(unsigned));
+}
+
+// One read per thread, rolled base by base: the state of one read's walk.
+// Bases stream in from the packed words (one load per 16 bases); the left
+// neighbour of a k-mer is the base its predecessor shifted out.
+struct ReadWalk {
+    uint64_t fwd, rc, kmask;
+    uint64_t wnext;    // index of the next packed word
+    uint32_t w;        // bases not yet consumed of the current word, MSB first
+    uint32_t wrem;     // how many
+    uint32_t L, p;     // read length, position of the current k-mer
+    uint32_t nb;       // base p+k (valid when p+k < L)
+    uint32_t lb;       // base p-1 (valid when p >= 1)
+    int k, top;
+    uint32_t left;     // occurrences still to emit
+};
+
+__device__ __forceinline__ uint32_t walk_next(const BuildArgs &a, ReadWalk &st) {
+    if (st.wrem == 0) {
+        st.w = ldw(a.packed, st.wnext++, a.n_words);
+        st.wrem = 16;
+    }
+    const uint32_t b = st.w >> 30;
+    st.w <<= 2;
+    st.wrem--;
+    return b;
+}
+
+__device__ __forceinline__ void walk_init(const BuildArgs &a, ReadWalk &st, uint64_t r) {
+    const uint32_t seg = seg_of(a, r);
+    st.k = k_of(a, seg);
+    st.L = a.read_len[r];
+    st.left = st.L >= (uint32_t)st.k ? st.L - (uint32_t)st.k + 1 : 0;
+    if (!st.left) return;
+    st.kmask = (1ull << (2 * st.k)) - 1;
+    st.top = 2 * (st.k - 1);
+    const uint64_t g0 = a.read_off[r];
+    st.wnext = (g0 >> 4) + 1;
+    st.w = ldw(a.packed, g0 >> 4, a.n_words) << (2 * (uint32_t)(g0 & 15));
+    st.wrem = 16 - (uint32_t)(g0 & 15);
+    st.fwd = st.rc = 0;
+    for (int i = 0; i < st.k; ++i) {
+        const uint32_t b = walk_next(a, st);
+        st.fwd = (st.fwd << 2) | b;
+        st.rc = (st.rc >> 2) | ((uint64_t)(3u - b) << st.top);
+    }
+    st.p = 0;
+    st.lb = 0;
+    st.nb = (uint32_t)st.k < st.L ? walk_next(a, st) : 0u;
+}
+
+// Emit the current occurrence (key, arc code) and advance to the next one.
+// Arc slots as make_occ (kmerGraph.cpp:240-296): right (f ? 0 : 4) +
+// base[p+k], left (f ? 4 : 0) + 3 - base[p-1], f = (forward k-mer is the
+// canonical one).
+__device__ __forceinline__ void walk_emit(const BuildArgs &a, ReadWalk &st, uint64_t &key,
+                                          unsigned &code) {
+    const bool f = st.fwd >= st.rc;
+    key = f ? st.fwd : st.rc;
+    code = 0;
+    if (st.left > 1) code = 0x08u | ((f ? 0u : 4u) + st.nb);  // p + k < L
+    if (st.p) code |= 0x80u | (((f ? 4u : 0u) + 3u - st.lb) << 4);
+    if (--st.left) {
+        const uint32_t b = st.nb;
+        st.lb = (uint32_t)(st.fwd >> st.top);
+        st.fwd = ((st.fwd << 2) | b) & st.kmask;
+        st.rc = (st.rc >> 2) | ((uint64_t)(3u - b) << st.top);
+        ++st.p;
+        if (st.left > 1) st.nb = walk_next(a, st);
+    }
+}
+
+// Level-1 records per partition, one thread per read (contiguous read ranges
+// per block).
+__global__ void __launch_bounds__(256) k_p1_count(BuildArgs a, PartArgs pa) {
     __shared__ unsigned hist[1 << kPartBitsMax];
     for (uint32_t j = threadIdx.x; j < pa.n_parts; j += blockDim.x) hist[j] = 0;
+    __syncthreads();
     const int shift = 64 - pa.bits;
-    for (uint64_t t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
-        __syncthreads();
-        const TileView v = load_tile(a, t, s);
-        __syncthreads();
-        const uint64_t A = t * kTileOcc;
-        const uint64_t B = umin64(A + kTileOcc, a.total_occ);
-        const uint64_t i0 = A + (uint64_t)threadIdx.x * kK1Items;
-        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B), [&](uint64_t key, unsigned, uint64_t, uint32_t) {
+    const uint64_t r0 = a.n_reads * blockIdx.x / gridDim.x;
+    const uint64_t r1 = a.n_reads * (blockIdx.x + 1) / gridDim.x;
+    for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        ReadWalk st;
+        walk_init(a, st, r);
+        while (st.left) {
+            uint64_t key;
+            unsigned code;
+            walk_emit(a, st, key, code);
             atomicAdd(&hist[mix64(key) >> shift], 1u);
-        });
+        }
     }
     __syncthreads();
     for (uint32_t j = threadIdx.x; j < pa.n_parts; j += blockDim.x)
         if (hist[j]) atomicAdd(&pa.part_count[j], (unsigned long long)hist[j]);
+}
+
+// Level-1 scatter, one thread per read: every round each thread emits up to
+// kK1Items records of its read into registers, taking its rank within the
+// partition from the shared histogram; the block orders the round's records
+// by partition in shared memory and writes one run per partition.
+__global__ void __launch_bounds__(256, 3) k_p1_scatter(BuildArgs a, PartArgs pa) {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    unsigned long long *sorted = reinterpret_cast<unsigned long long *>(dyn);
+    unsigned long long *gbase = sorted + kTileOcc;
+    unsigned *hist = reinterpret_cast<unsigned *>(gbase + pa.n_parts);
+    unsigned *loff = hist + pa.n_parts;
+    unsigned short *spart = reinterpret_cast<unsigned short *>(loff + pa.n_parts);
+    __shared__ uint64_t wb[8];
+    const int shift = 64 - pa.bits;
+    const uint32_t per = (pa.n_parts + blockDim.x - 1) / blockDim.x;
+    const uint64_t r0 = a.n_reads * blockIdx.x / gridDim.x;
+    const uint64_t r1 = a.n_reads * (blockIdx.x + 1) / gridDim.x;
+    for (uint64_t base = r0; base < r1; base += blockDim.x) {
+        const uint64_t r = base + threadIdx.x;
+        ReadWalk st;
+        st.left = 0;
+        if (r < r1) walk_init(a, st, r);
+        while (__syncthreads_or(st.left != 0)) {
+            for (uint32_t j = threadIdx.x; j < pa.n_parts; j += blockDim.x) hist[j] = 0;
+            __syncthreads();
+            unsigned long long rec[kK1Items];
+            unsigned pr[kK1Items];  // partition | rank << 16; ~0 for no record
+#pragma unroll
+            for (int j = 0; j < kK1Items; ++j) {
+                pr[j] = ~0u;
+                rec[j] = 0;
+                if (st.left) {
+                    uint64_t key;
+                    unsigned code;
+                    walk_emit(a, st, key, code);
+                    const uint64_t h = mix64(key);
+                    const unsigned part = (unsigned)(h >> shift);
+                    rec[j] = ((h << pa.bits) >> (pa.bits - 8)) | code;  // low 64-b1 bits << 8
+                    pr[j] = part | (atomicAdd(&hist[part], 1u) << 16);
+                }
+            }
+            __syncthreads();
+            uint64_t mine = 0;
+            for (uint32_t x = 0; x < per; ++x) {
+                const uint32_t j = threadIdx.x * per + x;
+                if (j < pa.n_parts) mine += hist[j];
+            }
+            uint64_t total;
+            uint64_t run = block_exclusive_scan<256>(mine, wb, &total);
+            for (uint32_t x = 0; x < per; ++x) {
+                const uint32_t j = threadIdx.x * per + x;
+                if (j < pa.n_parts) {
+                    const unsigned c = hist[j];
+                    loff[j] = (unsigned)run;
+                    run += c;
+                    gbase[j] = c ? atomicAdd(&pa.part_cursor[j], (unsigned long long)c) : 0;
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < kK1Items; ++j) {
+                if (pr[j] != ~0u) {
+                    const unsigned part = pr[j] & 0xffffu;
+                    const unsigned pos = loff[part] + (pr[j] >> 16);
+                    sorted[pos] = rec[j];
+                    spart[pos] = (unsigned short)part;
+                }
+            }
+            __syncthreads();
+            for (uint32_t j = threadIdx.x; j < (uint32_t)total; j += blockDim.x) {
+                const unsigned part = spart[j];
+                pa.records[gbase[part] + (j - loff[part])] = sorted[j];
+            }
+        }
+    }
 }
 
 // Exclusive prefix over the partitions (n_parts <= 1024, one block).
@@ -779,73 +938,6 @@ __global__ void __launch_bounds__(1024) k_part_prefix(PartArgs pa) {
         pa.part_cursor[j] = ex;
     }
     if (j == 0) pa.part_start[pa.n_parts] = total;
-}
-
-// Phase B: scatter the records, grouped by partition inside each tile so
-// that every warp writes runs of consecutive records.
-constexpr size_t kScatterDynSmem = kTileOcc * (sizeof(unsigned long long) + 2 * sizeof(unsigned short));
-
-__global__ void __launch_bounds__(kK1Block) k_part_scatter(BuildArgs a, PartArgs pa) {
-    extern __shared__ __align__(16) unsigned char dyn[];
-    unsigned long long *rec = reinterpret_cast<unsigned long long *>(dyn);
-    unsigned short *pid = reinterpret_cast<unsigned short *>(rec + kTileOcc);
-    unsigned short *perm = pid + kTileOcc;
-    __shared__ TileSmem s;
-    __shared__ unsigned hist[1 << kPartBitsMax];
-    __shared__ unsigned loff[1 << kPartBitsMax];
-    __shared__ unsigned long long gbase[1 << kPartBitsMax];
-    __shared__ uint64_t wb[kK1Block / 32];
-    const int shift = 64 - pa.bits;
-    const uint64_t lowmask = (1ull << shift) - 1;
-    const uint32_t per = (pa.n_parts + kK1Block - 1) / kK1Block;  // partitions per thread
-    for (uint64_t t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
-        __syncthreads();
-        for (uint32_t j = threadIdx.x; j < pa.n_parts; j += blockDim.x) hist[j] = 0;
-        const TileView v = load_tile(a, t, s);
-        __syncthreads();
-        const uint64_t A = t * kTileOcc;
-        const uint64_t B = umin64(A + kTileOcc, a.total_occ);
-        const uint32_t n = (uint32_t)(B - A);
-        uint32_t q = threadIdx.x * kK1Items;
-        const uint64_t i0 = A + q;
-        walk_run(a, v, s, i0, umin64(i0 + kK1Items, B), [&](uint64_t key, unsigned code, uint64_t, uint32_t) {
-            const uint64_t h = mix64(key);
-            const unsigned part = (unsigned)(h >> shift);
-            rec[q] = ((h & lowmask) << 8) | code;
-            pid[q] = (unsigned short)part;
-            atomicAdd(&hist[part], 1u);
-            ++q;
-        });
-        __syncthreads();
-        // local offsets of the partitions inside the tile, and their global runs
-        uint64_t mine = 0;
-        for (uint32_t x = 0; x < per; ++x) {
-            const uint32_t j = threadIdx.x * per + x;
-            if (j < pa.n_parts) mine += hist[j];
-        }
-        uint64_t run = block_exclusive_scan<kK1Block>(mine, wb, nullptr);
-        for (uint32_t x = 0; x < per; ++x) {
-            const uint32_t j = threadIdx.x * per + x;
-            if (j < pa.n_parts) {
-                const unsigned c = hist[j];
-                loff[j] = (unsigned)run;
-                run += c;
-                gbase[j] = c ? atomicAdd(&pa.part_cursor[j], (unsigned long long)c) : 0;
-                hist[j] = 0;
-            }
-        }
-        __syncthreads();
-        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-            const unsigned part = pid[i];
-            perm[loff[part] + atomicAdd(&hist[part], 1u)] = (unsigned short)i;
-        }
-        __syncthreads();
-        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
-            const unsigned i = perm[j];
-            const unsigned part = pid[i];
-            pa.records[gbase[part] + (j - loff[part])] = rec[i];
-        }
-    }
 }
 
 // Phase C: count the records of partitions [p0, p0+n) into their slices.
@@ -953,224 +1045,321 @@ __global__ void __launch_bounds__(kCBlock) k_part_compact(BuildArgs a, PartArgs 
 }
 
 // ---------------------------------------------------------------------
-// Bucketed build. Level-1 records come from k_part_scatter (2^b1 partitions,
+// Bucketed build. Level-1 records come from k_p1_scatter (2^b1 partitions,
 // record = low 64-b1 bits of h shifted left by 8 | arc code); the next b2
-// bits of h name the sub-bucket. Each bucket is then counted by one CTA in a
-// shared-memory hash table and compacted from there.
-constexpr int kBkChunk = 4096;    // records per block in the sub-bucket passes
-constexpr int kBkTable = 2048;    // shared-memory table entries per bucket
-constexpr int kBkSmemMax = 1400;  // larger buckets take the global-memory path
-constexpr int kBkBinsMax = 2 << 11;  // local bins of a chunk: two partitions x 2^b2 (b2 <= 11)
-constexpr int kBkPartsMax = 1 << kPartBitsMax;
+// bits of h name the sub-bucket. The level-2 passes walk each partition in
+// chunks of kBkChunk records (a chunk never spans two partitions). Each
+// bucket is then counted by one CTA in a shared-memory hash table sized to
+// the bucket, and compacted from there.
+constexpr int kBkItems = 16;                     // records per thread in a chunk
+constexpr int kBkChunk = 256 * kBkItems;         // records per chunk
+constexpr int kBkBinsMax = 1 << 10;              // sub-buckets per partition (b2 <= 10)
+constexpr int kBkTable = 4096;                   // largest shared-memory table (entries)
+constexpr uint64_t kBkRecMax = 65535;            // 16-bit slot counters cannot carry past this
+constexpr int kBkThreads = 512;                  // threads of a bucket CTA
+constexpr int kBkBatch = 8;                      // records loaded ahead per thread
+constexpr int kBkTable2 = 8192;                  // tier-2 table (entries), one CTA per SM
+constexpr int kBkThreads2 = 1024;
 
 __device__ __forceinline__ uint32_t sub_of(const BucketArgs &b, unsigned long long rec) {
     return b.b2 ? (uint32_t)((rec >> 8) >> (64 - b.b1 - b.b2)) : 0u;
 }
 
-// Level-1 partition of record index r (last p with part_start[p] <= r).
-__device__ __forceinline__ uint32_t part_of_rec(const unsigned long long *st, uint32_t n_parts,
-                                                uint64_t r) {
-    uint32_t lo = 0, hi = n_parts;
+// Chunks per partition, as an exclusive prefix (one block).
+__global__ void __launch_bounds__(1024) k_chunk_prefix(BucketArgs b) {
+    __shared__ uint64_t wb[32];
+    const uint32_t j = threadIdx.x;
+    uint64_t c = 0;
+    if (j < b.n_parts) c = (b.part_start[j + 1] - b.part_start[j] + kBkChunk - 1) / kBkChunk;
+    uint64_t total;
+    const uint64_t ex = block_exclusive_scan<1024>(c, wb, &total);
+    if (j < b.n_parts) b.chunk_start[j] = ex;
+    if (j == 0) b.chunk_start[b.n_parts] = total;
+}
+
+// Partition p and record range [r0, r1) of level-2 chunk q.
+__device__ __forceinline__ uint32_t chunk_range(const BucketArgs &b, uint64_t q, uint64_t &r0,
+                                                uint64_t &r1) {
+    uint32_t lo = 0, hi = b.n_parts;
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (st[mid] <= r) lo = mid;
+        if (b.chunk_start[mid] <= q) lo = mid;
         else hi = mid;
     }
+    r0 = b.part_start[lo] + (q - b.chunk_start[lo]) * kBkChunk;
+    r1 = umin64(r0 + kBkChunk, b.part_start[lo + 1]);
     return lo;
 }
 
+// Records per bucket (into cursor2).
 __global__ void __launch_bounds__(256) k_sub_hist(BucketArgs b) {
-    __shared__ unsigned long long st[kBkPartsMax + 1];
     __shared__ unsigned hist[kBkBinsMax];
     const uint32_t P2 = 1u << b.b2;
-    for (uint32_t j = threadIdx.x; j <= b.n_parts; j += blockDim.x) st[j] = b.part_start[j];
-    for (uint32_t j = threadIdx.x; j < 2 * P2; j += blockDim.x) hist[j] = 0;
-    __syncthreads();
-    const uint64_t r0 = (uint64_t)blockIdx.x * kBkChunk;
-    const uint64_t r1 = umin64(r0 + kBkChunk, b.n_rec);
-    const uint32_t p0 = part_of_rec(st, b.n_parts, r0);
-    for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-        const unsigned long long rec = b.rec1[r];
-        uint32_t p = p0;
-        while (p + 1 < b.n_parts && st[p + 1] <= r) ++p;
-        const uint32_t sub = sub_of(b, rec);
-        if (p - p0 < 2) atomicAdd(&hist[(p - p0) * P2 + sub], 1u);
-        else atomicAdd(&b.cursor2[(uint64_t)p * P2 + sub], 1ull);  // rare: tiny partitions
-    }
-    __syncthreads();
-    for (uint32_t j = threadIdx.x; j < 2 * P2; j += blockDim.x) {
-        const uint32_t p = p0 + j / P2;
-        if (hist[j] && p < b.n_parts) atomicAdd(&b.cursor2[(uint64_t)p * P2 + (j % P2)], (unsigned long long)hist[j]);
+    const uint64_t nq = b.chunk_start[b.n_parts];
+    for (uint64_t q = blockIdx.x; q < nq; q += gridDim.x) {
+        uint64_t r0, r1;
+        const uint32_t p = chunk_range(b, q, r0, r1);
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < P2; j += blockDim.x) hist[j] = 0;
+        __syncthreads();
+#pragma unroll 4
+        for (int it = 0; it < kBkItems; ++it) {
+            const uint64_t r = r0 + (uint64_t)it * 256 + threadIdx.x;
+            if (r < r1) atomicAdd(&hist[sub_of(b, b.rec1[r])], 1u);
+        }
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < P2; j += blockDim.x)
+            if (hist[j]) atomicAdd(&b.cursor2[(uint64_t)p * P2 + j], (unsigned long long)hist[j]);
     }
 }
 
+// Level-2 scatter: a chunk is held in registers, ordered by sub-bucket in
+// shared memory and written as one run per sub-bucket.
 constexpr size_t kSubScatterDyn = kBkChunk * sizeof(unsigned long long) +
-                                  2 * kBkChunk * sizeof(unsigned short) +
                                   kBkBinsMax * (2 * sizeof(unsigned) + sizeof(unsigned long long));
 
-__global__ void __launch_bounds__(256) k_sub_scatter(BucketArgs b) {
+__global__ void __launch_bounds__(256, 3) k_sub_scatter(BucketArgs b) {
     extern __shared__ __align__(16) unsigned char dyn[];
-    unsigned long long *rec = reinterpret_cast<unsigned long long *>(dyn);
-    unsigned long long *gbase = rec + kBkChunk;
+    unsigned long long *sorted = reinterpret_cast<unsigned long long *>(dyn);
+    unsigned long long *gbase = sorted + kBkChunk;
     unsigned *hist = reinterpret_cast<unsigned *>(gbase + kBkBinsMax);
     unsigned *loff = hist + kBkBinsMax;
-    unsigned short *bin = reinterpret_cast<unsigned short *>(loff + kBkBinsMax);
-    unsigned short *perm = bin + kBkChunk;
-    __shared__ unsigned long long st[kBkPartsMax + 1];
     __shared__ uint64_t wb[8];
-    const uint32_t P2 = 1u << b.b2, nb = 2 * P2;
-    for (uint32_t j = threadIdx.x; j <= b.n_parts; j += blockDim.x) st[j] = b.part_start[j];
-    for (uint32_t j = threadIdx.x; j < nb; j += blockDim.x) hist[j] = 0;
-    __syncthreads();
-    const uint64_t r0 = (uint64_t)blockIdx.x * kBkChunk;
-    const uint32_t n = (uint32_t)(umin64(r0 + kBkChunk, b.n_rec) - r0);
-    const uint32_t p0 = part_of_rec(st, b.n_parts, r0);
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-        const uint64_t r = r0 + i;
-        const unsigned long long v = b.rec1[r];
-        uint32_t p = p0;
-        while (p + 1 < b.n_parts && st[p + 1] <= r) ++p;
-        const uint32_t sub = sub_of(b, v);
-        if (p - p0 < 2) {
-            const uint32_t bn = (p - p0) * P2 + sub;
-            rec[i] = v;
-            bin[i] = (unsigned short)bn;
-            atomicAdd(&hist[bn], 1u);
-        } else {  // rare: a chunk spanning more than two partitions
-            const unsigned long long pos = atomicAdd(&b.cursor2[(uint64_t)p * P2 + sub], 1ull);
-            b.rec2[pos] = v;
-            bin[i] = 0xffff;
+    const uint32_t P2 = 1u << b.b2;
+    const uint32_t per = (P2 + 255) / 256;  // bins per thread in the scan
+    const uint64_t nq = b.chunk_start[b.n_parts];
+    for (uint64_t q = blockIdx.x; q < nq; q += gridDim.x) {
+        uint64_t r0, r1;
+        const uint32_t p = chunk_range(b, q, r0, r1);
+        unsigned long long v[kBkItems];
+#pragma unroll
+        for (int it = 0; it < kBkItems; ++it) {
+            const uint64_t r = r0 + (uint64_t)it * 256 + threadIdx.x;
+            v[it] = r < r1 ? b.rec1[r] : 0ull;
         }
-    }
-    __syncthreads();
-    // local offsets of the bins, global runs for each
-    const uint32_t per = (nb + blockDim.x - 1) / blockDim.x;
-    uint64_t mine = 0;
-    for (uint32_t x = 0; x < per; ++x) {
-        const uint32_t j = threadIdx.x * per + x;
-        if (j < nb) mine += hist[j];
-    }
-    uint64_t run = block_exclusive_scan<256>(mine, wb, nullptr);
-    for (uint32_t x = 0; x < per; ++x) {
-        const uint32_t j = threadIdx.x * per + x;
-        if (j < nb) {
-            const unsigned c = hist[j];
-            loff[j] = (unsigned)run;
-            run += c;
-            const uint32_t p = p0 + j / P2;
-            gbase[j] = (c && p < b.n_parts) ? atomicAdd(&b.cursor2[(uint64_t)p * P2 + (j % P2)], (unsigned long long)c) : 0;
-            hist[j] = 0;
+        __syncthreads();  // the previous chunk is written out
+        for (uint32_t j = threadIdx.x; j < P2; j += blockDim.x) hist[j] = 0;
+        __syncthreads();
+#pragma unroll
+        for (int it = 0; it < kBkItems; ++it)
+            if (r0 + (uint64_t)it * 256 + threadIdx.x < r1) atomicAdd(&hist[sub_of(b, v[it])], 1u);
+        __syncthreads();
+        uint64_t mine = 0;
+        for (uint32_t x = 0; x < per; ++x) {
+            const uint32_t j = threadIdx.x * per + x;
+            if (j < P2) mine += hist[j];
         }
-    }
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-        const unsigned bn = bin[i];
-        if (bn != 0xffff) perm[loff[bn] + atomicAdd(&hist[bn], 1u)] = (unsigned short)i;
-    }
-    __syncthreads();
-    const unsigned kept = loff[nb - 1] + hist[nb - 1];
-    for (uint32_t j = threadIdx.x; j < kept; j += blockDim.x) {
-        const unsigned i = perm[j];
-        const unsigned bn = bin[i];
-        b.rec2[gbase[bn] + (j - loff[bn])] = rec[i];
+        uint64_t run = block_exclusive_scan<256>(mine, wb, nullptr);
+        for (uint32_t x = 0; x < per; ++x) {
+            const uint32_t j = threadIdx.x * per + x;
+            if (j < P2) {
+                const unsigned c = hist[j];
+                loff[j] = (unsigned)run;
+                run += c;
+                gbase[j] = c ? atomicAdd(&b.cursor2[(uint64_t)p * P2 + j], (unsigned long long)c) : 0;
+                hist[j] = 0;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int it = 0; it < kBkItems; ++it) {
+            if (r0 + (uint64_t)it * 256 + threadIdx.x < r1) {
+                const uint32_t bn = sub_of(b, v[it]);
+                sorted[loff[bn] + atomicAdd(&hist[bn], 1u)] = v[it];
+            }
+        }
+        __syncthreads();
+        const uint32_t n = (uint32_t)(r1 - r0);
+        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+            const unsigned long long w = sorted[j];
+            const uint32_t bn = sub_of(b, w);
+            b.rec2[gbase[bn] + (j - loff[bn])] = w;
+        }
     }
 }
 
-constexpr size_t kBucketDyn = kBkTable * (sizeof(unsigned long long) + 4 * sizeof(unsigned));
+template <int T>
+constexpr size_t bucket_smem() { return (size_t)T * (sizeof(unsigned long long) + 4 * sizeof(unsigned)); }
 
-// One CTA per bucket: count in shared memory, cutoff, compact.
-__global__ void __launch_bounds__(256) k_bucket_count(BuildArgs a, BucketArgs b) {
-    extern __shared__ __align__(16) unsigned char dyn[];
-    unsigned long long *keys = reinterpret_cast<unsigned long long *>(dyn);
-    unsigned *cnt = reinterpret_cast<unsigned *>(keys + kBkTable);  // 8 x uint16 per entry
-    __shared__ uint64_t wb[8];
-    __shared__ unsigned long long s_base;
-    const uint64_t bk = blockIdx.x;
+// Eight saturated uint8 multiplicities of table entry s (8 x uint16
+// counters, slot t in half t&1 of word t>>1), after the -c cutoff
+// (graph.cpp:1105: a multiplicity below c becomes 0). SWAR on the 16-bit
+// halves: min(v, 255), then v + 0x8000 - c has bit 15 set iff v >= c (no
+// carry leaves a half since v <= 255 and 1 <= c <= 255).
+__device__ __forceinline__ uint64_t bucket_mult(const unsigned *cnt, uint32_t s, unsigned cbias,
+                                                bool cut_all) {
+    const uint4 cv = reinterpret_cast<const uint4 *>(cnt)[s];
+    unsigned w[4] = {cv.x, cv.y, cv.z, cv.w};
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        w[t] = __vminu2(w[t], 0x00ff00ffu);
+        if (cbias) {
+            const unsigned ge = ((w[t] + cbias) >> 15) & 0x00010001u;
+            w[t] &= ge * 0xffffu;
+        }
+    }
+    const uint64_t m = ((uint64_t)__byte_perm(w[2], w[3], 0x6420) << 32) | __byte_perm(w[0], w[1], 0x6420);
+    return cut_all ? 0 : m;
+}
+
+// Counts bucket bk in a shared-memory table of 2x the bucket's records (at
+// most kT entries), applies the cutoff and stages the survivors in the
+// bucket's own record range (keys in stage_keys, multiplicities over the
+// bucket's records, all read by then); k_bucket_gather packs them. A bucket
+// whose keys do not fit, or with more records than the 16-bit slot counters
+// hold, is appended to the overflow list instead. Returns with the block
+// converged.
+template <int kT, int kNT>
+__device__ void bucket_count_one(const BuildArgs &a, const BucketArgs &b, uint64_t bk,
+                                 unsigned long long *keys, unsigned *cnt, unsigned &s_over,
+                                 unsigned &s_kept, unsigned &s_used, unsigned long long *ovf,
+                                 unsigned *ovf_count, uint32_t ovf_cap) {
     const uint64_t rb = b.off2[bk], re = b.off2[bk + 1];
     const uint64_t nrec = re - rb;
-    if (nrec == 0) return;
-    if (nrec > (uint64_t)kBkSmemMax) {
+    if (nrec == 0) {
+        if (threadIdx.x == 0) b.surv[bk] = 0;
+        return;
+    }
+    uint32_t tsize = 256;
+    while (tsize < (uint32_t)kT && (uint64_t)tsize < 2 * nrec) tsize <<= 1;
+    const uint32_t tmask = tsize - 1;
+    bool over = nrec > kBkRecMax;
+    if (!over) {
+        // the first batch of records is in flight while the table is cleared
+        unsigned long long v[kBkBatch];
+#pragma unroll
+        for (int i = 0; i < kBkBatch; ++i) {
+            const uint64_t r = rb + (uint64_t)i * kNT + threadIdx.x;
+            v[i] = r < re ? b.rec2[r] : 0ull;
+        }
+        if (threadIdx.x == 0) s_over = 0;
+        for (uint32_t j = threadIdx.x; j < tsize; j += kNT) {
+            keys[j] = 0;
+            reinterpret_cast<uint4 *>(cnt)[j] = make_uint4(0, 0, 0, 0);
+        }
+        __syncthreads();
+        const uint64_t hp = (uint64_t)(bk >> b.b2) << (64 - b.b1);
+        bool full = false;
+        for (uint64_t base = rb; base < re && !full; base += (uint64_t)kNT * kBkBatch) {
+            if (base != rb) {
+#pragma unroll
+                for (int i = 0; i < kBkBatch; ++i) {  // the batch's loads are in flight together
+                    const uint64_t r = base + (uint64_t)i * kNT + threadIdx.x;
+                    v[i] = r < re ? b.rec2[r] : 0ull;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < kBkBatch; ++i) {
+                if (full || base + (uint64_t)i * kNT + threadIdx.x >= re) continue;
+                const unsigned long long h = hp | (v[i] >> 8);
+                uint32_t slot = (uint32_t)h & tmask;
+                uint32_t step = 0;
+                for (; step < tsize; ++step) {
+                    const unsigned long long old = atomicCAS(&keys[slot], 0ull, h);
+                    if (old == 0 || old == h) break;
+                    slot = (slot + 1) & tmask;
+                }
+                if (step == tsize) {  // table full
+                    s_over = 1;
+                    full = true;
+                    continue;
+                }
+                const unsigned code = (unsigned)v[i] & 0xffu;
+                if (code & 0x08u) {
+                    const unsigned t = code & 7u;
+                    atomicAdd(&cnt[4 * slot + (t >> 1)], 1u << (16 * (t & 1)));
+                }
+                if (code & 0x80u) {
+                    const unsigned t = (code >> 4) & 7u;
+                    atomicAdd(&cnt[4 * slot + (t >> 1)], 1u << (16 * (t & 1)));
+                }
+            }
+        }
+        __syncthreads();
+        over = s_over != 0;
+    }
+    if (over) {
         if (threadIdx.x == 0) {
-            const unsigned i = atomicAdd(b.big_count, 1u);
-            if (i < b.big_cap) b.big[i] = bk;
+            b.surv[bk] = 0;
+            const unsigned i = atomicAdd(ovf_count, 1u);
+            if (i < ovf_cap) ovf[i] = bk;
         }
         return;
     }
-    for (int j = threadIdx.x; j < kBkTable; j += blockDim.x) {
-        keys[j] = 0;
-        cnt[4 * j] = cnt[4 * j + 1] = cnt[4 * j + 2] = cnt[4 * j + 3] = 0;
-    }
-    __syncthreads();
-    const uint64_t hp = (uint64_t)(bk >> b.b2) << (64 - b.b1);
-    for (uint64_t r = rb + threadIdx.x; r < re; r += blockDim.x) {
-        const unsigned long long rec = b.rec2[r];
-        const unsigned long long h = hp | (rec >> 8);
-        uint32_t slot = (uint32_t)h & (kBkTable - 1);
-        for (int step = 0; step < kBkTable; ++step) {
-            const unsigned long long old = atomicCAS(&keys[slot], 0ull, h);
-            if (old == 0 || old == h) break;
-            slot = (slot + 1) & (kBkTable - 1);
-        }
-        const unsigned code = (unsigned)rec & 0xffu;
-        if (code & 0x08u) {
-            const unsigned t = code & 7u;
-            atomicAdd(&cnt[4 * slot + (t >> 1)], 1u << (16 * (t & 1)));
-        }
-        if (code & 0x80u) {
-            const unsigned t = (code >> 4) & 7u;
-            atomicAdd(&cnt[4 * slot + (t >> 1)], 1u << (16 * (t & 1)));
-        }
-    }
-    __syncthreads();
+    // one pass over the table: survivors are staged through a warp-aggregated
+    // shared counter
     const int c = a.cutoff;
-    const uint32_t thr = c <= 0 ? 0u : (c >= 256 ? 0u : (uint32_t)c * 0x01010101u);
-    constexpr int per = kBkTable / 256;
-    uint64_t ok[per], om[per];
-    unsigned keep = 0;
-    int nkeep = 0, nused = 0;
-#pragma unroll
-    for (int it = 0; it < per; ++it) {
-        const int s = it * 256 + threadIdx.x;
-        const unsigned long long h = keys[s];
-        ok[it] = om[it] = 0;
-        if (!h) continue;
-        nused++;
-        uint64_t m = 0;
-#pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            const unsigned v = (cnt[4 * s + (t >> 1)] >> (16 * (t & 1))) & 0xffffu;
-            m |= (uint64_t)(v > 255u ? 255u : v) << (8 * t);
-        }
-        if (thr) {
-            const uint32_t lo = (uint32_t)m & __vcmpgeu4((uint32_t)m, thr);
-            const uint32_t hi = (uint32_t)(m >> 32) & __vcmpgeu4((uint32_t)(m >> 32), thr);
-            m = ((uint64_t)hi << 32) | lo;
-        }
-        if (c >= 256) m = 0;
-        if (m) {
-            ok[it] = unmix64(h);
-            om[it] = m;
-            keep |= 1u << it;
-            nkeep++;
-        }
-    }
-    uint64_t total, used;
-    const uint64_t ex = block_exclusive_scan<256>((uint64_t)nkeep, wb, &total);
-    block_exclusive_scan<256>((uint64_t)nused, wb, &used);
+    const bool cut_all = c >= 256;
+    const unsigned cbias = (c > 0 && c < 256) ? (0x8000u - (unsigned)c) * 0x00010001u : 0u;
     if (threadIdx.x == 0) {
-        s_base = total ? atomicAdd(&a.counters[1], (unsigned long long)total) : 0;
-        if (used) atomicAdd(&a.counters[0], (unsigned long long)used);
+        s_kept = 0;
+        s_used = 0;
     }
     __syncthreads();
-    uint64_t pos = s_base + ex;
-#pragma unroll
-    for (int it = 0; it < per; ++it) {
-        if (keep & (1u << it)) {
-            if (pos < a.out_cap) {
-                a.out_keys[pos] = ok[it];
-                a.out_mult[pos] = om[it];
-            }
-            pos++;
+    const int lane = threadIdx.x & 31;
+    for (uint32_t base = 0; base < tsize; base += kNT) {  // tsize is a multiple of 256
+        const uint32_t sl = base + threadIdx.x;
+        const unsigned long long h = sl < tsize ? keys[sl] : 0ull;
+        const uint64_t m = h ? bucket_mult(cnt, sl, cbias, cut_all) : 0;
+        const unsigned used = __ballot_sync(kFull, h != 0);
+        const unsigned kept = __ballot_sync(kFull, m != 0);
+        unsigned wbase = 0;
+        if (lane == 0 && kept) wbase = atomicAdd(&s_kept, (unsigned)__popc(kept));
+        if (lane == 0 && used) atomicAdd(&s_used, (unsigned)__popc(used));
+        wbase = __shfl_sync(kFull, wbase, 0);
+        if (m) {
+            const uint64_t pos = rb + wbase + __popc(kept & ((1u << lane) - 1));
+            b.stage_keys[pos] = unmix64(h);
+            b.rec2[pos] = m;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        b.surv[bk] = s_kept;
+        if (s_used) atomicAdd(&a.counters[0], (unsigned long long)s_used);
+    }
+}
+
+// Tier 1: one CTA per bucket, tables of up to kBkTable entries; overflow to
+// the big list.
+__global__ void __launch_bounds__(kBkThreads, 2) k_bucket_count(BuildArgs a, BucketArgs b) {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    unsigned long long *keys = reinterpret_cast<unsigned long long *>(dyn);
+    unsigned *cnt = reinterpret_cast<unsigned *>(keys + kBkTable);  // 8 x uint16 per entry
+    __shared__ unsigned s_over, s_kept, s_used;
+    bucket_count_one<kBkTable, kBkThreads>(a, b, blockIdx.x, keys, cnt, s_over, s_kept, s_used,
+                                           b.big, b.big_count, b.big_cap);
+}
+
+// Tier 2: the buckets tier 1 could not hold, one persistent CTA per SM with
+// tables of up to kBkTable2 entries; overflow to the second list (counted in
+// a global-memory table by the host-driven path).
+__global__ void __launch_bounds__(kBkThreads2, 1) k_bucket_count_large(BuildArgs a, BucketArgs b) {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    unsigned long long *keys = reinterpret_cast<unsigned long long *>(dyn);
+    unsigned *cnt = reinterpret_cast<unsigned *>(keys + kBkTable2);
+    __shared__ unsigned s_over, s_kept, s_used;
+    const unsigned n = umin64(*b.big_count, b.big_cap);
+    for (unsigned i = blockIdx.x; i < n; i += gridDim.x) {
+        __syncthreads();  // the previous bucket's table is no longer read
+        bucket_count_one<kBkTable2, kBkThreads2>(a, b, b.big[i], keys, cnt, s_over, s_kept, s_used,
+                                                 b.big2, b.big2_count, b.big_cap);
+    }
+}
+
+// Packs the staged survivors of every bucket (warp per bucket) at the
+// bucket's survivor prefix; the total goes to counters[1], after which the
+// big-bucket path appends.
+__global__ void __launch_bounds__(256) k_bucket_gather(BuildArgs a, BucketArgs b, uint64_t n_buckets) {
+    const uint64_t bk = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (bk == 0 && lane == 0) a.counters[1] = b.surv_off[n_buckets];
+    if (bk >= n_buckets) return;
+    const uint64_t S = b.surv_off[bk], n = b.surv_off[bk + 1] - S, rb = b.off2[bk];
+    for (uint64_t i = lane; i < n; i += 32) {
+        if (S + i < a.out_cap) {
+            a.out_keys[S + i] = b.stage_keys[rb + i];
+            a.out_mult[S + i] = b.rec2[rb + i];
         }
     }
 }
@@ -1311,6 +1500,20 @@ __global__ void __launch_bounds__(256) k_probe(int kind, Entry *table, uint64_t 
 // ---------------------------------------------------------------------
 // Host launchers.
 
+int device_sm_count();
+
+// Blocks of a persistent kernel that are resident at once on the device.
+template <typename K>
+uint64_t resident_grid(K kernel, int threads, size_t dyn_smem) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, dyn_smem) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    return (uint64_t)per_sm * device_sm_count();
+}
+
 int device_sm_count() {
     int dev = 0, n = 0;
     cudaGetDevice(&dev);
@@ -1418,9 +1621,9 @@ int launch_compact(const BuildArgs &a, cudaStream_t s) {
 }
 
 int launch_part_count(const BuildArgs &a, const PartArgs &p, cudaStream_t s) {
-    if (a.n_tiles == 0) return 0;
-    const uint64_t grid = std::min<uint64_t>(a.n_tiles, (uint64_t)device_sm_count() * 8);
-    k_part_count<<<(unsigned)grid, kK1Block, 0, s>>>(a, p);
+    if (a.n_tiles == 0 || a.n_reads == 0) return 0;
+    const uint64_t grid = std::min<uint64_t>((a.n_reads + 255) / 256, resident_grid(k_p1_count, 256, 0));
+    k_p1_count<<<(unsigned)grid, 256, 0, s>>>(a, p);
     return 1;
 }
 
@@ -1430,11 +1633,11 @@ int launch_part_prefix(const PartArgs &p, cudaStream_t s) {
 }
 
 int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s) {
-    if (a.n_tiles == 0) return 0;
-    cudaFuncSetAttribute(k_part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)kScatterDynSmem);
-    const uint64_t grid = std::min<uint64_t>(a.n_tiles, (uint64_t)device_sm_count() * 3);
-    k_part_scatter<<<(unsigned)grid, kK1Block, kScatterDynSmem, s>>>(a, p);
+    if (a.n_tiles == 0 || a.n_reads == 0) return 0;
+    const size_t smem = p1_scatter_smem(p.n_parts);
+    cudaFuncSetAttribute(k_p1_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const uint64_t grid = std::min<uint64_t>((a.n_reads + 255) / 256, resident_grid(k_p1_scatter, 256, smem));
+    k_p1_scatter<<<(unsigned)grid, 256, smem, s>>>(a, p);
     return 1;
 }
 
@@ -1455,27 +1658,42 @@ int launch_part_wave(const BuildArgs &a, const PartArgs &p, uint32_t p0, uint32_
     return launches;
 }
 
+int launch_chunk_prefix(const BucketArgs &b, cudaStream_t s) {
+    k_chunk_prefix<<<1, 1024, 0, s>>>(b);
+    return 1;
+}
+
 int launch_sub_hist(const BucketArgs &b, cudaStream_t s) {
-    const uint64_t grid = (b.n_rec + kBkChunk - 1) / kBkChunk;
-    if (!grid) return 0;
+    if (!b.n_rec) return 0;
+    const uint64_t chunks = b.n_rec / kBkChunk + b.n_parts;  // bound on the partition-aligned chunks
+    const uint64_t grid = std::min<uint64_t>(chunks, resident_grid(k_sub_hist, 256, 0));
     k_sub_hist<<<(unsigned)grid, 256, 0, s>>>(b);
     return 1;
 }
 
 int launch_sub_scatter(const BucketArgs &b, cudaStream_t s) {
-    const uint64_t grid = (b.n_rec + kBkChunk - 1) / kBkChunk;
-    if (!grid) return 0;
+    if (!b.n_rec) return 0;
+    const uint64_t chunks = b.n_rec / kBkChunk + b.n_parts;
     cudaFuncSetAttribute(k_sub_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kSubScatterDyn);
+    const uint64_t grid = std::min<uint64_t>(chunks, resident_grid(k_sub_scatter, 256, kSubScatterDyn));
     k_sub_scatter<<<(unsigned)grid, 256, kSubScatterDyn, s>>>(b);
     return 1;
 }
 
 int launch_bucket_count(const BuildArgs &a, const BucketArgs &b, cudaStream_t s) {
     const uint64_t grid = (uint64_t)b.n_parts << b.b2;
-    cudaFuncSetAttribute(k_bucket_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)kBucketDyn);
-    k_bucket_count<<<(unsigned)grid, 256, kBucketDyn, s>>>(a, b);
+    const size_t smem1 = bucket_smem<kBkTable>(), smem2 = bucket_smem<kBkTable2>();
+    cudaFuncSetAttribute(k_bucket_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+    k_bucket_count<<<(unsigned)grid, kBkThreads, smem1, s>>>(a, b);
+    cudaFuncSetAttribute(k_bucket_count_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+    k_bucket_count_large<<<(unsigned)device_sm_count(), kBkThreads2, smem2, s>>>(a, b);
+    return 2;
+}
+
+int launch_bucket_gather(const BuildArgs &a, const BucketArgs &b, uint64_t n_buckets, cudaStream_t s) {
+    const uint64_t threads = std::max<uint64_t>(n_buckets, 1) * 32;
+    k_bucket_gather<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(a, b, n_buckets);
     return 1;
 }
 

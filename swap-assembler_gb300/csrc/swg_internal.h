@@ -100,10 +100,16 @@ struct BucketArgs {
     unsigned long long *rec2;              // records grouped by bucket
     unsigned long long *off2;              // [n_buckets + 1] bucket offsets
     unsigned long long *cursor2;           // [n_buckets] scatter cursors
+    unsigned long long *chunk_start;       // [n_parts + 1] level-2 chunks per partition, prefix
+    unsigned long long *surv;              // [n_buckets] survivors per bucket
+    unsigned long long *surv_off;          // [n_buckets + 1] their exclusive prefix
+    unsigned long long *stage_keys;        // [n_rec] survivor keys, staged at the bucket's offset
     uint64_t n_rec;
-    unsigned long long *big;               // buckets too large for shared memory
+    unsigned long long *big;               // buckets too large for a tier-1 table
     unsigned *big_count;
-    uint32_t big_cap;
+    unsigned long long *big2;              // ... and for a tier-2 table
+    unsigned *big2_count;
+    uint32_t big_cap;                      // capacity of each list
 };
 
 // Kernel launchers (kernels.cu). Each returns the number of launches made.
@@ -143,9 +149,11 @@ int launch_rec_len(const uint64_t *nl, uint64_t n_rec, int k, uint64_t *keep, ui
 int launch_rec_pack(const unsigned char *t, const uint64_t *nl, uint64_t n_rec, int k,
                     const uint64_t *read_idx, const uint64_t *word_off, uint64_t *off,
                     uint32_t *len, uint32_t *packed, cudaStream_t s);
+int launch_chunk_prefix(const BucketArgs &b, cudaStream_t s);
 int launch_sub_hist(const BucketArgs &b, cudaStream_t s);
 int launch_sub_scatter(const BucketArgs &b, cudaStream_t s);
 int launch_bucket_count(const BuildArgs &a, const BucketArgs &b, cudaStream_t s);
+int launch_bucket_gather(const BuildArgs &a, const BucketArgs &b, uint64_t n_buckets, cudaStream_t s);
 int launch_big_bucket(const BuildArgs &a, const BucketArgs &b, uint64_t bucket, uint64_t rb,
                       uint64_t re, Entry *table, uint64_t cap, cudaStream_t s);
 cudaError_t run_probe(int kind, uint64_t table_bytes, uint64_t n_ops, cudaStream_t s, float *ms);

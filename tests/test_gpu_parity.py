@@ -245,3 +245,24 @@ def test_bucketed_large_input_and_hot_buckets():
     g = gpu_build(text, 21, 2, algorithm=swapgb.ALGO_BUCKETED)
     assert g.info()["waves"] >= 1  # global-memory path taken
     assert_same_records(g, text, 21, 2)
+
+
+def test_bucketed_overflow_tiers(monkeypatch):
+    """Buckets of nearly distinct k-molecules larger than the tier-1 table:
+    recounted in the tier-2 table; larger still: the global-memory path."""
+    monkeypatch.setenv("SWG_BUCKET_RECORDS", "1000000")  # one bucket per partition
+    # 0.1x coverage of a random genome: almost every k-molecule is distinct,
+    # ~5.8K per bucket (tier-1 tables hold 4096)
+    text = swapgb.synth_fasta(seed=29, genome_len=20_000_000, n_reads=20_000, read_len=100,
+                              sub_rate=0.0, indel_rate=0.0)
+    g = gpu_build(text, 27, 0, algorithm=swapgb.ALGO_BUCKETED)
+    info = g.info()
+    assert info["slots"] == 1 and info["retries"] >= 1, info
+    assert_same_records(g, text, 27, 0)
+    # ~11.6K distinct per bucket: beyond the tier-2 tables (8192)
+    text = swapgb.synth_fasta(seed=31, genome_len=40_000_000, n_reads=40_000, read_len=100,
+                              sub_rate=0.0, indel_rate=0.0)
+    g = gpu_build(text, 27, 1, algorithm=swapgb.ALGO_BUCKETED)
+    info = g.info()
+    assert info["waves"] >= 1, info
+    assert_same_records(g, text, 27, 1)
