@@ -99,7 +99,9 @@ typedef struct swg_build_info {
                              global-memory table */
     uint32_t retries;     /* direct: rebuilds after a full table; bucketed: buckets
                              recounted in the larger (tier-2) shared-memory table */
-    double estimate;      /* direct: distinct-count estimate used for sizing */
+    double estimate;      /* direct: distinct-count estimate used for sizing;
+                             bucketed: 1 when a fixed-capacity partition overflowed
+                             and the build reran with exact partition counts */
     float ms[5];          /* as swg_graph_last_timings */
 } swg_build_info;
 

@@ -198,7 +198,7 @@ swg_status build_direct(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStrea
 swg_status build_partitioned(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s,
                              double load);
 swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s,
-                          double load);
+                          double load, bool counted = false);
 
 swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, uint64_t n_words,
                       const uint64_t *off, const uint32_t *len, uint64_t n_reads) {
@@ -717,29 +717,36 @@ swg_status batch_impl(swg_graph *g, const swg_opts *o, const swg_sample *sm, uin
 // the next hash bits, and every bucket is counted by one CTA in a
 // shared-memory hash table and compacted from there. Buckets too large for
 // shared memory (hot k-molecules) are counted in a global-memory table.
+// Bucketed build (kernels.cu, k_p1_* / k_sub_* / k_bucket_*). Level-1
+// partitions have a fixed capacity (1.125x the mean plus slack), so no count
+// pass precedes the scatter; a partition that overflows it (heavy repeats)
+// sets a status bit and the build reruns with exact per-partition counts.
 swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s,
-                          double load) {
+                          double load, bool counted) {
     swg_status st;
     g->algorithm = SWG_ALGO_BUCKETED;
     const uint64_t N = a.total_occ;
     int b1 = N <= (400ull << 20) ? 8 : (N <= (1600ull << 20) ? 9 : 10);
     const uint64_t P = 1ull << b1;
-    // sub-buckets of about kBucketRecords records (SWG_BUCKET_RECORDS overrides)
+    // sub-buckets of about `target` records (SWG_BUCKET_RECORDS overrides)
     double target = 6144.0;
     if (const char *e = std::getenv("SWG_BUCKET_RECORDS")) target = std::max(64.0, std::atof(e));
     int b2 = 0;
     while (b2 < 10 && (double)N / (double)(P << b2) > target) b2++;
+    const uint64_t fixed_cap = counted ? 0 : (N + P - 1) / P + (N + P - 1) / P / 8 + 16384;
+    const uint64_t rec1_cap = std::max<uint64_t>(counted ? N : P * fixed_cap, 1);
     swg::PartArgs pa;
     std::memset(&pa, 0, sizeof(pa));
     pa.bits = b1;
     pa.n_parts = (uint32_t)P;
     pa.load_num = 3;
     pa.load_den = 5;
-    if ((st = ensure(&g->d_part, &g->part_cap, 3 * P + 1, "partition table"))) return st;
+    pa.fixed_cap = fixed_cap;
+    if ((st = ensure(&g->d_part, &g->part_cap, 4 * P + 1, "partition table"))) return st;
     pa.part_count = g->d_part;
     pa.part_start = g->d_part + P;
     pa.part_cursor = g->d_part + 2 * P + 1;
-    if ((st = ensure(&g->d_records, &g->records_cap, std::max<uint64_t>(N, 1), "records"))) return st;
+    if ((st = ensure(&g->d_records, &g->records_cap, rec1_cap, "records"))) return st;
     if ((st = ensure(&g->d_rec2, &g->rec2_cap, std::max<uint64_t>(N, 1), "bucket records"))) return st;
     const uint64_t NB = P << b2;
     const uint64_t scratch = swg::gscan_scratch(NB);
@@ -747,26 +754,17 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     // survivor prefix [NB+1] | scan scratch | totals [2] | chunk prefix [P+1] |
     // second big list [NB]
     if ((st = ensure(&g->d_bk, &g->bk_cap, 5 * NB + 2 + scratch + 2 + P + 1, "bucket table"))) return st;
-    const uint64_t out_want = std::max<uint64_t>(N, 1);
-    if (g->out_cap < out_want || !g->d_out_keys || !g->d_out_mult) {
-        cudaFree(g->d_out_keys);
-        cudaFree(g->d_out_mult);
-        g->d_out_keys = g->d_out_mult = nullptr;
-        g->out_cap = 0;
-        SWG_CUDA(cudaMalloc(&g->d_out_keys, out_want * 8), "output keys");
-        SWG_CUDA(cudaMalloc(&g->d_out_mult, out_want * 8), "output multiplicities");
-        g->out_cap = out_want;
-    }
     pa.records = g->d_records;
-    a.out_keys = g->d_out_keys;
-    a.out_mult = g->d_out_mult;
-    a.out_cap = out_want;
     swg::BucketArgs bk;
     std::memset(&bk, 0, sizeof(bk));
     bk.b1 = b1;
     bk.b2 = b2;
     bk.n_parts = (uint32_t)P;
     bk.part_start = pa.part_start;
+    bk.part_cursor = pa.part_cursor;
+    bk.part_end = g->d_part + 3 * P + 1;
+    bk.fixed_cap = fixed_cap;
+    bk.status = &g->d_ctl->status;
     bk.rec1 = g->d_records;
     bk.rec2 = g->d_rec2;
     bk.cursor2 = g->d_bk;
@@ -784,9 +782,13 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     bk.big2 = bk.chunk_start + P + 1;
     bk.big2_count = &g->d_ctl->pad2;
 
-    SWG_CUDA(cudaMemsetAsync(pa.part_count, 0, P * 8, s), "clear partitions");
-    g->launches += swg::launch_part_count(a, pa, s);
-    g->launches += swg::launch_part_prefix(pa, s);
+    if (counted) {
+        SWG_CUDA(cudaMemsetAsync(pa.part_count, 0, P * 8, s), "clear partitions");
+        g->launches += swg::launch_part_count(a, pa, s);
+        g->launches += swg::launch_part_prefix(pa, s);
+    } else {
+        g->launches += swg::launch_part_init(pa, s);
+    }
     SWG_CUDA(cudaEventRecord(g->ev[1], s), "event");
     g->launches += swg::launch_part_scatter(a, pa, s);
     g->launches += swg::launch_chunk_prefix(bk, s);
@@ -805,33 +807,58 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
                                      reinterpret_cast<uint64_t *>(bk.surv_off), NB,
                                      reinterpret_cast<uint64_t *>(scr),
                                      reinterpret_cast<uint64_t *>(bk.surv_off + NB), s);
-    g->launches += swg::launch_bucket_gather(a, bk, NB, s);
     SWG_CUDA(cudaGetLastError(), "bucket count launch");
+    SWG_CUDA(cudaMemcpyAsync(&g->h_ctl->occ_total, bk.surv_off + NB, sizeof(uint64_t),
+                             cudaMemcpyDeviceToHost, s), "read survivor total");
     SWG_CUDA(cudaMemcpyAsync(g->h_ctl, g->d_ctl, sizeof(Control) - sizeof(uint64_t),
                              cudaMemcpyDeviceToHost, s), "read status");
     SWG_CUDA(cudaStreamSynchronize(s), "bucket count");
-    (void)tot;
+    if (!counted && (g->h_ctl->status & swg::kStatusPartOverflow)) {
+        // a level-1 partition outgrew its fixed capacity: recount exactly,
+        // from a clear control block
+        g->h_ctl->occ_total = N;
+        SWG_CUDA(cudaMemsetAsync(g->d_ctl, 0, sizeof(Control) - sizeof(uint64_t), s), "clear control");
+        return build_bucketed(g, o, a, s, load, true);
+    }
+    const uint64_t n_small = g->h_ctl->occ_total;
+    g->h_ctl->occ_total = N;
     const unsigned nbig = g->h_ctl->pad2;  // buckets no shared-memory table held
-    g->big_buckets = g->h_ctl->pad;
-    g->retries = g->h_ctl->pad;
-    if (nbig) {  // hot buckets: count them in a global-memory table, one after another
-        std::vector<unsigned long long> big(nbig), offs(NB + 1);
+    std::vector<unsigned long long> big(nbig), offs(nbig ? NB + 1 : 0);
+    uint64_t big_records = 0;
+    if (nbig) {
         SWG_CUDA(cudaMemcpyAsync(big.data(), bk.big2, nbig * 8, cudaMemcpyDeviceToHost, s), "read big buckets");
         SWG_CUDA(cudaMemcpyAsync(offs.data(), bk.off2, (NB + 1) * 8, cudaMemcpyDeviceToHost, s),
                  "read bucket offsets");
         SWG_CUDA(cudaStreamSynchronize(s), "big buckets");
-        for (unsigned i = 0; i < nbig; i++) {
-            const uint64_t bb = big[i], rb = offs[bb], re = offs[bb + 1];
-            const uint64_t cap = (uint64_t)std::ceil((double)(re - rb) / load) + 64;
-            if ((st = ensure(&g->d_arena, &g->arena_cap, cap, "big-bucket table"))) return st;
-            SWG_CUDA(cudaMemsetAsync(g->d_arena, 0, cap * sizeof(Entry), s), "clear big-bucket table");
-            g->launches += swg::launch_big_bucket(a, bk, bb, rb, re, g->d_arena, cap, s);
-        }
-        SWG_CUDA(cudaGetLastError(), "big bucket launch");
-        SWG_CUDA(cudaMemcpyAsync(g->h_ctl, g->d_ctl, sizeof(Control) - sizeof(uint64_t),
-                                 cudaMemcpyDeviceToHost, s), "read status");
+        for (unsigned i = 0; i < nbig; i++) big_records += offs[big[i] + 1] - offs[big[i]];
     }
+    // output: the survivors of the shared-memory buckets, then at most one
+    // per record of the big buckets
+    const uint64_t out_want = std::max<uint64_t>(n_small + big_records, 1);
+    if (g->out_cap < out_want || !g->d_out_keys || !g->d_out_mult) {
+        cudaFree(g->d_out_keys);
+        cudaFree(g->d_out_mult);
+        g->d_out_keys = g->d_out_mult = nullptr;
+        g->out_cap = 0;
+        SWG_CUDA(cudaMalloc(&g->d_out_keys, out_want * 8), "output keys");
+        SWG_CUDA(cudaMalloc(&g->d_out_mult, out_want * 8), "output multiplicities");
+        g->out_cap = out_want;
+    }
+    a.out_keys = g->d_out_keys;
+    a.out_mult = g->d_out_mult;
+    a.out_cap = g->out_cap;
+    g->launches += swg::launch_bucket_gather(a, bk, NB, s);
+    for (unsigned i = 0; i < nbig; i++) {  // count them in a global-memory table, one after another
+        const uint64_t bb = big[i], rb = offs[bb], re = offs[bb + 1];
+        const uint64_t cap = (uint64_t)std::ceil((double)(re - rb) / load) + 64;
+        if ((st = ensure(&g->d_arena, &g->arena_cap, cap, "big-bucket table"))) return st;
+        SWG_CUDA(cudaMemsetAsync(g->d_arena, 0, cap * sizeof(Entry), s), "clear big-bucket table");
+        g->launches += swg::launch_big_bucket(a, bk, bb, rb, re, g->d_arena, cap, s);
+    }
+    SWG_CUDA(cudaGetLastError(), "gather launch");
     SWG_CUDA(cudaEventRecord(g->ev[3], s), "event");
+    SWG_CUDA(cudaMemcpyAsync(g->h_ctl, g->d_ctl, sizeof(Control) - sizeof(uint64_t),
+                             cudaMemcpyDeviceToHost, s), "read status");
     SWG_CUDA(cudaEventRecord(g->ev[4], s), "event");
     SWG_CUDA(cudaStreamSynchronize(s), "build");
     const unsigned status = g->h_ctl->status;
@@ -843,6 +870,9 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
         swg::set_error("a big-bucket table reached the probe limit");
         return SWG_ERR_TABLE_FULL;
     }
+    g->big_buckets = g->h_ctl->pad;
+    g->retries = g->h_ctl->pad;
+    g->estimate = counted ? 1.0 : 0.0;  // bucketed: 1 when the exact-count rerun was needed
     g->parts = (uint32_t)P;
     g->slots = (uint32_t)(1u << b2);
     g->waves = nbig;

@@ -920,10 +920,20 @@ __global__ void __launch_bounds__(256, 3) k_p1_scatter(BuildArgs a, PartArgs pa)
             __syncthreads();
             for (uint32_t j = threadIdx.x; j < (uint32_t)total; j += blockDim.x) {
                 const unsigned part = spart[j];
-                pa.records[gbase[part] + (j - loff[part])] = sorted[j];
+                const uint64_t dst = gbase[part] + (j - loff[part]);
+                // fixed-capacity regions: records past the region are dropped
+                // (the overflow is flagged after the scatter)
+                if (!pa.fixed_cap || dst < (uint64_t)(part + 1) * pa.fixed_cap) pa.records[dst] = sorted[j];
             }
         }
     }
+}
+
+// Fixed-capacity partition regions: partition p starts at p * fixed_cap.
+__global__ void k_part_init(PartArgs pa) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j <= pa.n_parts) pa.part_start[j] = (unsigned long long)j * pa.fixed_cap;
+    if (j < pa.n_parts) pa.part_cursor[j] = (unsigned long long)j * pa.fixed_cap;
 }
 
 // Exclusive prefix over the partitions (n_parts <= 1024, one block).
@@ -1065,12 +1075,22 @@ __device__ __forceinline__ uint32_t sub_of(const BucketArgs &b, unsigned long lo
     return b.b2 ? (uint32_t)((rec >> 8) >> (64 - b.b1 - b.b2)) : 0u;
 }
 
-// Chunks per partition, as an exclusive prefix (one block).
+// End of every partition's records (its cursor, clamped to a fixed-capacity
+// region, flagging an overflow) and the chunks per partition as an exclusive
+// prefix (one block).
 __global__ void __launch_bounds__(1024) k_chunk_prefix(BucketArgs b) {
     __shared__ uint64_t wb[32];
     const uint32_t j = threadIdx.x;
     uint64_t c = 0;
-    if (j < b.n_parts) c = (b.part_start[j + 1] - b.part_start[j] + kBkChunk - 1) / kBkChunk;
+    if (j < b.n_parts) {
+        uint64_t end = b.part_cursor[j];
+        if (b.fixed_cap && end > b.part_start[j] + b.fixed_cap) {
+            atomicOr(b.status, kStatusPartOverflow);
+            end = b.part_start[j] + b.fixed_cap;
+        }
+        b.part_end[j] = end;
+        c = (end - b.part_start[j] + kBkChunk - 1) / kBkChunk;
+    }
     uint64_t total;
     const uint64_t ex = block_exclusive_scan<1024>(c, wb, &total);
     if (j < b.n_parts) b.chunk_start[j] = ex;
@@ -1087,7 +1107,7 @@ __device__ __forceinline__ uint32_t chunk_range(const BucketArgs &b, uint64_t q,
         else hi = mid;
     }
     r0 = b.part_start[lo] + (q - b.chunk_start[lo]) * kBkChunk;
-    r1 = umin64(r0 + kBkChunk, b.part_start[lo + 1]);
+    r1 = umin64(r0 + kBkChunk, b.part_end[lo]);
     return lo;
 }
 
@@ -1624,6 +1644,11 @@ int launch_part_count(const BuildArgs &a, const PartArgs &p, cudaStream_t s) {
     if (a.n_tiles == 0 || a.n_reads == 0) return 0;
     const uint64_t grid = std::min<uint64_t>((a.n_reads + 255) / 256, resident_grid(k_p1_count, 256, 0));
     k_p1_count<<<(unsigned)grid, 256, 0, s>>>(a, p);
+    return 1;
+}
+
+int launch_part_init(const PartArgs &p, cudaStream_t s) {
+    k_part_init<<<(p.n_parts + 256) / 256, 256, 0, s>>>(p);
     return 1;
 }
 

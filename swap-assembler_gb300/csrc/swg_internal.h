@@ -23,6 +23,7 @@ struct __align__(16) Entry {
 enum : unsigned {
     kStatusTableFull = 1u,  // probe limit reached or table nearly full
     kStatusCasLimit = 2u,   // a bounded CAS retry loop gave up
+    kStatusPartOverflow = 4u,  // a fixed-capacity partition overflowed (bucketed build)
 };
 
 constexpr int kK1Block = 256;
@@ -88,6 +89,7 @@ struct PartArgs {
     uint64_t slot_cap;
     uint32_t n_slots;
     int load_num, load_den;            // slice capacity = count * den / num + 16
+    uint64_t fixed_cap;                // bucketed: records per partition region, 0 = counted
 };
 
 // Bucketed build: the level-1 partition records are split again by the next
@@ -96,6 +98,10 @@ struct BucketArgs {
     int b1, b2;                            // partition bits, sub-bucket bits
     uint32_t n_parts;                      // 1 << b1
     const unsigned long long *part_start;  // [n_parts + 1] level-1 offsets
+    const unsigned long long *part_cursor; // [n_parts] level-1 cursors after the scatter
+    unsigned long long *part_end;          // [n_parts] end of each partition's records
+    uint64_t fixed_cap;                    // fixed partition capacity, 0 = counted
+    unsigned *status;
     const unsigned long long *rec1;        // level-1 records
     unsigned long long *rec2;              // records grouped by bucket
     unsigned long long *off2;              // [n_buckets + 1] bucket offsets
@@ -132,6 +138,7 @@ int launch_gather_prefix(const uint64_t *prefix, const uint64_t *idx, uint32_t n
 int launch_compact(const BuildArgs &a, cudaStream_t s);
 int launch_part_count(const BuildArgs &a, const PartArgs &p, cudaStream_t s);
 int launch_part_prefix(const PartArgs &p, cudaStream_t s);
+int launch_part_init(const PartArgs &p, cudaStream_t s);
 int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s);
 int launch_part_wave(const BuildArgs &a, const PartArgs &p, uint32_t p0, uint32_t n,
                      uint64_t rec_begin, uint64_t rec_end, cudaStream_t s);

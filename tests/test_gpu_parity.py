@@ -243,7 +243,9 @@ def test_bucketed_large_input_and_hot_buckets():
     reads = ["A" * 250, "AC" * 125] * 30000 + ["ACGTTGCA" * 20] * 500
     text = "".join(">h%d\n%s\n" % (i, r) for i, r in enumerate(reads)).encode()
     g = gpu_build(text, 21, 2, algorithm=swapgb.ALGO_BUCKETED)
-    assert g.info()["waves"] >= 1  # global-memory path taken
+    info = g.info()
+    assert info["waves"] >= 1, info  # global-memory path taken
+    assert info["estimate"] == 1.0, info  # fixed-capacity partition overflowed: exact recount
     assert_same_records(g, text, 21, 2)
 
 
