@@ -102,7 +102,7 @@ struct swg_graph {
     // bucketed workspace
     unsigned long long *d_rec2 = nullptr;
     uint64_t rec2_cap = 0;
-    unsigned long long *d_bk = nullptr;  // cursor2 [nb] | off2 [nb+1] | big [nb] | scratch
+    unsigned long long *d_bk = nullptr;  // bucketed build: bucket cursors, offsets, lists, prefixes
     uint64_t bk_cap = 0;
     Entry *d_arena = nullptr;
     uint64_t arena_cap = 0;
@@ -733,8 +733,13 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     if (const char *e = std::getenv("SWG_BUCKET_RECORDS")) target = std::max(64.0, std::atof(e));
     int b2 = 0;
     while (b2 < 10 && (double)N / (double)(P << b2) > target) b2++;
+    const uint64_t NB = P << b2;
+    // fixed capacities: partitions 1.125x their mean + 16K, buckets 1.5x + 256
     const uint64_t fixed_cap = counted ? 0 : (N + P - 1) / P + (N + P - 1) / P / 8 + 16384;
-    const uint64_t rec1_cap = std::max<uint64_t>(counted ? N : P * fixed_cap, 1);
+    const uint64_t cap2 = counted ? 0 : (N + NB - 1) / NB + (N + NB - 1) / NB / 2 + 256;
+    // the level-1 buffer also stages the survivor keys at bucket offsets
+    const uint64_t rec1_cap = std::max<uint64_t>(counted ? N : std::max(P * fixed_cap, NB * cap2), 1);
+    const uint64_t rec2_cap = std::max<uint64_t>(counted ? N : NB * cap2, 1);
     swg::PartArgs pa;
     std::memset(&pa, 0, sizeof(pa));
     pa.bits = b1;
@@ -747,13 +752,12 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     pa.part_start = g->d_part + P;
     pa.part_cursor = g->d_part + 2 * P + 1;
     if ((st = ensure(&g->d_records, &g->records_cap, rec1_cap, "records"))) return st;
-    if ((st = ensure(&g->d_rec2, &g->rec2_cap, std::max<uint64_t>(N, 1), "bucket records"))) return st;
-    const uint64_t NB = P << b2;
+    if ((st = ensure(&g->d_rec2, &g->rec2_cap, rec2_cap, "bucket records"))) return st;
     const uint64_t scratch = swg::gscan_scratch(NB);
-    // d_bk: cursors / survivor counts [NB] | offsets [NB+1] | big list [NB] |
-    // survivor prefix [NB+1] | scan scratch | totals [2] | chunk prefix [P+1] |
-    // second big list [NB]
-    if ((st = ensure(&g->d_bk, &g->bk_cap, 5 * NB + 2 + scratch + 2 + P + 1, "bucket table"))) return st;
+    // d_bk: cursors [NB] | offsets [NB+1] | big list [NB] | survivor prefix
+    // [NB+1] | scan scratch | totals [2] | chunk prefix [P+1] | second big
+    // list [NB] | survivors per bucket [NB]
+    if ((st = ensure(&g->d_bk, &g->bk_cap, 6 * NB + 2 + scratch + 2 + P + 1, "bucket table"))) return st;
     pa.records = g->d_records;
     swg::BucketArgs bk;
     std::memset(&bk, 0, sizeof(bk));
@@ -773,13 +777,14 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     bk.big_cap = (uint32_t)std::min<uint64_t>(NB, 0xffffffffu);
     bk.big_count = &g->d_ctl->pad;
     bk.n_rec = N;
-    bk.surv = bk.cursor2;  // the cursors are spent once the records are grouped
     bk.surv_off = g->d_bk + 3 * NB + 1;
     bk.stage_keys = g->d_records;  // level-1 records are spent too
     unsigned long long *scr = bk.surv_off + NB + 1;
     unsigned long long *tot = scr + scratch;
     bk.chunk_start = tot + 2;
     bk.big2 = bk.chunk_start + P + 1;
+    bk.surv = bk.big2 + NB;
+    bk.cap2 = cap2;
     bk.big2_count = &g->d_ctl->pad2;
 
     if (counted) {
@@ -792,13 +797,17 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     SWG_CUDA(cudaEventRecord(g->ev[1], s), "event");
     g->launches += swg::launch_part_scatter(a, pa, s);
     g->launches += swg::launch_chunk_prefix(bk, s);
-    SWG_CUDA(cudaMemsetAsync(bk.cursor2, 0, NB * 8, s), "clear bucket counts");
-    g->launches += swg::launch_sub_hist(bk, s);
-    g->launches += swg::launch_gscan(reinterpret_cast<const uint64_t *>(bk.cursor2),
-                                     reinterpret_cast<uint64_t *>(bk.off2), NB,
-                                     reinterpret_cast<uint64_t *>(scr),
-                                     reinterpret_cast<uint64_t *>(bk.off2 + NB), s);
-    SWG_CUDA(cudaMemcpyAsync(bk.cursor2, bk.off2, NB * 8, cudaMemcpyDeviceToDevice, s), "bucket cursors");
+    if (counted) {  // exact bucket offsets
+        SWG_CUDA(cudaMemsetAsync(bk.cursor2, 0, NB * 8, s), "clear bucket counts");
+        g->launches += swg::launch_sub_hist(bk, s);
+        g->launches += swg::launch_gscan(reinterpret_cast<const uint64_t *>(bk.cursor2),
+                                         reinterpret_cast<uint64_t *>(bk.off2), NB,
+                                         reinterpret_cast<uint64_t *>(scr),
+                                         reinterpret_cast<uint64_t *>(bk.off2 + NB), s);
+        SWG_CUDA(cudaMemcpyAsync(bk.cursor2, bk.off2, NB * 8, cudaMemcpyDeviceToDevice, s), "bucket cursors");
+    } else {
+        g->launches += swg::launch_bucket_init(bk, NB, s);
+    }
     g->launches += swg::launch_sub_scatter(bk, s);
     SWG_CUDA(cudaGetLastError(), "bucket scatter launch");
     SWG_CUDA(cudaEventRecord(g->ev[2], s), "event");
@@ -814,7 +823,7 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
                              cudaMemcpyDeviceToHost, s), "read status");
     SWG_CUDA(cudaStreamSynchronize(s), "bucket count");
     if (!counted && (g->h_ctl->status & swg::kStatusPartOverflow)) {
-        // a level-1 partition outgrew its fixed capacity: recount exactly,
+        // a partition or bucket outgrew its fixed capacity: recount exactly,
         // from a clear control block
         g->h_ctl->occ_total = N;
         SWG_CUDA(cudaMemsetAsync(g->d_ctl, 0, sizeof(Control) - sizeof(uint64_t), s), "clear control");
@@ -823,14 +832,21 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     const uint64_t n_small = g->h_ctl->occ_total;
     g->h_ctl->occ_total = N;
     const unsigned nbig = g->h_ctl->pad2;  // buckets no shared-memory table held
-    std::vector<unsigned long long> big(nbig), offs(nbig ? NB + 1 : 0);
+    std::vector<unsigned long long> big(nbig), rng(nbig ? NB + 1 : 0), rb_of(nbig), re_of(nbig);
     uint64_t big_records = 0;
     if (nbig) {
         SWG_CUDA(cudaMemcpyAsync(big.data(), bk.big2, nbig * 8, cudaMemcpyDeviceToHost, s), "read big buckets");
-        SWG_CUDA(cudaMemcpyAsync(offs.data(), bk.off2, (NB + 1) * 8, cudaMemcpyDeviceToHost, s),
-                 "read bucket offsets");
+        // counted: the offsets; fixed capacity: the final cursors
+        SWG_CUDA(cudaMemcpyAsync(rng.data(), counted ? bk.off2 : bk.cursor2, (counted ? NB + 1 : NB) * 8,
+                                 cudaMemcpyDeviceToHost, s),
+                 "read bucket ranges");
         SWG_CUDA(cudaStreamSynchronize(s), "big buckets");
-        for (unsigned i = 0; i < nbig; i++) big_records += offs[big[i] + 1] - offs[big[i]];
+        for (unsigned i = 0; i < nbig; i++) {
+            const uint64_t bb = big[i];
+            rb_of[i] = counted ? rng[bb] : bb * cap2;
+            re_of[i] = counted ? rng[bb + 1] : std::min<uint64_t>(rng[bb], bb * cap2 + cap2);
+            big_records += re_of[i] - rb_of[i];
+        }
     }
     // output: the survivors of the shared-memory buckets, then at most one
     // per record of the big buckets
@@ -849,7 +865,7 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     a.out_cap = g->out_cap;
     g->launches += swg::launch_bucket_gather(a, bk, NB, s);
     for (unsigned i = 0; i < nbig; i++) {  // count them in a global-memory table, one after another
-        const uint64_t bb = big[i], rb = offs[bb], re = offs[bb + 1];
+        const uint64_t bb = big[i], rb = rb_of[i], re = re_of[i];
         const uint64_t cap = (uint64_t)std::ceil((double)(re - rb) / load) + 64;
         if ((st = ensure(&g->d_arena, &g->arena_cap, cap, "big-bucket table"))) return st;
         SWG_CUDA(cudaMemsetAsync(g->d_arena, 0, cap * sizeof(Entry), s), "clear big-bucket table");

@@ -25,6 +25,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "dev_util.cuh"
 #include "swg_internal.h"
@@ -751,8 +752,8 @@ __device__ __forceinline__ uint64_t slice_cap_of(const PartArgs &pa, unsigned lo
 
 // Shared memory of k_p1_scatter: a round's records, their partitions and
 // order, and per partition its count, local offset and global run base.
-size_t p1_scatter_smem(uint32_t n_parts) {
-    return kTileOcc * (sizeof(unsigned long long) + sizeof(unsigned short)) +
+size_t p1_scatter_smem(uint32_t n_parts, int round) {
+    return (size_t)round * (sizeof(unsigned long long) + sizeof(unsigned short)) +
            (size_t)n_parts * (sizeof(unsigned long long) + 2 * sizeof(unsigned));
 }
 
@@ -854,14 +855,15 @@ __global__ void __launch_bounds__(256) k_p1_count(BuildArgs a, PartArgs pa) {
 // kK1Items records of its read into registers, taking its rank within the
 // partition from the shared histogram; the block orders the round's records
 // by partition in shared memory and writes one run per partition.
-__global__ void __launch_bounds__(256, 3) k_p1_scatter(BuildArgs a, PartArgs pa) {
+template <int NT, int IT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs pa) {
     extern __shared__ __align__(16) unsigned char dyn[];
     unsigned long long *sorted = reinterpret_cast<unsigned long long *>(dyn);
-    unsigned long long *gbase = sorted + kTileOcc;
+    unsigned long long *gbase = sorted + NT * IT;
     unsigned *hist = reinterpret_cast<unsigned *>(gbase + pa.n_parts);
     unsigned *loff = hist + pa.n_parts;
     unsigned short *spart = reinterpret_cast<unsigned short *>(loff + pa.n_parts);
-    __shared__ uint64_t wb[8];
+    __shared__ uint64_t wb[NT / 32];
     const int shift = 64 - pa.bits;
     const uint32_t per = (pa.n_parts + blockDim.x - 1) / blockDim.x;
     const uint64_t r0 = a.n_reads * blockIdx.x / gridDim.x;
@@ -874,10 +876,10 @@ __global__ void __launch_bounds__(256, 3) k_p1_scatter(BuildArgs a, PartArgs pa)
         while (__syncthreads_or(st.left != 0)) {
             for (uint32_t j = threadIdx.x; j < pa.n_parts; j += blockDim.x) hist[j] = 0;
             __syncthreads();
-            unsigned long long rec[kK1Items];
-            unsigned pr[kK1Items];  // partition | rank << 16; ~0 for no record
+            unsigned long long rec[IT];
+            unsigned pr[IT];  // partition | rank << 16; ~0 for no record
 #pragma unroll
-            for (int j = 0; j < kK1Items; ++j) {
+            for (int j = 0; j < IT; ++j) {
                 pr[j] = ~0u;
                 rec[j] = 0;
                 if (st.left) {
@@ -897,7 +899,7 @@ __global__ void __launch_bounds__(256, 3) k_p1_scatter(BuildArgs a, PartArgs pa)
                 if (j < pa.n_parts) mine += hist[j];
             }
             uint64_t total;
-            uint64_t run = block_exclusive_scan<256>(mine, wb, &total);
+            uint64_t run = block_exclusive_scan<NT>(mine, wb, &total);
             for (uint32_t x = 0; x < per; ++x) {
                 const uint32_t j = threadIdx.x * per + x;
                 if (j < pa.n_parts) {
@@ -909,7 +911,7 @@ __global__ void __launch_bounds__(256, 3) k_p1_scatter(BuildArgs a, PartArgs pa)
             }
             __syncthreads();
 #pragma unroll
-            for (int j = 0; j < kK1Items; ++j) {
+            for (int j = 0; j < IT; ++j) {
                 if (pr[j] != ~0u) {
                     const unsigned part = pr[j] & 0xffffu;
                     const unsigned pos = loff[part] + (pr[j] >> 16);
@@ -1075,6 +1077,24 @@ __device__ __forceinline__ uint32_t sub_of(const BucketArgs &b, unsigned long lo
     return b.b2 ? (uint32_t)((rec >> 8) >> (64 - b.b1 - b.b2)) : 0u;
 }
 
+// Record range [rb, re) of bucket bk: counted buckets from the offsets,
+// fixed-capacity buckets from their region and final cursor.
+__device__ __forceinline__ void bucket_range(const BucketArgs &b, uint64_t bk, uint64_t &rb, uint64_t &re) {
+    if (b.cap2) {
+        rb = bk * b.cap2;
+        re = umin64(b.cursor2[bk], rb + b.cap2);
+    } else {
+        rb = b.off2[bk];
+        re = b.off2[bk + 1];
+    }
+}
+
+// Fixed-capacity bucket regions: bucket j starts at j * cap2.
+__global__ void k_bucket_init(BucketArgs b, uint64_t n_buckets) {
+    const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n_buckets) b.cursor2[j] = j * b.cap2;
+}
+
 // End of every partition's records (its cursor, clamped to a fixed-capacity
 // region, flagging an overflow) and the chunks per partition as an exclusive
 // prefix (one block).
@@ -1138,38 +1158,39 @@ __global__ void __launch_bounds__(256) k_sub_hist(BucketArgs b) {
 constexpr size_t kSubScatterDyn = kBkChunk * sizeof(unsigned long long) +
                                   kBkBinsMax * (2 * sizeof(unsigned) + sizeof(unsigned long long));
 
-__global__ void __launch_bounds__(256, 3) k_sub_scatter(BucketArgs b) {
+template <int NT, int IT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_sub_scatter(BucketArgs b) {
     extern __shared__ __align__(16) unsigned char dyn[];
     unsigned long long *sorted = reinterpret_cast<unsigned long long *>(dyn);
     unsigned long long *gbase = sorted + kBkChunk;
     unsigned *hist = reinterpret_cast<unsigned *>(gbase + kBkBinsMax);
     unsigned *loff = hist + kBkBinsMax;
-    __shared__ uint64_t wb[8];
+    __shared__ uint64_t wb[NT / 32];
     const uint32_t P2 = 1u << b.b2;
-    const uint32_t per = (P2 + 255) / 256;  // bins per thread in the scan
+    const uint32_t per = (P2 + NT - 1) / NT;  // bins per thread in the scan
     const uint64_t nq = b.chunk_start[b.n_parts];
     for (uint64_t q = blockIdx.x; q < nq; q += gridDim.x) {
         uint64_t r0, r1;
         const uint32_t p = chunk_range(b, q, r0, r1);
-        unsigned long long v[kBkItems];
+        unsigned long long v[IT];
 #pragma unroll
-        for (int it = 0; it < kBkItems; ++it) {
-            const uint64_t r = r0 + (uint64_t)it * 256 + threadIdx.x;
+        for (int it = 0; it < IT; ++it) {
+            const uint64_t r = r0 + (uint64_t)it * NT + threadIdx.x;
             v[it] = r < r1 ? b.rec1[r] : 0ull;
         }
         __syncthreads();  // the previous chunk is written out
         for (uint32_t j = threadIdx.x; j < P2; j += blockDim.x) hist[j] = 0;
         __syncthreads();
 #pragma unroll
-        for (int it = 0; it < kBkItems; ++it)
-            if (r0 + (uint64_t)it * 256 + threadIdx.x < r1) atomicAdd(&hist[sub_of(b, v[it])], 1u);
+        for (int it = 0; it < IT; ++it)
+            if (r0 + (uint64_t)it * NT + threadIdx.x < r1) atomicAdd(&hist[sub_of(b, v[it])], 1u);
         __syncthreads();
         uint64_t mine = 0;
         for (uint32_t x = 0; x < per; ++x) {
             const uint32_t j = threadIdx.x * per + x;
             if (j < P2) mine += hist[j];
         }
-        uint64_t run = block_exclusive_scan<256>(mine, wb, nullptr);
+        uint64_t run = block_exclusive_scan<NT>(mine, wb, nullptr);
         for (uint32_t x = 0; x < per; ++x) {
             const uint32_t j = threadIdx.x * per + x;
             if (j < P2) {
@@ -1182,24 +1203,32 @@ __global__ void __launch_bounds__(256, 3) k_sub_scatter(BucketArgs b) {
         }
         __syncthreads();
 #pragma unroll
-        for (int it = 0; it < kBkItems; ++it) {
-            if (r0 + (uint64_t)it * 256 + threadIdx.x < r1) {
+        for (int it = 0; it < IT; ++it) {
+            if (r0 + (uint64_t)it * NT + threadIdx.x < r1) {
                 const uint32_t bn = sub_of(b, v[it]);
                 sorted[loff[bn] + atomicAdd(&hist[bn], 1u)] = v[it];
             }
         }
         __syncthreads();
         const uint32_t n = (uint32_t)(r1 - r0);
+        const uint64_t bk0 = (uint64_t)p * P2;
         for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
             const unsigned long long w = sorted[j];
             const uint32_t bn = sub_of(b, w);
-            b.rec2[gbase[bn] + (j - loff[bn])] = w;
+            const uint64_t dst = gbase[bn] + (j - loff[bn]);
+            // fixed-capacity buckets: records past the region are dropped (the
+            // overflow is flagged by the bucket count)
+            if (!b.cap2 || dst < (bk0 + bn + 1) * b.cap2) b.rec2[dst] = w;
         }
     }
 }
 
+// Shared memory of a bucket CTA: T keys, T x 8 uint16 counters, and the list
+// of used slots (uint16).
 template <int T>
-constexpr size_t bucket_smem() { return (size_t)T * (sizeof(unsigned long long) + 4 * sizeof(unsigned)); }
+constexpr size_t bucket_smem() {
+    return (size_t)T * (sizeof(unsigned long long) + 4 * sizeof(unsigned) + sizeof(unsigned short));
+}
 
 // Eight saturated uint8 multiplicities of table entry s (8 x uint16
 // counters, slot t in half t&1 of word t>>1), after the -c cutoff
@@ -1222,45 +1251,73 @@ __device__ __forceinline__ uint64_t bucket_mult(const unsigned *cnt, uint32_t s,
     return cut_all ? 0 : m;
 }
 
-// Counts bucket bk in a shared-memory table of 2x the bucket's records (at
-// most kT entries), applies the cutoff and stages the survivors in the
-// bucket's own record range (keys in stage_keys, multiplicities over the
-// bucket's records, all read by then); k_bucket_gather packs them. A bucket
+// Persistent bucket counting. The CTA clears its table once; a bucket's
+// keys are inserted into the first tsize entries (2x the bucket's records,
+// at most kT), every newly used slot is appended to a shared list, and the
+// compaction walks that list only, staging the survivors in the bucket's own
+// record range (keys in stage_keys, multiplicities over the bucket's
+// records, all read by then) and clearing the slots for the next bucket.
+// The next bucket's first records are loaded during the compaction. A bucket
 // whose keys do not fit, or with more records than the 16-bit slot counters
-// hold, is appended to the overflow list instead. Returns with the block
-// converged.
+// hold, is appended to the overflow list instead. Buckets are
+// list[0..n_items) if list is given, else 0..n_items.
 template <int kT, int kNT>
-__device__ void bucket_count_one(const BuildArgs &a, const BucketArgs &b, uint64_t bk,
-                                 unsigned long long *keys, unsigned *cnt, unsigned &s_over,
-                                 unsigned &s_kept, unsigned &s_used, unsigned long long *ovf,
-                                 unsigned *ovf_count, uint32_t ovf_cap) {
-    const uint64_t rb = b.off2[bk], re = b.off2[bk + 1];
-    const uint64_t nrec = re - rb;
-    if (nrec == 0) {
-        if (threadIdx.x == 0) b.surv[bk] = 0;
-        return;
+__device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_items,
+                            const unsigned long long *list, unsigned long long *ovf,
+                            unsigned *ovf_count, uint32_t ovf_cap) {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    unsigned long long *keys = reinterpret_cast<unsigned long long *>(dyn);
+    unsigned *cnt = reinterpret_cast<unsigned *>(keys + kT);  // 8 x uint16 per entry
+    unsigned short *used_list = reinterpret_cast<unsigned short *>(cnt + 4 * kT);
+    __shared__ unsigned s_over, s_nused, s_kept;
+    const int lane = threadIdx.x & 31;
+    for (uint32_t j = threadIdx.x; j < (uint32_t)kT; j += kNT) {
+        keys[j] = 0;
+        reinterpret_cast<uint4 *>(cnt)[j] = make_uint4(0, 0, 0, 0);
     }
-    uint32_t tsize = 256;
-    while (tsize < (uint32_t)kT && (uint64_t)tsize < 2 * nrec) tsize <<= 1;
-    const uint32_t tmask = tsize - 1;
-    bool over = nrec > kBkRecMax;
-    if (!over) {
-        // the first batch of records is in flight while the table is cleared
-        unsigned long long v[kBkBatch];
+    const int c = a.cutoff;
+    const bool cut_all = c >= 256;
+    const unsigned cbias = (c > 0 && c < 256) ? (0x8000u - (unsigned)c) * 0x00010001u : 0u;
+    unsigned long long v[kBkBatch];
+    uint64_t v_for = ~0ull;  // bucket whose first batch the registers v hold
+    for (uint64_t it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const uint64_t bk = list ? list[it] : it;
+        uint64_t rb, re;
+        bucket_range(b, bk, rb, re);
+        const uint64_t nrec = re - rb;
+        if (b.cap2 && threadIdx.x == 0 && b.cursor2[bk] > re) atomicOr(b.status, kStatusPartOverflow);
+        __syncthreads();  // the previous bucket's compaction (and the clear) is done
+        if (threadIdx.x == 0) {
+            s_over = 0;
+            s_nused = 0;
+            s_kept = 0;
+        }
+        if (nrec == 0) {
+            if (threadIdx.x == 0) b.surv[bk] = 0;
+            continue;
+        }
+        uint32_t tsize = 256;
+        while (tsize < (uint32_t)kT && (uint64_t)tsize < 2 * nrec) tsize <<= 1;
+        const uint32_t tmask = tsize - 1;
+        if (nrec > kBkRecMax) {
+            if (threadIdx.x == 0) {
+                b.surv[bk] = 0;
+                const unsigned i = atomicAdd(ovf_count, 1u);
+                if (i < ovf_cap) ovf[i] = bk;
+            }
+            continue;
+        }
+        if (v_for != bk) {
 #pragma unroll
-        for (int i = 0; i < kBkBatch; ++i) {
-            const uint64_t r = rb + (uint64_t)i * kNT + threadIdx.x;
-            v[i] = r < re ? b.rec2[r] : 0ull;
+            for (int i = 0; i < kBkBatch; ++i) {
+                const uint64_t r = rb + (uint64_t)i * kNT + threadIdx.x;
+                v[i] = r < re ? b.rec2[r] : 0ull;
+            }
         }
-        if (threadIdx.x == 0) s_over = 0;
-        for (uint32_t j = threadIdx.x; j < tsize; j += kNT) {
-            keys[j] = 0;
-            reinterpret_cast<uint4 *>(cnt)[j] = make_uint4(0, 0, 0, 0);
-        }
-        __syncthreads();
+        __syncthreads();  // counters reset
         const uint64_t hp = (uint64_t)(bk >> b.b2) << (64 - b.b1);
         bool full = false;
-        for (uint64_t base = rb; base < re && !full; base += (uint64_t)kNT * kBkBatch) {
+        for (uint64_t base = rb; base < re; base += (uint64_t)kNT * kBkBatch) {
             if (base != rb) {
 #pragma unroll
                 for (int i = 0; i < kBkBatch; ++i) {  // the batch's loads are in flight together
@@ -1270,101 +1327,110 @@ __device__ void bucket_count_one(const BuildArgs &a, const BucketArgs &b, uint64
             }
 #pragma unroll
             for (int i = 0; i < kBkBatch; ++i) {
-                if (full || base + (uint64_t)i * kNT + threadIdx.x >= re) continue;
-                const unsigned long long h = hp | (v[i] >> 8);
-                uint32_t slot = (uint32_t)h & tmask;
-                uint32_t step = 0;
-                for (; step < tsize; ++step) {
-                    const unsigned long long old = atomicCAS(&keys[slot], 0ull, h);
-                    if (old == 0 || old == h) break;
-                    slot = (slot + 1) & tmask;
+                const bool valid = !full && base + (uint64_t)i * kNT + threadIdx.x < re;
+                bool fresh = false;
+                uint32_t slot = 0;
+                if (valid) {
+                    const unsigned long long h = hp | (v[i] >> 8);
+                    slot = (uint32_t)h & tmask;
+                    uint32_t step = 0;
+                    unsigned long long old = 0;
+                    for (; step < tsize; ++step) {
+                        old = atomicCAS(&keys[slot], 0ull, h);
+                        if (old == 0 || old == h) break;
+                        slot = (slot + 1) & tmask;
+                    }
+                    if (step == tsize) {  // table full
+                        s_over = 1;
+                        full = true;
+                    } else {
+                        fresh = old == 0;
+                        const unsigned code = (unsigned)v[i] & 0xffu;
+                        if (code & 0x08u) {
+                            const unsigned t = code & 7u;
+                            atomicAdd(&cnt[4 * slot + (t >> 1)], 1u << (16 * (t & 1)));
+                        }
+                        if (code & 0x80u) {
+                            const unsigned t = (code >> 4) & 7u;
+                            atomicAdd(&cnt[4 * slot + (t >> 1)], 1u << (16 * (t & 1)));
+                        }
+                    }
                 }
-                if (step == tsize) {  // table full
-                    s_over = 1;
-                    full = true;
-                    continue;
-                }
-                const unsigned code = (unsigned)v[i] & 0xffu;
-                if (code & 0x08u) {
-                    const unsigned t = code & 7u;
-                    atomicAdd(&cnt[4 * slot + (t >> 1)], 1u << (16 * (t & 1)));
-                }
-                if (code & 0x80u) {
-                    const unsigned t = (code >> 4) & 7u;
-                    atomicAdd(&cnt[4 * slot + (t >> 1)], 1u << (16 * (t & 1)));
+                const unsigned fm = __ballot_sync(kFull, fresh);
+                if (fm) {  // append the warp's new slots to the used list
+                    unsigned at = 0;
+                    if (lane == __ffs(fm) - 1) at = atomicAdd(&s_nused, (unsigned)__popc(fm));
+                    at = __shfl_sync(kFull, at, __ffs(fm) - 1);
+                    if (fresh) used_list[at + __popc(fm & ((1u << lane) - 1))] = (unsigned short)slot;
                 }
             }
         }
         __syncthreads();
-        over = s_over != 0;
-    }
-    if (over) {
+        const bool over = s_over != 0;
+        const uint32_t nused = s_nused;
+        // the next bucket's first batch loads while this one is compacted
+        const uint64_t nit = it + gridDim.x;
+        v_for = ~0ull;
+        if (nit < n_items) {
+            const uint64_t nbk = list ? list[nit] : nit;
+            uint64_t nrb, nre;
+            bucket_range(b, nbk, nrb, nre);
+#pragma unroll
+            for (int i = 0; i < kBkBatch; ++i) {
+                const uint64_t r = nrb + (uint64_t)i * kNT + threadIdx.x;
+                v[i] = r < nre ? b.rec2[r] : 0ull;
+            }
+            v_for = nbk;
+        }
+        for (uint32_t base = 0; base < nused; base += kNT) {
+            const uint32_t j = base + threadIdx.x;
+            unsigned long long h = 0;
+            uint64_t m = 0;
+            if (j < nused) {
+                const uint32_t sl = used_list[j];
+                h = keys[sl];
+                if (!over) m = bucket_mult(cnt, sl, cbias, cut_all);
+                keys[sl] = 0;
+                reinterpret_cast<uint4 *>(cnt)[sl] = make_uint4(0, 0, 0, 0);
+            }
+            const unsigned kept = __ballot_sync(kFull, m != 0);
+            if (kept) {
+                unsigned at = 0;
+                if (lane == __ffs(kept) - 1) at = atomicAdd(&s_kept, (unsigned)__popc(kept));
+                at = __shfl_sync(kFull, at, __ffs(kept) - 1);
+                if (m) {
+                    const uint64_t pos = rb + at + __popc(kept & ((1u << lane) - 1));
+                    b.stage_keys[pos] = unmix64(h);
+                    b.rec2[pos] = m;
+                }
+            }
+        }
+        __syncthreads();
         if (threadIdx.x == 0) {
-            b.surv[bk] = 0;
-            const unsigned i = atomicAdd(ovf_count, 1u);
-            if (i < ovf_cap) ovf[i] = bk;
+            if (over) {
+                b.surv[bk] = 0;
+                const unsigned i = atomicAdd(ovf_count, 1u);
+                if (i < ovf_cap) ovf[i] = bk;
+            } else {
+                b.surv[bk] = s_kept;
+                if (nused) atomicAdd(&a.counters[0], (unsigned long long)nused);
+            }
         }
-        return;
-    }
-    // one pass over the table: survivors are staged through a warp-aggregated
-    // shared counter
-    const int c = a.cutoff;
-    const bool cut_all = c >= 256;
-    const unsigned cbias = (c > 0 && c < 256) ? (0x8000u - (unsigned)c) * 0x00010001u : 0u;
-    if (threadIdx.x == 0) {
-        s_kept = 0;
-        s_used = 0;
-    }
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    for (uint32_t base = 0; base < tsize; base += kNT) {  // tsize is a multiple of 256
-        const uint32_t sl = base + threadIdx.x;
-        const unsigned long long h = sl < tsize ? keys[sl] : 0ull;
-        const uint64_t m = h ? bucket_mult(cnt, sl, cbias, cut_all) : 0;
-        const unsigned used = __ballot_sync(kFull, h != 0);
-        const unsigned kept = __ballot_sync(kFull, m != 0);
-        unsigned wbase = 0;
-        if (lane == 0 && kept) wbase = atomicAdd(&s_kept, (unsigned)__popc(kept));
-        if (lane == 0 && used) atomicAdd(&s_used, (unsigned)__popc(used));
-        wbase = __shfl_sync(kFull, wbase, 0);
-        if (m) {
-            const uint64_t pos = rb + wbase + __popc(kept & ((1u << lane) - 1));
-            b.stage_keys[pos] = unmix64(h);
-            b.rec2[pos] = m;
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        b.surv[bk] = s_kept;
-        if (s_used) atomicAdd(&a.counters[0], (unsigned long long)s_used);
     }
 }
 
-// Tier 1: one CTA per bucket, tables of up to kBkTable entries; overflow to
-// the big list.
-__global__ void __launch_bounds__(kBkThreads, 2) k_bucket_count(BuildArgs a, BucketArgs b) {
-    extern __shared__ __align__(16) unsigned char dyn[];
-    unsigned long long *keys = reinterpret_cast<unsigned long long *>(dyn);
-    unsigned *cnt = reinterpret_cast<unsigned *>(keys + kBkTable);  // 8 x uint16 per entry
-    __shared__ unsigned s_over, s_kept, s_used;
-    bucket_count_one<kBkTable, kBkThreads>(a, b, blockIdx.x, keys, cnt, s_over, s_kept, s_used,
-                                           b.big, b.big_count, b.big_cap);
+// Tier 1: tables of up to kBkTable entries, two persistent CTAs per SM over
+// all buckets; overflow to the big list.
+__global__ void __launch_bounds__(kBkThreads, 2) k_bucket_count(BuildArgs a, BucketArgs b, uint64_t n_buckets) {
+    bucket_pass<kBkTable, kBkThreads>(a, b, n_buckets, nullptr, b.big, b.big_count, b.big_cap);
 }
 
 // Tier 2: the buckets tier 1 could not hold, one persistent CTA per SM with
 // tables of up to kBkTable2 entries; overflow to the second list (counted in
 // a global-memory table by the host-driven path).
 __global__ void __launch_bounds__(kBkThreads2, 1) k_bucket_count_large(BuildArgs a, BucketArgs b) {
-    extern __shared__ __align__(16) unsigned char dyn[];
-    unsigned long long *keys = reinterpret_cast<unsigned long long *>(dyn);
-    unsigned *cnt = reinterpret_cast<unsigned *>(keys + kBkTable2);
-    __shared__ unsigned s_over, s_kept, s_used;
     const unsigned n = umin64(*b.big_count, b.big_cap);
-    for (unsigned i = blockIdx.x; i < n; i += gridDim.x) {
-        __syncthreads();  // the previous bucket's table is no longer read
-        bucket_count_one<kBkTable2, kBkThreads2>(a, b, b.big[i], keys, cnt, s_over, s_kept, s_used,
-                                                 b.big2, b.big2_count, b.big_cap);
-    }
+    bucket_pass<kBkTable2, kBkThreads2>(a, b, n, b.big, b.big2, b.big2_count, b.big_cap);
 }
 
 // Packs the staged survivors of every bucket (warp per bucket) at the
@@ -1375,7 +1441,9 @@ __global__ void __launch_bounds__(256) k_bucket_gather(BuildArgs a, BucketArgs b
     const int lane = threadIdx.x & 31;
     if (bk == 0 && lane == 0) a.counters[1] = b.surv_off[n_buckets];
     if (bk >= n_buckets) return;
-    const uint64_t S = b.surv_off[bk], n = b.surv_off[bk + 1] - S, rb = b.off2[bk];
+    uint64_t rb, re;
+    bucket_range(b, bk, rb, re);
+    const uint64_t S = b.surv_off[bk], n = b.surv_off[bk + 1] - S;
     for (uint64_t i = lane; i < n; i += 32) {
         if (S + i < a.out_cap) {
             a.out_keys[S + i] = b.stage_keys[rb + i];
@@ -1657,13 +1725,34 @@ int launch_part_prefix(const PartArgs &p, cudaStream_t s) {
     return 1;
 }
 
+// Block shape of the two scatter passes: threads, records per thread per
+// round, resident blocks per SM (SWG_SCATTER_SHAPE = 0, 1 or 2 selects one).
+int scatter_shape() {
+    static int shape = [] {
+        const char *e = std::getenv("SWG_SCATTER_SHAPE");
+        const int v = e ? std::atoi(e) : 0;
+        return v >= 0 && v <= 2 ? v : 0;
+    }();
+    return shape;
+}
+
+template <int NT, int IT, int MINB>
+int launch_p1_scatter_shape(const BuildArgs &a, const PartArgs &p, cudaStream_t s) {
+    auto kern = k_p1_scatter<NT, IT, MINB>;
+    const size_t smem = p1_scatter_smem(p.n_parts, NT * IT);
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const uint64_t grid = std::min<uint64_t>((a.n_reads + NT - 1) / NT, resident_grid(kern, NT, smem));
+    kern<<<(unsigned)grid, NT, smem, s>>>(a, p);
+    return 1;
+}
+
 int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s) {
     if (a.n_tiles == 0 || a.n_reads == 0) return 0;
-    const size_t smem = p1_scatter_smem(p.n_parts);
-    cudaFuncSetAttribute(k_p1_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    const uint64_t grid = std::min<uint64_t>((a.n_reads + 255) / 256, resident_grid(k_p1_scatter, 256, smem));
-    k_p1_scatter<<<(unsigned)grid, 256, smem, s>>>(a, p);
-    return 1;
+    switch (scatter_shape()) {
+        case 1: return launch_p1_scatter_shape<512, 8, 2>(a, p, s);
+        case 2: return launch_p1_scatter_shape<256, 8, 4>(a, p, s);
+        default: return launch_p1_scatter_shape<256, 16, 3>(a, p, s);
+    }
 }
 
 int launch_part_wave(const BuildArgs &a, const PartArgs &p, uint32_t p0, uint32_t n, uint64_t rb,
@@ -1696,24 +1785,41 @@ int launch_sub_hist(const BucketArgs &b, cudaStream_t s) {
     return 1;
 }
 
-int launch_sub_scatter(const BucketArgs &b, cudaStream_t s) {
-    if (!b.n_rec) return 0;
-    const uint64_t chunks = b.n_rec / kBkChunk + b.n_parts;
-    cudaFuncSetAttribute(k_sub_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)kSubScatterDyn);
-    const uint64_t grid = std::min<uint64_t>(chunks, resident_grid(k_sub_scatter, 256, kSubScatterDyn));
-    k_sub_scatter<<<(unsigned)grid, 256, kSubScatterDyn, s>>>(b);
+template <int NT, int IT, int MINB>
+int launch_sub_scatter_shape(const BucketArgs &b, cudaStream_t s) {
+    static_assert(NT * IT == kBkChunk, "a level-2 chunk is one block's round");
+    auto kern = k_sub_scatter<NT, IT, MINB>;
+    const uint64_t chunks = b.n_rec / kBkChunk + b.n_parts;  // bound on the partition-aligned chunks
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSubScatterDyn);
+    const uint64_t grid = std::min<uint64_t>(chunks, resident_grid(kern, NT, kSubScatterDyn));
+    kern<<<(unsigned)grid, NT, kSubScatterDyn, s>>>(b);
     return 1;
 }
 
+int launch_sub_scatter(const BucketArgs &b, cudaStream_t s) {
+    if (!b.n_rec) return 0;
+    switch (scatter_shape()) {
+        case 1: return launch_sub_scatter_shape<512, 8, 2>(b, s);
+        case 2: return launch_sub_scatter_shape<512, 8, 3>(b, s);
+        default: return launch_sub_scatter_shape<256, 16, 3>(b, s);
+    }
+}
+
 int launch_bucket_count(const BuildArgs &a, const BucketArgs &b, cudaStream_t s) {
-    const uint64_t grid = (uint64_t)b.n_parts << b.b2;
+    const uint64_t nb = (uint64_t)b.n_parts << b.b2;
     const size_t smem1 = bucket_smem<kBkTable>(), smem2 = bucket_smem<kBkTable2>();
     cudaFuncSetAttribute(k_bucket_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
-    k_bucket_count<<<(unsigned)grid, kBkThreads, smem1, s>>>(a, b);
+    const uint64_t grid = std::min<uint64_t>(nb, resident_grid(k_bucket_count, kBkThreads, smem1));
+    k_bucket_count<<<(unsigned)grid, kBkThreads, smem1, s>>>(a, b, nb);
     cudaFuncSetAttribute(k_bucket_count_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
     k_bucket_count_large<<<(unsigned)device_sm_count(), kBkThreads2, smem2, s>>>(a, b);
     return 2;
+}
+
+int launch_bucket_init(const BucketArgs &b, uint64_t n_buckets, cudaStream_t s) {
+    if (!n_buckets) return 0;
+    k_bucket_init<<<(unsigned)((n_buckets + 255) / 256), 256, 0, s>>>(b, n_buckets);
+    return 1;
 }
 
 int launch_bucket_gather(const BuildArgs &a, const BucketArgs &b, uint64_t n_buckets, cudaStream_t s) {

@@ -23,7 +23,7 @@ struct __align__(16) Entry {
 enum : unsigned {
     kStatusTableFull = 1u,  // probe limit reached or table nearly full
     kStatusCasLimit = 2u,   // a bounded CAS retry loop gave up
-    kStatusPartOverflow = 4u,  // a fixed-capacity partition overflowed (bucketed build)
+    kStatusPartOverflow = 4u,  // a fixed-capacity partition or bucket overflowed (bucketed build)
 };
 
 constexpr int kK1Block = 256;
@@ -104,8 +104,9 @@ struct BucketArgs {
     unsigned *status;
     const unsigned long long *rec1;        // level-1 records
     unsigned long long *rec2;              // records grouped by bucket
-    unsigned long long *off2;              // [n_buckets + 1] bucket offsets
+    unsigned long long *off2;              // [n_buckets + 1] bucket offsets (counted buckets)
     unsigned long long *cursor2;           // [n_buckets] scatter cursors
+    uint64_t cap2;                         // fixed bucket capacity (bucket j at j * cap2), 0 = counted
     unsigned long long *chunk_start;       // [n_parts + 1] level-2 chunks per partition, prefix
     unsigned long long *surv;              // [n_buckets] survivors per bucket
     unsigned long long *surv_off;          // [n_buckets + 1] their exclusive prefix
@@ -159,6 +160,7 @@ int launch_rec_pack(const unsigned char *t, const uint64_t *nl, uint64_t n_rec, 
 int launch_chunk_prefix(const BucketArgs &b, cudaStream_t s);
 int launch_sub_hist(const BucketArgs &b, cudaStream_t s);
 int launch_sub_scatter(const BucketArgs &b, cudaStream_t s);
+int launch_bucket_init(const BucketArgs &b, uint64_t n_buckets, cudaStream_t s);
 int launch_bucket_count(const BuildArgs &a, const BucketArgs &b, cudaStream_t s);
 int launch_bucket_gather(const BuildArgs &a, const BucketArgs &b, uint64_t n_buckets, cudaStream_t s);
 int launch_big_bucket(const BuildArgs &a, const BucketArgs &b, uint64_t bucket, uint64_t rb,
