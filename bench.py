@@ -4,9 +4,13 @@ Workload (one step = one full graph build over one batch of reads):
   seeded synthetic genome of 5 Mbp (GC 50%), 2.5M reads x 100 bp sampled
   from both strands at 50x, 1% iid substitutions + 0.1% single-base indels,
   k=31, c=5 (uint64 keys, saturating uint8 multiplicities).
-A step = occurrence prefix + tile table + HyperLogLog sizing + table clear +
-K1 extract/count + K2 cutoff/compaction, with the packed reads resident in
-HBM. L2 is flushed (a 256 MiB write) before every timed step.
+A step = one swg_graph_build_device call with the default algorithm (the
+bucketed one for this workload: occurrence total, level-1 hash-partition
+scatter of the k-mer occurrence records, level-2 bucket scatter, per-bucket
+counting + cutoff in shared-memory tables, survivor gather), with the packed
+reads resident in HBM. --algo direct selects the one-pass HBM-table build
+(HyperLogLog sizing, table clear, K1 extract/count, K2 cutoff/compaction).
+L2 is flushed (a 256 MiB write) before every timed step.
 
 Prints ONE JSON line (rank 0). `e2e` repeats the measurement through the
 C-ABI call on HOST (pinned) packed reads, with the host->device copy of the
@@ -48,7 +52,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-samples measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-requests measurement")
-    ap.add_argument("--algo", default="direct", choices=["direct", "partitioned", "bucketed"])
+    ap.add_argument("--algo", default="default", choices=["default", "direct", "partitioned", "bucketed"])
     ap.add_argument("--order", default="input", choices=["input", "minimizer"],
                     help="read order of the direct algorithm")
     ap.add_argument("--reads", type=int, default=0,
@@ -56,7 +60,7 @@ def parse_args():
     return ap.parse_args()
 
 
-def config_dict(algo: str = "direct", order: str = "input") -> dict:
+def config_dict(algo: str = "default", order: str = "input") -> dict:
     return {"algorithm": algo, "read_order": order, "workload": "plain single-sample build: 5 Mbp genome (GC 50%), 2.5M x 100 bp reads "
                         "at 50x from both strands, 1% subs + 0.1% indels, k=31, c=5",
             "genome_bp": WORKLOAD["genome_len"], "reads": WORKLOAD["n_reads"],
@@ -130,8 +134,11 @@ def measured_peaks() -> dict:
     return {}
 
 
-def k_count_traffic_per_occ() -> tuple[float | None, str | None]:
-    p = ROOT / "profiles" / "k_count_ncu.json"
+def traffic_per_occ(kernel: str) -> tuple[float | None, str | None]:
+    """DRAM bytes (read + write) per k-mer occurrence of one kernel, from an
+    ncu capture summarised under profiles/ (scaled to a full launch by the
+    occurrences it processes)."""
+    p = ROOT / "profiles" / ("%s_ncu.json" % kernel)
     if not p.exists():
         return None, None
     d = json.loads(p.read_text())
@@ -380,8 +387,8 @@ def main() -> int:
     n_bases = reads.n_bases
     n_occ = int((reads.len.astype(np.int64) - K + 1).clip(min=0).sum())
     stream = torch.cuda.current_stream(dev)
-    algo = {"direct": swapgb.ALGO_DIRECT, "partitioned": swapgb.ALGO_PARTITIONED,
-            "bucketed": swapgb.ALGO_BUCKETED}[args.algo]
+    algo = {"default": swapgb.ALGO_DEFAULT, "direct": swapgb.ALGO_DIRECT,
+            "partitioned": swapgb.ALGO_PARTITIONED, "bucketed": swapgb.ALGO_BUCKETED}[args.algo]
     order = swapgb.ORDER_MINIMIZER if args.order == "minimizer" else swapgb.ORDER_INPUT
     opts = swapgb.Opts(k=K, cutoff=CUTOFF, stream=stream.cuda_stream, algorithm=algo,
                        read_order=order)
@@ -478,13 +485,27 @@ def main() -> int:
     peak_src = "of measured" if hbm else "of fallback"
     hbm = hbm or 6800.0
     info = g.info()
+    used = info["algorithm"]  # what the default resolved to
     mean_ms = [statistics.mean(m[i] for m in phase_ms) for i in range(5)]
     n_with_occ = int((reads.len >= K).sum())
-    if algo == swapgb.ALGO_DIRECT:
-        kname, k_ms = "k_count", mean_ms[2]
+    kfile = None
+    if used == swapgb.ALGO_DIRECT:
+        kname, k_ms, kfile = "k_count", mean_ms[2], "k_count"
         algo_bytes = n_occ * 64 + n_bases / 4 + reads.n_reads * 12
         model = ("64 B per k-mer occurrence (one 32 B sector of the hash-table entry read + "
                  "written back) + 0.25 B per base + 12 B per read")
+    elif used == swapgb.ALGO_BUCKETED:
+        # the longer of the two single-kernel phases, each timed by events
+        # around that kernel's launch on the build stream
+        if mean_ms[1] >= mean_ms[3]:
+            kname, k_ms, kfile = "k_p1_scatter", mean_ms[1], "k_p1_scatter"
+            algo_bytes = n_bases / 4 + reads.n_reads * 12 + n_occ * 8
+            model = ("packed reads in (0.25 B per base + 12 B per read), one 8 B record per "
+                     "k-mer occurrence out")
+        else:
+            kname, k_ms, kfile = "k_bucket_count", mean_ms[3], "k_bucket_count"
+            algo_bytes = n_occ * 8 + survivors * 16
+            model = "one 8 B record per k-mer occurrence in, 16 B per surviving k-molecule staged"
     else:
         # the whole partitioned build: every kernel, DRAM bytes it cannot avoid
         kname, k_ms = "partitioned build (all kernels)", mean_ms[4]
@@ -493,7 +514,7 @@ def main() -> int:
                  "(0.25 B/base + 12 B/read each), 16 B per surviving k-molecule written; "
                  "partition slices stay in L2")
     achieved = algo_bytes / (k_ms * 1e-3) / 1e9
-    tpo, tsrc = k_count_traffic_per_occ() if algo == swapgb.ALGO_DIRECT else (None, None)
+    tpo, tsrc = traffic_per_occ(kfile) if kfile else (None, None)
     roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hbm,
                 "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src,
                 "traffic": (tpo * n_occ) if tpo else None, "traffic_source": tsrc,
@@ -506,15 +527,15 @@ def main() -> int:
         r_l2 = swapgb.probe_random_access("load16_cas128", 48 << 20, 1 << 30, stream.cuda_stream)
         # per read of length L: (L-k+1) key probes + 2(L-k) slot increments
         ops = n_occ + 2 * (n_occ - n_with_occ)
-        count_ms = mean_ms[2]
+        count_ms = mean_ms[3] if used == swapgb.ALGO_BUCKETED else mean_ms[2]
         atomic = {"R_red_add_u32_per_s": r_red, "dram_load16_cas128_per_s": r_pat,
                   "l2_load16_cas128_per_s": r_l2, "table_bytes": table_bytes,
                   "ops_per_step": ops, "achieved_ops_per_s": ops / (mean_ms[4] * 1e-3),
                   "frac_of_R": ops / (mean_ms[4] * 1e-3) / r_red,
                   "occurrences_per_s_counting_phase": n_occ / (count_ms * 1e-3),
-                  "frac_counting_phase_vs_" + ("dram" if algo == swapgb.ALGO_DIRECT else "l2")
+                  "frac_counting_phase_vs_" + ("dram" if used == swapgb.ALGO_DIRECT else "l2")
                   + "_load16_cas128": (n_occ / (count_ms * 1e-3))
-                  / (r_pat if algo == swapgb.ALGO_DIRECT else r_l2)}
+                  / (r_pat if used == swapgb.ALGO_DIRECT else r_l2)}
     batched = None
     if rank == 0 and not args.no_batch and not args.reads:
         batched = batched_metrics(stream.cuda_stream)
@@ -530,7 +551,8 @@ def main() -> int:
             "metric": METRIC, "value": value, "unit": "bases/s", "n_gpus": world,
             "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-            "data": "synthetic (seeded generator, no dataset)", "config": config_dict(args.algo, args.order),
+            "data": "synthetic (seeded generator, no dataset)", "config": dict(config_dict(args.algo, args.order),
+                                                                    algorithm_used={1: "direct", 2: "partitioned", 3: "bucketed"}[used]),
             "e2e": {"value": aggregate_value(n_bases, world, e2e_s * 1e3), "unit": "bases/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": "swg_graph_build_fasta on the pinned FASTA text (framing + packing on "

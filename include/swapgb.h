@@ -63,7 +63,9 @@ typedef enum swg_status {
 } swg_status;
 
 /* Counting algorithms (same results, different memory traffic). */
-#define SWG_ALGO_DEFAULT 0     /* direct */
+#define SWG_ALGO_DEFAULT 0     /* bucketed when its workspace (~26 bytes per k-mer
+                                  occurrence) fits in device memory, else direct;
+                                  direct for SWG_ORDER_MINIMIZER */
 #define SWG_ALGO_DIRECT 1      /* one pass into a device-wide table in HBM */
 #define SWG_ALGO_PARTITIONED 2 /* hash-partitioned records, each partition counted in L2 */
 #define SWG_ALGO_BUCKETED 3    /* records split into buckets counted in shared memory */
@@ -264,10 +266,12 @@ swg_status swg_records_write_kmer_graph(const uint64_t *keys, const uint8_t *mul
 swg_status swg_records_write_node_lines(const uint64_t *keys, const uint8_t *mult, uint64_t n,
                                         const char *path);
 /* Device times (ms) of the last build's phases, from CUDA events on the build
- * stream: [0] sizing (occurrence prefix, tiles, distinct estimate or partition
- * histogram), [1] preparation (table clear, or record scatter), [2] counting
- * (K1, or every wave's partition count + compaction), [3] cutoff+compaction
- * (direct only), [4] whole build. Also the launch count of the last build. */
+ * stream. Direct / partitioned: [0] sizing (occurrence prefix, tiles, distinct
+ * estimate or partition histogram), [1] preparation (table clear, or record
+ * scatter), [2] counting (K1, or every wave's partition count + compaction),
+ * [3] cutoff+compaction (direct only). Bucketed: [0] setup, [1] level-1
+ * scatter kernel, [2] level-2 scatter, [3] bucket counting kernels. [4] whole
+ * build. Also the launch count of the last build. */
 swg_status swg_graph_last_timings(const swg_graph *g, float ms[5], int *launches);
 swg_status swg_graph_build_info(const swg_graph *g, swg_build_info *info);
 

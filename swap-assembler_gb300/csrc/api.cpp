@@ -61,7 +61,7 @@ struct swg_graph {
     // pinned host mirrors
     Control *h_ctl = nullptr;
     unsigned *h_hll = nullptr;
-    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     // result of the last build
     bool built = false;
     int k = 0;
@@ -200,6 +200,22 @@ swg_status build_partitioned(swg_graph *g, const swg_opts *o, BuildArgs &a, cuda
 swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s,
                           double load, bool counted = false);
 
+// The default algorithm is the bucketed one while its workspace (two record
+// buffers of about 1.5 x 8 bytes per occurrence, plus the output) fits in
+// 80% of the device memory that is free or already held by this handle's
+// record buffers; otherwise the direct one, whose table grows with the
+// distinct k-molecules instead of the occurrences.
+bool bucketed_fits(const swg_graph *g, uint64_t occurrences) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    const double held = 8.0 * (double)(g->records_cap + g->rec2_cap);
+    const double need = 26.0 * (double)occurrences + (64 << 20);
+    return need <= 0.8 * ((double)free_b + held);
+}
+
 swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, uint64_t n_words,
                       const uint64_t *off, const uint32_t *len, uint64_t n_reads) {
     swg_status st = check_opts(o);
@@ -261,6 +277,8 @@ swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, u
 
     if (o->algorithm == SWG_ALGO_PARTITIONED) return build_partitioned(g, o, a, s, load);
     if (o->algorithm == SWG_ALGO_BUCKETED) return build_bucketed(g, o, a, s, load);
+    if (o->algorithm == SWG_ALGO_DEFAULT && o->read_order == SWG_ORDER_INPUT && bucketed_fits(g, a.total_occ))
+        return build_bucketed(g, o, a, s, load);
     return build_direct(g, o, a, s, load);
 }
 
@@ -796,6 +814,7 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     }
     SWG_CUDA(cudaEventRecord(g->ev[1], s), "event");
     g->launches += swg::launch_part_scatter(a, pa, s);
+    SWG_CUDA(cudaEventRecord(g->ev[2], s), "event");
     g->launches += swg::launch_chunk_prefix(bk, s);
     if (counted) {  // exact bucket offsets
         SWG_CUDA(cudaMemsetAsync(bk.cursor2, 0, NB * 8, s), "clear bucket counts");
@@ -810,8 +829,9 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     }
     g->launches += swg::launch_sub_scatter(bk, s);
     SWG_CUDA(cudaGetLastError(), "bucket scatter launch");
-    SWG_CUDA(cudaEventRecord(g->ev[2], s), "event");
+    SWG_CUDA(cudaEventRecord(g->ev[3], s), "event");
     g->launches += swg::launch_bucket_count(a, bk, s);
+    SWG_CUDA(cudaEventRecord(g->ev[5], s), "event");
     g->launches += swg::launch_gscan(reinterpret_cast<const uint64_t *>(bk.surv),
                                      reinterpret_cast<uint64_t *>(bk.surv_off), NB,
                                      reinterpret_cast<uint64_t *>(scr),
@@ -872,7 +892,6 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
         g->launches += swg::launch_big_bucket(a, bk, bb, rb, re, g->d_arena, cap, s);
     }
     SWG_CUDA(cudaGetLastError(), "gather launch");
-    SWG_CUDA(cudaEventRecord(g->ev[3], s), "event");
     SWG_CUDA(cudaMemcpyAsync(g->h_ctl, g->d_ctl, sizeof(Control) - sizeof(uint64_t),
                              cudaMemcpyDeviceToHost, s), "read status");
     SWG_CUDA(cudaEventRecord(g->ev[4], s), "event");
@@ -897,9 +916,11 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     g->n_out = g->h_ctl->counters[1];
     g->built = true;
     float t[5] = {0, 0, 0, 0, 0};
+    // [0] setup, [1] level-1 scatter, [2] level-2 scatter, [3] bucket count
     cudaEventElapsedTime(&t[0], g->ev[0], g->ev[1]);
     cudaEventElapsedTime(&t[1], g->ev[1], g->ev[2]);
     cudaEventElapsedTime(&t[2], g->ev[2], g->ev[3]);
+    cudaEventElapsedTime(&t[3], g->ev[3], g->ev[5]);
     cudaEventElapsedTime(&t[4], g->ev[0], g->ev[4]);
     std::memcpy(g->ms, t, sizeof(t));
     return SWG_OK;
@@ -963,7 +984,7 @@ swg_status swg_graph_create(swg_graph **out) {
     if (!g) return SWG_ERR_OOM;
     cudaError_t e = cudaGetDevice(&g->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->own, cudaStreamNonBlocking);
-    for (int i = 0; e == cudaSuccess && i < 5; i++) e = cudaEventCreate(&g->ev[i]);
+    for (int i = 0; e == cudaSuccess && i < 7; i++) e = cudaEventCreate(&g->ev[i]);
     if (e == cudaSuccess) e = cudaMalloc(&g->d_hll, sizeof(unsigned) << swg::kHllBits);
     if (e == cudaSuccess) e = cudaMalloc(&g->d_ctl, sizeof(Control));
     if (e == cudaSuccess) e = cudaMallocHost(&g->h_ctl, sizeof(Control));

@@ -1,6 +1,7 @@
 // Autotuner: picks the table load factor and the counting scheme (direct
-// table in input order, direct table in minimizer order, or hash-partitioned
-// slices) for a (k, read-length band), by timing trial builds of a sample on
+// table in input order, direct table in minimizer order, hash-partitioned
+// slices, or shared-memory buckets) for a (k, read-length band), by timing
+// trial builds of a sample on
 // this GPU, and keeps the choices in a cache file (one JSON object per line:
 // {"k": K, "band": B, "load": X, "algorithm": A, "read_order": O, "ms": T}).
 #include <algorithm>
@@ -58,7 +59,8 @@ swg_status swg_autotune(const swg_opts *base, const uint32_t *d_packed, uint64_t
                           {0.7, SWG_ALGO_DIRECT, SWG_ORDER_INPUT},
                           {0.8, SWG_ALGO_DIRECT, SWG_ORDER_INPUT},
                           {0.6, SWG_ALGO_DIRECT, SWG_ORDER_MINIMIZER},
-                          {0.6, SWG_ALGO_PARTITIONED, SWG_ORDER_INPUT}};
+                          {0.6, SWG_ALGO_PARTITIONED, SWG_ORDER_INPUT},
+                          {0.6, SWG_ALGO_BUCKETED, SWG_ORDER_INPUT}};
     swg_graph *g = nullptr;
     swg_status st = swg_graph_create(&g);
     if (st) return st;
