@@ -191,7 +191,19 @@ def batched_metrics(stream_ptr: int, repeats: int = 3) -> dict:
     import torch
     import swapgb
     specs = batched_samples()
-    reads = [swapgb.reads_from_fasta(swapgb.synth_fasta(**p), 27) for p in specs]
+
+    class PinnedReads:
+        """A sample's packed reads staged in pinned host memory (both arms read it)."""
+
+        def __init__(self, r):
+            self._t = [torch.from_numpy(a.copy()).pin_memory()
+                       for a in (r.packed.view(np.int32), r.off.view(np.int64), r.len.view(np.int32))]
+            self.packed = self._t[0].numpy().view(np.uint32)
+            self.off = self._t[1].numpy().view(np.uint64)
+            self.len = self._t[2].numpy().view(np.uint32)
+            self.n_words, self.n_reads, self.n_bases = r.n_words, r.n_reads, r.n_bases
+
+    reads = [PinnedReads(swapgb.reads_from_fasta(swapgb.synth_fasta(**p), 27)) for p in specs]
     bases = sum(r.n_bases for r in reads)
     opts = swapgb.Opts(k=27, cutoff=3, stream=stream_ptr)
     plain, batch = swapgb.Graph(), swapgb.Graph()
@@ -200,17 +212,21 @@ def batched_metrics(stream_ptr: int, repeats: int = 3) -> dict:
     for r in reads:
         plain.build_reads(opts, r)
     torch.cuda.synchronize()
-    t_plain, t_batch = [], []
+    t_plain, t_batch, dev_plain, dev_batch = [], [], [], []
     for _ in range(repeats):
         t0 = time.perf_counter()
+        dp = 0.0
         for r in reads:
             plain.build_reads(opts, r)
+            dp += plain.info()["ms"][4]
         torch.cuda.synchronize()
         t_plain.append(time.perf_counter() - t0)
+        dev_plain.append(dp)
         t0 = time.perf_counter()
         batch.build_batch(opts, samples)
         torch.cuda.synchronize()
         t_batch.append(time.perf_counter() - t0)
+        dev_batch.append(batch.info()["ms"][4])
     # spot check: the last sample of the batch equals its plain build
     kp, mp = plain.copy_out(sorted=True)
     kb, mb = batch.batch_copy_out(len(reads) - 1)
@@ -222,9 +238,11 @@ def batched_metrics(stream_ptr: int, repeats: int = 3) -> dict:
             "plain_s": tp, "batched_s": tb,
             "plain_samples_per_s": len(reads) / tp, "batched_samples_per_s": len(reads) / tb,
             "batched_bases_per_s": bases / tb, "speedup": tp / tb,
+            "device_ms_plain_sum": min(dev_plain), "device_ms_batched": min(dev_batch),
+            "batched_algorithm": {1: "direct", 2: "partitioned", 3: "bucketed"}[batch.info()["algorithm"]],
             "last_sample_identical": same,
-            "path": "host packed reads -> device-resident graphs; plain = swg_graph_build per "
-                    "sample, batched = one swg_batch_build"}
+            "path": "pinned host packed reads -> device-resident graphs; plain = swg_graph_build "
+                    "per sample, batched = one swg_batch_build"}
 
 
 def served_metrics(duration_s: float = 10.0, rate: float = 50.0, seed: int = 5) -> dict:

@@ -33,6 +33,7 @@ struct Control {  // device-side control block
     unsigned long long counters[2];  // inserted keys, survivors
     unsigned pad2;                   // bucketed build: tier-2 overflow count
     unsigned pad3;
+    unsigned long long work[2];      // bucketed build: read batches handed out (count, scatter)
     uint64_t occ_total;              // last: the memsets of the control block stop before it
 };
 
@@ -122,6 +123,12 @@ struct swg_graph {
     uint64_t seg_meta_cap = 0;
     double *d_est = nullptr;
     uint64_t est_cap = 0;
+    // tagged bucketed batch: survivors grouped by sample, per-sample cursors
+    unsigned long long *d_out2_keys = nullptr;
+    unsigned long long *d_out2_mult = nullptr;
+    uint64_t out2_cap = 0;
+    unsigned long long *d_seg_cursor = nullptr;
+    uint64_t seg_cursor_cap = 0;
     unsigned *d_hll_seg = nullptr;
     uint64_t hll_seg_cap = 0;
 };
@@ -412,6 +419,7 @@ swg_status build_partitioned(swg_graph *g, const swg_opts *o, BuildArgs &a, cuda
     std::memset(&pa, 0, sizeof(pa));
     pa.bits = bits;
     pa.n_parts = 1u << bits;
+    pa.work = g->d_ctl->work;  // zeroed with the control block at the start of the build
     pa.load_num = 3;  // slice capacity = count / 0.6 + 16
     pa.load_den = 5;
     if (load != 0.6) {
@@ -509,6 +517,70 @@ swg_status build_partitioned(swg_graph *g, const swg_opts *o, BuildArgs &a, cuda
 
 // ---------------------------------------------------------------------
 // Batched build: all samples are segments of one build (direct algorithm).
+// Batched build on the bucketed scheme: the sample index sits in the top tb
+// bits of every key (tb = 0 for one sample), each bucket applies its keys'
+// own sample cutoffs and counts per sample, and a final pass moves the
+// survivors into per-sample ranges with the tag stripped.
+swg_status batch_bucketed(swg_graph *g, const swg_opts *o, const swg_sample *sm, uint32_t S,
+                          BuildArgs &a, cudaStream_t s, double load, int tb) {
+    swg_status st;
+    a.tag_bits = S > 1 ? tb : 0;
+    a.cutoff = sm[0].cutoff;  // the single sample's, when untagged
+    a.k = sm[0].k;
+    SWG_CUDA(cudaMemsetAsync(g->d_ctl, 0, sizeof(Control) - sizeof(uint64_t), s), "clear control");
+    SWG_CUDA(cudaMemsetAsync(g->d_seg_counts, 0, 2ull * S * 8, s), "clear counters");
+    if ((st = build_bucketed(g, o, a, s, load))) return st;
+    g->n_samples = S;
+    g->s_tbase.assign(S, 0);
+    g->s_tcap.assign(S, 0);
+    g->s_out.assign(S, 0);
+    g->s_distinct.assign(S, 0);
+    if (!a.tag_bits) {
+        g->s_out[0] = g->n_out;
+        g->s_distinct[0] = g->n_distinct;
+        g->s_tcap[0] = g->n_out;
+        return SWG_OK;
+    }
+    std::vector<unsigned long long> counts(2 * (uint64_t)S);
+    SWG_CUDA(cudaMemcpyAsync(counts.data(), g->d_seg_counts, counts.size() * 8, cudaMemcpyDeviceToHost, s),
+             "read sample counters");
+    SWG_CUDA(cudaStreamSynchronize(s), "sample counters");
+    std::vector<unsigned long long> cur(S);
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < S; i++) {
+        g->s_distinct[i] = counts[2 * i];
+        g->s_out[i] = counts[2 * i + 1];
+        g->s_tbase[i] = total;
+        g->s_tcap[i] = counts[2 * i + 1];
+        cur[i] = total;
+        total += counts[2 * i + 1];
+    }
+    if (total != g->n_out) {
+        swg::set_error("batch: per-sample survivor counts disagree with the total");
+        return SWG_ERR_CUDA;
+    }
+    if ((st = ensure(&g->d_seg_cursor, &g->seg_cursor_cap, S, "sample cursors"))) return st;
+    if (g->out2_cap < total || !g->d_out2_keys || !g->d_out2_mult) {
+        cudaFree(g->d_out2_keys);
+        cudaFree(g->d_out2_mult);
+        g->d_out2_keys = g->d_out2_mult = nullptr;
+        g->out2_cap = 0;
+        const uint64_t want = std::max<uint64_t>(total, 1);
+        SWG_CUDA(cudaMalloc(&g->d_out2_keys, want * 8), "grouped keys");
+        SWG_CUDA(cudaMalloc(&g->d_out2_mult, want * 8), "grouped multiplicities");
+        g->out2_cap = want;
+    }
+    SWG_CUDA(cudaMemcpyAsync(g->d_seg_cursor, cur.data(), S * 8, cudaMemcpyHostToDevice, s), "sample cursors");
+    g->launches += swg::launch_group_by_sample(g->d_out_keys, g->d_out_mult, total, a.tag_bits, S,
+                                               g->d_seg_cursor, g->d_out2_keys, g->d_out2_mult, s);
+    SWG_CUDA(cudaGetLastError(), "group launch");
+    SWG_CUDA(cudaStreamSynchronize(s), "group by sample");
+    std::swap(g->d_out_keys, g->d_out2_keys);
+    std::swap(g->d_out_mult, g->d_out2_mult);
+    std::swap(g->out_cap, g->out2_cap);
+    return SWG_OK;
+}
+
 swg_status batch_impl(swg_graph *g, const swg_opts *o, const swg_sample *sm, uint32_t S) {
     if (!o || !sm || S == 0) {
         swg::set_error("batch: no samples");
@@ -618,6 +690,19 @@ swg_status batch_impl(swg_graph *g, const swg_opts *o, const swg_sample *sm, uin
     const uint64_t *occ_pre = meta.data() + 2 * S + 1;
     a.total_occ = occ_pre[S];
     g->occurrences = a.total_occ;
+    g->s_occ.assign(S, 0);
+    for (uint32_t i = 0; i < S; i++) g->s_occ[i] = occ_pre[i + 1] - occ_pre[i];
+    {
+        // every key tagged with its sample in one bucketed build, when the tag
+        // fits above the longest k-mer
+        int kmax = 1, tb = 0;
+        for (uint32_t i = 0; i < S; i++) kmax = std::max(kmax, sm[i].k);
+        while ((1u << tb) < S) tb++;
+        if ((o->algorithm == SWG_ALGO_DEFAULT || o->algorithm == SWG_ALGO_BUCKETED) &&
+            o->read_order == SWG_ORDER_INPUT && S <= swg::kMaxTagSamples && 2 * kmax + tb <= 64 &&
+            (o->algorithm == SWG_ALGO_BUCKETED || bucketed_fits(g, a.total_occ)))
+            return batch_bucketed(g, o, sm, S, a, s, load, tb);
+    }
     a.n_tiles = (a.total_occ + swg::kTileOcc - 1) / swg::kTileOcc;
     if ((st = ensure(&g->d_tiles, &g->tiles_cap, a.n_tiles, "tile table"))) return st;
     a.tile_first_read = g->d_tiles;
@@ -640,8 +725,6 @@ swg_status batch_impl(swg_graph *g, const swg_opts *o, const swg_sample *sm, uin
         cap[i] = (uint64_t)std::ceil(std::max(e, 1.0) / load) + 64;
     }
     const uint64_t chunk = 256 * 8;  // k_compact chunk: sample regions start on it
-    g->s_occ.assign(S, 0);
-    for (uint32_t i = 0; i < S; i++) g->s_occ[i] = occ_pre[i + 1] - occ_pre[i];
     for (int attempt = 0; attempt < 6; ++attempt) {
         uint64_t total = 0;
         for (uint32_t i = 0; i < S; i++) {
@@ -744,7 +827,10 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     swg_status st;
     g->algorithm = SWG_ALGO_BUCKETED;
     const uint64_t N = a.total_occ;
-    int b1 = N <= (400ull << 20) ? 8 : (N <= (1600ull << 20) ? 9 : 10);
+    // level-1 partitions: 256, 512 past 400M occurrences (a level-1 round of
+    // 4096 records still writes runs of 8), 1024 only past 6.4G
+    int b1 = N <= (400ull << 20) ? 8 : (N <= (6400ull << 20) ? 9 : 10);
+    if (const char *e = std::getenv("SWG_PART_BITS")) b1 = std::min(10, std::max(8, std::atoi(e)));
     const uint64_t P = 1ull << b1;
     // sub-buckets of about `target` records (SWG_BUCKET_RECORDS overrides)
     double target = 6144.0;
@@ -765,11 +851,13 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     pa.load_num = 3;
     pa.load_den = 5;
     pa.fixed_cap = fixed_cap;
+    pa.work = g->d_ctl->work;
     if ((st = ensure(&g->d_part, &g->part_cap, 4 * P + 1, "partition table"))) return st;
     pa.part_count = g->d_part;
     pa.part_start = g->d_part + P;
     pa.part_cursor = g->d_part + 2 * P + 1;
-    if ((st = ensure(&g->d_records, &g->records_cap, rec1_cap, "records"))) return st;
+    // +2: the level-2 bulk copies round a chunk's end up to an even record
+    if ((st = ensure(&g->d_records, &g->records_cap, rec1_cap + 2, "records"))) return st;
     if ((st = ensure(&g->d_rec2, &g->rec2_cap, rec2_cap, "bucket records"))) return st;
     const uint64_t scratch = swg::gscan_scratch(NB);
     // d_bk: cursors [NB] | offsets [NB+1] | big list [NB] | survivor prefix
@@ -847,6 +935,8 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
         // from a clear control block
         g->h_ctl->occ_total = N;
         SWG_CUDA(cudaMemsetAsync(g->d_ctl, 0, sizeof(Control) - sizeof(uint64_t), s), "clear control");
+        if (a.tag_bits)
+            SWG_CUDA(cudaMemsetAsync(a.seg_counts, 0, 2ull * a.n_segs * 8, s), "clear sample counters");
         return build_bucketed(g, o, a, s, load, true);
     }
     const uint64_t n_small = g->h_ctl->occ_total;
@@ -1028,6 +1118,9 @@ void swg_graph_free(swg_graph *g) {
     cudaFree(g->d_seg_status);
     cudaFree(g->d_seg_meta);
     cudaFree(g->d_est);
+    cudaFree(g->d_out2_keys);
+    cudaFree(g->d_out2_mult);
+    cudaFree(g->d_seg_cursor);
     cudaFree(g->d_hll_seg);
     cudaFree(g->d_bucket);
     cudaFree(g->d_poff);

@@ -758,23 +758,27 @@ size_t p1_scatter_smem(uint32_t n_parts, int round) {
 }
 
 // One read per thread, rolled base by base: the state of one read's walk.
-// Bases stream in from the packed words (one load per 16 bases); the left
+// Bases stream in from the packed words (one load per 16 bases, issued 16
+// bases before they are needed); the left
 // neighbour of a k-mer is the base its predecessor shifted out.
 struct ReadWalk {
     uint64_t fwd, rc, kmask;
     uint64_t wnext;    // index of the next packed word
     uint32_t w;        // bases not yet consumed of the current word, MSB first
+    uint32_t wn;       // the next word, loaded ahead
     uint32_t wrem;     // how many
     uint32_t L, p;     // read length, position of the current k-mer
     uint32_t nb;       // base p+k (valid when p+k < L)
     uint32_t lb;       // base p-1 (valid when p >= 1)
     int k, top;
     uint32_t left;     // occurrences still to emit
+    uint64_t tag;      // sample index in the key's top bits (tagged batch), else 0
 };
 
 __device__ __forceinline__ uint32_t walk_next(const BuildArgs &a, ReadWalk &st) {
     if (st.wrem == 0) {
-        st.w = ldw(a.packed, st.wnext++, a.n_words);
+        st.w = st.wn;
+        st.wn = ldw(a.packed, ++st.wnext, a.n_words);  // 16 bases ahead of its use
         st.wrem = 16;
     }
     const uint32_t b = st.w >> 30;
@@ -786,6 +790,7 @@ __device__ __forceinline__ uint32_t walk_next(const BuildArgs &a, ReadWalk &st) 
 __device__ __forceinline__ void walk_init(const BuildArgs &a, ReadWalk &st, uint64_t r) {
     const uint32_t seg = seg_of(a, r);
     st.k = k_of(a, seg);
+    st.tag = a.tag_bits ? (uint64_t)seg << (64 - a.tag_bits) : 0ull;
     st.L = a.read_len[r];
     st.left = st.L >= (uint32_t)st.k ? st.L - (uint32_t)st.k + 1 : 0;
     if (!st.left) return;
@@ -794,6 +799,7 @@ __device__ __forceinline__ void walk_init(const BuildArgs &a, ReadWalk &st, uint
     const uint64_t g0 = a.read_off[r];
     st.wnext = (g0 >> 4) + 1;
     st.w = ldw(a.packed, g0 >> 4, a.n_words) << (2 * (uint32_t)(g0 & 15));
+    st.wn = ldw(a.packed, st.wnext, a.n_words);
     st.wrem = 16 - (uint32_t)(g0 & 15);
     st.fwd = st.rc = 0;
     for (int i = 0; i < st.k; ++i) {
@@ -813,7 +819,7 @@ __device__ __forceinline__ void walk_init(const BuildArgs &a, ReadWalk &st, uint
 __device__ __forceinline__ void walk_emit(const BuildArgs &a, ReadWalk &st, uint64_t &key,
                                           unsigned &code) {
     const bool f = st.fwd >= st.rc;
-    key = f ? st.fwd : st.rc;
+    key = (f ? st.fwd : st.rc) | st.tag;
     code = 0;
     if (st.left > 1) code = 0x08u | ((f ? 0u : 4u) + st.nb);  // p + k < L
     if (st.p) code |= 0x80u | (((f ? 4u : 0u) + 3u - st.lb) << 4);
@@ -827,23 +833,29 @@ __device__ __forceinline__ void walk_emit(const BuildArgs &a, ReadWalk &st, uint
     }
 }
 
-// Level-1 records per partition, one thread per read (contiguous read ranges
-// per block).
+// Level-1 records per partition, one thread per read (blocks take batches of
+// reads as they finish the previous one: reads of uneven length stay balanced).
 __global__ void __launch_bounds__(256) k_p1_count(BuildArgs a, PartArgs pa) {
     __shared__ unsigned hist[1 << kPartBitsMax];
     for (uint32_t j = threadIdx.x; j < pa.n_parts; j += blockDim.x) hist[j] = 0;
     __syncthreads();
+    __shared__ unsigned long long s_base;
     const int shift = 64 - pa.bits;
-    const uint64_t r0 = a.n_reads * blockIdx.x / gridDim.x;
-    const uint64_t r1 = a.n_reads * (blockIdx.x + 1) / gridDim.x;
-    for (uint64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-        ReadWalk st;
-        walk_init(a, st, r);
-        while (st.left) {
-            uint64_t key;
-            unsigned code;
-            walk_emit(a, st, key, code);
-            atomicAdd(&hist[mix64(key) >> shift], 1u);
+    for (;;) {  // batches of blockDim.x reads, handed out as blocks finish them
+        if (threadIdx.x == 0) s_base = atomicAdd(&pa.work[0], (unsigned long long)blockDim.x);
+        __syncthreads();
+        const uint64_t r = s_base + threadIdx.x;
+        if (s_base >= a.n_reads) break;
+        __syncthreads();  // s_base read by all
+        if (r < a.n_reads) {
+            ReadWalk st;
+            walk_init(a, st, r);
+            while (st.left) {
+                uint64_t key;
+                unsigned code;
+                walk_emit(a, st, key, code);
+                atomicAdd(&hist[mix64(key) >> shift], 1u);
+            }
         }
     }
     __syncthreads();
@@ -866,13 +878,16 @@ __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs p
     __shared__ uint64_t wb[NT / 32];
     const int shift = 64 - pa.bits;
     const uint32_t per = (pa.n_parts + blockDim.x - 1) / blockDim.x;
-    const uint64_t r0 = a.n_reads * blockIdx.x / gridDim.x;
-    const uint64_t r1 = a.n_reads * (blockIdx.x + 1) / gridDim.x;
-    for (uint64_t base = r0; base < r1; base += blockDim.x) {
+    __shared__ unsigned long long s_base;
+    for (;;) {  // batches of NT reads, handed out as blocks finish them
+        if (threadIdx.x == 0) s_base = atomicAdd(&pa.work[1], (unsigned long long)NT);
+        __syncthreads();
+        const uint64_t base = s_base;
+        if (base >= a.n_reads) break;
         const uint64_t r = base + threadIdx.x;
         ReadWalk st;
         st.left = 0;
-        if (r < r1) walk_init(a, st, r);
+        if (r < a.n_reads) walk_init(a, st, r);
         while (__syncthreads_or(st.left != 0)) {
             for (uint32_t j = threadIdx.x; j < pa.n_parts; j += blockDim.x) hist[j] = 0;
             __syncthreads();
@@ -1223,12 +1238,209 @@ __global__ void __launch_bounds__(NT, MINB) k_sub_scatter(BucketArgs b) {
     }
 }
 
+// ---- bulk (TMA) copies into shared memory, tracked by an mbarrier ----
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// Orders this CTA's earlier generic-proxy shared-memory accesses before later
+// bulk copies into the same memory.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// dst, src and bytes are multiples of 16.
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+constexpr int kMaxWait = 1 << 20;  // try_wait rounds before a copy is given up on
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    for (int i = 0; i < kMaxWait; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// Level-2 scatter with the chunks brought in by bulk copies: while a chunk is
+// ordered by sub-bucket and written out, the block's next chunk is already
+// in flight into the other staging buffer. A chunk's staging buffer also
+// holds it once ordered. Copies start at an even record (16-byte aligned)
+// and end after an even record; the record buffer has two records of slack.
+constexpr int kSubBuf = kBkChunk + 2;  // records per staging buffer
+constexpr size_t kSubScatterTmaDyn = 2 * (size_t)kSubBuf * sizeof(unsigned long long) +
+                                     kBkBinsMax * (2 * sizeof(unsigned) + sizeof(unsigned long long));
+
+__global__ void __launch_bounds__(256, 2) k_sub_scatter_tma(BucketArgs b) {
+    constexpr int NT = 256, IT = kBkChunk / 256;
+    extern __shared__ __align__(16) unsigned char dyn[];
+    unsigned long long *const buf0 = reinterpret_cast<unsigned long long *>(dyn);  // two staging buffers
+    unsigned long long *gbase = buf0 + 2 * kSubBuf;
+    unsigned *hist = reinterpret_cast<unsigned *>(gbase + kBkBinsMax);
+    unsigned *loff = hist + kBkBinsMax;
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ uint64_t wb[NT / 32];
+    const uint32_t P2 = 1u << b.b2;
+    const uint32_t per = (P2 + NT - 1) / NT;  // bins per thread in the scan
+    const uint64_t nq = b.chunk_start[b.n_parts];
+    const uint64_t stride = gridDim.x;
+    auto issue = [&](uint64_t q, int k) {
+        uint64_t r0, r1;
+        chunk_range(b, q, r0, r1);
+        const uint64_t a0 = r0 & ~1ull, a1 = (r1 + 1) & ~1ull;
+        bulk_load(buf0 + k * kSubBuf, b.rec1 + a0, (uint32_t)((a1 - a0) * sizeof(unsigned long long)), &bar[k]);
+    };
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+        if (blockIdx.x < nq) issue(blockIdx.x, 0);
+        if (blockIdx.x + stride < nq) issue(blockIdx.x + stride, 1);
+    }
+    __syncthreads();
+    uint32_t parity = 0;  // bit k: phase parity of bar[k]
+    int k = 0;
+    for (uint64_t q = blockIdx.x; q < nq; q += stride, k ^= 1) {
+        const bool ok = mbar_wait(&bar[k], (parity >> k) & 1u);
+        if (__syncthreads_or(!ok)) {  // a copy never completed: flag it, let the others land, leave
+            if (threadIdx.x == 0) {
+                atomicOr(b.status, kStatusCasLimit);
+                mbar_wait(&bar[k ^ 1], (parity >> (k ^ 1)) & 1u);
+            }
+            return;
+        }
+        parity ^= 1u << k;
+        unsigned long long *cur = buf0 + k * kSubBuf;
+        uint64_t r0, r1;
+        const uint32_t p = chunk_range(b, q, r0, r1);
+        const uint32_t off = (uint32_t)(r0 & 1);
+        const uint32_t n = (uint32_t)(r1 - r0);
+        unsigned long long v[IT];
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+            const uint32_t i = (uint32_t)it * NT + threadIdx.x;
+            v[it] = i < n ? cur[off + i] : 0ull;
+        }
+        for (uint32_t j = threadIdx.x; j < P2; j += NT) hist[j] = 0;
+        __syncthreads();  // v read from the staging buffer; the histogram cleared
+#pragma unroll
+        for (int it = 0; it < IT; ++it)
+            if ((uint32_t)it * NT + threadIdx.x < n) atomicAdd(&hist[sub_of(b, v[it])], 1u);
+        __syncthreads();
+        uint64_t mine = 0;
+        for (uint32_t x = 0; x < per; ++x) {
+            const uint32_t j = threadIdx.x * per + x;
+            if (j < P2) mine += hist[j];
+        }
+        uint64_t run = block_exclusive_scan<NT>(mine, wb, nullptr);
+        for (uint32_t x = 0; x < per; ++x) {
+            const uint32_t j = threadIdx.x * per + x;
+            if (j < P2) {
+                const unsigned c = hist[j];
+                loff[j] = (unsigned)run;
+                run += c;
+                gbase[j] = c ? atomicAdd(&b.cursor2[(uint64_t)p * P2 + j], (unsigned long long)c) : 0;
+                hist[j] = 0;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+            if ((uint32_t)it * NT + threadIdx.x < n) {
+                const uint32_t bn = sub_of(b, v[it]);
+                cur[loff[bn] + atomicAdd(&hist[bn], 1u)] = v[it];
+            }
+        }
+        __syncthreads();
+        const uint64_t bk0 = (uint64_t)p * P2;
+        for (uint32_t j = threadIdx.x; j < n; j += NT) {
+            const unsigned long long w = cur[j];
+            const uint32_t bn = sub_of(b, w);
+            const uint64_t dst = gbase[bn] + (j - loff[bn]);
+            // fixed-capacity buckets: records past the region are dropped (the
+            // overflow is flagged by the bucket count)
+            if (!b.cap2 || dst < (bk0 + bn + 1) * b.cap2) b.rec2[dst] = w;
+        }
+        __syncthreads();  // the buffer is read out
+        if (threadIdx.x == 0 && q + 2 * stride < nq) {
+            fence_proxy_async_smem();
+            issue(q + 2 * stride, k);
+        }
+    }
+}
+
+// Tagged batch: moves every survivor into its sample's range (cursor[s]
+// starts at the sample's survivor prefix) and strips the tag from the key.
+// A round of 2048 survivors takes its rank within each sample from a shared
+// histogram and one range per sample from the global cursor.
+__global__ void __launch_bounds__(256) k_group_by_sample(const unsigned long long *__restrict__ in_keys,
+                                                         const unsigned long long *__restrict__ in_mult,
+                                                         uint64_t n, int tag_bits, uint32_t n_samples,
+                                                         unsigned long long *cursor,
+                                                         unsigned long long *__restrict__ out_keys,
+                                                         unsigned long long *__restrict__ out_mult) {
+    constexpr int IT = 8;
+    __shared__ unsigned hist[kMaxTagSamples];
+    __shared__ unsigned long long base[kMaxTagSamples];
+    const int shift = 64 - tag_bits;
+    const uint64_t mask = (1ull << shift) - 1;
+    for (uint64_t c0 = (uint64_t)blockIdx.x * 256 * IT; c0 < n; c0 += (uint64_t)gridDim.x * 256 * IT) {
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < n_samples; j += 256) hist[j] = 0;
+        __syncthreads();
+        unsigned long long kv[IT], mv[IT];
+        unsigned pr[IT];  // sample | rank << 10
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+            const uint64_t i = c0 + (uint64_t)it * 256 + threadIdx.x;
+            pr[it] = ~0u;
+            kv[it] = mv[it] = 0;
+            if (i < n) {
+                kv[it] = in_keys[i];
+                mv[it] = in_mult[i];
+                const unsigned smp = (unsigned)(kv[it] >> shift);
+                pr[it] = smp | (atomicAdd(&hist[smp], 1u) << 10);
+            }
+        }
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < n_samples; j += 256)
+            base[j] = hist[j] ? atomicAdd(&cursor[j], (unsigned long long)hist[j]) : 0;
+        __syncthreads();
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+            if (pr[it] != ~0u) {
+                const uint64_t pos = base[pr[it] & 1023u] + (pr[it] >> 10);
+                out_keys[pos] = kv[it] & mask;
+                out_mult[pos] = mv[it];
+            }
+        }
+    }
+}
+
 // Shared memory of a bucket CTA: T keys, T x 8 uint16 counters, and the list
 // of used slots (uint16).
 template <int T>
 constexpr size_t bucket_smem() {
     return (size_t)T * (sizeof(unsigned long long) + 4 * sizeof(unsigned) + sizeof(unsigned short));
 }
+// ... plus, for a tagged batch, per-sample distinct and survivor counters.
+constexpr size_t kBucketTagSmem = 2 * kMaxTagSamples * sizeof(unsigned);
 
 // Eight saturated uint8 multiplicities of table entry s (8 x uint16
 // counters, slot t in half t&1 of word t>>1), after the -c cutoff
@@ -1269,12 +1481,17 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
     unsigned long long *keys = reinterpret_cast<unsigned long long *>(dyn);
     unsigned *cnt = reinterpret_cast<unsigned *>(keys + kT);  // 8 x uint16 per entry
     unsigned short *used_list = reinterpret_cast<unsigned short *>(cnt + 4 * kT);
+    unsigned *s_dist = reinterpret_cast<unsigned *>(used_list + kT);  // tagged batch only
+    unsigned *s_surv = s_dist + kMaxTagSamples;
     __shared__ unsigned s_over, s_nused, s_kept;
     const int lane = threadIdx.x & 31;
+    const int tb = a.tag_bits;
     for (uint32_t j = threadIdx.x; j < (uint32_t)kT; j += kNT) {
         keys[j] = 0;
         reinterpret_cast<uint4 *>(cnt)[j] = make_uint4(0, 0, 0, 0);
     }
+    if (tb)
+        for (uint32_t j = threadIdx.x; j < a.n_segs; j += kNT) s_dist[j] = s_surv[j] = 0;
     const int c = a.cutoff;
     const bool cut_all = c >= 256;
     const unsigned cbias = (c > 0 && c < 256) ? (0x8000u - (unsigned)c) * 0x00010001u : 0u;
@@ -1389,7 +1606,18 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
             if (j < nused) {
                 const uint32_t sl = used_list[j];
                 h = keys[sl];
-                if (!over) m = bucket_mult(cnt, sl, cbias, cut_all);
+                if (!over) {
+                    if (tb) {  // the sample's own cutoff, per-sample counts
+                        const uint32_t smp = (uint32_t)(unmix64(h) >> (64 - tb));
+                        const int cs = a.segs[smp].cutoff;
+                        m = bucket_mult(cnt, sl, (cs > 0 && cs < 256) ? (0x8000u - (unsigned)cs) * 0x00010001u : 0u,
+                                        cs >= 256);
+                        atomicAdd(&s_dist[smp], 1u);
+                        if (m) atomicAdd(&s_surv[smp], 1u);
+                    } else {
+                        m = bucket_mult(cnt, sl, cbias, cut_all);
+                    }
+                }
                 keys[sl] = 0;
                 reinterpret_cast<uint4 *>(cnt)[sl] = make_uint4(0, 0, 0, 0);
             }
@@ -1415,6 +1643,13 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
                 b.surv[bk] = s_kept;
                 if (nused) atomicAdd(&a.counters[0], (unsigned long long)nused);
             }
+        }
+    }
+    if (tb) {
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < a.n_segs; j += kNT) {
+            if (s_dist[j]) atomicAdd(&a.seg_counts[2 * j], (unsigned long long)s_dist[j]);
+            if (s_surv[j]) atomicAdd(&a.seg_counts[2 * j + 1], (unsigned long long)s_surv[j]);
         }
     }
 }
@@ -1498,12 +1733,24 @@ __global__ void __launch_bounds__(kCBlock) k_big_compact(BuildArgs a, const Entr
         if (!e.x) continue;
         nused++;
         uint64_t v = e.y;
-        if (thr) {
-            const uint32_t lo = (uint32_t)v & __vcmpgeu4((uint32_t)v, thr);
-            const uint32_t hi = (uint32_t)(v >> 32) & __vcmpgeu4((uint32_t)(v >> 32), thr);
+        uint32_t th = thr;
+        int cc = c;
+        uint32_t smp = 0;
+        if (a.tag_bits) {  // tagged batch: the sample's own cutoff, per-sample counts
+            smp = (uint32_t)(unmix64(e.x) >> (64 - a.tag_bits));
+            cc = a.segs[smp].cutoff;
+            th = cc <= 0 ? 0u : (cc >= 256 ? 0u : (uint32_t)cc * 0x01010101u);
+        }
+        if (th) {
+            const uint32_t lo = (uint32_t)v & __vcmpgeu4((uint32_t)v, th);
+            const uint32_t hi = (uint32_t)(v >> 32) & __vcmpgeu4((uint32_t)(v >> 32), th);
             v = ((uint64_t)hi << 32) | lo;
         }
-        if (c >= 256) v = 0;
+        if (cc >= 256) v = 0;
+        if (a.tag_bits) {
+            atomicAdd(&a.seg_counts[2 * smp], 1ull);
+            if (v) atomicAdd(&a.seg_counts[2 * smp + 1], 1ull);
+        }
         if (v) {
             keys[it] = unmix64(e.x);
             cnts[it] = v;
@@ -1628,7 +1875,7 @@ int launch_tiles(const BuildArgs &a, cudaStream_t s) {
 }
 
 int launch_hll(const BuildArgs &a, cudaStream_t s) {
-    if (a.n_tiles == 0 || a.n_reads == 0) return 0;
+    if (a.total_occ == 0 || a.n_reads == 0) return 0;
     const uint64_t grid = std::min<uint64_t>((a.n_reads + 255) / 256, (uint64_t)device_sm_count() * 8);
     k_hll_reads<<<(unsigned)grid, 256, 0, s>>>(a);
     return 1;
@@ -1709,7 +1956,7 @@ int launch_compact(const BuildArgs &a, cudaStream_t s) {
 }
 
 int launch_part_count(const BuildArgs &a, const PartArgs &p, cudaStream_t s) {
-    if (a.n_tiles == 0 || a.n_reads == 0) return 0;
+    if (a.total_occ == 0 || a.n_reads == 0) return 0;
     const uint64_t grid = std::min<uint64_t>((a.n_reads + 255) / 256, resident_grid(k_p1_count, 256, 0));
     k_p1_count<<<(unsigned)grid, 256, 0, s>>>(a, p);
     return 1;
@@ -1726,12 +1973,13 @@ int launch_part_prefix(const PartArgs &p, cudaStream_t s) {
 }
 
 // Block shape of the two scatter passes: threads, records per thread per
-// round, resident blocks per SM (SWG_SCATTER_SHAPE = 0, 1 or 2 selects one).
+// round, resident blocks per SM (SWG_SCATTER_SHAPE = 0..3 selects one; 3 is
+// the level-2 scatter with bulk-copy staging).
 int scatter_shape() {
     static int shape = [] {
         const char *e = std::getenv("SWG_SCATTER_SHAPE");
         const int v = e ? std::atoi(e) : 0;
-        return v >= 0 && v <= 2 ? v : 0;
+        return v >= 0 && v <= 3 ? v : 0;
     }();
     return shape;
 }
@@ -1747,7 +1995,7 @@ int launch_p1_scatter_shape(const BuildArgs &a, const PartArgs &p, cudaStream_t 
 }
 
 int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s) {
-    if (a.n_tiles == 0 || a.n_reads == 0) return 0;
+    if (a.total_occ == 0 || a.n_reads == 0) return 0;
     switch (scatter_shape()) {
         case 1: return launch_p1_scatter_shape<512, 8, 2>(a, p, s);
         case 2: return launch_p1_scatter_shape<256, 8, 4>(a, p, s);
@@ -1802,12 +2050,22 @@ int launch_sub_scatter(const BucketArgs &b, cudaStream_t s) {
         case 1: return launch_sub_scatter_shape<512, 8, 2>(b, s);
         case 2: return launch_sub_scatter_shape<512, 8, 3>(b, s);
         default: return launch_sub_scatter_shape<256, 16, 3>(b, s);
+        case 3: {  // bulk-copy staging (measured slower on GB300: 2 blocks/SM instead of 3)
+            const uint64_t chunks = b.n_rec / kBkChunk + b.n_parts;
+            cudaFuncSetAttribute(k_sub_scatter_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kSubScatterTmaDyn);
+            const uint64_t grid =
+                std::min<uint64_t>(chunks, resident_grid(k_sub_scatter_tma, 256, kSubScatterTmaDyn));
+            k_sub_scatter_tma<<<(unsigned)grid, 256, kSubScatterTmaDyn, s>>>(b);
+            return 1;
+        }
     }
 }
 
 int launch_bucket_count(const BuildArgs &a, const BucketArgs &b, cudaStream_t s) {
     const uint64_t nb = (uint64_t)b.n_parts << b.b2;
-    const size_t smem1 = bucket_smem<kBkTable>(), smem2 = bucket_smem<kBkTable2>();
+    const size_t tag = a.tag_bits ? kBucketTagSmem : 0;
+    const size_t smem1 = bucket_smem<kBkTable>() + tag, smem2 = bucket_smem<kBkTable2>() + tag;
     cudaFuncSetAttribute(k_bucket_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
     const uint64_t grid = std::min<uint64_t>(nb, resident_grid(k_bucket_count, kBkThreads, smem1));
     k_bucket_count<<<(unsigned)grid, kBkThreads, smem1, s>>>(a, b, nb);
@@ -1819,6 +2077,16 @@ int launch_bucket_count(const BuildArgs &a, const BucketArgs &b, cudaStream_t s)
 int launch_bucket_init(const BucketArgs &b, uint64_t n_buckets, cudaStream_t s) {
     if (!n_buckets) return 0;
     k_bucket_init<<<(unsigned)((n_buckets + 255) / 256), 256, 0, s>>>(b, n_buckets);
+    return 1;
+}
+
+int launch_group_by_sample(const unsigned long long *in_keys, const unsigned long long *in_mult,
+                           uint64_t n, int tag_bits, uint32_t n_samples, unsigned long long *cursor,
+                           unsigned long long *out_keys, unsigned long long *out_mult, cudaStream_t s) {
+    if (!n) return 0;
+    const uint64_t grid = std::min<uint64_t>((n + 2047) / 2048, (uint64_t)device_sm_count() * 8);
+    k_group_by_sample<<<(unsigned)grid, 256, 0, s>>>(in_keys, in_mult, n, tag_bits, n_samples, cursor,
+                                                     out_keys, out_mult);
     return 1;
 }
 

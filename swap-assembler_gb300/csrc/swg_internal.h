@@ -70,7 +70,11 @@ struct BuildArgs {
     uint32_t n_segs;
     unsigned long long *seg_counts;    // [2 * n_segs]: inserted, survivors
     unsigned *seg_status;              // [n_segs]
+    int tag_bits;                      // bucketed batch: the read's sample index sits in the
+                                       // top tag_bits bits of every key (0 = no tag)
 };
+
+constexpr uint32_t kMaxTagSamples = 1024;  // samples of one tagged bucketed batch
 
 // Partitioned build: records {hash low bits, arc code} scattered by the top
 // bits of mix64(key) into n_parts partitions, each counted in a table slice
@@ -90,6 +94,7 @@ struct PartArgs {
     uint32_t n_slots;
     int load_num, load_den;            // slice capacity = count * den / num + 16
     uint64_t fixed_cap;                // bucketed: records per partition region, 0 = counted
+    unsigned long long *work;          // bucketed: [2] read-batch counters (count, scatter), zeroed
 };
 
 // Bucketed build: the level-1 partition records are split again by the next
@@ -163,6 +168,9 @@ int launch_sub_scatter(const BucketArgs &b, cudaStream_t s);
 int launch_bucket_init(const BucketArgs &b, uint64_t n_buckets, cudaStream_t s);
 int launch_bucket_count(const BuildArgs &a, const BucketArgs &b, cudaStream_t s);
 int launch_bucket_gather(const BuildArgs &a, const BucketArgs &b, uint64_t n_buckets, cudaStream_t s);
+int launch_group_by_sample(const unsigned long long *in_keys, const unsigned long long *in_mult,
+                           uint64_t n, int tag_bits, uint32_t n_samples, unsigned long long *cursor,
+                           unsigned long long *out_keys, unsigned long long *out_mult, cudaStream_t s);
 int launch_big_bucket(const BuildArgs &a, const BucketArgs &b, uint64_t bucket, uint64_t rb,
                       uint64_t re, Entry *table, uint64_t cap, cudaStream_t s);
 cudaError_t run_probe(int kind, uint64_t table_bytes, uint64_t n_ops, cudaStream_t s, float *ms);

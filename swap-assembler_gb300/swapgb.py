@@ -423,8 +423,8 @@ def synth_fasta(**kw) -> bytes:
     n = _synth_lib().swg_synth_fasta(C.byref(p), C.byref(buf))
     if n < 0:
         raise RuntimeError("synthetic read generation failed")
-    try:
-        return C.string_at(buf.value, n)
+    try:  # (string_at takes a C int size: no good past 2 GiB)
+        return bytes((C.c_ubyte * n).from_address(buf.value)) if n else b""
     finally:
         _synth_lib().swg_synth_free(buf)
 

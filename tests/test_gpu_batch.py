@@ -71,3 +71,48 @@ def test_batch_handle_reuse_and_single_sample_calls(texts):
     keys, mult = g.copy_out()
     pk, pm = _plain(texts[1], 27, 3)
     assert np.array_equal(keys, pk) and np.array_equal(mult, pm)
+
+
+# samples whose k leaves room for the sample tag above the k-mer (k <= 27):
+# the default batch runs them through one tagged bucketed build
+TAGGED = [i for i, (_, k, _) in enumerate(SAMPLES) if k <= 27]
+
+
+@pytest.mark.parametrize("algo", [swapgb.ALGO_DEFAULT, swapgb.ALGO_DIRECT])
+def test_tagged_batch_equals_plain_builds(texts, algo):
+    short = swapgb.reads_from_fasta(b">a\nACGTACGT\n>b\nACG\n", 21)
+    batch = [(swapgb.reads_from_fasta(texts[i], SAMPLES[i][1]), SAMPLES[i][1], SAMPLES[i][2])
+             for i in TAGGED] + [(short, 21, 2)]
+    g = swapgb.Graph()
+    g.build_batch(swapgb.Opts(algorithm=algo), batch)
+    assert g.info()["algorithm"] == (swapgb.ALGO_BUCKETED if algo == swapgb.ALGO_DEFAULT
+                                     else swapgb.ALGO_DIRECT)
+    for j, i in enumerate(TAGGED):
+        keys, mult = g.batch_copy_out(j)
+        pk, pm = _plain(texts[i], SAMPLES[i][1], SAMPLES[i][2])
+        assert np.array_equal(keys, pk) and np.array_equal(mult, pm), "sample %d" % i
+        occ, distinct, surv = g.batch_info(j)
+        assert surv == keys.size and distinct >= surv and occ > 0
+    assert g.batch_info(len(batch) - 1) == (0, 0, 0)
+
+
+def test_tagged_batch_many_samples_and_overflow():
+    """300 samples (9 tag bits, k=21), one of them a single hot k-mer that
+    overflows its fixed-capacity partition: the batch reruns with exact
+    counts and every sample still equals its own plain build."""
+    hot = "".join(">h%d\n%s\n" % (i, "A" * 150) for i in range(3000)).encode()
+    texts = [swapgb.synth_fasta(seed=500 + i, genome_len=3_000 + 97 * i, n_reads=300 + 5 * i,
+                                read_len=(75, 100, 150)[i % 3], sub_rate=0.005) for i in range(299)]
+    texts.insert(137, hot)
+    batch = [(swapgb.reads_from_fasta(t, 21), 21, 2 + (i % 3)) for i, t in enumerate(texts)]
+    g = swapgb.Graph()
+    g.build_batch(swapgb.Opts(), batch)
+    info = g.info()
+    assert info["algorithm"] == swapgb.ALGO_BUCKETED and info["estimate"] == 1.0, info
+    for i in list(range(0, 300, 23)) + [137, 299]:
+        keys, mult = g.batch_copy_out(i)
+        pk, pm = _plain(texts[i], 21, 2 + (i % 3))
+        assert np.array_equal(keys, pk) and np.array_equal(mult, pm), "sample %d" % i
+    ok, om = oracle.records(texts[137], 21, 2 + (137 % 3))
+    keys, mult = g.batch_copy_out(137)
+    assert np.array_equal(keys, ok) and np.array_equal(mult, om)
