@@ -36,9 +36,23 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "swap-assembler_gb300"))
 
 METRIC = "bases/s into filtered k-mer graph on 1 GB300"
-WORKLOAD = dict(seed=2, genome_len=5_000_000, gc=0.5, n_reads=2_500_000, read_len=100,
-                sub_rate=0.01, indel_rate=0.001)
-K, CUTOFF = 31, 5
+# The plain single-sample workloads (seeded synthetic reads with these shapes
+# and error rates); the bench line is quoted on workload 2 by default.
+CONFIGS = {
+    1: (dict(seed=1, genome_len=1_000_000, gc=0.5, n_reads=300_000, read_len=100, sub_rate=0.005),
+        21, 2, "plain single-sample build: 1 Mbp uniform genome, 300k x 100 bp reads at 30x from "
+               "both strands, 0.5% subs, k=21, c=2"),
+    2: (dict(seed=2, genome_len=5_000_000, gc=0.5, n_reads=2_500_000, read_len=100,
+             sub_rate=0.01, indel_rate=0.001),
+        31, 5, "plain single-sample build: 5 Mbp genome (GC 50%), 2.5M x 100 bp reads at 50x "
+               "from both strands, 1% subs + 0.1% indels, k=31, c=5"),
+    3: (dict(seed=3, genome_len=100_000_000, gc=0.5, repeat_frac=0.05, tandem_frac=0.02,
+             n_reads=20_000_000, read_len=150, sub_rate=0.005),
+        31, 3, "plain single-sample build, skewed: 100 Mbp genome with 5% repeat families "
+               "(1-5 kbp units, 2-200 copies, 1% divergence) + 2% tandem repeats (2-6 bp units), "
+               "20M x 150 bp reads at 30x, 0.5% subs, k=31, c=3"),
+}
+WORKLOAD, K, CUTOFF, DESC = CONFIGS[2]
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -56,13 +70,18 @@ def parse_args():
     ap.add_argument("--order", default="input", choices=["input", "minimizer"],
                     help="read order of the direct algorithm")
     ap.add_argument("--reads", type=int, default=0,
-                    help="smaller case for profiling: this many reads, genome scaled to keep 50x")
-    return ap.parse_args()
+                    help="smaller case for profiling: this many reads, genome scaled to keep the coverage")
+    ap.add_argument("--config", type=int, default=2, choices=sorted(CONFIGS),
+                    help="plain workload: 1 = 1 Mbp/30x/k21 c2, 2 = 5 Mbp/50x/k31 c5 (default), "
+                         "3 = 100 Mbp with repeats/30x/150 bp/k31 c3")
+    args = ap.parse_args()
+    global WORKLOAD, K, CUTOFF, DESC
+    WORKLOAD, K, CUTOFF, DESC = CONFIGS[args.config]
+    return args
 
 
 def config_dict(algo: str = "default", order: str = "input") -> dict:
-    return {"algorithm": algo, "read_order": order, "workload": "plain single-sample build: 5 Mbp genome (GC 50%), 2.5M x 100 bp reads "
-                        "at 50x from both strands, 1% subs + 0.1% indels, k=31, c=5",
+    return {"algorithm": algo, "read_order": order, "workload": DESC,
             "genome_bp": WORKLOAD["genome_len"], "reads": WORKLOAD["n_reads"],
             "read_len": WORKLOAD["read_len"], "k": K, "c": CUTOFF,
             "inputs": "packed 2-bit reads resident in HBM", "l2": "flushed before every step"}

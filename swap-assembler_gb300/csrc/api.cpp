@@ -129,6 +129,8 @@ struct swg_graph {
     uint64_t out2_cap = 0;
     unsigned long long *d_seg_cursor = nullptr;
     uint64_t seg_cursor_cap = 0;
+    unsigned long long *d_bigmeta = nullptr;  // bucketed: big-bucket ranges for the global table
+    uint64_t bigmeta_cap = 0;
     unsigned *d_hll_seg = nullptr;
     uint64_t hll_seg_cap = 0;
 };
@@ -818,10 +820,13 @@ swg_status batch_impl(swg_graph *g, const swg_opts *o, const swg_sample *sm, uin
 // the next hash bits, and every bucket is counted by one CTA in a
 // shared-memory hash table and compacted from there. Buckets too large for
 // shared memory (hot k-molecules) are counted in a global-memory table.
-// Bucketed build (kernels.cu, k_p1_* / k_sub_* / k_bucket_*). Level-1
-// partitions have a fixed capacity (1.125x the mean plus slack), so no count
-// pass precedes the scatter; a partition that overflows it (heavy repeats)
-// sets a status bit and the build reruns with exact per-partition counts.
+// Bucketed build (kernels.cu, k_p1_* / k_sub_* / k_bucket_*). A sampled pass
+// (every 16th batch of reads, from 16M occurrences; uniform below) sizes
+// every level-1 partition and every bucket;
+// the scatters write into those regions, so no exact count pass precedes
+// them. A partition or bucket that outgrows its region (a sampling miss) sets
+// a status bit, the later kernels skip their work, and the build reruns with
+// exact counts (counted = true).
 swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s,
                           double load, bool counted) {
     swg_status st;
@@ -838,31 +843,29 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     int b2 = 0;
     while (b2 < 10 && (double)N / (double)(P << b2) > target) b2++;
     const uint64_t NB = P << b2;
-    // fixed capacities: partitions 1.125x their mean + 16K, buckets 1.5x + 256
-    const uint64_t fixed_cap = counted ? 0 : (N + P - 1) / P + (N + P - 1) / P / 8 + 16384;
-    const uint64_t cap2 = counted ? 0 : (N + NB - 1) / NB + (N + NB - 1) / NB / 2 + 256;
-    // the level-1 buffer also stages the survivor keys at bucket offsets
-    const uint64_t rec1_cap = std::max<uint64_t>(counted ? N : std::max(P * fixed_cap, NB * cap2), 1);
-    const uint64_t rec2_cap = std::max<uint64_t>(counted ? N : NB * cap2, 1);
+    // region bounds: partitions <= 1.25 N + 4097 P, buckets <= 1.5 N + 257 NB;
+    // the level-1 buffer also stages survivor keys at bucket offsets
+    const uint64_t rec1_bound = counted ? N : N + N / 4 + 4097 * P;
+    const uint64_t rec2_bound = counted ? N : N + N / 2 + 257 * NB;
     swg::PartArgs pa;
     std::memset(&pa, 0, sizeof(pa));
     pa.bits = b1;
     pa.n_parts = (uint32_t)P;
     pa.load_num = 3;
     pa.load_den = 5;
-    pa.fixed_cap = fixed_cap;
     pa.work = g->d_ctl->work;
     if ((st = ensure(&g->d_part, &g->part_cap, 4 * P + 1, "partition table"))) return st;
     pa.part_count = g->d_part;
     pa.part_start = g->d_part + P;
     pa.part_cursor = g->d_part + 2 * P + 1;
-    // +2: the level-2 bulk copies round a chunk's end up to an even record
-    if ((st = ensure(&g->d_records, &g->records_cap, rec1_cap + 2, "records"))) return st;
-    if ((st = ensure(&g->d_rec2, &g->rec2_cap, rec2_cap, "bucket records"))) return st;
+    // +2: the level-2 bulk copies may round a chunk's end up to an even record
+    if ((st = ensure(&g->d_records, &g->records_cap, std::max(rec1_bound, rec2_bound) + 2, "records")))
+        return st;
+    if ((st = ensure(&g->d_rec2, &g->rec2_cap, std::max<uint64_t>(rec2_bound, 1), "bucket records"))) return st;
     const uint64_t scratch = swg::gscan_scratch(NB);
-    // d_bk: cursors [NB] | offsets [NB+1] | big list [NB] | survivor prefix
-    // [NB+1] | scan scratch | totals [2] | chunk prefix [P+1] | second big
-    // list [NB] | survivors per bucket [NB]
+    // d_bk: cursors [NB] | regions [NB+1] | big list [NB] | survivor prefix
+    // [NB+1] | scan scratch | sampled total [2] | chunk prefix [P+1] | second
+    // big list [NB] | survivors per bucket [NB]
     if ((st = ensure(&g->d_bk, &g->bk_cap, 6 * NB + 2 + scratch + 2 + P + 1, "bucket table"))) return st;
     pa.records = g->d_records;
     swg::BucketArgs bk;
@@ -873,7 +876,6 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     bk.part_start = pa.part_start;
     bk.part_cursor = pa.part_cursor;
     bk.part_end = g->d_part + 3 * P + 1;
-    bk.fixed_cap = fixed_cap;
     bk.status = &g->d_ctl->status;
     bk.rec1 = g->d_records;
     bk.rec2 = g->d_rec2;
@@ -884,27 +886,38 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     bk.big_count = &g->d_ctl->pad;
     bk.n_rec = N;
     bk.surv_off = g->d_bk + 3 * NB + 1;
-    bk.stage_keys = g->d_records;  // level-1 records are spent too
+    bk.stage_keys = g->d_records;  // level-1 records are spent by then
     unsigned long long *scr = bk.surv_off + NB + 1;
-    unsigned long long *tot = scr + scratch;
-    bk.chunk_start = tot + 2;
+    unsigned long long *sampled = scr + scratch;
+    bk.chunk_start = sampled + 2;
     bk.big2 = bk.chunk_start + P + 1;
-    bk.surv = bk.big2 + NB;
-    bk.cap2 = cap2;
     bk.big2_count = &g->d_ctl->pad2;
+    bk.surv = bk.big2 + NB;
 
+    SWG_CUDA(cudaMemsetAsync(pa.part_count, 0, P * 8, s), "clear partitions");
     if (counted) {
-        SWG_CUDA(cudaMemsetAsync(pa.part_count, 0, P * 8, s), "clear partitions");
         g->launches += swg::launch_part_count(a, pa, s);
         g->launches += swg::launch_part_prefix(pa, s);
     } else {
-        g->launches += swg::launch_part_init(pa, s);
+        SWG_CUDA(cudaMemsetAsync(bk.cursor2, 0, NB * 8, s), "clear bucket samples");
+        // from 16M occurrences every 16th batch of reads is sampled; smaller
+        // inputs get uniform regions (an empty sample), whose slack covers
+        // their spread
+        if (N >= (16ull << 20)) g->launches += swg::launch_p1_sample(a, pa, bk, 16, s);
+        g->launches += swg::launch_part_caps(pa, N, sampled, s);
+        // bucket regions from the same sample (surv serves as scratch)
+        g->launches += swg::launch_bucket_caps(bk.cursor2, sampled, N, NB, bk.surv, s);
+        g->launches += swg::launch_gscan(reinterpret_cast<const uint64_t *>(bk.surv),
+                                         reinterpret_cast<uint64_t *>(bk.off2), NB,
+                                         reinterpret_cast<uint64_t *>(scr),
+                                         reinterpret_cast<uint64_t *>(bk.off2 + NB), s);
+        SWG_CUDA(cudaMemcpyAsync(bk.cursor2, bk.off2, NB * 8, cudaMemcpyDeviceToDevice, s), "bucket cursors");
     }
     SWG_CUDA(cudaEventRecord(g->ev[1], s), "event");
     g->launches += swg::launch_part_scatter(a, pa, s);
     SWG_CUDA(cudaEventRecord(g->ev[2], s), "event");
     g->launches += swg::launch_chunk_prefix(bk, s);
-    if (counted) {  // exact bucket offsets
+    if (counted) {  // exact bucket regions
         SWG_CUDA(cudaMemsetAsync(bk.cursor2, 0, NB * 8, s), "clear bucket counts");
         g->launches += swg::launch_sub_hist(bk, s);
         g->launches += swg::launch_gscan(reinterpret_cast<const uint64_t *>(bk.cursor2),
@@ -912,8 +925,6 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
                                          reinterpret_cast<uint64_t *>(scr),
                                          reinterpret_cast<uint64_t *>(bk.off2 + NB), s);
         SWG_CUDA(cudaMemcpyAsync(bk.cursor2, bk.off2, NB * 8, cudaMemcpyDeviceToDevice, s), "bucket cursors");
-    } else {
-        g->launches += swg::launch_bucket_init(bk, NB, s);
     }
     g->launches += swg::launch_sub_scatter(bk, s);
     SWG_CUDA(cudaGetLastError(), "bucket scatter launch");
@@ -931,7 +942,7 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
                              cudaMemcpyDeviceToHost, s), "read status");
     SWG_CUDA(cudaStreamSynchronize(s), "bucket count");
     if (!counted && (g->h_ctl->status & swg::kStatusPartOverflow)) {
-        // a partition or bucket outgrew its fixed capacity: recount exactly,
+        // a partition or bucket outgrew its sampled region: recount exactly,
         // from a clear control block
         g->h_ctl->occ_total = N;
         SWG_CUDA(cudaMemsetAsync(g->d_ctl, 0, sizeof(Control) - sizeof(uint64_t), s), "clear control");
@@ -939,24 +950,30 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
             SWG_CUDA(cudaMemsetAsync(a.seg_counts, 0, 2ull * a.n_segs * 8, s), "clear sample counters");
         return build_bucketed(g, o, a, s, load, true);
     }
+    if (g->h_ctl->status & swg::kStatusPartOverflow) {
+        swg::set_error("bucketed build: a region overflowed with exact counts");
+        return SWG_ERR_CUDA;
+    }
     const uint64_t n_small = g->h_ctl->occ_total;
     g->h_ctl->occ_total = N;
     const unsigned nbig = g->h_ctl->pad2;  // buckets no shared-memory table held
-    std::vector<unsigned long long> big(nbig), rng(nbig ? NB + 1 : 0), rb_of(nbig), re_of(nbig);
+    std::vector<unsigned long long> meta;   // rb [n] | hash prefix [n] | record prefix [n+1]
     uint64_t big_records = 0;
     if (nbig) {
+        std::vector<unsigned long long> big(nbig), off(NB + 1), cur(NB);
         SWG_CUDA(cudaMemcpyAsync(big.data(), bk.big2, nbig * 8, cudaMemcpyDeviceToHost, s), "read big buckets");
-        // counted: the offsets; fixed capacity: the final cursors
-        SWG_CUDA(cudaMemcpyAsync(rng.data(), counted ? bk.off2 : bk.cursor2, (counted ? NB + 1 : NB) * 8,
-                                 cudaMemcpyDeviceToHost, s),
-                 "read bucket ranges");
+        SWG_CUDA(cudaMemcpyAsync(off.data(), bk.off2, (NB + 1) * 8, cudaMemcpyDeviceToHost, s), "read regions");
+        SWG_CUDA(cudaMemcpyAsync(cur.data(), bk.cursor2, NB * 8, cudaMemcpyDeviceToHost, s), "read cursors");
         SWG_CUDA(cudaStreamSynchronize(s), "big buckets");
+        meta.resize(3 * (uint64_t)nbig + 1);
         for (unsigned i = 0; i < nbig; i++) {
-            const uint64_t bb = big[i];
-            rb_of[i] = counted ? rng[bb] : bb * cap2;
-            re_of[i] = counted ? rng[bb + 1] : std::min<uint64_t>(rng[bb], bb * cap2 + cap2);
-            big_records += re_of[i] - rb_of[i];
+            const uint64_t bb = big[i], rb = off[bb], re = std::min<uint64_t>(cur[bb], off[bb + 1]);
+            meta[i] = rb;
+            meta[nbig + i] = (unsigned long long)(bb >> b2) << (64 - b1);
+            meta[2 * nbig + i] = big_records;
+            big_records += re - rb;
         }
+        meta[3 * (uint64_t)nbig] = big_records;
     }
     // output: the survivors of the shared-memory buckets, then at most one
     // per record of the big buckets
@@ -974,12 +991,14 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     a.out_mult = g->d_out_mult;
     a.out_cap = g->out_cap;
     g->launches += swg::launch_bucket_gather(a, bk, NB, s);
-    for (unsigned i = 0; i < nbig; i++) {  // count them in a global-memory table, one after another
-        const uint64_t bb = big[i], rb = rb_of[i], re = re_of[i];
-        const uint64_t cap = (uint64_t)std::ceil((double)(re - rb) / load) + 64;
+    if (nbig) {  // all big buckets in one global-memory table (disjoint keys)
+        if ((st = ensure(&g->d_bigmeta, &g->bigmeta_cap, meta.size(), "big-bucket list"))) return st;
+        SWG_CUDA(cudaMemcpyAsync(g->d_bigmeta, meta.data(), meta.size() * 8, cudaMemcpyHostToDevice, s),
+                 "big-bucket list");
+        const uint64_t cap = (uint64_t)std::ceil((double)big_records / load) + 64;
         if ((st = ensure(&g->d_arena, &g->arena_cap, cap, "big-bucket table"))) return st;
         SWG_CUDA(cudaMemsetAsync(g->d_arena, 0, cap * sizeof(Entry), s), "clear big-bucket table");
-        g->launches += swg::launch_big_bucket(a, bk, bb, rb, re, g->d_arena, cap, s);
+        g->launches += swg::launch_big_multi(a, bk, g->d_bigmeta, nbig, big_records, g->d_arena, cap, s);
     }
     SWG_CUDA(cudaGetLastError(), "gather launch");
     SWG_CUDA(cudaMemcpyAsync(g->h_ctl, g->d_ctl, sizeof(Control) - sizeof(uint64_t),
@@ -1121,6 +1140,7 @@ void swg_graph_free(swg_graph *g) {
     cudaFree(g->d_out2_keys);
     cudaFree(g->d_out2_mult);
     cudaFree(g->d_seg_cursor);
+    cudaFree(g->d_bigmeta);
     cudaFree(g->d_hll_seg);
     cudaFree(g->d_bucket);
     cudaFree(g->d_poff);

@@ -754,7 +754,7 @@ __device__ __forceinline__ uint64_t slice_cap_of(const PartArgs &pa, unsigned lo
 // order, and per partition its count, local offset and global run base.
 size_t p1_scatter_smem(uint32_t n_parts, int round) {
     return (size_t)round * (sizeof(unsigned long long) + sizeof(unsigned short)) +
-           (size_t)n_parts * (sizeof(unsigned long long) + 2 * sizeof(unsigned));
+           (size_t)n_parts * (sizeof(unsigned long long) + 3 * sizeof(unsigned));
 }
 
 // One read per thread, rolled base by base: the state of one read's walk.
@@ -863,6 +863,77 @@ __global__ void __launch_bounds__(256) k_p1_count(BuildArgs a, PartArgs pa) {
         if (hist[j]) atomicAdd(&pa.part_count[j], (unsigned long long)hist[j]);
 }
 
+// Sampled sizes: every stride-th batch of reads, each record counted in its
+// level-1 partition (shared histogram, flushed to part_count) and its bucket
+// (cursor2, as a histogram). Reads are sampled whole, so a hot key weighs in
+// with all its occurrences in the sampled reads.
+__global__ void __launch_bounds__(256) k_p1_sample(BuildArgs a, PartArgs pa, BucketArgs b, uint32_t stride) {
+    __shared__ unsigned hist[1 << kPartBitsMax];
+    __shared__ unsigned long long s_base;
+    for (uint32_t j = threadIdx.x; j < pa.n_parts; j += blockDim.x) hist[j] = 0;
+    const int shift = 64 - pa.bits, bshift = 64 - b.b1 - b.b2;
+    for (;;) {
+        if (threadIdx.x == 0)
+            s_base = atomicAdd(&pa.work[0], 1ull) * (unsigned long long)blockDim.x * stride;
+        __syncthreads();
+        const uint64_t base = s_base;
+        if (base >= a.n_reads) break;
+        __syncthreads();  // s_base read by all
+        const uint64_t r = base + threadIdx.x;
+        if (r < a.n_reads) {
+            ReadWalk st;
+            walk_init(a, st, r);
+            while (st.left) {
+                uint64_t key;
+                unsigned code;
+                walk_emit(a, st, key, code);
+                const uint64_t h = mix64(key);
+                atomicAdd(&hist[h >> shift], 1u);
+                atomicAdd(&b.cursor2[h >> bshift], 1ull);
+            }
+        }
+    }
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < pa.n_parts; j += blockDim.x)
+        if (hist[j]) atomicAdd(&pa.part_count[j], (unsigned long long)hist[j]);
+}
+
+// Partition regions from the sampled counts: 1.25 x the partition's share of
+// the n_rec records + 4096, laid out by exclusive prefix (one block); the
+// sampled total goes to *sampled. Sum of regions <= 1.25 n_rec + 4097 P.
+__global__ void __launch_bounds__(1024) k_part_caps(PartArgs pa, uint64_t n_rec, unsigned long long *sampled) {
+    __shared__ uint64_t wb[32];
+    const uint32_t j = threadIdx.x;
+    const uint64_t c = j < pa.n_parts ? pa.part_count[j] : 0;
+    uint64_t total;
+    block_exclusive_scan<1024>(c, wb, &total);
+    uint64_t cap = 0;
+    if (j < pa.n_parts) {
+        const double share = total ? (double)c / (double)total : 1.0 / (double)pa.n_parts;
+        cap = (uint64_t)(share * (double)n_rec * 1.25) + 4096;
+    }
+    uint64_t all;
+    const uint64_t ex = block_exclusive_scan<1024>(cap, wb, &all);
+    if (j < pa.n_parts) {
+        pa.part_start[j] = ex;
+        pa.part_cursor[j] = ex;
+    }
+    if (j == 0) {
+        pa.part_start[pa.n_parts] = all;
+        *sampled = total;
+    }
+}
+
+// Bucket regions from the sampled counts (counts): 1.5 x the bucket's share
+// of the records + 256, into caps (scanned afterwards). Sum <= 1.5 n_rec + 257 nb.
+__global__ void k_bucket_caps(const unsigned long long *counts, const unsigned long long *sampled,
+                              uint64_t n_rec, uint64_t nb, unsigned long long *caps) {
+    const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nb) return;
+    const uint64_t t = *sampled;
+    const double share = t ? (double)counts[j] / (double)t : 1.0 / (double)nb;
+    caps[j] = (uint64_t)(share * (double)n_rec * 1.5) + 256;
+}
 // Level-1 scatter, one thread per read: every round each thread emits up to
 // kK1Items records of its read into registers, taking its rank within the
 // partition from the shared histogram; the block orders the round's records
@@ -874,7 +945,8 @@ __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs p
     unsigned long long *gbase = sorted + NT * IT;
     unsigned *hist = reinterpret_cast<unsigned *>(gbase + pa.n_parts);
     unsigned *loff = hist + pa.n_parts;
-    unsigned short *spart = reinterpret_cast<unsigned short *>(loff + pa.n_parts);
+    unsigned *fit = loff + pa.n_parts;  // records of the run that fit the partition's region
+    unsigned short *spart = reinterpret_cast<unsigned short *>(fit + pa.n_parts);
     __shared__ uint64_t wb[NT / 32];
     const int shift = 64 - pa.bits;
     const uint32_t per = (pa.n_parts + blockDim.x - 1) / blockDim.x;
@@ -921,7 +993,15 @@ __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs p
                     const unsigned c = hist[j];
                     loff[j] = (unsigned)run;
                     run += c;
-                    gbase[j] = c ? atomicAdd(&pa.part_cursor[j], (unsigned long long)c) : 0;
+                    unsigned long long g0 = 0;
+                    unsigned f = 0;
+                    if (c) {
+                        g0 = atomicAdd(&pa.part_cursor[j], (unsigned long long)c);
+                        const unsigned long long lim = pa.part_start[j + 1];  // region end
+                        f = g0 + c <= lim ? c : (g0 < lim ? (unsigned)(lim - g0) : 0u);
+                    }
+                    gbase[j] = g0;
+                    fit[j] = f;
                 }
             }
             __syncthreads();
@@ -937,21 +1017,14 @@ __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs p
             __syncthreads();
             for (uint32_t j = threadIdx.x; j < (uint32_t)total; j += blockDim.x) {
                 const unsigned part = spart[j];
-                const uint64_t dst = gbase[part] + (j - loff[part]);
-                // fixed-capacity regions: records past the region are dropped
-                // (the overflow is flagged after the scatter)
-                if (!pa.fixed_cap || dst < (uint64_t)(part + 1) * pa.fixed_cap) pa.records[dst] = sorted[j];
+                // records past the partition's region are dropped (the overflow
+                // is flagged after the scatter and the build recounts)
+                if (j - loff[part] < fit[part]) pa.records[gbase[part] + (j - loff[part])] = sorted[j];
             }
         }
     }
 }
 
-// Fixed-capacity partition regions: partition p starts at p * fixed_cap.
-__global__ void k_part_init(PartArgs pa) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j <= pa.n_parts) pa.part_start[j] = (unsigned long long)j * pa.fixed_cap;
-    if (j < pa.n_parts) pa.part_cursor[j] = (unsigned long long)j * pa.fixed_cap;
-}
 
 // Exclusive prefix over the partitions (n_parts <= 1024, one block).
 __global__ void __launch_bounds__(1024) k_part_prefix(PartArgs pa) {
@@ -1092,25 +1165,14 @@ __device__ __forceinline__ uint32_t sub_of(const BucketArgs &b, unsigned long lo
     return b.b2 ? (uint32_t)((rec >> 8) >> (64 - b.b1 - b.b2)) : 0u;
 }
 
-// Record range [rb, re) of bucket bk: counted buckets from the offsets,
-// fixed-capacity buckets from their region and final cursor.
+// Record range [rb, re) of bucket bk: its region starts at off2[bk]; the
+// records end at its cursor, clamped to the region (off2[bk+1]).
 __device__ __forceinline__ void bucket_range(const BucketArgs &b, uint64_t bk, uint64_t &rb, uint64_t &re) {
-    if (b.cap2) {
-        rb = bk * b.cap2;
-        re = umin64(b.cursor2[bk], rb + b.cap2);
-    } else {
-        rb = b.off2[bk];
-        re = b.off2[bk + 1];
-    }
+    rb = b.off2[bk];
+    re = umin64(b.cursor2[bk], b.off2[bk + 1]);
 }
 
-// Fixed-capacity bucket regions: bucket j starts at j * cap2.
-__global__ void k_bucket_init(BucketArgs b, uint64_t n_buckets) {
-    const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < n_buckets) b.cursor2[j] = j * b.cap2;
-}
-
-// End of every partition's records (its cursor, clamped to a fixed-capacity
+// End of every partition's records (its cursor, clamped to the partition's
 // region, flagging an overflow) and the chunks per partition as an exclusive
 // prefix (one block).
 __global__ void __launch_bounds__(1024) k_chunk_prefix(BucketArgs b) {
@@ -1119,9 +1181,9 @@ __global__ void __launch_bounds__(1024) k_chunk_prefix(BucketArgs b) {
     uint64_t c = 0;
     if (j < b.n_parts) {
         uint64_t end = b.part_cursor[j];
-        if (b.fixed_cap && end > b.part_start[j] + b.fixed_cap) {
+        if (end > b.part_start[j + 1]) {  // the partition outgrew its region
             atomicOr(b.status, kStatusPartOverflow);
-            end = b.part_start[j] + b.fixed_cap;
+            end = b.part_start[j + 1];
         }
         b.part_end[j] = end;
         c = (end - b.part_start[j] + kBkChunk - 1) / kBkChunk;
@@ -1171,7 +1233,7 @@ __global__ void __launch_bounds__(256) k_sub_hist(BucketArgs b) {
 // Level-2 scatter: a chunk is held in registers, ordered by sub-bucket in
 // shared memory and written as one run per sub-bucket.
 constexpr size_t kSubScatterDyn = kBkChunk * sizeof(unsigned long long) +
-                                  kBkBinsMax * (2 * sizeof(unsigned) + sizeof(unsigned long long));
+                                  kBkBinsMax * (3 * sizeof(unsigned) + sizeof(unsigned long long));
 
 template <int NT, int IT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) k_sub_scatter(BucketArgs b) {
@@ -1180,10 +1242,11 @@ __global__ void __launch_bounds__(NT, MINB) k_sub_scatter(BucketArgs b) {
     unsigned long long *gbase = sorted + kBkChunk;
     unsigned *hist = reinterpret_cast<unsigned *>(gbase + kBkBinsMax);
     unsigned *loff = hist + kBkBinsMax;
+    unsigned *fit = loff + kBkBinsMax;  // records of the run that fit the bucket's region
     __shared__ uint64_t wb[NT / 32];
     const uint32_t P2 = 1u << b.b2;
     const uint32_t per = (P2 + NT - 1) / NT;  // bins per thread in the scan
-    const uint64_t nq = b.chunk_start[b.n_parts];
+    const uint64_t nq = *b.status & kStatusPartOverflow ? 0 : b.chunk_start[b.n_parts];  // recount ahead
     for (uint64_t q = blockIdx.x; q < nq; q += gridDim.x) {
         uint64_t r0, r1;
         const uint32_t p = chunk_range(b, q, r0, r1);
@@ -1212,7 +1275,16 @@ __global__ void __launch_bounds__(NT, MINB) k_sub_scatter(BucketArgs b) {
                 const unsigned c = hist[j];
                 loff[j] = (unsigned)run;
                 run += c;
-                gbase[j] = c ? atomicAdd(&b.cursor2[(uint64_t)p * P2 + j], (unsigned long long)c) : 0;
+                unsigned long long g0 = 0;
+                unsigned f = 0;
+                if (c) {
+                    const uint64_t bkj = (uint64_t)p * P2 + j;
+                    g0 = atomicAdd(&b.cursor2[bkj], (unsigned long long)c);
+                    const unsigned long long lim = b.off2[bkj + 1];  // region end
+                    f = g0 + c <= lim ? c : (g0 < lim ? (unsigned)(lim - g0) : 0u);
+                }
+                gbase[j] = g0;
+                fit[j] = f;
                 hist[j] = 0;
             }
         }
@@ -1226,14 +1298,12 @@ __global__ void __launch_bounds__(NT, MINB) k_sub_scatter(BucketArgs b) {
         }
         __syncthreads();
         const uint32_t n = (uint32_t)(r1 - r0);
-        const uint64_t bk0 = (uint64_t)p * P2;
         for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
             const unsigned long long w = sorted[j];
             const uint32_t bn = sub_of(b, w);
-            const uint64_t dst = gbase[bn] + (j - loff[bn]);
-            // fixed-capacity buckets: records past the region are dropped (the
-            // overflow is flagged by the bucket count)
-            if (!b.cap2 || dst < (bk0 + bn + 1) * b.cap2) b.rec2[dst] = w;
+            // records past the bucket's region are dropped (the overflow is
+            // flagged by the bucket count and the build recounts)
+            if (j - loff[bn] < fit[bn]) b.rec2[gbase[bn] + (j - loff[bn])] = w;
         }
     }
 }
@@ -1298,7 +1368,7 @@ __global__ void __launch_bounds__(256, 2) k_sub_scatter_tma(BucketArgs b) {
     __shared__ uint64_t wb[NT / 32];
     const uint32_t P2 = 1u << b.b2;
     const uint32_t per = (P2 + NT - 1) / NT;  // bins per thread in the scan
-    const uint64_t nq = b.chunk_start[b.n_parts];
+    const uint64_t nq = *b.status & kStatusPartOverflow ? 0 : b.chunk_start[b.n_parts];  // recount ahead
     const uint64_t stride = gridDim.x;
     auto issue = [&](uint64_t q, int k) {
         uint64_t r0, r1;
@@ -1373,9 +1443,9 @@ __global__ void __launch_bounds__(256, 2) k_sub_scatter_tma(BucketArgs b) {
             const unsigned long long w = cur[j];
             const uint32_t bn = sub_of(b, w);
             const uint64_t dst = gbase[bn] + (j - loff[bn]);
-            // fixed-capacity buckets: records past the region are dropped (the
-            // overflow is flagged by the bucket count)
-            if (!b.cap2 || dst < (bk0 + bn + 1) * b.cap2) b.rec2[dst] = w;
+            // records past the bucket's region are dropped (the overflow is
+            // flagged by the bucket count and the build recounts)
+            if (dst < b.off2[bk0 + bn + 1]) b.rec2[dst] = w;
         }
         __syncthreads();  // the buffer is read out
         if (threadIdx.x == 0 && q + 2 * stride < nq) {
@@ -1502,7 +1572,7 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
         uint64_t rb, re;
         bucket_range(b, bk, rb, re);
         const uint64_t nrec = re - rb;
-        if (b.cap2 && threadIdx.x == 0 && b.cursor2[bk] > re) atomicOr(b.status, kStatusPartOverflow);
+        if (threadIdx.x == 0 && b.cursor2[bk] > re) atomicOr(b.status, kStatusPartOverflow);
         __syncthreads();  // the previous bucket's compaction (and the clear) is done
         if (threadIdx.x == 0) {
             s_over = 0;
@@ -1657,6 +1727,7 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
 // Tier 1: tables of up to kBkTable entries, two persistent CTAs per SM over
 // all buckets; overflow to the big list.
 __global__ void __launch_bounds__(kBkThreads, 2) k_bucket_count(BuildArgs a, BucketArgs b, uint64_t n_buckets) {
+    if (*b.status & kStatusPartOverflow) return;  // a partition overflowed: the build recounts
     bucket_pass<kBkTable, kBkThreads>(a, b, n_buckets, nullptr, b.big, b.big_count, b.big_cap);
 }
 
@@ -1664,6 +1735,7 @@ __global__ void __launch_bounds__(kBkThreads, 2) k_bucket_count(BuildArgs a, Buc
 // tables of up to kBkTable2 entries; overflow to the second list (counted in
 // a global-memory table by the host-driven path).
 __global__ void __launch_bounds__(kBkThreads2, 1) k_bucket_count_large(BuildArgs a, BucketArgs b) {
+    if (*b.status & kStatusPartOverflow) return;
     const unsigned n = umin64(*b.big_count, b.big_cap);
     bucket_pass<kBkTable2, kBkThreads2>(a, b, n, b.big, b.big2, b.big2_count, b.big_cap);
 }
@@ -1687,19 +1759,29 @@ __global__ void __launch_bounds__(256) k_bucket_gather(BuildArgs a, BucketArgs b
     }
 }
 
-// Buckets too large for shared memory: count in a global-memory table.
-__global__ void __launch_bounds__(kK1Block) k_big_insert(BuildArgs a, uint64_t hp, const unsigned long long *rec2,
-                                                         uint64_t rb, uint64_t re, Entry *table,
-                                                         uint64_t cap) {
+
+// All buckets no shared-memory table held, in one global-memory table (their
+// keys are disjoint): meta = rb [n] | hash prefix [n] | record prefix [n+1].
+__global__ void __launch_bounds__(kK1Block) k_big_insert_multi(BuildArgs a, const unsigned long long *rec2,
+                                                               const unsigned long long *meta, uint32_t n,
+                                                               Entry *table, uint64_t cap) {
     const int lane = threadIdx.x & 31;
+    const unsigned long long *rbs = meta, *hps = meta + n, *pre = meta + 2 * n;
+    const uint64_t total = pre[n];
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t base = rb + (uint64_t)blockIdx.x * blockDim.x; base < re; base += stride) {
-        const uint64_t r = base + threadIdx.x;
-        const bool valid = r < re;
+    for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < total; base += stride) {
+        const uint64_t i = base + threadIdx.x;
+        const bool valid = i < total;
         const unsigned vmask = __ballot_sync(kFull, valid);
         if (!valid) continue;
-        const unsigned long long rec = rec2[r];
-        const uint64_t h = hp | (rec >> 8);
+        uint32_t lo = 0, hi = n;  // last bucket j with pre[j] <= i
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (pre[mid] <= i) lo = mid;
+            else hi = mid;
+        }
+        const unsigned long long rec = rec2[rbs[lo] + (i - pre[lo])];
+        const uint64_t h = hps[lo] | (rec >> 8);
         uint64_t inc = code_inc((unsigned)rec & 0xffu);
         const unsigned peers = __match_any_sync(vmask, h);
         if (__any_sync(vmask, peers != (1u << lane))) {
@@ -1962,10 +2044,6 @@ int launch_part_count(const BuildArgs &a, const PartArgs &p, cudaStream_t s) {
     return 1;
 }
 
-int launch_part_init(const PartArgs &p, cudaStream_t s) {
-    k_part_init<<<(p.n_parts + 256) / 256, 256, 0, s>>>(p);
-    return 1;
-}
 
 int launch_part_prefix(const PartArgs &p, cudaStream_t s) {
     k_part_prefix<<<1, 1024, 0, s>>>(p);
@@ -2074,11 +2152,6 @@ int launch_bucket_count(const BuildArgs &a, const BucketArgs &b, cudaStream_t s)
     return 2;
 }
 
-int launch_bucket_init(const BucketArgs &b, uint64_t n_buckets, cudaStream_t s) {
-    if (!n_buckets) return 0;
-    k_bucket_init<<<(unsigned)((n_buckets + 255) / 256), 256, 0, s>>>(b, n_buckets);
-    return 1;
-}
 
 int launch_group_by_sample(const unsigned long long *in_keys, const unsigned long long *in_mult,
                            uint64_t n, int tag_bits, uint32_t n_samples, unsigned long long *cursor,
@@ -2096,17 +2169,38 @@ int launch_bucket_gather(const BuildArgs &a, const BucketArgs &b, uint64_t n_buc
     return 1;
 }
 
-int launch_big_bucket(const BuildArgs &a, const BucketArgs &b, uint64_t bucket, uint64_t rb,
-                      uint64_t re, Entry *table, uint64_t cap, cudaStream_t s) {
-    const uint64_t hp = (uint64_t)(bucket >> b.b2) << (64 - b.b1);
-    const uint64_t blocks = std::min<uint64_t>((re - rb + kK1Block - 1) / kK1Block,
-                                               (uint64_t)device_sm_count() * 8);
-    k_big_insert<<<(unsigned)std::max<uint64_t>(blocks, 1), kK1Block, 0, s>>>(a, hp, b.rec2, rb, re,
-                                                                              table, cap);
+int launch_p1_sample(const BuildArgs &a, const PartArgs &p, const BucketArgs &b, uint32_t stride,
+                     cudaStream_t s) {
+    if (a.total_occ == 0 || a.n_reads == 0) return 0;
+    const uint64_t batches = (a.n_reads + 255) / 256;
+    const uint64_t grid = std::min<uint64_t>((batches + stride - 1) / stride, resident_grid(k_p1_sample, 256, 0));
+    k_p1_sample<<<(unsigned)std::max<uint64_t>(grid, 1), 256, 0, s>>>(a, p, b, stride);
+    return 1;
+}
+
+int launch_part_caps(const PartArgs &p, uint64_t n_rec, unsigned long long *sampled, cudaStream_t s) {
+    k_part_caps<<<1, 1024, 0, s>>>(p, n_rec, sampled);
+    return 1;
+}
+
+int launch_bucket_caps(const unsigned long long *counts, const unsigned long long *sampled, uint64_t n_rec,
+                       uint64_t nb, unsigned long long *caps, cudaStream_t s) {
+    k_bucket_caps<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(counts, sampled, n_rec, nb, caps);
+    return 1;
+}
+
+int launch_big_multi(const BuildArgs &a, const BucketArgs &b, const unsigned long long *meta, uint32_t n,
+                     uint64_t records, Entry *table, uint64_t cap, cudaStream_t s) {
+    if (!n) return 0;
+    const uint64_t blocks =
+        std::min<uint64_t>((records + kK1Block - 1) / kK1Block, (uint64_t)device_sm_count() * 8);
+    k_big_insert_multi<<<(unsigned)std::max<uint64_t>(blocks, 1), kK1Block, 0, s>>>(a, b.rec2, meta, n, table,
+                                                                                     cap);
     const uint64_t per = (uint64_t)kCBlock * kCItems;
     k_big_compact<<<(unsigned)((cap + per - 1) / per), kCBlock, 0, s>>>(a, table, cap);
     return 2;
 }
+
 
 cudaError_t run_probe(int kind, uint64_t table_bytes, uint64_t n_ops, cudaStream_t s, float *ms) {
     Entry *table = nullptr;

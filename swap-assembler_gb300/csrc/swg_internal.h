@@ -23,7 +23,7 @@ struct __align__(16) Entry {
 enum : unsigned {
     kStatusTableFull = 1u,  // probe limit reached or table nearly full
     kStatusCasLimit = 2u,   // a bounded CAS retry loop gave up
-    kStatusPartOverflow = 4u,  // a fixed-capacity partition or bucket overflowed (bucketed build)
+    kStatusPartOverflow = 4u,  // a partition or bucket outgrew its region (bucketed build)
 };
 
 constexpr int kK1Block = 256;
@@ -93,7 +93,6 @@ struct PartArgs {
     uint64_t slot_cap;
     uint32_t n_slots;
     int load_num, load_den;            // slice capacity = count * den / num + 16
-    uint64_t fixed_cap;                // bucketed: records per partition region, 0 = counted
     unsigned long long *work;          // bucketed: [2] read-batch counters (count, scatter), zeroed
 };
 
@@ -105,13 +104,11 @@ struct BucketArgs {
     const unsigned long long *part_start;  // [n_parts + 1] level-1 offsets
     const unsigned long long *part_cursor; // [n_parts] level-1 cursors after the scatter
     unsigned long long *part_end;          // [n_parts] end of each partition's records
-    uint64_t fixed_cap;                    // fixed partition capacity, 0 = counted
     unsigned *status;
     const unsigned long long *rec1;        // level-1 records
     unsigned long long *rec2;              // records grouped by bucket
-    unsigned long long *off2;              // [n_buckets + 1] bucket offsets (counted buckets)
+    unsigned long long *off2;              // [n_buckets + 1] bucket regions (region j = [off2[j], off2[j+1]))
     unsigned long long *cursor2;           // [n_buckets] scatter cursors
-    uint64_t cap2;                         // fixed bucket capacity (bucket j at j * cap2), 0 = counted
     unsigned long long *chunk_start;       // [n_parts + 1] level-2 chunks per partition, prefix
     unsigned long long *surv;              // [n_buckets] survivors per bucket
     unsigned long long *surv_off;          // [n_buckets + 1] their exclusive prefix
@@ -144,7 +141,13 @@ int launch_gather_prefix(const uint64_t *prefix, const uint64_t *idx, uint32_t n
 int launch_compact(const BuildArgs &a, cudaStream_t s);
 int launch_part_count(const BuildArgs &a, const PartArgs &p, cudaStream_t s);
 int launch_part_prefix(const PartArgs &p, cudaStream_t s);
-int launch_part_init(const PartArgs &p, cudaStream_t s);
+int launch_p1_sample(const BuildArgs &a, const PartArgs &p, const BucketArgs &b, uint32_t stride,
+                     cudaStream_t s);
+int launch_part_caps(const PartArgs &p, uint64_t n_rec, unsigned long long *sampled, cudaStream_t s);
+int launch_bucket_caps(const unsigned long long *counts, const unsigned long long *sampled, uint64_t n_rec,
+                       uint64_t nb, unsigned long long *caps, cudaStream_t s);
+int launch_big_multi(const BuildArgs &a, const BucketArgs &b, const unsigned long long *meta, uint32_t n,
+                     uint64_t records, Entry *table, uint64_t cap, cudaStream_t s);
 int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s);
 int launch_part_wave(const BuildArgs &a, const PartArgs &p, uint32_t p0, uint32_t n,
                      uint64_t rec_begin, uint64_t rec_end, cudaStream_t s);
@@ -165,14 +168,11 @@ int launch_rec_pack(const unsigned char *t, const uint64_t *nl, uint64_t n_rec, 
 int launch_chunk_prefix(const BucketArgs &b, cudaStream_t s);
 int launch_sub_hist(const BucketArgs &b, cudaStream_t s);
 int launch_sub_scatter(const BucketArgs &b, cudaStream_t s);
-int launch_bucket_init(const BucketArgs &b, uint64_t n_buckets, cudaStream_t s);
 int launch_bucket_count(const BuildArgs &a, const BucketArgs &b, cudaStream_t s);
 int launch_bucket_gather(const BuildArgs &a, const BucketArgs &b, uint64_t n_buckets, cudaStream_t s);
 int launch_group_by_sample(const unsigned long long *in_keys, const unsigned long long *in_mult,
                            uint64_t n, int tag_bits, uint32_t n_samples, unsigned long long *cursor,
                            unsigned long long *out_keys, unsigned long long *out_mult, cudaStream_t s);
-int launch_big_bucket(const BuildArgs &a, const BucketArgs &b, uint64_t bucket, uint64_t rb,
-                      uint64_t re, Entry *table, uint64_t cap, cudaStream_t s);
 cudaError_t run_probe(int kind, uint64_t table_bytes, uint64_t n_ops, cudaStream_t s, float *ms);
 int device_sm_count();
 

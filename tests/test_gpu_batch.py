@@ -97,9 +97,9 @@ def test_tagged_batch_equals_plain_builds(texts, algo):
 
 
 def test_tagged_batch_many_samples_and_overflow():
-    """300 samples (9 tag bits, k=21), one of them a single hot k-mer that
-    overflows its fixed-capacity partition: the batch reruns with exact
-    counts and every sample still equals its own plain build."""
+    """300 samples (9 tag bits, k=21), one of them a single hot k-mer whose
+    bucket no shared-memory table holds (the global-table path): every sample
+    still equals its own plain build."""
     hot = "".join(">h%d\n%s\n" % (i, "A" * 150) for i in range(3000)).encode()
     texts = [swapgb.synth_fasta(seed=500 + i, genome_len=3_000 + 97 * i, n_reads=300 + 5 * i,
                                 read_len=(75, 100, 150)[i % 3], sub_rate=0.005) for i in range(299)]
@@ -108,7 +108,7 @@ def test_tagged_batch_many_samples_and_overflow():
     g = swapgb.Graph()
     g.build_batch(swapgb.Opts(), batch)
     info = g.info()
-    assert info["algorithm"] == swapgb.ALGO_BUCKETED and info["estimate"] == 1.0, info
+    assert info["algorithm"] == swapgb.ALGO_BUCKETED and info["waves"] >= 1, info
     for i in list(range(0, 300, 23)) + [137, 299]:
         keys, mult = g.batch_copy_out(i)
         pk, pm = _plain(texts[i], 21, 2 + (i % 3))

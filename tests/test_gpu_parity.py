@@ -245,8 +245,23 @@ def test_bucketed_large_input_and_hot_buckets():
     g = gpu_build(text, 21, 2, algorithm=swapgb.ALGO_BUCKETED)
     info = g.info()
     assert info["waves"] >= 1, info  # global-memory path taken
-    assert info["estimate"] == 1.0, info  # fixed-capacity partition overflowed: exact recount
     assert_same_records(g, text, 21, 2)
+
+
+def test_bucketed_sampling_miss_recounts():
+    """Partitions and buckets are sized from every 16th batch of 256 reads; a
+    hot key that lives only in unsampled reads overflows its region, and the
+    build reruns with exact counts."""
+    text = swapgb.synth_fasta(seed=41, genome_len=6_000_000, n_reads=300_000, read_len=150,
+                              sub_rate=0.005)  # 36M occurrences: the sampled sizing
+    lines = text.split(b"\n")
+    hot = b"".join(b">hot%d\n%s\n" % (i, b"A" * 250) for i in range(250))
+    # reads 300..549: batches 1-2 of 256 reads, which the sample skips
+    text = b"\n".join(lines[:600]) + b"\n" + hot + b"\n".join(lines[600:])
+    g = gpu_build(text, 31, 2, algorithm=swapgb.ALGO_BUCKETED)
+    info = g.info()
+    assert info["estimate"] == 1.0, info  # the exact recount ran
+    assert_same_records(g, text, 31, 2)
 
 
 def test_bucketed_overflow_tiers(monkeypatch):
