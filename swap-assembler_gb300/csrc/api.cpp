@@ -1209,7 +1209,8 @@ swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *te
     const uint64_t n = len - (uint64_t)(first - text);
     SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
     cudaStream_t s = stream_of(g, o);
-    if ((st = ensure(&g->d_text, &g->text_cap, n + 16, "FASTA text"))) return st;
+    // +64: the packing kernel's aligned 16-byte loads read up to 31 bytes past a record
+    if ((st = ensure(&g->d_text, &g->text_cap, n + 64, "FASTA text"))) return st;
     SWG_CUDA(cudaMemcpyAsync(g->d_text, first, n, cudaMemcpyHostToDevice, s), "copy FASTA text");
     const uint64_t nc = swg::framing_chunks(n);
     // workspace: counts [nc] | scratch [S] | total [2] | newline positions [nl] | records x3

@@ -10,6 +10,8 @@
 // each packed word belongs to one read and is written by one thread.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "dev_util.cuh"
 #include "swg_internal.h"
 
@@ -17,36 +19,55 @@ namespace swg {
 namespace {
 
 constexpr int kFBlock = 256;
-constexpr int kFBytes = 16;
+constexpr int kFVec = 4;                                    // 16-byte loads per thread
+constexpr int kFBytes = 16 * kFVec;                         // bytes per thread
 constexpr uint64_t kFChunk = (uint64_t)kFBlock * kFBytes;  // bytes per block
 constexpr int kGItems = 8;
 constexpr uint64_t kGChunk = (uint64_t)kFBlock * kGItems;  // items per scan block
 
-__device__ __forceinline__ void load16(const unsigned char *__restrict__ t, uint64_t n, uint64_t i,
-                                       unsigned char b[kFBytes]) {
-    if (i + kFBytes <= n) {
-        const uint4 v = *reinterpret_cast<const uint4 *>(t + i);  // i is a multiple of 16
-        const unsigned w[4] = {v.x, v.y, v.z, v.w};
+// A thread's kFBytes bytes at i (a multiple of 16) as 32-bit words; bytes
+// past n read as 1 (neither a newline nor a NUL).
+__device__ __forceinline__ void load_words(const unsigned char *__restrict__ t, uint64_t n, uint64_t i,
+                                           uint32_t w[kFBytes / 4]) {
 #pragma unroll
-        for (int j = 0; j < kFBytes; ++j) b[j] = (unsigned char)(w[j >> 2] >> (8 * (j & 3)));
-    } else {
+    for (int v = 0; v < kFVec; ++v) {
+        const uint64_t a = i + 16 * (uint64_t)v;
+        if (a + 16 <= n) {
+            const uint4 x = *reinterpret_cast<const uint4 *>(t + a);
+            w[4 * v] = x.x;
+            w[4 * v + 1] = x.y;
+            w[4 * v + 2] = x.z;
+            w[4 * v + 3] = x.w;
+        } else {
 #pragma unroll
-        for (int j = 0; j < kFBytes; ++j) b[j] = i + j < n ? t[i + j] : (unsigned char)1;
+            for (int q = 0; q < 4; ++q) {
+                uint32_t x = 0;
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const uint64_t at = a + 4 * q + b;
+                    x |= (uint32_t)(at < n ? t[at] : (unsigned char)1) << (8 * b);
+                }
+                w[4 * v + q] = x;
+            }
+        }
     }
 }
+
+// 0xff in every byte of x equal to '\n'.
+__device__ __forceinline__ uint32_t nl_mask(uint32_t x) { return __vcmpeq4(x, 0x0a0a0a0au); }
 
 // Newlines per chunk; any NUL byte raises flag.
 __global__ void __launch_bounds__(kFBlock) k_nl_count(const unsigned char *__restrict__ t, uint64_t n,
                                                       uint64_t *__restrict__ counts,
                                                       unsigned *__restrict__ flag) {
     __shared__ uint64_t wb[kFBlock / 32];
-    unsigned char b[kFBytes];
-    load16(t, n, (uint64_t)blockIdx.x * kFChunk + (uint64_t)threadIdx.x * kFBytes, b);
+    uint32_t w[kFBytes / 4];
+    load_words(t, n, (uint64_t)blockIdx.x * kFChunk + (uint64_t)threadIdx.x * kFBytes, w);
     unsigned c = 0, z = 0;
 #pragma unroll
-    for (int j = 0; j < kFBytes; ++j) {
-        c += b[j] == '\n';
-        z |= b[j] == 0;
+    for (int q = 0; q < kFBytes / 4; ++q) {
+        c += __popc(nl_mask(w[q])) >> 3;
+        z |= __vcmpeq4(w[q], 0u);
     }
     uint64_t total;
     block_exclusive_scan<kFBlock>(c, wb, &total);
@@ -60,15 +81,21 @@ __global__ void __launch_bounds__(kFBlock) k_nl_pos(const unsigned char *__restr
                                                     uint64_t *__restrict__ nl) {
     __shared__ uint64_t wb[kFBlock / 32];
     const uint64_t base = (uint64_t)blockIdx.x * kFChunk + (uint64_t)threadIdx.x * kFBytes;
-    unsigned char b[kFBytes];
-    load16(t, n, base, b);
+    uint32_t w[kFBytes / 4];
+    load_words(t, n, base, w);
     unsigned c = 0;
 #pragma unroll
-    for (int j = 0; j < kFBytes; ++j) c += b[j] == '\n';
+    for (int q = 0; q < kFBytes / 4; ++q) c += __popc(nl_mask(w[q])) >> 3;
     uint64_t pos = chunk_base[blockIdx.x] + block_exclusive_scan<kFBlock>(c, wb, nullptr);
 #pragma unroll
-    for (int j = 0; j < kFBytes; ++j)
-        if (b[j] == '\n') nl[pos++] = base + j;
+    for (int q = 0; q < kFBytes / 4; ++q) {
+        uint32_t m = nl_mask(w[q]);
+        while (m) {
+            const int bit = __ffs(m) - 1;  // lowest set byte: bits bit..bit+7
+            nl[pos++] = base + 4 * q + (bit >> 3);
+            m &= ~(0xffu << bit);
+        }
+    }
 }
 
 // Generic exclusive scan of uint64 (in place allowed).
@@ -146,31 +173,91 @@ __device__ __forceinline__ uint32_t code_of(unsigned char ch) {
     }
 }
 
-// One warp per record: kept reads get their offset/length and packed words.
-__global__ void k_rec_pack(const unsigned char *__restrict__ t, const uint64_t *__restrict__ nl,
-                           uint64_t n_rec, int k, const uint64_t *__restrict__ read_idx,
-                           const uint64_t *__restrict__ word_off, uint64_t *__restrict__ off,
-                           uint32_t *__restrict__ len, uint32_t *__restrict__ packed) {
-    const uint64_t r = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (r >= n_rec) return;
-    const uint64_t start = nl[2 * r] + 1, end = nl[2 * r + 1];
-    const uint64_t L = end - start;
-    if (L < (uint64_t)k) return;
-    const uint64_t w0 = word_off[r];
-    if (lane == 0) {
-        const uint64_t ri = read_idx[r];
-        off[ri] = w0 * 16;
-        len[ri] = (uint32_t)L;
-    }
-    const uint64_t nw = (L + 15) / 16;
-    for (uint64_t w = lane; w < nw; w += 32) {
-        uint32_t word = 0;
-        const uint64_t p = start + w * 16;
+// Kept reads get their offset/length and packed words. A warp takes 32
+// records at a time: each lane loads one record's newline positions, packed
+// offset and read index (coalesced), a warp scan lays the 32 records' packed
+// words out, and the lanes then build those words round-robin — every lane
+// busy, each on the record its word falls in (binary search over the 33
+// prefixes). A word (16 bases, first base in the top bits) comes from two
+// aligned 16-byte loads of the text shifted by the record's alignment, every
+// byte mapped through a 256-entry table. The text buffer has 64 bytes of
+// slack past its end.
+__global__ void __launch_bounds__(256) k_rec_pack(const unsigned char *__restrict__ t,
+                                                  const uint64_t *__restrict__ nl, uint64_t n_rec, int k,
+                                                  const uint64_t *__restrict__ read_idx,
+                                                  const uint64_t *__restrict__ word_off,
+                                                  uint64_t *__restrict__ off, uint32_t *__restrict__ len,
+                                                  uint32_t *__restrict__ packed) {
+    __shared__ unsigned char lut[256];
+    __shared__ uint32_t s_pre[8][33];
+    __shared__ uint64_t s_start[8][32], s_w0[8][32];
+    __shared__ uint32_t s_len[8][32];
+    lut[threadIdx.x] = (unsigned char)code_of((unsigned char)threadIdx.x);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t g0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; g0 < n_rec;
+         g0 += nwarps * 32) {
+        const uint64_t r = g0 + lane;
+        uint64_t my_start = 0, my_w0 = 0;
+        uint32_t my_len = 0, my_nw = 0;
+        if (r < n_rec) {
+            my_start = nl[2 * r] + 1;
+            const uint64_t L = nl[2 * r + 1] - my_start;
+            if (L >= (uint64_t)k) {
+                my_len = (uint32_t)L;
+                my_nw = (uint32_t)((L + 15) / 16);
+                my_w0 = word_off[r];
+                const uint64_t ri = read_idx[r];
+                off[ri] = my_w0 * 16;
+                len[ri] = my_len;
+            }
+        }
+        uint32_t inc = my_nw;  // inclusive warp scan of the word counts
 #pragma unroll
-        for (int j = 0; j < 16; ++j)
-            if (p + j < end) word |= code_of(t[p + j]) << (30 - 2 * j);
-        packed[w0 + w] = word;
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, d);
+            if (lane >= d) inc += y;
+        }
+        s_pre[wp][lane] = inc - my_nw;
+        if (lane == 31) s_pre[wp][32] = inc;
+        s_start[wp][lane] = my_start;
+        s_w0[wp][lane] = my_w0;
+        s_len[wp][lane] = my_len;
+        __syncwarp();
+        const uint32_t T = s_pre[wp][32];
+        for (uint32_t tw = lane; tw < T; tw += 32) {
+            uint32_t lo = 0, hi = 32;  // last record j with s_pre[j] <= tw
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (s_pre[wp][mid] <= tw) lo = mid;
+                else hi = mid;
+            }
+            const uint64_t start = s_start[wp][lo];
+            const uint32_t w = tw - s_pre[wp][lo];
+            const uint32_t q = (uint32_t)(start & 15) >> 2, sh = 8 * (uint32_t)(start & 3);
+            const uint4 *a16 = reinterpret_cast<const uint4 *>(t + (start & ~15ull));
+            const uint4 a = a16[w], b = a16[w + 1];
+            const uint32_t win[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+            uint32_t sel[5];  // win[q .. q+4], selected without divergence
+#pragma unroll
+            for (int i = 0; i < 5; ++i)
+                sel[i] = q == 0 ? win[i] : (q == 1 ? win[i + 1] : (q == 2 ? win[i + 2] : win[i + 3]));
+            const uint32_t left = s_len[wp][lo] - 16 * w;  // bases of the read from this word on
+            uint32_t word = 0;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const uint32_t x = __funnelshift_r(sel[i], sel[i + 1], sh);
+#pragma unroll
+                for (int bb = 0; bb < 4; ++bb) {
+                    const int jj = 4 * i + bb;
+                    const uint32_t c = (uint32_t)jj < left ? (uint32_t)lut[(x >> (8 * bb)) & 0xffu] : 0u;
+                    word |= c << (30 - 2 * jj);
+                }
+            }
+            packed[s_w0[wp][lo] + w] = word;
+        }
+        __syncwarp();
     }
 }
 
@@ -220,9 +307,11 @@ int launch_rec_pack(const unsigned char *t, const uint64_t *nl, uint64_t n_rec, 
                     const uint64_t *read_idx, const uint64_t *word_off, uint64_t *off,
                     uint32_t *len, uint32_t *packed, cudaStream_t s) {
     if (!n_rec) return 0;
-    const uint64_t threads = n_rec * 32;
-    k_rec_pack<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(t, nl, n_rec, k, read_idx,
-                                                                 word_off, off, len, packed);
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint64_t blocks = std::min<uint64_t>((n_rec + 255) / 256, (uint64_t)std::max(sms, 1) * 16);
+    k_rec_pack<<<(unsigned)blocks, 256, 0, s>>>(t, nl, n_rec, k, read_idx, word_off, off, len, packed);
     return 1;
 }
 
