@@ -1365,22 +1365,30 @@ swg_status swg_graph_stats(const swg_graph *g, int64_t out[5]) {
     return SWG_OK;
 }
 
+// Both text outputs are formatted on the device (emit.cu) from the
+// device-resident records and streamed to the file.
+static swg_status writable(const swg_graph *g) {
+    if (!g->built || g->n_samples) {
+        swg::set_error(g->n_samples ? "batched build: use the swg_batch_* calls" : "graph has not been built");
+        return SWG_ERR_BAD_STATE;
+    }
+    return SWG_OK;
+}
+
 swg_status swg_graph_write_kmer_graph(const swg_graph *g, const char *path) {
     if (!g || !path) return SWG_ERR_BAD_INPUT;
-    std::vector<uint64_t> k, m;
-    swg_status st = fetch_sorted(g, k, m);
+    swg_status st = writable(g);
     if (st) return st;
-    return swg::write_kmer_graph(k.data(), reinterpret_cast<const uint8_t *>(m.data()), g->n_out,
-                                 g->k, path);
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    return swg::emit_kmer_graph(g->d_out_keys, g->d_out_mult, g->n_out, g->k, path, g->own);
 }
 
 swg_status swg_graph_write_node_lines(const swg_graph *g, const char *path) {
     if (!g || !path) return SWG_ERR_BAD_INPUT;
-    std::vector<uint64_t> k, m;
-    swg_status st = fetch_sorted(g, k, m);
+    swg_status st = writable(g);
     if (st) return st;
-    return swg::write_node_lines(k.data(), reinterpret_cast<const uint8_t *>(m.data()), g->n_out,
-                                 path);
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    return swg::emit_node_lines(g->d_out_keys, g->d_out_mult, g->n_out, g->k, path, g->own);
 }
 
 static swg_status sorted_copy(const uint64_t *keys, const uint8_t *mult, uint64_t n,

@@ -190,6 +190,12 @@ swg_status write_node_lines(const uint64_t *keys, const uint8_t *mult, uint64_t 
 void graph_stats(const uint8_t *mult, uint64_t n, int k, int64_t out[5]);
 void sort_records(uint64_t *keys, uint64_t *mult8, uint64_t n);
 uint64_t revcomp_host(uint64_t x, int k);
+// Device emission of the text outputs (emit.cu), byte-identical with the host
+// writers: records on the device, any order.
+swg_status emit_node_lines(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n,
+                           int k, const char *path, cudaStream_t s);
+swg_status emit_kmer_graph(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n, int k,
+                           const char *path, cudaStream_t s);
 uint64_t kmer_graph_neighbour(uint64_t key, int slot, int k);
 
 }  // namespace swg

@@ -283,3 +283,20 @@ def test_bucketed_overflow_tiers(monkeypatch):
     info = g.info()
     assert info["waves"] >= 1, info
     assert_same_records(g, text, 27, 1)
+
+
+@pytest.mark.parametrize("k,c", [(9, 2), (20, 0), (21, 2), (31, 3)])
+def test_device_text_equals_host_writers(k, c, tmp_path):
+    """kmerGraph.txt and the node lines formatted on the device are byte-for-
+    byte the host writers' output for the same records (odd and even k: the
+    neighbour-id quirk depends on k's parity; c=0 keeps every arc)."""
+    text = swapgb.synth_fasta(seed=61 + k, genome_len=200_000, n_reads=40_000, read_len=100,
+                              sub_rate=0.01, repeat_frac=0.05, tandem_frac=0.02)
+    g = gpu_build(text, k, c)
+    g.write_kmer_graph(tmp_path / "dev_kmerGraph.txt")
+    g.write_node_lines(tmp_path / "dev_nodes.txt")
+    keys, mult = g.copy_out(sorted=False)
+    swapgb.records_write_kmer_graph(keys, mult, k, tmp_path / "host_kmerGraph.txt")
+    swapgb.records_write_node_lines(keys, mult, tmp_path / "host_nodes.txt")
+    assert (tmp_path / "dev_kmerGraph.txt").read_bytes() == (tmp_path / "host_kmerGraph.txt").read_bytes()
+    assert (tmp_path / "dev_nodes.txt").read_bytes() == (tmp_path / "host_nodes.txt").read_bytes()
