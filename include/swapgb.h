@@ -63,9 +63,9 @@ typedef enum swg_status {
 } swg_status;
 
 /* Counting algorithms (same results, different memory traffic). */
-#define SWG_ALGO_DEFAULT 0     /* bucketed when its workspace (~26 bytes per k-mer
-                                  occurrence) fits in device memory, else direct;
-                                  direct for SWG_ORDER_MINIMIZER */
+#define SWG_ALGO_DEFAULT 0     /* bucketed when its workspace (at most 40 bytes per
+                                  k-mer occurrence) fits in device memory, else
+                                  direct; direct for SWG_ORDER_MINIMIZER */
 #define SWG_ALGO_DIRECT 1      /* one pass into a device-wide table in HBM */
 #define SWG_ALGO_PARTITIONED 2 /* hash-partitioned records, each partition counted in L2 */
 #define SWG_ALGO_BUCKETED 3    /* records split into buckets counted in shared memory */
@@ -102,8 +102,8 @@ typedef struct swg_build_info {
     uint32_t retries;     /* direct: rebuilds after a full table; bucketed: buckets
                              recounted in the larger (tier-2) shared-memory table */
     double estimate;      /* direct: distinct-count estimate used for sizing;
-                             bucketed: 1 when a fixed-capacity partition overflowed
-                             and the build reran with exact partition counts */
+                             bucketed: 1 when a partition or bucket outgrew its
+                             sampled region and the build reran with exact counts */
     float ms[5];          /* as swg_graph_last_timings */
 } swg_build_info;
 

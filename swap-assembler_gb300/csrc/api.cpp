@@ -107,7 +107,6 @@ struct swg_graph {
     uint64_t bk_cap = 0;
     Entry *d_arena = nullptr;
     uint64_t arena_cap = 0;
-    uint32_t big_buckets = 0;
     // batched build (n_samples == 0 after a single-sample build)
     uint32_t n_samples = 0;
     std::vector<uint64_t> s_tbase, s_tcap, s_out, s_distinct, s_occ;
@@ -209,11 +208,12 @@ swg_status build_partitioned(swg_graph *g, const swg_opts *o, BuildArgs &a, cuda
 swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s,
                           double load, bool counted = false);
 
-// The default algorithm is the bucketed one while its workspace (two record
-// buffers of about 1.5 x 8 bytes per occurrence, plus the output) fits in
-// 80% of the device memory that is free or already held by this handle's
-// record buffers; otherwise the direct one, whose table grows with the
-// distinct k-molecules instead of the occurrences.
+// The default algorithm is the bucketed one while its worst-case workspace
+// (two record buffers of at most 1.5 x 8 bytes per occurrence, plus an
+// output of up to 16 bytes per occurrence) fits in 80% of the device memory
+// that is free or already held by this handle's record buffers; otherwise the
+// direct one, whose table grows with the distinct k-molecules instead of the
+// occurrences.
 bool bucketed_fits(const swg_graph *g, uint64_t occurrences) {
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
@@ -221,7 +221,7 @@ bool bucketed_fits(const swg_graph *g, uint64_t occurrences) {
         return false;
     }
     const double held = 8.0 * (double)(g->records_cap + g->rec2_cap);
-    const double need = 26.0 * (double)occurrences + (64 << 20);
+    const double need = 40.0 * (double)occurrences + (64 << 20);
     return need <= 0.8 * ((double)free_b + held);
 }
 
@@ -1014,7 +1014,6 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
         swg::set_error("a big-bucket table reached the probe limit");
         return SWG_ERR_TABLE_FULL;
     }
-    g->big_buckets = g->h_ctl->pad;
     g->retries = g->h_ctl->pad;
     g->estimate = counted ? 1.0 : 0.0;  // bucketed: 1 when the exact-count rerun was needed
     g->parts = (uint32_t)P;

@@ -67,9 +67,13 @@ struct swg_server {
 
 namespace {
 
+// Inputs + 32 B per table slot at the load factor (about 53 B per k-mer
+// occurrence at 0.6: covers the direct build's table and output and the
+// bucketed build's record buffers and output, at most 40 B per occurrence)
+// + 16 MiB for the bucketed build's fixed region slack.
 uint64_t footprint_of(uint64_t reads, uint64_t words, uint64_t occ, double load) {
     const uint64_t cap = (uint64_t)((double)occ / load) + 2048;
-    return words * 4 + reads * (8 + 4 + 8 + 4) + cap * 16 * 2;
+    return words * 4 + reads * (8 + 4 + 8 + 4) + cap * 16 * 2 + (16ull << 20);
 }
 
 void worker_main(swg_server *srv) {
