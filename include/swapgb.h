@@ -64,8 +64,9 @@ typedef enum swg_status {
 
 /* Counting algorithms (same results, different memory traffic). */
 #define SWG_ALGO_DEFAULT 0     /* bucketed when its workspace (at most 40 bytes per
-                                  k-mer occurrence) fits in device memory, else
-                                  direct; direct for SWG_ORDER_MINIMIZER */
+                                  k-mer occurrence) fits in device memory and no
+                                  read is longer than 16384 bases, else direct;
+                                  direct for SWG_ORDER_MINIMIZER */
 #define SWG_ALGO_DIRECT 1      /* one pass into a device-wide table in HBM */
 #define SWG_ALGO_PARTITIONED 2 /* hash-partitioned records, each partition counted in L2 */
 #define SWG_ALGO_BUCKETED 3    /* records split into buckets counted in shared memory */

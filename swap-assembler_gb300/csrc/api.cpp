@@ -34,6 +34,8 @@ struct Control {  // device-side control block
     unsigned pad2;                   // bucketed build: tier-2 overflow count
     unsigned pad3;
     unsigned long long work[2];      // bucketed build: read batches handed out (count, scatter)
+    unsigned max_len;                // longest read (occurrence scan)
+    unsigned pad4;
     uint64_t occ_total;              // last: the memsets of the control block stop before it
 };
 
@@ -214,6 +216,8 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
 // that is free or already held by this handle's record buffers; otherwise the
 // direct one, whose table grows with the distinct k-molecules instead of the
 // occurrences.
+constexpr unsigned kBucketedMaxRead = 16384;  // longest read the default sends to the bucketed build
+
 bool bucketed_fits(const swg_graph *g, uint64_t occurrences) {
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
@@ -268,11 +272,16 @@ swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, u
     SWG_CUDA(cudaEventRecord(g->ev[0], s), "event");
     SWG_CUDA(cudaMemsetAsync(g->d_ctl, 0, sizeof(Control), s), "memset control");
     SWG_CUDA(cudaMemsetAsync(g->d_prefix, 0, sizeof(uint64_t), s), "memset prefix");
+    a.max_len = &g->d_ctl->max_len;
     g->launches += swg::launch_occ_scan(a, s);
+    a.max_len = nullptr;
     SWG_CUDA(cudaGetLastError(), "occurrence scan launch");
     SWG_CUDA(cudaMemcpyAsync(&g->h_ctl->occ_total, g->d_prefix + n_reads, sizeof(uint64_t),
                              cudaMemcpyDeviceToHost, s),
              "read occurrence total");
+    SWG_CUDA(cudaMemcpyAsync(&g->h_ctl->max_len, &g->d_ctl->max_len, sizeof(unsigned),
+                             cudaMemcpyDeviceToHost, s),
+             "read longest read");
     SWG_CUDA(cudaStreamSynchronize(s), "occurrence scan");
     a.total_occ = g->h_ctl->occ_total;
     g->occurrences = a.total_occ;
@@ -286,7 +295,10 @@ swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, u
 
     if (o->algorithm == SWG_ALGO_PARTITIONED) return build_partitioned(g, o, a, s, load);
     if (o->algorithm == SWG_ALGO_BUCKETED) return build_bucketed(g, o, a, s, load);
-    if (o->algorithm == SWG_ALGO_DEFAULT && o->read_order == SWG_ORDER_INPUT && bucketed_fits(g, a.total_occ))
+    // the bucketed build walks one read per thread: reads of more than 16 kbp
+    // (long-read data) would leave the GPU waiting on a few threads
+    if (o->algorithm == SWG_ALGO_DEFAULT && o->read_order == SWG_ORDER_INPUT &&
+        g->h_ctl->max_len <= kBucketedMaxRead && bucketed_fits(g, a.total_occ))
         return build_bucketed(g, o, a, s, load);
     return build_direct(g, o, a, s, load);
 }

@@ -177,13 +177,22 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_reduce(BuildArgs a) {
     __shared__ uint64_t wb[kScanBlock / 32];
     const uint64_t base = (uint64_t)blockIdx.x * kScanChunk;
     uint64_t s = 0;
+    uint32_t longest = 0;
     for (int it = 0; it < kScanItems; ++it) {
         const uint64_t r = base + (uint64_t)it * kScanBlock + threadIdx.x;
-        if (r < a.n_reads) s += occ_of(a.read_len[r], k_of(a, seg_of(a, r)));
+        if (r < a.n_reads) {
+            const uint32_t L = a.read_len[r];
+            s += occ_of(L, k_of(a, seg_of(a, r)));
+            longest = max(longest, L);
+        }
     }
     uint64_t total;
     block_exclusive_scan<kScanBlock>(s, wb, &total);
     if (threadIdx.x == 0) a.scan_blocks[blockIdx.x] = total;
+    if (a.max_len) {  // the longest read, for the choice of algorithm
+        longest = __reduce_max_sync(kFull, longest);
+        if ((threadIdx.x & 31) == 0 && longest) atomicMax(a.max_len, longest);
+    }
 }
 
 __global__ void __launch_bounds__(1024) k_scan_blocks(uint64_t *block_sums, uint64_t nb,

@@ -72,6 +72,7 @@ struct BuildArgs {
     unsigned *seg_status;              // [n_segs]
     int tag_bits;                      // bucketed batch: the read's sample index sits in the
                                        // top tag_bits bits of every key (0 = no tag)
+    unsigned *max_len;                 // if set, the occurrence scan records the longest read
 };
 
 constexpr uint32_t kMaxTagSamples = 1024;  // samples of one tagged bucketed batch

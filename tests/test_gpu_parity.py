@@ -300,3 +300,18 @@ def test_device_text_equals_host_writers(k, c, tmp_path):
     swapgb.records_write_node_lines(keys, mult, tmp_path / "host_nodes.txt")
     assert (tmp_path / "dev_kmerGraph.txt").read_bytes() == (tmp_path / "host_kmerGraph.txt").read_bytes()
     assert (tmp_path / "dev_nodes.txt").read_bytes() == (tmp_path / "host_nodes.txt").read_bytes()
+
+
+def test_long_reads_take_the_direct_build():
+    """Reads longer than 16 kbp would leave the one-thread-per-read bucketed
+    walker waiting on a few threads: the default builds them directly."""
+    text = swapgb.synth_fasta(seed=71, genome_len=400_000, n_reads=60, read_len=20_000,
+                              sub_rate=0.002)
+    g = gpu_build(text, 31, 1)
+    assert g.info()["algorithm"] == swapgb.ALGO_DIRECT
+    assert_same_records(g, text, 31, 1)
+    text = swapgb.synth_fasta(seed=72, genome_len=400_000, n_reads=600, read_len=2_000,
+                              sub_rate=0.002)
+    g = gpu_build(text, 31, 1)
+    assert g.info()["algorithm"] == swapgb.ALGO_BUCKETED
+    assert_same_records(g, text, 31, 1)
