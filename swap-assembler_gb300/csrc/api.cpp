@@ -833,7 +833,7 @@ swg_status batch_impl(swg_graph *g, const swg_opts *o, const swg_sample *sm, uin
 // shared-memory hash table and compacted from there. Buckets too large for
 // shared memory (hot k-molecules) are counted in a global-memory table.
 // Bucketed build (kernels.cu, k_p1_* / k_sub_* / k_bucket_*). A sampled pass
-// (every 16th batch of reads, from 16M occurrences; uniform below) sizes
+// (every 16th batch of reads, from 64M occurrences; uniform below) sizes
 // every level-1 partition and every bucket;
 // the scatters write into those regions, so no exact count pass precedes
 // them. A partition or bucket that outgrows its region (a sampling miss) sets
@@ -850,10 +850,13 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     if (const char *e = std::getenv("SWG_PART_BITS")) b1 = std::min(10, std::max(8, std::atoi(e)));
     const uint64_t P = 1ull << b1;
     // sub-buckets of about `target` records (SWG_BUCKET_RECORDS overrides)
-    double target = 6144.0;
+    double target = 4096.0;
     if (const char *e = std::getenv("SWG_BUCKET_RECORDS")) target = std::max(64.0, std::atof(e));
     int b2 = 0;
     while (b2 < 10 && (double)N / (double)(P << b2) > target) b2++;
+    // at most 512 sub-buckets (level-2 runs of >= 8 records per 4096-record
+    // chunk) while the buckets stay under 4x the target
+    if (b2 == 10 && (double)N / (double)(P << 9) <= 4 * target) b2 = 9;
     const uint64_t NB = P << b2;
     // region bounds: partitions <= 1.25 N + 4097 P, buckets <= 1.5 N + 257 NB;
     // the level-1 buffer also stages survivor keys at bucket offsets
@@ -912,10 +915,10 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
         g->launches += swg::launch_part_prefix(pa, s);
     } else {
         SWG_CUDA(cudaMemsetAsync(bk.cursor2, 0, NB * 8, s), "clear bucket samples");
-        // from 16M occurrences every 16th batch of reads is sampled; smaller
+        // from 64M occurrences every 16th batch of reads is sampled; smaller
         // inputs get uniform regions (an empty sample), whose slack covers
-        // their spread
-        if (N >= (16ull << 20)) g->launches += swg::launch_p1_sample(a, pa, bk, 16, s);
+        // their spread (a skewed one recounts)
+        if (N >= (64ull << 20)) g->launches += swg::launch_p1_sample(a, pa, bk, 16, s);
         g->launches += swg::launch_part_caps(pa, N, sampled, s);
         // bucket regions from the same sample (surv serves as scratch)
         g->launches += swg::launch_bucket_caps(bk.cursor2, sampled, N, NB, bk.surv, s);

@@ -252,8 +252,8 @@ def test_bucketed_sampling_miss_recounts():
     """Partitions and buckets are sized from every 16th batch of 256 reads; a
     hot key that lives only in unsampled reads overflows its region, and the
     build reruns with exact counts."""
-    text = swapgb.synth_fasta(seed=41, genome_len=6_000_000, n_reads=300_000, read_len=150,
-                              sub_rate=0.005)  # 36M occurrences: the sampled sizing
+    text = swapgb.synth_fasta(seed=41, genome_len=12_000_000, n_reads=600_000, read_len=150,
+                              sub_rate=0.005)  # 72M occurrences: the sampled sizing
     lines = text.split(b"\n")
     hot = b"".join(b">hot%d\n%s\n" % (i, b"A" * 250) for i in range(250))
     # reads 300..549: batches 1-2 of 256 reads, which the sample skips
