@@ -315,3 +315,27 @@ def test_long_reads_take_the_direct_build():
     g = gpu_build(text, 31, 1)
     assert g.info()["algorithm"] == swapgb.ALGO_BUCKETED
     assert_same_records(g, text, 31, 1)
+
+
+@pytest.mark.parametrize("shape", [1, 2, 3])
+def test_scatter_shapes(shape, tmp_path):
+    """The other block shapes of the two scatters (SWG_SCATTER_SHAPE, read
+    once per process; 3 = level-2 chunks brought in by bulk copies into
+    double-buffered shared memory) give the same graph."""
+    import os
+    import subprocess
+    import sys
+    fa = tmp_path / "reads.fa"
+    swapgb.synth_fasta_file(str(fa), seed=81, genome_len=2_000_000, n_reads=400_000, read_len=100,
+                            sub_rate=0.01, repeat_frac=0.05, tandem_frac=0.02)
+    out = tmp_path / "graph.npz"
+    code = ("import sys, numpy as np; sys.path.insert(0, %r); import swapgb\n"
+            "t = open(%r, 'rb').read(); r = swapgb.reads_from_fasta(t, 31)\n"
+            "g = swapgb.Graph().build_reads(swapgb.Opts(k=31, cutoff=2, algorithm=swapgb.ALGO_BUCKETED), r)\n"
+            "k, m = g.copy_out(sorted=True); np.savez(%r, k=k, m=m)\n"
+            % (str(swapgb.PKG), str(fa), str(out)))
+    env = dict(os.environ, SWG_SCATTER_SHAPE=str(shape))
+    subprocess.run([sys.executable, "-c", code], env=env, check=True, timeout=300)
+    got = np.load(out)
+    okeys, omult = oracle.records(fa.read_bytes(), 31, 2)
+    assert np.array_equal(got["k"], okeys) and np.array_equal(got["m"], omult)
