@@ -1,11 +1,17 @@
 // C ABI of the k-mer graph builder (declared in include/swapgb.h).
 //
-// A build runs on one CUDA stream:
-//   occurrence prefix (3 launches) -> tile table -> [HyperLogLog estimate]
-//   -> table clear -> K1 extract+count -> K2 cutoff+compaction
-// with two host synchronisations (occurrence total, then the distinct-count
-// estimate) and one at the end (status, survivor count). A table that fills
-// up is detected on the device and the build is repeated with a larger table.
+// A build runs on one CUDA stream. It starts with the occurrence prefix (3
+// launches; the host reads the occurrence total and the longest read), then
+// one of:
+//   bucketed (the default): sampled region sizes -> level-1 partition scatter
+//     -> level-2 bucket scatter -> shared-memory bucket counting + cutoff ->
+//     (host reads the survivor total) -> survivor gather [-> big buckets in a
+//     global table]; a region overflow reruns it with exact counts;
+//   direct: tile table -> HyperLogLog estimate (host reads it) -> table clear
+//     -> K1 extract+count -> K2 cutoff+compaction; a table that fills up is
+//     detected on the device and the build is repeated with a larger table;
+//   partitioned: record scatter -> waves of L2-resident partition slices.
+// A last synchronisation reads the status and the survivor count.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
