@@ -19,6 +19,10 @@
  *   distNodeGraph::graphStatistics ............. graph.cpp:1569-1627 -> swg_graph_stats
  *   distNodeGraph::printKmerGraph (-s output) .. graph.cpp:3352-3440 -> swg_graph_write_kmer_graph
  *   distNodeGraph::printLocalNodeGraph ......... graph.cpp:555-572 -> swg_graph_write_node_lines
+ *   distNodeGraph::simplifyDistNodeGraph ....... graph.cpp:1392-1566 (+ recvProc 1204-1389)
+ *                                                -> swg_graph_merge
+ *   distNodeGraph::gatherDistNodeGraph, -d file  graph.cpp:576-696, 3617-3621
+ *                                                -> swg_graph_write_merged / swg_graph_copy_merged
  *
  * Packed read layout (host or device memory):
  *   packed   uint32 words; base i of the concatenated read stream sits in
@@ -260,6 +264,36 @@ swg_status swg_graph_write_kmer_graph(const swg_graph *g, const char *path);
 /* Node lines "K A# # ...# m0 .. m7" (graph.cpp:569), sorted by key; readable by
  * the reference's readDistNodeGraph (graph.cpp:898-941). */
 swg_status swg_graph_write_node_lines(const swg_graph *g, const char *path);
+/* Merging of semi-extended k-molecules over the built graph: the reference's
+ * SWAP merge (simplifyDistNodeGraph, graph.cpp:1392-1566, edge messages
+ * graph.cpp:1289-1345). Every node with exactly one arc on each side that does
+ * not lead back to itself is merged into its neighbours; the remaining nodes'
+ * arcs then spell whole chains up to the next remaining node. Arc strings are
+ * those of any complete merge order; a merged arc's multiplicity is the
+ * reference's running weighted average (graph.cpp:1322-1324, including its
+ * int truncation) taken in one fixed visiting order: a chain of m merged
+ * nodes numbered 1..m from its smaller end arc (key, then slot), node p at
+ * level ctz(p), levels in increasing order. A cycle of merged nodes is cut at
+ * its largest key, which keeps the cycle on its two arcs. The result stays on
+ * the device (as the -d file's text) until the next build. SWG_ERR_BAD_STATE
+ * without a single-sample build; the graph must hold at most 2^29 k-molecules. */
+swg_status swg_graph_merge(swg_graph *g);
+typedef struct swg_merge_info {
+    uint64_t nodes;      /* nodes left (lines of the -d file) */
+    uint64_t chains;     /* chains of merged nodes */
+    uint64_t cycles;     /* cycles of merged nodes (cut at their largest key) */
+    uint64_t text_bytes; /* size of the -d file */
+    float ms;            /* device time of the merge, including its text */
+    int launches;        /* kernel launches of the merge */
+} swg_merge_info;
+swg_status swg_graph_merge_info(const swg_graph *g, swg_merge_info *info);
+/* The merged graph as the reference's -d file contigGraph.txt
+ * (gatherDistNodeGraph lines, graph.cpp:615-645: id, 8 arcs each closed by
+ * '#', 8 multiplicities, blank-padded to sum(arc length + 1) + 61 bytes; then
+ * the final '\n' of graph.cpp:3620), lines in key order. copy_merged needs
+ * cap >= the text size (*n receives it either way). */
+swg_status swg_graph_write_merged(const swg_graph *g, const char *path);
+swg_status swg_graph_copy_merged(const swg_graph *g, char *buf, uint64_t cap, uint64_t *n);
 /* Host-only writers for records already in host memory (keys[n], mult[8*n],
  * any order): the same two file formats as above. */
 swg_status swg_records_write_kmer_graph(const uint64_t *keys, const uint8_t *mult, uint64_t n,

@@ -70,6 +70,21 @@ int oracle_write_node_lines(const oracle_graph *g, const char *path);
 /* graph.cpp:1569-1627 totals: nodes, edges, edge-length sum, tips, bubbles. */
 void oracle_graph_stats(const oracle_graph *g, int k, int64_t out[5]);
 
+/* Merging of semi-extended k-molecules (merge_oracle.c, graph.cpp:1204-1566)
+ * over n nodes (keys, 8 multiplicities each, as the build leaves them),
+ * visited in `order` (n node indices). Writes the gathered node lines of the
+ * surviving nodes in visiting order, plus the closing '\n' of the -d file
+ * (graph.cpp:576-696, 3617-3621), into *text (free with oracle_free_text).
+ * Returns 0 or a negative error (-10 neighbour missing, -11 no arc back to
+ * the sender, -12 unlock of an unlocked node: the reference exits on each). */
+#define MERGE_TIMING_REFERENCE 0 /* one rank's lazy message handling */
+#define MERGE_TIMING_IMMEDIATE 1 /* every message applied when sent */
+int oracle_merge(int k, uint64_t n, const uint64_t *keys, const uint8_t *mult, const uint64_t *order,
+                 int timing, char **text, uint64_t *text_len, uint64_t *n_lines);
+void oracle_free_text(char *text);
+/* The visiting order the GPU merge follows (see merge_oracle.c). */
+int oracle_merge_tree_order(int k, uint64_t n, const uint64_t *keys, const uint8_t *mult, uint64_t *order);
+
 /* Neighbour id printed in kmerGraph.txt for slot s of key K (graph.cpp:3380-3427). */
 uint64_t oracle_kmer_graph_neighbour(uint64_t key, int slot, int k);
 uint64_t oracle_revcomp(uint64_t x, int k);

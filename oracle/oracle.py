@@ -55,6 +55,12 @@ def lib() -> C.CDLL:
         L.oracle_kmer_graph_neighbour.restype = u64
         L.oracle_revcomp.argtypes = [u64, i32]
         L.oracle_revcomp.restype = u64
+        L.oracle_merge.argtypes = [i32, u64, P, P, P, i32, C.POINTER(C.c_void_p),
+                                   C.POINTER(u64), C.POINTER(u64)]
+        L.oracle_merge.restype = i32
+        L.oracle_free_text.argtypes = [P]
+        L.oracle_merge_tree_order.argtypes = [i32, u64, P, P, P]
+        L.oracle_merge_tree_order.restype = i32
         _lib = L
     return _lib
 
@@ -139,6 +145,57 @@ def revcomp(x: int, k: int) -> int:
     return lib().oracle_revcomp(x, k)
 
 
+MERGE_TIMING_REFERENCE = 0
+MERGE_TIMING_IMMEDIATE = 1
+
+
+def merge_tree_order(keys: np.ndarray, mult: np.ndarray, k: int) -> np.ndarray:
+    """The node visiting order of the GPU merge (merge_oracle.c)."""
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    mult = np.ascontiguousarray(mult, dtype=np.uint8).reshape(-1, 8)
+    order = np.zeros(max(keys.size, 1), dtype=np.uint64)
+    e = lib().oracle_merge_tree_order(k, keys.size, keys.ctypes.data, mult.ctypes.data, order.ctypes.data)
+    if e:
+        raise OracleError(e)
+    return order[: keys.size]
+
+
+def merge_text(keys: np.ndarray, mult: np.ndarray, k: int, order=None,
+               timing: int = MERGE_TIMING_IMMEDIATE) -> bytes:
+    """Merge semi-extended k-molecules visiting the nodes in `order` (node
+    indices; default: the GPU merge's order) and return the -d file text
+    (gathered node lines in visiting order, then '\n')."""
+    keys = np.ascontiguousarray(keys, dtype=np.uint64)
+    mult = np.ascontiguousarray(mult, dtype=np.uint8).reshape(-1, 8)
+    if order is None:
+        order = merge_tree_order(keys, mult, k)
+    order = np.ascontiguousarray(order, dtype=np.uint64)
+    assert order.size == keys.size
+    ptr, n, lines = C.c_void_p(), C.c_uint64(), C.c_uint64()
+    e = lib().oracle_merge(k, keys.size, keys.ctypes.data, mult.ctypes.data, order.ctypes.data,
+                           timing, C.byref(ptr), C.byref(n), C.byref(lines))
+    if e:
+        raise OracleError(e)
+    try:
+        return C.string_at(ptr.value, n.value) if n.value else b""
+    finally:
+        lib().oracle_free_text(ptr)
+
+
+def parse_node_lines(text: bytes) -> tuple[np.ndarray, np.ndarray]:
+    """Keys and 8 multiplicities from node lines (graph.cpp:569 layout), in
+    file order."""
+    keys, mult = [], []
+    for line in text.splitlines():
+        if not line.strip():
+            continue
+        f = line.split()
+        keys.append(int(f[0]))
+        mult.append([int(x) for x in f[-8:]])
+    return (np.array(keys, dtype=np.uint64),
+            np.array(mult, dtype=np.uint8).reshape(-1, 8))
+
+
 # ---- the reference itself (only where it was compiled from its sources) ----
 
 def reference_available() -> bool:
@@ -174,6 +231,19 @@ def run_reference(fasta_path: str, k: int, cutoff: int, outdir: str, timeout: fl
     out["nodes"] = sorted(Path(b, "nodes.txt").read_text().splitlines(),
                           key=lambda s: int(s.split()[0]))
     return out
+
+
+def run_reference_merge(fasta_path: str, k: int, cutoff: int, outdir: str,
+                        timeout: float = 600) -> tuple[bytes, bytes]:
+    """The reference's node dump with -d: its nodes before the merge, in the
+    order its merge visits them, and its contigGraph.txt after the merge
+    (graph.cpp:1392-1566, 576-696). outdir must not exist."""
+    r = subprocess.run([str(REF_DUMP), "-k", str(k), "-c", str(cutoff), "-i", str(fasta_path),
+                        "-o", str(outdir), "-d"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                       timeout=timeout, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference merge failed: %s" % r.stdout[-2000:])
+    return Path(outdir, "nodes.txt").read_bytes(), Path(outdir, "contigGraph.txt").read_bytes()
 
 
 def cores() -> int:

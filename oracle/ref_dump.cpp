@@ -8,8 +8,12 @@
 //
 // Call sequence = the reference main() up to the node build
 // (graph.cpp:3452-3561), then printLocalNodeGraph (graph.cpp:555-572) into
-// <o>/nodes.txt instead of the gather/merge stages. Usage is the reference's
-// own: ref_dump -k K -c C -i reads.fa -o <new dir>
+// <o>/nodes.txt instead of the gather/merge stages. nodes.txt lists the nodes
+// in the node map's iteration order, which is the order the merge stage
+// visits them (graph.cpp:1412). With -d the run continues like the
+// reference's own -d run: simplifyDistNodeGraph (graph.cpp:1392-1566), then
+// gatherDistNodeGraph written to <o>/contigGraph.txt (graph.cpp:3611-3621).
+// Usage is the reference's own: ref_dump -k K -c C -i reads.fa -o <new dir> [-d]
 #define main swap_reference_main
 #include "graph.cpp"
 #undef main
@@ -31,6 +35,13 @@ int main(int argc, char *argv[]) {
     strcpy(parameters.kmerGraph, parameters.outputPath);
     strcat(parameters.kmerGraph, "/nodes.txt");
     nodeGraph->printLocalNodeGraph(&parameters, &MPIcontrol);
+    if (parameters.distGraphFlag) {
+        nodeGraph->simplifyDistNodeGraph(&parameters, &MPIcontrol);
+        char *rBuf = nodeGraph->gatherDistNodeGraph(&parameters, &MPIcontrol);
+        FILE *fp = fopen(parameters.graphPath, "w");
+        fprintf(fp, "%s\n", rBuf);
+        fclose(fp);
+    }
     MPIcontrol.finalize();
     return 0;
 }

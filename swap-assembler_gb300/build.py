@@ -67,10 +67,12 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict[str, Path]:
     jobs.append((OBJ / "framing.o", [fr, *headers],
                  [nvcc, *ARCH, "-lineinfo", "-Xcompiler", "-fPIC", *common, "-c", str(fr), "-o",
                   str(OBJ / "framing.o")]))
-    em = CSRC / "emit.cu"
-    jobs.append((OBJ / "emit.o", [em, *headers],
-                 [nvcc, *ARCH, "-lineinfo", "-Xcompiler", "-fPIC", *common, "-c", str(em), "-o",
-                  str(OBJ / "emit.o")]))
+    for name in ("emit.cu", "merge.cu"):
+        src = CSRC / name
+        o = OBJ / (name[:-3] + ".o")
+        jobs.append((o, [src, CSRC / "text_dev.cuh", *headers],
+                     [nvcc, *ARCH, "-lineinfo", "-Xcompiler", "-fPIC", *common, "-c", str(src), "-o",
+                      str(o)]))
     na = CSRC / "noalloc.cu"
     jobs.append((OBJ / "noalloc.o", [na, *headers],
                  [nvcc, *ARCH, "-lineinfo", "-Xcompiler", "-fPIC", *common, "-c", str(na), "-o",
@@ -93,7 +95,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict[str, Path]:
         list(ex.map(lambda j: _run(j[2]), todo))
 
     lib = PKG / "libswapgb.so"
-    lib_objs = [OBJ / n for n in ("kernels.o", "framing.o", "emit.o", "noalloc.o", "api.o", "reads.o",
+    lib_objs = [OBJ / n for n in ("kernels.o", "framing.o", "emit.o", "merge.o", "noalloc.o", "api.o", "reads.o",
                                   "writers.o", "server.o", "autotune.o")]
     if _stale(lib, lib_objs):
         _run([nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, lib_objs), "-lpthread"])

@@ -138,6 +138,12 @@ struct swg_graph {
     uint64_t seg_cursor_cap = 0;
     unsigned long long *d_bigmeta = nullptr;  // bucketed: big-bucket ranges for the global table
     uint64_t bigmeta_cap = 0;
+    // merged graph (swg_graph_merge): the -d file's text on the device
+    char *d_mtext = nullptr;
+    uint64_t mtext_cap = 0;
+    bool merged = false;
+    swg::MergeResult mres;
+    float merge_ms = 0;
     unsigned *d_hll_seg = nullptr;
     uint64_t hll_seg_cap = 0;
 };
@@ -250,6 +256,7 @@ swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, u
     SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
     cudaStream_t s = stream_of(g, o);
     g->built = false;
+    g->merged = false;
     g->n_samples = 0;
     g->k = o->k;
     g->cutoff = o->cutoff;
@@ -635,6 +642,7 @@ swg_status batch_impl(swg_graph *g, const swg_opts *o, const swg_sample *sm, uin
     cudaStream_t s = stream_of(g, o);
     const double load = o->load_factor > 0 ? o->load_factor : 0.6;
     g->built = false;
+    g->merged = false;
     g->launches = 0;
     g->retries = 0;
     g->algorithm = SWG_ALGO_DIRECT;
@@ -1161,6 +1169,7 @@ void swg_graph_free(swg_graph *g) {
     cudaFree(g->d_out2_mult);
     cudaFree(g->d_seg_cursor);
     cudaFree(g->d_bigmeta);
+    cudaFree(g->d_mtext);
     cudaFree(g->d_hll_seg);
     cudaFree(g->d_bucket);
     cudaFree(g->d_poff);
@@ -1409,6 +1418,70 @@ swg_status swg_graph_write_node_lines(const swg_graph *g, const char *path) {
     if (st) return st;
     SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
     return swg::emit_node_lines(g->d_out_keys, g->d_out_mult, g->n_out, g->k, path, g->own);
+}
+
+// Merging of semi-extended k-molecules (merge.cu) over the built graph; the
+// result is the -d file's text, kept on the device until the next build.
+swg_status swg_graph_merge(swg_graph *g) {
+    if (!g) return SWG_ERR_BAD_INPUT;
+    swg_status st = writable(g);
+    if (st) return st;
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    g->merged = false;
+    cudaEvent_t e0 = g->ev[0], e1 = g->ev[1];
+    SWG_CUDA(cudaEventRecord(e0, g->own), "merge timing");
+    st = swg::merge_graph(g->d_out_keys, g->d_out_mult, g->n_out, g->k, g->own, &g->d_mtext, &g->mtext_cap,
+                          &g->mres);
+    if (st) return st;
+    SWG_CUDA(cudaEventRecord(e1, g->own), "merge timing");
+    SWG_CUDA(cudaEventSynchronize(e1), "merge timing");
+    SWG_CUDA(cudaEventElapsedTime(&g->merge_ms, e0, e1), "merge timing");
+    g->merged = true;
+    return SWG_OK;
+}
+
+static swg_status merged_state(const swg_graph *g) {
+    if (!g->merged) {
+        swg::set_error("no merged graph: call swg_graph_merge after the build");
+        return SWG_ERR_BAD_STATE;
+    }
+    return SWG_OK;
+}
+
+swg_status swg_graph_merge_info(const swg_graph *g, swg_merge_info *info) {
+    if (!g || !info) return SWG_ERR_BAD_INPUT;
+    swg_status st = merged_state(g);
+    if (st) return st;
+    info->nodes = g->mres.nodes;
+    info->chains = g->mres.chains;
+    info->cycles = g->mres.cycles;
+    info->text_bytes = g->mres.text_bytes;
+    info->ms = g->merge_ms;
+    info->launches = g->mres.launches;
+    return SWG_OK;
+}
+
+swg_status swg_graph_copy_merged(const swg_graph *g, char *buf, uint64_t cap, uint64_t *n) {
+    if (!g || !n) return SWG_ERR_BAD_INPUT;
+    swg_status st = merged_state(g);
+    if (st) return st;
+    *n = g->mres.text_bytes;
+    if (cap < *n || (*n && !buf)) {
+        swg::set_error("buffer smaller than the merged text");
+        return SWG_ERR_BAD_INPUT;
+    }
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    SWG_CUDA(cudaMemcpyAsync(buf, g->d_mtext, *n, cudaMemcpyDeviceToHost, g->own), "merged text copy");
+    SWG_CUDA(cudaStreamSynchronize(g->own), "merged text copy");
+    return SWG_OK;
+}
+
+swg_status swg_graph_write_merged(const swg_graph *g, const char *path) {
+    if (!g || !path) return SWG_ERR_BAD_INPUT;
+    swg_status st = merged_state(g);
+    if (st) return st;
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    return swg::stream_to_file(g->d_mtext, g->mres.text_bytes, path, g->own);
 }
 
 static swg_status sorted_copy(const uint64_t *keys, const uint8_t *mult, uint64_t n,

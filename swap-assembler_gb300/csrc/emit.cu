@@ -16,70 +16,10 @@
 #include <string>
 
 #include "swg_internal.h"
+#include "text_dev.cuh"
 
 namespace swg {
 namespace {
-
-__constant__ unsigned long long kPow10[20] = {1ull,
-                                              10ull,
-                                              100ull,
-                                              1000ull,
-                                              10000ull,
-                                              100000ull,
-                                              1000000ull,
-                                              10000000ull,
-                                              100000000ull,
-                                              1000000000ull,
-                                              10000000000ull,
-                                              100000000000ull,
-                                              1000000000000ull,
-                                              10000000000000ull,
-                                              100000000000000ull,
-                                              1000000000000000ull,
-                                              10000000000000000ull,
-                                              100000000000000000ull,
-                                              1000000000000000000ull,
-                                              10000000000000000000ull};
-
-// Decimal digits of v ("%llu").
-__device__ __forceinline__ int ndig(uint64_t v) {
-    int d = 1;
-#pragma unroll
-    for (int i = 1; i < 20; ++i) d += v >= kPow10[i];
-    return d;
-}
-
-__device__ __forceinline__ char *put_u64(char *p, uint64_t v) {
-    const int d = ndig(v);
-    for (int j = d - 1; j >= 0; --j) {
-        p[j] = (char)('0' + (int)(v % 10));
-        v /= 10;
-    }
-    return p + d;
-}
-
-// Reverse complement of a k-mer in the low 2k bits (kmerGraph.cpp:5-14):
-// complement = bitwise NOT, reverse the 2-bit groups (bit reverse + swap of
-// the bits inside each group).
-__device__ __forceinline__ uint64_t rc_dev(uint64_t a, int k) {
-    const uint64_t r = __brevll(~a);
-    const uint64_t s = ((r >> 1) & 0x5555555555555555ull) | ((r & 0x5555555555555555ull) << 1);
-    return s >> (64 - 2 * k);
-}
-
-// Neighbour id printed for slot s of key K (the host kmer_graph_neighbour):
-// descriptor K (s < 4) or rc(K) (s >= 4), base s%4 appended, last k bases N;
-// N if canonical, else complement(N) with base s flipped back (k odd) — the
-// reference's nReverseStr[i] indexing (graph.cpp:3393,3423).
-__device__ __forceinline__ uint64_t neighbour_dev(uint64_t key, int slot, int k) {
-    const uint64_t kmask = (1ull << (2 * k)) - 1;
-    const uint64_t d = slot < 4 ? key : rc_dev(key, k);
-    const uint64_t nn = ((d << 2) | (uint64_t)(slot & 3)) & kmask;
-    if (nn >= rc_dev(nn, k)) return nn;
-    uint64_t out = nn ^ kmask;
-    if (k & 1) out ^= 3ull << (2 * (k - 1 - slot));
-    return out;
-}
 
 // ---- node lines: "K A# # ... # m0 .. m7\n" (arc string "ACGT"[s%4] iff m_s != 0)
 __global__ void k_node_len(const unsigned long long *__restrict__ mult, const unsigned long long *__restrict__ keys,
@@ -176,26 +116,7 @@ __global__ void k_kg_write(const unsigned long long *__restrict__ tok, const uns
 
 inline unsigned blocks_for(uint64_t n) { return (unsigned)((n + 255) / 256); }
 
-// Stream-ordered device scratch, freed on every return path.
-struct Scratch {
-    cudaStream_t s;
-    void *p[16] = {};
-    int n = 0;
-    explicit Scratch(cudaStream_t st) : s(st) {}
-    template <typename T>
-    bool get(T **out, uint64_t count) {
-        *out = nullptr;
-        if (cudaMallocAsync((void **)out, std::max<uint64_t>(count, 1) * sizeof(T), s) != cudaSuccess) {
-            cudaGetLastError();
-            return false;
-        }
-        p[n++] = *out;
-        return true;
-    }
-    ~Scratch() {
-        for (int i = 0; i < n; ++i) cudaFreeAsync(p[i], s);
-    }
-};
+}  // namespace
 
 swg_status cuda_err(cudaError_t e, const char *what) {
     cudaGetLastError();
@@ -203,11 +124,6 @@ swg_status cuda_err(cudaError_t e, const char *what) {
     return e == cudaErrorMemoryAllocation ? SWG_ERR_OOM : SWG_ERR_CUDA;
 }
 
-#define EMIT_CUDA(call, what)                           \
-    do {                                                \
-        const cudaError_t e_ = (call);                  \
-        if (e_ != cudaSuccess) return cuda_err(e_, what); \
-    } while (0)
 
 // Exclusive prefix of len[0..n) into off[0..n], off[n] = total (bytes).
 swg_status scan_lengths(const uint64_t *len, uint64_t *off, uint64_t n, Scratch &scr, cudaStream_t s) {
@@ -265,8 +181,6 @@ swg_status stream_to_file(const char *d_text, uint64_t bytes, const char *path, 
     }
     return SWG_OK;
 }
-
-}  // namespace
 
 swg_status emit_node_lines(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n,
                            int k, const char *path, cudaStream_t s) {

@@ -1,0 +1,665 @@
+// Merging of semi-extended k-molecules on the device: the result of the
+// reference's SWAP merge loop (simplifyDistNodeGraph, graph.cpp:1392-1566,
+// with the edge messages of recvProc, graph.cpp:1204-1389) over the filtered
+// k-mer graph, written as the gathered node lines of its -d file
+// contigGraph.txt (gatherDistNodeGraph, graph.cpp:576-696).
+//
+// A node with exactly one arc on each side whose arcs do not lead back to
+// itself is merged away; all other nodes end the chains of merged nodes, and
+// each end arc finally spells the whole chain up to the next end node (the
+// arc strings do not depend on the order the merge visits nodes in). The
+// multiplicity of a merged arc is the reference's running weighted average
+// (graph.cpp:1322-1324: 64-bit sum kept in an int, divided by the new length,
+// truncated to 8 bits), which does depend on that order. The device follows
+// one fixed order: a chain of m merged nodes is numbered 1..m from its
+// smaller end arc (node key, then slot) and node p is visited at level
+// ctz(p), so each level merges disjoint pairs of neighbouring segments — a
+// pairwise tree reduction of the chain's unit arcs. A cycle made only of
+// mergeable nodes is cut at its largest key, which is visited last and keeps
+// the whole cycle on its two arcs.
+//
+// Steps (one stream): order the nodes by key; open-addressing index key ->
+// node; per node the neighbour of each arc; for every mergeable node two
+// directed walk states; list ranking of the walks with a sparse ruling set
+// (every 64th state on average plus every walk head starts a ruler; a ruler
+// walks to the next one, then the rulers' own list is ranked by pointer
+// jumping); cycles (states no ruler reaches, or rulers whose list never
+// ends) are found, cut and ranked by pointer jumping; chains are laid out in
+// power-of-two aligned segments so the tree reduction runs level by level in
+// place; finally every surviving node formats its line and every merged
+// node writes its two bases straight into the arc strings of the two ends.
+#include <cuda_runtime.h>
+
+#include <cooperative_groups.h>
+#include <cub/device/device_radix_sort.cuh>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+
+#include "swg_internal.h"
+#include "text_dev.cuh"
+
+namespace swg {
+namespace {
+
+constexpr unsigned long long kTerm = 1ull << 63;  // walk successor: end arc code (node * 8 + slot)
+constexpr unsigned kNone = 0xffffffffu;
+constexpr unsigned long long kEmptyKey = ~0ull;
+constexpr int kClasses = 40;  // chain segment size classes 2^0 .. 2^39
+
+// error bits
+constexpr unsigned kErrIndex = 1u, kErrNeighbour = 2u, kErrWalk = 4u, kErrCycle = 8u;
+
+__device__ __forceinline__ uint64_t fmix64(uint64_t x) {  // MurmurHash3 finaliser
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdull;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ull;
+    x ^= x >> 33;
+    return x;
+}
+
+namespace cg = cooperative_groups;
+
+// Counter increments aggregated over the threads of a warp that make them
+// together (one atomic per counter per warp); returns this thread's slot.
+__device__ __forceinline__ unsigned long long agg_inc(unsigned long long *ctr) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(ctr, (unsigned long long)g.size());
+    return g.shfl(base, 0) + g.thread_rank();
+}
+
+// The same for threads that target different counters ctr[label], each
+// adding step(label).
+__device__ __forceinline__ unsigned long long agg_add_labeled(unsigned long long *ctr, int label,
+                                                              unsigned long long step) {
+    cg::coalesced_group g = cg::labeled_partition(cg::coalesced_threads(), label);
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(ctr + label, step * g.size());
+    return g.shfl(base, 0) + step * g.thread_rank();
+}
+
+struct MergeArgs {
+    int k;
+    uint64_t n;
+    const unsigned long long *keys;  // ascending
+    const unsigned long long *mult;  // byte s = multiplicity of slot s
+    unsigned long long *hk;
+    unsigned *hv;
+    uint64_t hmask;
+    unsigned *nb;              // n*8: (neighbour << 1) | arrival side, kNone for an empty slot
+    unsigned char *fl;         // bit0 mergeable, bits1-2 right slot, bits3-4 left slot - 4
+    unsigned long long *succ;  // 2n walk states: next state or kTerm | end arc
+    unsigned *own, *off;       // ruler of each state, distance from it
+    unsigned *rpos;            // ruler list position of a ruler state
+    unsigned *rlist;
+    unsigned long long *rn0, *rn1, *rl0, *rl1;  // ruler list: next ruler / end arc, states to the end
+    unsigned *len;             // per state: states from it to the end of its walk
+    unsigned long long *term;  // per state: kTerm | end arc reached
+    unsigned *clist;
+    unsigned long long *cx0, *cx1, *cy0, *cy1;  // cycle pointer jumping
+    unsigned *chain_of;        // per arc code: chain id (set at the chain's start arc)
+    unsigned long long *ch_eoff;
+    unsigned *ch_m;
+    unsigned long long *ch_dfwd, *ch_drev;
+    unsigned char *ent;        // chain unit-arc multiplicities, reduced in place
+    unsigned *ent_chain;
+    unsigned long long *cls_count, *cls_cursor;
+    unsigned long long *ctr;   // [0] rulers [1] cycle states [2] chains [3] cycles cut [4] merged nodes
+    unsigned *err;
+};
+
+__device__ __forceinline__ unsigned lookup(const MergeArgs &a, uint64_t key) {
+    uint64_t h = fmix64(key) & a.hmask;
+    for (uint64_t probe = 0; probe <= a.hmask; ++probe) {
+        const unsigned long long v = a.hk[h];
+        if (v == key) return a.hv[h];
+        if (v == kEmptyKey) return kNone;
+        h = (h + 1) & a.hmask;
+    }
+    return kNone;
+}
+
+__device__ __forceinline__ unsigned mbyte(uint64_t m, int s) { return (unsigned)(m >> (8 * s)) & 0xffu; }
+__device__ __forceinline__ bool is_m(const MergeArgs &a, uint64_t i) { return a.fl[i] & 1u; }
+__device__ __forceinline__ int rslot(unsigned char f) { return (f >> 1) & 3; }
+__device__ __forceinline__ int lslot(unsigned char f) { return 4 + ((f >> 3) & 3); }
+
+__global__ void k_mg_index(MergeArgs a) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const unsigned long long key = a.keys[i];
+    uint64_t h = fmix64(key) & a.hmask;
+    for (uint64_t probe = 0; probe <= a.hmask; ++probe) {
+        const unsigned long long prev = atomicCAS(&a.hk[h], kEmptyKey, key);
+        if (prev == kEmptyKey || prev == key) {
+            a.hv[h] = (unsigned)i;
+            return;
+        }
+        h = (h + 1) & a.hmask;
+    }
+    atomicOr(a.err, kErrIndex);
+}
+
+// Neighbour of every arc (node::getNodeID, graph.cpp:164-196: oriented k-mer
+// plus the arc base, last k bases, canonical id and the side reached) and
+// whether the node is merged away.
+__global__ void k_mg_classify(MergeArgs a) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const int k = a.k;
+    const uint64_t kmask = (1ull << (2 * k)) - 1;
+    const uint64_t key = a.keys[i], m = a.mult[i], rk = rc_dev(key, k);
+    int rc = 0, lc = 0, rs = 0, ls = 4;
+    bool self = false;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        unsigned v = kNone;
+        if (mbyte(m, s)) {
+            const uint64_t e = (((s < 4 ? key : rk) << 2) | (uint64_t)(s & 3)) & kmask;
+            const uint64_t r = rc_dev(e, k);
+            const unsigned side = e >= r;
+            const unsigned j = lookup(a, side ? e : r);
+            if (j == kNone) {
+                atomicOr(a.err, kErrNeighbour);
+            } else {
+                v = (j << 1) | side;
+                self |= (uint64_t)j == i;
+            }
+            if (s < 4) ++rc, rs = s;
+            else ++lc, ls = s;
+        }
+        a.nb[i * 8 + s] = v;
+    }
+    const bool merged = rc == 1 && lc == 1 && !self;
+    a.fl[i] = (unsigned char)((merged ? 1 : 0) | (rs << 1) | ((ls - 4) << 3));
+    if (merged) agg_inc(&a.ctr[4]);
+}
+
+// Walk state 2i+d of a merged node: d = 0 traverses it as its key (leaves by
+// the right arc), d = 1 as the reverse complement (leaves by the left arc).
+// The successor is the next merged node's state, or the end arc that points
+// back from the end node reached: its side of arrival picks the half, the
+// first base of the k-mer just left gives the slot.
+__device__ __forceinline__ unsigned long long walk_next(const MergeArgs &a, uint64_t i, int d) {
+    const unsigned char f = a.fl[i];
+    const unsigned v = a.nb[i * 8 + (d ? lslot(f) : rslot(f))];
+    const uint64_t j = v >> 1;
+    const unsigned side = v & 1u;
+    if (is_m(a, j)) return 2 * j + (side ? 0 : 1);
+    const uint64_t o = d ? rc_dev(a.keys[i], a.k) : a.keys[i];
+    const unsigned first = (unsigned)(o >> (2 * (a.k - 1))) & 3u;
+    return kTerm | (j * 8 + (side ? 4 : 0) + 3 - first);
+}
+
+__global__ void k_mg_states(MergeArgs a) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || !is_m(a, i)) return;
+    a.succ[2 * i] = walk_next(a, i, 0);
+    a.succ[2 * i + 1] = walk_next(a, i, 1);
+}
+
+// A ruler: the first state of a walk (its twin leaves to an end) or, on
+// average, one state in 64.
+__device__ __forceinline__ bool is_ruler(const MergeArgs &a, uint64_t st) {
+    return (a.succ[st ^ 1] & kTerm) || (fmix64(st) & 63) == 0;
+}
+
+__global__ void k_mg_rulers(MergeArgs a) {
+    const uint64_t st = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (st >= 2 * a.n || !is_m(a, st >> 1) || !is_ruler(a, st)) return;
+    const unsigned p = (unsigned)agg_inc(&a.ctr[0]);
+    a.rpos[st] = p;
+    a.rlist[p] = (unsigned)st;
+}
+
+__global__ void k_mg_walk(MergeArgs a, uint64_t n_rul) {
+    const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_rul) return;
+    const unsigned r = a.rlist[p];
+    a.own[r] = r;
+    a.off[r] = 0;
+    uint64_t cur = r;
+    for (unsigned o = 1; o <= 2 * a.n; ++o) {
+        const unsigned long long nx = a.succ[cur];
+        if (nx & kTerm) {
+            a.rn0[p] = nx;
+            a.rl0[p] = o;
+            return;
+        }
+        if (is_ruler(a, nx)) {
+            a.rn0[p] = a.rpos[nx];
+            a.rl0[p] = o;
+            return;
+        }
+        a.own[nx] = r;
+        a.off[nx] = o;
+        cur = nx;
+    }
+    atomicOr(a.err, kErrWalk);
+}
+
+__global__ void k_mg_rjump(const unsigned long long *__restrict__ rn_in, const unsigned long long *__restrict__ rl_in,
+                           unsigned long long *__restrict__ rn_out, unsigned long long *__restrict__ rl_out,
+                           uint64_t n_rul) {
+    const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n_rul) return;
+    const unsigned long long nx = rn_in[p];
+    if (nx & kTerm) {
+        rn_out[p] = nx;
+        rl_out[p] = rl_in[p];
+    } else {
+        rn_out[p] = rn_in[nx];
+        rl_out[p] = rl_in[p] + rl_in[nx];
+    }
+}
+
+__global__ void k_mg_finish(MergeArgs a, const unsigned long long *__restrict__ rn,
+                            const unsigned long long *__restrict__ rl) {
+    const uint64_t st = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (st >= 2 * a.n || !is_m(a, st >> 1)) return;
+    const unsigned o = a.own[st];
+    if (o != kNone) {
+        const unsigned p = a.rpos[o];
+        if (rn[p] & kTerm) {
+            a.len[st] = (unsigned)(rl[p] - a.off[st]);
+            a.term[st] = rn[p];
+            return;
+        }
+    }
+    a.len[st] = 0;
+    a.term[st] = 0;
+    a.clist[agg_inc(&a.ctr[1])] = (unsigned)st;
+}
+
+// ---- cycles of merged nodes: largest key by pointer jumping, cut there
+__global__ void k_mg_cyc_init(MergeArgs a, uint64_t c) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= c) return;
+    const unsigned st = a.clist[t];
+    a.cx0[st] = a.keys[st >> 1];
+    a.cy0[st] = a.succ[st];
+}
+
+__global__ void k_mg_cyc_max(MergeArgs a, uint64_t c, const unsigned long long *__restrict__ mx_in,
+                             const unsigned long long *__restrict__ nx_in, unsigned long long *__restrict__ mx_out,
+                             unsigned long long *__restrict__ nx_out) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= c) return;
+    const unsigned st = a.clist[t];
+    const unsigned long long nx = nx_in[st];
+    mx_out[st] = max(mx_in[st], mx_in[nx]);
+    nx_out[st] = nx_in[nx];
+}
+
+__global__ void k_mg_cyc_cut(MergeArgs a, uint64_t c, const unsigned long long *__restrict__ mx) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= c) return;
+    const unsigned st = a.clist[t];
+    if (a.keys[st >> 1] == mx[st]) {
+        a.fl[st >> 1] &= (unsigned char)~1u;  // both states of the node store the same
+        if (!(st & 1)) atomicAdd(&a.ctr[3], 1ull);
+    }
+}
+
+__global__ void k_mg_cyc_succ(MergeArgs a, uint64_t c) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= c) return;
+    const unsigned st = a.clist[t];
+    if (!is_m(a, st >> 1)) return;
+    a.cy0[st] = walk_next(a, st >> 1, (int)(st & 1));
+    a.cx0[st] = 1;
+}
+
+__global__ void k_mg_cyc_rank(MergeArgs a, uint64_t c, const unsigned long long *__restrict__ ln_in,
+                              const unsigned long long *__restrict__ nx_in, unsigned long long *__restrict__ ln_out,
+                              unsigned long long *__restrict__ nx_out) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= c) return;
+    const unsigned st = a.clist[t];
+    if (!is_m(a, st >> 1)) return;
+    const unsigned long long nx = nx_in[st];
+    if (nx & kTerm) {
+        ln_out[st] = ln_in[st];
+        nx_out[st] = nx;
+    } else {
+        ln_out[st] = ln_in[st] + ln_in[nx];
+        nx_out[st] = nx_in[nx];
+    }
+}
+
+__global__ void k_mg_cyc_done(MergeArgs a, uint64_t c, const unsigned long long *__restrict__ ln,
+                              const unsigned long long *__restrict__ nx) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= c) return;
+    const unsigned st = a.clist[t];
+    if (!is_m(a, st >> 1)) return;
+    if (!(nx[st] & kTerm)) atomicOr(a.err, kErrCycle);
+    a.len[st] = (unsigned)ln[st];
+    a.term[st] = nx[st];
+}
+
+// ---- chains
+struct ChainPos {
+    unsigned m, pos;
+    uint64_t start;  // the smaller end arc code: the chain's start
+    bool fwd;        // the chain runs through this node as its key (state 2i)
+};
+
+__device__ __forceinline__ ChainPos chain_pos(const MergeArgs &a, uint64_t i) {
+    ChainPos c;
+    const unsigned la = a.len[2 * i], lb = a.len[2 * i + 1];
+    const uint64_t beta = a.term[2 * i] & ~kTerm, alpha = a.term[2 * i + 1] & ~kTerm;
+    c.m = la + lb - 1;
+    c.fwd = alpha < beta;  // nodes are in key order, so arc codes order by (key, slot)
+    c.pos = c.fwd ? lb : la;
+    c.start = c.fwd ? alpha : beta;
+    return c;
+}
+
+__device__ __forceinline__ int size_class(unsigned m) {  // ceil(log2(m + 1))
+    return m == 0 ? 0 : 64 - __clzll((unsigned long long)m);
+}
+
+__global__ void k_mg_chain_count(MergeArgs a) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || !is_m(a, i)) return;
+    const ChainPos c = chain_pos(a, i);
+    if (c.pos == 1) agg_add_labeled(a.cls_count, size_class(c.m), 1);
+}
+
+__global__ void k_mg_chain_alloc(MergeArgs a) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || !is_m(a, i)) return;
+    const ChainPos c = chain_pos(a, i);
+    if (c.pos != 1) return;
+    const int cl = size_class(c.m);
+    const unsigned id = (unsigned)agg_inc(&a.ctr[2]);
+    a.ch_eoff[id] = agg_add_labeled(a.cls_cursor, cl, 1ull << cl);
+    a.ch_m[id] = c.m;
+    a.chain_of[c.start] = id;
+}
+
+// Unit arc p (0..m) of a chain: between its nodes at positions p and p+1
+// (0 and m+1 are the end nodes); node p stores the arc it leaves by, node 1
+// also the arc it enters by.
+__global__ void k_mg_entries(MergeArgs a) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || !is_m(a, i)) return;
+    const ChainPos c = chain_pos(a, i);
+    const unsigned id = a.chain_of[c.start];
+    const uint64_t e = a.ch_eoff[id];
+    const unsigned char f = a.fl[i];
+    const uint64_t m = a.mult[i];
+    a.ent[e + c.pos] = (unsigned char)mbyte(m, c.fwd ? rslot(f) : lslot(f));
+    a.ent_chain[e + c.pos] = id;
+    if (c.pos == 1) {
+        a.ent[e] = (unsigned char)mbyte(m, c.fwd ? lslot(f) : rslot(f));
+        a.ent_chain[e] = id;
+    }
+}
+
+// One level of the pairwise reduction: the node at position (2b+1)*2^t
+// merges segment b (left) with segment b+1 (right), graph.cpp:1322-1324.
+__global__ void k_mg_level(MergeArgs a, uint64_t n_pairs, int t) {
+    const uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_pairs) return;
+    const uint64_t e = q << (t + 1);
+    const unsigned id = a.ent_chain[e];
+    if (id == kNone) return;
+    const uint64_t m = a.ch_m[id];
+    const uint64_t b = (e - a.ch_eoff[id]) >> t;
+    if (((b + 1) << t) > m) return;  // no node in the middle: the segment carries over
+    const uint64_t ll = 1ull << t;
+    const uint64_t lr = min((b + 2) << t, m + 1) - ((b + 1) << t);
+    const uint64_t sum = (uint64_t)a.ent[e] * ll + (uint64_t)a.ent[e + ll] * lr;
+    const int pre = (int)(unsigned)sum;
+    a.ent[e] = (unsigned char)((uint64_t)(int64_t)pre / (ll + lr));
+}
+
+// ---- the gathered node lines (graph.cpp:615-645): id, per slot " " + arc + "#",
+// 8 multiplicities, blanks up to sum(len+1)+61 bytes, '\n' as the last byte.
+__device__ __forceinline__ uint64_t first_state(unsigned v) {
+    return 2 * (uint64_t)(v >> 1) + ((v & 1u) ? 0 : 1);
+}
+
+__global__ void k_mg_line_len(MergeArgs a, uint64_t *__restrict__ out) {
+    const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.n) return;
+    if (is_m(a, j)) {
+        out[j] = 0;
+        return;
+    }
+    const uint64_t m = a.mult[j];
+    uint64_t l = 69;
+    for (int s = 0; s < 8; ++s) {
+        if (!mbyte(m, s)) continue;
+        const unsigned v = a.nb[j * 8 + s];
+        l += 1 + (is_m(a, v >> 1) ? a.len[first_state(v)] : 0);
+    }
+    out[j] = l;
+}
+
+__global__ void k_mg_line_write(MergeArgs a, const uint64_t *__restrict__ off, char *__restrict__ text) {
+    const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.n || is_m(a, j)) return;
+    const uint64_t m = a.mult[j];
+    char *const start = text + off[j];
+    char *p = put_u64(start, a.keys[j]);
+    unsigned mm[8];
+    uint64_t vlen = 69;
+    for (int s = 0; s < 8; ++s) {
+        *p++ = ' ';
+        mm[s] = mbyte(m, s);
+        if (mm[s]) {
+            *p = "ACGT"[s & 3];
+            const unsigned v = a.nb[j * 8 + s];
+            uint64_t l = 1;
+            if (is_m(a, v >> 1)) {
+                const uint64_t st = first_state(v);
+                const uint64_t mine = j * 8 + s, other = a.term[st] & ~kTerm;
+                const unsigned id = a.chain_of[min(mine, other)];
+                const unsigned long long dest = (unsigned long long)(p - text);
+                if (mine < other) a.ch_dfwd[id] = dest;
+                else a.ch_drev[id] = dest;
+                mm[s] = a.ent[a.ch_eoff[id]];
+                l += a.len[st];
+            }
+            p += l;
+            vlen += l;
+        }
+        *p++ = '#';
+    }
+    for (int s = 0; s < 8; ++s) {
+        *p++ = ' ';
+        p = put_u64(p, mm[s]);
+    }
+    while ((uint64_t)(p - start) < vlen - 1) *p++ = ' ';
+    *p = '\n';
+}
+
+__global__ void k_mg_chars(MergeArgs a, char *__restrict__ text) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.n || !is_m(a, i)) return;
+    const ChainPos c = chain_pos(a, i);
+    const unsigned id = a.chain_of[c.start];
+    const unsigned char f = a.fl[i];
+    const int out_fwd = c.fwd ? rslot(f) : lslot(f);  // leaving towards the chain's far end
+    const int out_rev = c.fwd ? lslot(f) : rslot(f);
+    text[a.ch_dfwd[id] + c.pos] = "ACGT"[out_fwd & 3];
+    text[a.ch_drev[id] + (c.m + 1 - c.pos)] = "ACGT"[out_rev & 3];
+}
+
+inline unsigned blocks(uint64_t n) { return (unsigned)std::max<uint64_t>((n + 255) / 256, 1); }
+
+int ceil_log2(uint64_t v) {
+    int r = 0;
+    while ((1ull << r) < v) ++r;
+    return r;
+}
+
+}  // namespace
+
+swg_status merge_graph(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n, int k,
+                       cudaStream_t s, char **d_text, uint64_t *text_cap, MergeResult *res) {
+    *res = MergeResult();
+    if (n >= (1ull << 29)) {
+        set_error("merge: more than 2^29 k-molecules");
+        return SWG_ERR_BAD_INPUT;
+    }
+    Scratch scr(s);
+    MergeArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.k = k;
+    a.n = n;
+    unsigned long long *keys = nullptr, *mult = nullptr, *ctr = nullptr;
+    uint64_t hcap = 1024;
+    while (hcap < 2 * n) hcap *= 2;
+    a.hmask = hcap - 1;
+    uint64_t *lens = nullptr, *loff = nullptr;
+    if (!scr.get(&keys, n) || !scr.get(&mult, n) || !scr.get(&a.hk, hcap) || !scr.get(&a.hv, hcap) ||
+        !scr.get(&a.nb, 8 * n) || !scr.get(&a.fl, n) || !scr.get(&a.succ, 2 * n) || !scr.get(&a.own, 2 * n) ||
+        !scr.get(&a.off, 2 * n) || !scr.get(&a.rpos, 2 * n) || !scr.get(&a.rlist, 2 * n) ||
+        !scr.get(&a.len, 2 * n) || !scr.get(&a.term, 2 * n) || !scr.get(&a.clist, 2 * n) ||
+        !scr.get(&a.chain_of, 8 * n) || !scr.get(&ctr, 8 + 2 * kClasses) || !scr.get(&a.err, 1) ||
+        !scr.get(&lens, n) || !scr.get(&loff, n + 1))
+        return cuda_err(cudaErrorMemoryAllocation, "merge workspace");
+    a.ctr = ctr;
+    a.cls_count = ctr + 8;
+    a.cls_cursor = ctr + 8 + kClasses;
+    EMIT_CUDA(cudaMemsetAsync(ctr, 0, (8 + 2 * kClasses) * sizeof(unsigned long long), s), "merge clear");
+    EMIT_CUDA(cudaMemsetAsync(a.err, 0, sizeof(unsigned), s), "merge clear");
+    EMIT_CUDA(cudaMemsetAsync(a.hk, 0xff, hcap * sizeof(unsigned long long), s), "merge clear");
+    EMIT_CUDA(cudaMemsetAsync(a.own, 0xff, 2 * n * sizeof(unsigned), s), "merge clear");
+    // nodes in key order: lines come out sorted and arc codes compare like (key, slot)
+    if (n) {
+        size_t tb = 0;
+        EMIT_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, d_keys, keys, d_mult, mult, (int64_t)n, 0, 2 * k, s),
+                  "sort size");
+        unsigned char *tmp = nullptr;
+        if (!scr.get(&tmp, tb)) return cuda_err(cudaErrorMemoryAllocation, "sort scratch");
+        EMIT_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tb, d_keys, keys, d_mult, mult, (int64_t)n, 0, 2 * k, s),
+                  "sort");
+    }
+    a.keys = keys;
+    a.mult = mult;
+    int launches = 0;
+    k_mg_index<<<blocks(n), 256, 0, s>>>(a);
+    k_mg_classify<<<blocks(n), 256, 0, s>>>(a);
+    k_mg_states<<<blocks(n), 256, 0, s>>>(a);
+    k_mg_rulers<<<blocks(2 * n), 256, 0, s>>>(a);
+    launches += 4;
+    unsigned long long h[5];
+    unsigned herr = 0;
+    EMIT_CUDA(cudaMemcpyAsync(h, ctr, sizeof(h), cudaMemcpyDeviceToHost, s), "ruler count");
+    EMIT_CUDA(cudaMemcpyAsync(&herr, a.err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "merge status");
+    EMIT_CUDA(cudaStreamSynchronize(s), "ruler count");
+    if (herr) {
+        set_error("merge: node index or neighbour lookup failed (arc without its neighbour k-molecule)");
+        return SWG_ERR_BAD_INPUT;
+    }
+    const uint64_t n_rul = h[0];
+    if (!scr.get(&a.rn0, n_rul) || !scr.get(&a.rn1, n_rul) || !scr.get(&a.rl0, n_rul) || !scr.get(&a.rl1, n_rul))
+        return cuda_err(cudaErrorMemoryAllocation, "ruler list");
+    const unsigned long long *rn = a.rn0, *rl = a.rl0;
+    if (n_rul) {
+        k_mg_walk<<<blocks(n_rul), 256, 0, s>>>(a, n_rul);
+        ++launches;
+        const int rounds = ceil_log2(n_rul) + 1;
+        unsigned long long *bn[2] = {a.rn0, a.rn1}, *bl[2] = {a.rl0, a.rl1};
+        for (int r = 0; r < rounds; ++r) {
+            k_mg_rjump<<<blocks(n_rul), 256, 0, s>>>(bn[r & 1], bl[r & 1], bn[(r + 1) & 1], bl[(r + 1) & 1], n_rul);
+            ++launches;
+        }
+        rn = bn[rounds & 1];
+        rl = bl[rounds & 1];
+    }
+    k_mg_finish<<<blocks(2 * n), 256, 0, s>>>(a, rn, rl);
+    ++launches;
+    EMIT_CUDA(cudaMemcpyAsync(h, ctr, sizeof(h), cudaMemcpyDeviceToHost, s), "cycle count");
+    EMIT_CUDA(cudaStreamSynchronize(s), "cycle count");
+    const uint64_t n_cyc_states = h[1];
+    if (n_cyc_states) {
+        if (!scr.get(&a.cx0, 2 * n) || !scr.get(&a.cx1, 2 * n) || !scr.get(&a.cy0, 2 * n) ||
+            !scr.get(&a.cy1, 2 * n))
+            return cuda_err(cudaErrorMemoryAllocation, "cycle workspace");
+        const uint64_t c = n_cyc_states;
+        const int rounds = ceil_log2(c) + 1;
+        unsigned long long *bx[2] = {a.cx0, a.cx1}, *by[2] = {a.cy0, a.cy1};
+        k_mg_cyc_init<<<blocks(c), 256, 0, s>>>(a, c);
+        for (int r = 0; r < rounds; ++r)
+            k_mg_cyc_max<<<blocks(c), 256, 0, s>>>(a, c, bx[r & 1], by[r & 1], bx[(r + 1) & 1], by[(r + 1) & 1]);
+        k_mg_cyc_cut<<<blocks(c), 256, 0, s>>>(a, c, bx[rounds & 1]);
+        k_mg_cyc_succ<<<blocks(c), 256, 0, s>>>(a, c);
+        for (int r = 0; r < rounds; ++r)
+            k_mg_cyc_rank<<<blocks(c), 256, 0, s>>>(a, c, bx[r & 1], by[r & 1], bx[(r + 1) & 1], by[(r + 1) & 1]);
+        k_mg_cyc_done<<<blocks(c), 256, 0, s>>>(a, c, bx[rounds & 1], by[rounds & 1]);
+        launches += 4 + 2 * rounds;
+    }
+    k_mg_chain_count<<<blocks(n), 256, 0, s>>>(a);
+    ++launches;
+    unsigned long long cls[kClasses];
+    EMIT_CUDA(cudaMemcpyAsync(cls, a.cls_count, sizeof(cls), cudaMemcpyDeviceToHost, s), "chain classes");
+    EMIT_CUDA(cudaMemcpyAsync(h, ctr, sizeof(h), cudaMemcpyDeviceToHost, s), "cycle cuts");
+    EMIT_CUDA(cudaMemcpyAsync(&herr, a.err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "merge status");
+    EMIT_CUDA(cudaStreamSynchronize(s), "chain classes");
+    if (herr) {
+        set_error("merge: a walk did not end (internal error)");
+        return SWG_ERR_TIMEOUT;
+    }
+    // segments of 2^c entries, largest class first: every offset is aligned
+    unsigned long long cursor[kClasses];
+    uint64_t total = 0, n_chains = 0;
+    int top = 0;
+    for (int c = kClasses - 1; c >= 0; --c) {
+        cursor[c] = total;
+        total += cls[c] << c;
+        n_chains += cls[c];
+        if (cls[c] && !top) top = c;
+    }
+    EMIT_CUDA(cudaMemcpyAsync(a.cls_cursor, cursor, sizeof(cursor), cudaMemcpyHostToDevice, s), "chain layout");
+    if (!scr.get(&a.ch_eoff, n_chains) || !scr.get(&a.ch_m, n_chains) || !scr.get(&a.ch_dfwd, n_chains) ||
+        !scr.get(&a.ch_drev, n_chains) || !scr.get(&a.ent, total) || !scr.get(&a.ent_chain, total))
+        return cuda_err(cudaErrorMemoryAllocation, "chain workspace");
+    EMIT_CUDA(cudaMemsetAsync(a.ent_chain, 0xff, std::max<uint64_t>(total, 1) * sizeof(unsigned), s), "chain clear");
+    k_mg_chain_alloc<<<blocks(n), 256, 0, s>>>(a);
+    k_mg_entries<<<blocks(n), 256, 0, s>>>(a);
+    launches += 2;
+    for (int t = 0; t < top; ++t) {
+        const uint64_t pairs = total >> (t + 1);
+        if (!pairs) break;
+        k_mg_level<<<blocks(pairs), 256, 0, s>>>(a, pairs, t);
+        ++launches;
+    }
+    k_mg_line_len<<<blocks(n), 256, 0, s>>>(a, lens);
+    ++launches;
+    swg_status st = scan_lengths(lens, loff, n, scr, s);
+    if (st) return st;
+    uint64_t bytes = 0;
+    EMIT_CUDA(cudaMemcpyAsync(&bytes, loff + n, 8, cudaMemcpyDeviceToHost, s), "text size");
+    EMIT_CUDA(cudaStreamSynchronize(s), "text size");
+    if (bytes + 1 > *text_cap) {
+        if (*d_text) cudaFree(*d_text);
+        *d_text = nullptr;
+        *text_cap = 0;
+        EMIT_CUDA(cudaMalloc((void **)d_text, bytes + 1), "merged text");
+        *text_cap = bytes + 1;
+    }
+    k_mg_line_write<<<blocks(n), 256, 0, s>>>(a, loff, *d_text);
+    k_mg_chars<<<blocks(n), 256, 0, s>>>(a, *d_text);
+    launches += 2;
+    EMIT_CUDA(cudaMemsetAsync(*d_text + bytes, '\n', 1, s), "merged text");
+    EMIT_CUDA(cudaGetLastError(), "merge kernels");
+    EMIT_CUDA(cudaStreamSynchronize(s), "merge");
+    res->text_bytes = bytes + 1;
+    res->nodes = n - h[4] + h[3];
+    res->chains = n_chains;
+    res->cycles = h[3];
+    res->rulers = n_rul;
+    res->launches = launches + 3;  // + the scan
+    return SWG_OK;
+}
+
+}  // namespace swg

@@ -1,5 +1,5 @@
 // swap — command line of the GPU k-mer graph build, with the reference's
-// interface: swap -k <kmerlength> -c <cutoff> -i <input fasta> -o <output dir> [-s]
+// interface: swap -k <kmerlength> -c <cutoff> -i <input fasta> -o <output dir> [-s] [-d]
 //
 // Flags, defaults (k=23, c=5) and checks follow parameter::getopt and
 // getParameters (sequence.cpp:4-183): k odd in 19..31 (sequence.cpp:44), the
@@ -9,6 +9,9 @@
 //                  (graph.cpp:3352-3440), lines sorted by first token;
 //   nodes.txt      every surviving k-molecule with its 8 edge multiplicities
 //                  (graph.cpp:569 layout), the input of the merging stage;
+//   contigGraph.txt with -d and without -s (graph.cpp:3617-3621), the graph
+//                  after merging its semi-extended k-molecules (the merge of
+//                  simplifyDistNodeGraph, graph.cpp:1392-1566, run on the GPU);
 //   logtime.txt    phase times.
 // stdout carries the reference's graph totals (graph.cpp:1621-1625).
 // Unlike the reference, every failure exits with a nonzero status.
@@ -43,7 +46,7 @@ int fail(swg_status st, const char *what) {
 }  // namespace
 
 int main(int argc, char **argv) {
-    int k = 23, c = 5, kmer_graph = 0;
+    int k = 23, c = 5, kmer_graph = 0, dist_graph = 0;
     std::string in, out;
     for (int i = 1; i < argc; i++) {
         const char *a = argv[i];
@@ -88,7 +91,8 @@ int main(int argc, char **argv) {
                 out = argv[++i];
                 break;
             case 's': kmer_graph = 1; break;
-            default: break;  // -j -d -p select contig-stage outputs, which this build does not run
+            case 'd': dist_graph = 1; break;
+            default: break;  // -j -p select contig-stage outputs, which this build does not run
         }
     }
     if (in.empty() || out.empty()) {
@@ -144,6 +148,17 @@ int main(int argc, char **argv) {
         return fail(st, "writing kmerGraph.txt");
     if ((st = swg_graph_write_node_lines(g, (out + "/nodes.txt").c_str())))
         return fail(st, "writing nodes.txt");
+    // the reference merges only without -s, and writes the merged graph with -d
+    // (graph.cpp:3578, 3617)
+    swg_merge_info minfo;
+    std::memset(&minfo, 0, sizeof(minfo));
+    const bool merge = dist_graph && !kmer_graph;
+    if (merge) {
+        if ((st = swg_graph_merge(g))) return fail(st, "merging semi-extended k-molecules");
+        if ((st = swg_graph_merge_info(g, &minfo))) return fail(st, "merge info");
+        if ((st = swg_graph_write_merged(g, (out + "/contigGraph.txt").c_str())))
+            return fail(st, "writing contigGraph.txt");
+    }
     const double t3 = now_s();
     float ms[5];
     int launches = 0;
@@ -160,6 +175,10 @@ int main(int argc, char **argv) {
         std::fprintf(lf, "Time spend in Constructing Graph %.5f (framing on the device; build %.5f: %s %.5f, %s %.5f, %s %.5f, %s %.5f)\n",
                      t2 - t1, ms[4] * 1e-3, ph[0], ms[0] * 1e-3, ph[1], ms[1] * 1e-3, ph[2], ms[2] * 1e-3,
                      ph[3], ms[3] * 1e-3);
+        if (merge)
+            std::fprintf(lf, "Time spend in Simplify DistGraph %.5f (device; %llu nodes left, %llu chains, %llu cycles)\n",
+                         minfo.ms * 1e-3, (unsigned long long)minfo.nodes, (unsigned long long)minfo.chains,
+                         (unsigned long long)minfo.cycles);
         std::fprintf(lf, "Time spend in writing output %.5f\n", t3 - t2);
         std::fprintf(lf, "Time spend in All step %.5f\n", t3 - t0);
         std::fclose(lf);

@@ -193,6 +193,16 @@ void sort_records(uint64_t *keys, uint64_t *mult8, uint64_t n);
 uint64_t revcomp_host(uint64_t x, int k);
 // Device emission of the text outputs (emit.cu), byte-identical with the host
 // writers: records on the device, any order.
+// Device text -> file through two pinned 64 MiB buffers (emit.cu).
+swg_status stream_to_file(const char *d_text, uint64_t bytes, const char *path, cudaStream_t s);
+// Merging of semi-extended k-molecules (merge.cu): the -d file's text
+// (gathered node lines + final '\n') into *d_text (grown as needed).
+struct MergeResult {
+    uint64_t text_bytes = 0, nodes = 0, chains = 0, cycles = 0, rulers = 0;
+    int launches = 0;
+};
+swg_status merge_graph(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n, int k,
+                       cudaStream_t s, char **d_text, uint64_t *text_cap, MergeResult *res);
 swg_status emit_node_lines(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n,
                            int k, const char *path, cudaStream_t s);
 swg_status emit_kmer_graph(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n, int k,

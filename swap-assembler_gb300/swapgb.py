@@ -63,6 +63,14 @@ class BuildInfo(C.Structure):
         return d
 
 
+class MergeInfo(C.Structure):
+    _fields_ = [("nodes", C.c_uint64), ("chains", C.c_uint64), ("cycles", C.c_uint64),
+                ("text_bytes", C.c_uint64), ("ms", C.c_float), ("launches", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class Sample(C.Structure):
     _fields_ = [("packed", C.c_void_p), ("n_words", C.c_uint64), ("read_off", C.c_void_p),
                 ("read_len", C.c_void_p), ("n_reads", C.c_uint64), ("k", C.c_int),
@@ -125,6 +133,10 @@ def lib() -> C.CDLL:
             "swg_graph_stats": (i32, [P, C.POINTER(C.c_int64)]),
             "swg_graph_write_kmer_graph": (i32, [P, C.c_char_p]),
             "swg_graph_write_node_lines": (i32, [P, C.c_char_p]),
+            "swg_graph_merge": (i32, [P]),
+            "swg_graph_merge_info": (i32, [P, C.POINTER(MergeInfo)]),
+            "swg_graph_write_merged": (i32, [P, C.c_char_p]),
+            "swg_graph_copy_merged": (i32, [P, P, u64, pu64]),
             "swg_records_write_kmer_graph": (i32, [P, P, u64, i32, C.c_char_p]),
             "swg_records_write_node_lines": (i32, [P, P, u64, C.c_char_p]),
             "swg_graph_last_timings": (i32, [P, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
@@ -285,6 +297,28 @@ class Graph:
     def write_node_lines(self, path: str) -> None:
         _check(lib().swg_graph_write_node_lines(self._h, str(path).encode()),
                "swg_graph_write_node_lines")
+
+    def merge(self) -> "Graph":
+        """Merge the semi-extended k-molecules of the built graph on the device."""
+        _check(lib().swg_graph_merge(self._h), "swg_graph_merge")
+        return self
+
+    def merge_info(self) -> dict:
+        info = MergeInfo()
+        _check(lib().swg_graph_merge_info(self._h, C.byref(info)), "swg_graph_merge_info")
+        return info.as_dict()
+
+    def merged_text(self) -> bytes:
+        """The merged graph as the -d file's bytes (contigGraph.txt)."""
+        n = C.c_uint64()
+        lib().swg_graph_copy_merged(self._h, None, 0, C.byref(n))
+        buf = C.create_string_buffer(max(n.value, 1))
+        _check(lib().swg_graph_copy_merged(self._h, C.addressof(buf), n.value, C.byref(n)),
+               "swg_graph_copy_merged")
+        return buf.raw[: n.value]
+
+    def write_merged(self, path: str) -> None:
+        _check(lib().swg_graph_write_merged(self._h, str(path).encode()), "swg_graph_write_merged")
 
     def build_fasta(self, opts: Opts, text) -> "Graph":
         """Frame and pack the FASTA on the device, then build. `text` is bytes

@@ -124,3 +124,41 @@ SYNTH_CASES = [
 
 def synth_text(case: dict) -> bytes:
     return b"".join(synth_fasta(**p) for p in case["params"])
+
+
+def _circular_reads(rng: random.Random, genome_len: int, n: int, L: int) -> list[str]:
+    g = _rand_seq(rng, genome_len)
+    gg = g + g[:L]  # reads wrap around the end: a circular genome
+    out = []
+    for _ in range(n):
+        st = rng.randrange(genome_len)
+        r = gg[st:st + L]
+        out.append(_revcomp(r) if rng.random() < 0.5 else r)
+    return out
+
+
+def _merge_cases() -> list[dict]:
+    rng = random.Random(1392)
+    cycles = (_circular_reads(rng, 500, 200, 80) + ["ACGTT" * 30] * 5 + ["AC" * 50] * 4 +
+              _circular_reads(rng, 1200, 400, 100))
+    return [
+        dict(name="merge_errors_k21", k=21, c=1, why="1% errors kept by c=1: many tips and bubbles",
+             params=[dict(seed=31, genome_len=6000, n_reads=1500, read_len=100, sub_rate=0.01)]),
+        dict(name="merge_repeats_k31", k=31, c=2, why="repeat families and tandem repeats, k31",
+             params=[dict(seed=32, genome_len=8000, repeat_frac=0.1, tandem_frac=0.05, n_reads=2000,
+                          read_len=150, sub_rate=0.005)]),
+        dict(name="merge_cycles_k23", k=23, c=3, text=_fasta(cycles),
+             why="isolated cycles: two circular genomes and two tandem repeats"),
+        dict(name="merge_k19_c0", k=19, c=0, why="k19, c=0, indels",
+             params=[dict(seed=33, genome_len=3000, n_reads=800, read_len=75, sub_rate=0.02,
+                          indel_rate=0.002)]),
+    ]
+
+
+# Merge stage (graph.cpp:1392-1566) cases; make_merge_golden.py stores the
+# reference's visiting order and a hash of its -d output for each.
+MERGE_CASES = _merge_cases()
+
+
+def case_text(case: dict) -> bytes:
+    return case["text"] if "text" in case else synth_text(case)

@@ -1,0 +1,141 @@
+"""GPU merge of semi-extended k-molecules (swg_graph_merge) against the CPU
+restatement run in the same visiting order with every message applied at
+once (oracle/merge_oracle.c). The lines must be identical (the device writes
+them in key order, the restatement in visiting order, so lines are compared
+as sorted sets), and the file sizes equal."""
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+import swapgb
+from cases import MERGE_CASES, SYNTH_CASES, case_text
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parent.parent
+SWAP = ROOT / "swap-assembler_gb300" / "bin" / "swap"
+
+
+def _lines(text: bytes) -> list[bytes]:
+    return sorted(l for l in text.split(b"\n") if l)
+
+
+def _gpu_merge(text: bytes, k: int, c: int, algorithm: int = swapgb.ALGO_DEFAULT) -> tuple[bytes, dict]:
+    g = swapgb.Graph()
+    g.build_fasta(swapgb.Opts(k=k, cutoff=c, algorithm=algorithm), text)
+    g.merge()
+    return g.merged_text(), g.merge_info()
+
+
+def _check(text: bytes, k: int, c: int, algorithm: int = swapgb.ALGO_DEFAULT) -> dict:
+    got, info = _gpu_merge(text, k, c, algorithm)
+    keys, mult = oracle.records(text, k, c)
+    want = oracle.merge_text(keys, mult, k)
+    assert len(got) == len(want) == info["text_bytes"]
+    assert got.endswith(b"\n")
+    gl, wl = _lines(got), _lines(want)
+    assert len(gl) == len(wl) == info["nodes"]
+    assert gl == wl
+    firsts = [int(l.split(b" ", 1)[0]) for l in got.split(b"\n") if l]
+    assert firsts == sorted(firsts)  # key order
+    return info
+
+
+@pytest.mark.parametrize("case", MERGE_CASES, ids=lambda c: c["name"])
+def test_merge_matches_oracle(case):
+    info = _check(case_text(case), case["k"], case["c"])
+    if case["name"] == "merge_cycles_k23":
+        assert info["cycles"] >= 3
+
+
+@pytest.mark.parametrize("case", [c for c in SYNTH_CASES if c["name"] != "c1_full"], ids=lambda c: c["name"])
+def test_merge_matches_oracle_synthetic(case):
+    _check(case_text(case), case["k"], case["c"])
+
+
+def test_merge_same_for_both_builds():
+    case = MERGE_CASES[0]
+    text = case_text(case)
+    a, _ = _gpu_merge(text, case["k"], case["c"], swapgb.ALGO_BUCKETED)
+    b, _ = _gpu_merge(text, case["k"], case["c"], swapgb.ALGO_DIRECT)
+    assert a == b
+
+
+def test_merge_full_size_workload():
+    """The 1 Mbp, 300k-read workload: about a million k-molecules."""
+    case = next(c for c in SYNTH_CASES if c["name"] == "c1_full")
+    info = _check(case_text(case), case["k"], case["c"])
+    assert info["chains"] > 0
+
+
+def test_merge_long_chains():
+    """An error-free 400 kbp genome at high cutoff: few, very long chains
+    (the ruling-set walks and the deep reduction levels)."""
+    text = swapgb.synth_fasta(seed=77, genome_len=400_000, n_reads=200_000, read_len=100, sub_rate=0.0)
+    info = _check(text, 31, 3)
+    assert info["nodes"] < 1000
+
+
+def test_merge_cycles_of_every_size():
+    """Isolated cycles of length 1 (a node whose arcs lead to itself), 2, 3,
+    5 and a circular genome."""
+    import random
+    rng = random.Random(5)
+    g = "".join(rng.choice("ACGT") for _ in range(3000))
+    reads = [g[i:i + 100] if i + 100 <= 3000 else g[i:] + g[:i + 100 - 3000] for i in range(0, 3000, 7)]
+    units = ["A", "AC", "ACG", "ACGTT", "AACCGGTTAC"]
+    reads += [u * (120 // len(u)) for u in units for _ in range(4)]
+    text = "".join(">r%d\n%s\n" % (i, r) for i, r in enumerate(reads)).encode()
+    for k in (19, 25, 31):
+        _check(text, k, 2)
+
+
+def test_merge_empty_graph():
+    text = swapgb.synth_fasta(seed=8, genome_len=5000, n_reads=100, read_len=100)
+    got, info = _gpu_merge(text, 21, 255)
+    assert got == b"\n" and info["nodes"] == 0
+
+
+def test_merge_file_and_states(tmp_path):
+    case = MERGE_CASES[1]
+    g = swapgb.Graph()
+    with pytest.raises(swapgb.SwgError):
+        g.merge()  # nothing built
+    g.build_fasta(swapgb.Opts(k=case["k"], cutoff=case["c"]), case_text(case))
+    with pytest.raises(swapgb.SwgError):
+        g.merged_text()  # not merged yet
+    g.merge()
+    p = tmp_path / "contigGraph.txt"
+    g.write_merged(str(p))
+    assert p.read_bytes() == g.merged_text()
+    g.build_fasta(swapgb.Opts(k=case["k"], cutoff=case["c"]), case_text(case))
+    with pytest.raises(swapgb.SwgError):
+        g.merge_info()  # a new build drops the merged graph
+    r = swapgb.reads_from_fasta(case_text(case), case["k"])
+    g.build_batch(swapgb.Opts(), [(r, case["k"], case["c"])])
+    with pytest.raises(swapgb.SwgError):
+        g.merge()  # batched results are per sample
+
+
+def test_cli_writes_contig_graph(tmp_path):
+    case = MERGE_CASES[0]
+    fa = tmp_path / "in.fa"
+    fa.write_bytes(case_text(case))
+    out = tmp_path / "o"
+    r = subprocess.run([str(SWAP), "-k", str(case["k"]), "-c", str(case["c"]), "-i", str(fa), "-o", str(out),
+                        "-d"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout
+    got = (out / "contigGraph.txt").read_bytes()
+    keys, mult = oracle.records(case_text(case), case["k"], case["c"])
+    assert _lines(got) == _lines(oracle.merge_text(keys, mult, case["k"]))
+    assert "Simplify DistGraph" in (out / "logtime.txt").read_text()
+    # with -s the reference stops after kmerGraph.txt: no merge
+    out2 = tmp_path / "o2"
+    r = subprocess.run([str(SWAP), "-k", str(case["k"]), "-c", str(case["c"]), "-i", str(fa), "-o", str(out2),
+                        "-d", "-s"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout
+    assert (out2 / "kmerGraph.txt").exists() and not (out2 / "contigGraph.txt").exists()

@@ -1,0 +1,124 @@
+"""The CPU restatement of the merge stage (oracle/merge_oracle.c) against the
+reference: replaying the reference's own visiting order with its one-rank
+message timing gives its -d output byte for byte, from the stored fixtures
+(tests/golden/make_merge_golden.py) and, where the reference was compiled
+here, live. Plus the properties the GPU merge relies on: the arc strings do
+not depend on the visiting order, and a complete merge leaves no mergeable
+node."""
+import hashlib
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+from cases import MERGE_CASES, SYNTH_CASES, case_text
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+MERGE_GOLDEN = json.loads((GOLDEN / "merge_cases.json").read_text())
+
+
+def _lines(text: bytes) -> list[bytes]:
+    return sorted(l for l in text.split(b"\n") if l)
+
+
+def _arc_strings(text: bytes) -> dict[int, list[bytes]]:
+    out = {}
+    for line in text.split(b"\n"):
+        if not line:
+            continue
+        head, rest = line.split(b" ", 1)
+        fields = rest.split(b"#")[:8]
+        out[int(head)] = [f.strip() for f in fields]
+    return out
+
+
+@pytest.mark.parametrize("case", MERGE_CASES, ids=lambda c: c["name"])
+def test_merge_replays_reference_fixture(case):
+    g = MERGE_GOLDEN[case["name"]]
+    text = case_text(case)
+    assert hashlib.sha256(text).hexdigest() == g["input_sha256"]
+    keys, mult = oracle.records(text, case["k"], case["c"])
+    assert keys.size == g["nodes"]
+    order = np.load(GOLDEN / (case["name"] + ".order.npy")).astype(np.uint64)
+    out = oracle.merge_text(keys, mult, case["k"], order=order, timing=oracle.MERGE_TIMING_REFERENCE)
+    assert len(out) == g["merged_bytes"]
+    assert hashlib.sha256(out).hexdigest() == g["merged_sha256"]
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference not compiled here")
+@pytest.mark.parametrize("case", [c for c in SYNTH_CASES if c["name"] in ("c1_small", "c3_small", "k25_c1")],
+                         ids=lambda c: c["name"])
+def test_merge_replays_live_reference(case, tmp_path):
+    fa = tmp_path / "in.fa"
+    fa.write_bytes(case_text(case))
+    nodes, ref = oracle.run_reference_merge(str(fa), case["k"], case["c"], str(tmp_path / "o"))
+    keys, mult = oracle.parse_node_lines(nodes)
+    out = oracle.merge_text(keys, mult, case["k"], order=np.arange(keys.size),
+                            timing=oracle.MERGE_TIMING_REFERENCE)
+    assert out == ref
+
+
+@pytest.mark.parametrize("case", MERGE_CASES, ids=lambda c: c["name"])
+def test_arc_strings_do_not_depend_on_the_order(case):
+    """Nodes with other than one arc per side are never merged and end up
+    with the same arc strings whatever the order; only which node of an
+    isolated cycle is left (and where its cycle string starts) depends on it."""
+    keys, mult = oracle.records(case_text(case), case["k"], case["c"])
+    ref_order = np.load(GOLDEN / (case["name"] + ".order.npy")).astype(np.uint64)
+    rng = np.random.default_rng(7)
+    texts = [oracle.merge_text(keys, mult, case["k"], order=o) for o in
+             (None, ref_order, rng.permutation(keys.size).astype(np.uint64), np.arange(keys.size)[::-1].copy())]
+    one_each = {int(key) for key, m in zip(keys, mult) if np.count_nonzero(m[:4]) == 1 and np.count_nonzero(m[4:]) == 1}
+    arcs = [_arc_strings(t) for t in texts]
+    ends = [{key: a for key, a in x.items() if key not in one_each} for x in arcs]
+    for x, e in zip(arcs[1:], ends[1:]):
+        assert e == ends[0]
+        assert len(x) == len(arcs[0])
+        assert sum(len(s) for v in x.values() for s in v) == sum(len(s) for v in arcs[0].values() for s in v)
+
+
+@pytest.mark.parametrize("case", MERGE_CASES, ids=lambda c: c["name"])
+def test_complete_merge_leaves_no_mergeable_node(case):
+    k = case["k"]
+    keys, mult = oracle.records(case_text(case), k, case["c"])
+    out = oracle.merge_text(keys, mult, k)
+    left = _arc_strings(out)
+    codes = {ord("A"): 0, ord("C"): 1, ord("G"): 2, ord("T"): 3}
+    mask = (1 << (2 * k)) - 1
+    for key, arcs in left.items():
+        right = [s for s in range(4) if arcs[s]]
+        lft = [s for s in range(4, 8) if arcs[s]]
+        if len(right) != 1 or len(lft) != 1:
+            continue
+        # one arc per side: one of them must lead back to the node itself
+        ends = []
+        for s in (right[0], lft[0]):
+            v = key if s < 4 else oracle.revcomp(key, k)
+            for ch in arcs[s][-k:]:
+                v = ((v << 2) | codes[ch]) & mask
+            ends.append(max(v, oracle.revcomp(v, k)))
+        assert key in ends, key
+
+
+def test_reference_timing_keeps_what_a_complete_merge_removes():
+    """At one rank the reference leaves nodes its pending messages kept
+    locked and loses its last merge; the complete merge has fewer lines."""
+    case = MERGE_CASES[0]
+    keys, mult = oracle.records(case_text(case), case["k"], case["c"])
+    order = np.load(GOLDEN / (case["name"] + ".order.npy")).astype(np.uint64)
+    lazy = oracle.merge_text(keys, mult, case["k"], order=order, timing=oracle.MERGE_TIMING_REFERENCE)
+    full = oracle.merge_text(keys, mult, case["k"], order=order)
+    assert len(_lines(full)) < len(_lines(lazy))
+
+
+def test_merge_tree_order_is_a_permutation():
+    case = MERGE_CASES[2]
+    keys, mult = oracle.records(case_text(case), case["k"], case["c"])
+    order = oracle.merge_tree_order(keys, mult, case["k"])
+    assert np.array_equal(np.sort(order), np.arange(keys.size, dtype=np.uint64))
+
+
+def test_merge_of_nothing_is_one_newline():
+    assert oracle.merge_text(np.zeros(0, np.uint64), np.zeros((0, 8), np.uint8), 21) == b"\n"
