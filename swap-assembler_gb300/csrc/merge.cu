@@ -18,16 +18,19 @@
 // mergeable nodes is cut at its largest key, which is visited last and keeps
 // the whole cycle on its two arcs.
 //
-// Steps (one stream): order the nodes by key; open-addressing index key ->
-// node; per node the neighbour of each arc; for every mergeable node two
+// Steps (one stream): open-addressing index key -> node (16-byte entries);
+// per node the neighbour of each arc; for every mergeable node two
 // directed walk states; list ranking of the walks with a sparse ruling set
 // (every 64th state on average plus every walk head starts a ruler; a ruler
 // walks to the next one, then the rulers' own list is ranked by pointer
 // jumping); cycles (states no ruler reaches, or rulers whose list never
 // ends) are found, cut and ranked by pointer jumping; chains are laid out in
 // power-of-two aligned segments so the tree reduction runs level by level in
-// place; finally every surviving node formats its line and every merged
-// node writes its two bases straight into the arc strings of the two ends.
+// place; finally the surviving nodes are ordered by key, each formats its
+// line and every merged node writes its two bases straight into the arc
+// strings of the two ends. Node indices follow the build's output order,
+// which the result does not depend on: chains are numbered by the keys of
+// their end nodes.
 #include <cuda_runtime.h>
 
 #include <cooperative_groups.h>
@@ -84,15 +87,14 @@ __device__ __forceinline__ unsigned long long agg_add_labeled(unsigned long long
 struct MergeArgs {
     int k;
     uint64_t n;
-    const unsigned long long *keys;  // ascending
+    const unsigned long long *keys;
     const unsigned long long *mult;  // byte s = multiplicity of slot s
-    unsigned long long *hk;
-    unsigned *hv;
+    ulonglong2 *ht;                  // index: x = key (kEmptyKey when free), y = node
     uint64_t hmask;
     unsigned *nb;              // n*8: (neighbour << 1) | arrival side, kNone for an empty slot
     unsigned char *fl;         // bit0 mergeable, bits1-2 right slot, bits3-4 left slot - 4
     unsigned long long *succ;  // 2n walk states: next state or kTerm | end arc
-    unsigned *own, *off;       // ruler of each state, distance from it
+    unsigned long long *oo;    // per state: its ruler << 32 | distance from it (~0: none)
     unsigned *rpos;            // ruler list position of a ruler state
     unsigned *rlist;
     unsigned long long *rn0, *rn1, *rl0, *rl1;  // ruler list: next ruler / end arc, states to the end
@@ -108,15 +110,18 @@ struct MergeArgs {
     unsigned *ent_chain;
     unsigned long long *cls_count, *cls_cursor;
     unsigned long long *ctr;   // [0] rulers [1] cycle states [2] chains [3] cycles cut [4] merged nodes
+                               // [5] surviving nodes
+    unsigned long long *skey;  // surviving nodes: keys, then (sorted) node indices
+    unsigned *sidx;
     unsigned *err;
 };
 
 __device__ __forceinline__ unsigned lookup(const MergeArgs &a, uint64_t key) {
     uint64_t h = fmix64(key) & a.hmask;
     for (uint64_t probe = 0; probe <= a.hmask; ++probe) {
-        const unsigned long long v = a.hk[h];
-        if (v == key) return a.hv[h];
-        if (v == kEmptyKey) return kNone;
+        const ulonglong2 e = a.ht[h];
+        if (e.x == key) return (unsigned)e.y;
+        if (e.x == kEmptyKey) return kNone;
         h = (h + 1) & a.hmask;
     }
     return kNone;
@@ -133,9 +138,9 @@ __global__ void k_mg_index(MergeArgs a) {
     const unsigned long long key = a.keys[i];
     uint64_t h = fmix64(key) & a.hmask;
     for (uint64_t probe = 0; probe <= a.hmask; ++probe) {
-        const unsigned long long prev = atomicCAS(&a.hk[h], kEmptyKey, key);
+        const unsigned long long prev = atomicCAS(&a.ht[h].x, kEmptyKey, key);
         if (prev == kEmptyKey || prev == key) {
-            a.hv[h] = (unsigned)i;
+            a.ht[h].y = i;
             return;
         }
         h = (h + 1) & a.hmask;
@@ -194,65 +199,91 @@ __device__ __forceinline__ unsigned long long walk_next(const MergeArgs &a, uint
     return kTerm | (j * 8 + (side ? 4 : 0) + 3 - first);
 }
 
+__device__ __forceinline__ bool ruler_of(uint64_t st, const ulonglong2 &pair);
+
+// Both walk states of a merged node, and which of them start rulers.
 __global__ void k_mg_states(MergeArgs a) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n || !is_m(a, i)) return;
-    a.succ[2 * i] = walk_next(a, i, 0);
-    a.succ[2 * i + 1] = walk_next(a, i, 1);
+    const ulonglong2 pair = make_ulonglong2(walk_next(a, i, 0), walk_next(a, i, 1));
+    *reinterpret_cast<ulonglong2 *>(a.succ + 2 * i) = pair;
+    for (int d = 0; d < 2; ++d) {
+        if (!ruler_of(2 * i + d, pair)) continue;
+        const unsigned p = (unsigned)agg_inc(&a.ctr[0]);
+        a.rlist[p] = (unsigned)(2 * i + d);
+    }
+}
+
+// The successors of a node's two states sit side by side: one 16-byte load.
+__device__ __forceinline__ ulonglong2 succ_pair(const MergeArgs &a, uint64_t st) {
+    return *reinterpret_cast<const ulonglong2 *>(a.succ + (st & ~1ull));
 }
 
 // A ruler: the first state of a walk (its twin leaves to an end) or, on
 // average, one state in 64.
-__device__ __forceinline__ bool is_ruler(const MergeArgs &a, uint64_t st) {
-    return (a.succ[st ^ 1] & kTerm) || (fmix64(st) & 63) == 0;
+__device__ __forceinline__ bool ruler_of(uint64_t st, const ulonglong2 &pair) {
+    const unsigned long long twin = (st & 1) ? pair.x : pair.y;
+    return (twin & kTerm) || (fmix64(st) & 63) == 0;
 }
 
-__global__ void k_mg_rulers(MergeArgs a) {
-    const uint64_t st = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (st >= 2 * a.n || !is_m(a, st >> 1) || !is_ruler(a, st)) return;
-    const unsigned p = (unsigned)agg_inc(&a.ctr[0]);
-    a.rpos[st] = p;
-    a.rlist[p] = (unsigned)st;
+// The ruler list position of every ruler state (read when a walk meets it).
+__global__ void k_mg_rpos(MergeArgs a) {
+    const uint64_t n_rul = a.ctr[0];
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_rul;
+         p += (uint64_t)gridDim.x * blockDim.x)
+        a.rpos[a.rlist[p]] = (unsigned)p;
 }
 
-__global__ void k_mg_walk(MergeArgs a, uint64_t n_rul) {
-    const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n_rul) return;
-    const unsigned r = a.rlist[p];
-    a.own[r] = r;
-    a.off[r] = 0;
-    uint64_t cur = r;
-    for (unsigned o = 1; o <= 2 * a.n; ++o) {
-        const unsigned long long nx = a.succ[cur];
-        if (nx & kTerm) {
-            a.rn0[p] = nx;
-            a.rl0[p] = o;
-            return;
+// Each ruler walks to the next ruler or the walk's end, labelling the states
+// on the way with (its list position, distance); per step one 16-byte load
+// and one 8-byte store. Grid-stride over the ruler count on the device.
+__global__ void k_mg_walk(MergeArgs a) {
+    const uint64_t n_rul = a.ctr[0];
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_rul;
+         p += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned r = a.rlist[p];
+        const unsigned long long tag = p << 32;
+        a.oo[r] = tag;
+        uint64_t cur = r;
+        ulonglong2 pr = succ_pair(a, r);
+        bool done = false;
+        for (unsigned o = 1; o <= 2 * a.n; ++o) {
+            const unsigned long long nx = (cur & 1) ? pr.y : pr.x;
+            if (nx & kTerm) {
+                a.rn0[p] = nx;
+                a.rl0[p] = o;
+                done = true;
+                break;
+            }
+            const ulonglong2 pn = succ_pair(a, nx);
+            if (ruler_of(nx, pn)) {
+                a.rn0[p] = a.rpos[nx];
+                a.rl0[p] = o;
+                done = true;
+                break;
+            }
+            a.oo[nx] = tag | o;
+            cur = nx;
+            pr = pn;
         }
-        if (is_ruler(a, nx)) {
-            a.rn0[p] = a.rpos[nx];
-            a.rl0[p] = o;
-            return;
-        }
-        a.own[nx] = r;
-        a.off[nx] = o;
-        cur = nx;
+        if (!done) atomicOr(a.err, kErrWalk);
     }
-    atomicOr(a.err, kErrWalk);
 }
 
 __global__ void k_mg_rjump(const unsigned long long *__restrict__ rn_in, const unsigned long long *__restrict__ rl_in,
                            unsigned long long *__restrict__ rn_out, unsigned long long *__restrict__ rl_out,
-                           uint64_t n_rul) {
-    const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= n_rul) return;
-    const unsigned long long nx = rn_in[p];
-    if (nx & kTerm) {
-        rn_out[p] = nx;
-        rl_out[p] = rl_in[p];
-    } else {
-        rn_out[p] = rn_in[nx];
-        rl_out[p] = rl_in[p] + rl_in[nx];
+                           const unsigned long long *__restrict__ count) {
+    const uint64_t n_rul = *count;
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n_rul;
+         p += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long nx = rn_in[p];
+        if (nx & kTerm) {
+            rn_out[p] = nx;
+            rl_out[p] = rl_in[p];
+        } else {
+            rn_out[p] = rn_in[nx];
+            rl_out[p] = rl_in[p] + rl_in[nx];
+        }
     }
 }
 
@@ -260,11 +291,11 @@ __global__ void k_mg_finish(MergeArgs a, const unsigned long long *__restrict__ 
                             const unsigned long long *__restrict__ rl) {
     const uint64_t st = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (st >= 2 * a.n || !is_m(a, st >> 1)) return;
-    const unsigned o = a.own[st];
-    if (o != kNone) {
-        const unsigned p = a.rpos[o];
+    const unsigned long long oo = a.oo[st];
+    if (oo != ~0ull) {
+        const unsigned p = (unsigned)(oo >> 32);
         if (rn[p] & kTerm) {
-            a.len[st] = (unsigned)(rl[p] - a.off[st]);
+            a.len[st] = (unsigned)(rl[p] - (oo & 0xffffffffull));
             a.term[st] = rn[p];
             return;
         }
@@ -342,6 +373,13 @@ __global__ void k_mg_cyc_done(MergeArgs a, uint64_t c, const unsigned long long 
 }
 
 // ---- chains
+// End arcs compare by (key of the end node, slot). Only end nodes' keys are
+// read here: a small, cache-resident set.
+__device__ __forceinline__ bool arc_less(const MergeArgs &a, uint64_t x, uint64_t y) {
+    const unsigned long long kx = a.keys[x >> 3], ky = a.keys[y >> 3];
+    return kx < ky || (kx == ky && (x & 7) < (y & 7));
+}
+
 struct ChainPos {
     unsigned m, pos;
     uint64_t start;  // the smaller end arc code: the chain's start
@@ -353,7 +391,7 @@ __device__ __forceinline__ ChainPos chain_pos(const MergeArgs &a, uint64_t i) {
     const unsigned la = a.len[2 * i], lb = a.len[2 * i + 1];
     const uint64_t beta = a.term[2 * i] & ~kTerm, alpha = a.term[2 * i + 1] & ~kTerm;
     c.m = la + lb - 1;
-    c.fwd = alpha < beta;  // nodes are in key order, so arc codes order by (key, slot)
+    c.fwd = arc_less(a, alpha, beta);
     c.pos = c.fwd ? lb : la;
     c.start = c.fwd ? alpha : beta;
     return c;
@@ -425,13 +463,20 @@ __device__ __forceinline__ uint64_t first_state(unsigned v) {
     return 2 * (uint64_t)(v >> 1) + ((v & 1u) ? 0 : 1);
 }
 
-__global__ void k_mg_line_len(MergeArgs a, uint64_t *__restrict__ out) {
+// The nodes left (not merged away), listed for the key-order sort.
+__global__ void k_mg_survivors(MergeArgs a) {
     const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= a.n) return;
-    if (is_m(a, j)) {
-        out[j] = 0;
-        return;
-    }
+    if (j >= a.n || is_m(a, j)) return;
+    const unsigned long long q = agg_inc(&a.ctr[5]);
+    a.skey[q] = a.keys[j];
+    a.sidx[q] = (unsigned)j;
+}
+
+__global__ void k_mg_line_len(MergeArgs a, const unsigned *__restrict__ order, uint64_t n_lines,
+                              uint64_t *__restrict__ out) {
+    const uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_lines) return;
+    const uint64_t j = order[q];
     const uint64_t m = a.mult[j];
     uint64_t l = 69;
     for (int s = 0; s < 8; ++s) {
@@ -439,14 +484,16 @@ __global__ void k_mg_line_len(MergeArgs a, uint64_t *__restrict__ out) {
         const unsigned v = a.nb[j * 8 + s];
         l += 1 + (is_m(a, v >> 1) ? a.len[first_state(v)] : 0);
     }
-    out[j] = l;
+    out[q] = l;
 }
 
-__global__ void k_mg_line_write(MergeArgs a, const uint64_t *__restrict__ off, char *__restrict__ text) {
-    const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= a.n || is_m(a, j)) return;
+__global__ void k_mg_line_write(MergeArgs a, const unsigned *__restrict__ order, uint64_t n_lines,
+                                const uint64_t *__restrict__ off, char *__restrict__ text) {
+    const uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_lines) return;
+    const uint64_t j = order[q];
     const uint64_t m = a.mult[j];
-    char *const start = text + off[j];
+    char *const start = text + off[q];
     char *p = put_u64(start, a.keys[j]);
     unsigned mm[8];
     uint64_t vlen = 69;
@@ -460,9 +507,10 @@ __global__ void k_mg_line_write(MergeArgs a, const uint64_t *__restrict__ off, c
             if (is_m(a, v >> 1)) {
                 const uint64_t st = first_state(v);
                 const uint64_t mine = j * 8 + s, other = a.term[st] & ~kTerm;
-                const unsigned id = a.chain_of[min(mine, other)];
+                const bool first = arc_less(a, mine, other);  // this end starts the chain
+                const unsigned id = a.chain_of[first ? mine : other];
                 const unsigned long long dest = (unsigned long long)(p - text);
-                if (mine < other) a.ch_dfwd[id] = dest;
+                if (first) a.ch_dfwd[id] = dest;
                 else a.ch_drev[id] = dest;
                 mm[s] = a.ent[a.ch_eoff[id]];
                 l += a.len[st];
@@ -514,72 +562,58 @@ swg_status merge_graph(const unsigned long long *d_keys, const unsigned long lon
     std::memset(&a, 0, sizeof(a));
     a.k = k;
     a.n = n;
-    unsigned long long *keys = nullptr, *mult = nullptr, *ctr = nullptr;
+    unsigned long long *ctr = nullptr;
     uint64_t hcap = 1024;
     while (hcap < 2 * n) hcap *= 2;
     a.hmask = hcap - 1;
-    uint64_t *lens = nullptr, *loff = nullptr;
-    if (!scr.get(&keys, n) || !scr.get(&mult, n) || !scr.get(&a.hk, hcap) || !scr.get(&a.hv, hcap) ||
-        !scr.get(&a.nb, 8 * n) || !scr.get(&a.fl, n) || !scr.get(&a.succ, 2 * n) || !scr.get(&a.own, 2 * n) ||
-        !scr.get(&a.off, 2 * n) || !scr.get(&a.rpos, 2 * n) || !scr.get(&a.rlist, 2 * n) ||
+    if (!scr.get(&a.ht, hcap) || !scr.get(&a.nb, 8 * n) || !scr.get(&a.fl, n) || !scr.get(&a.succ, 2 * n) ||
+        !scr.get(&a.oo, 2 * n) || !scr.get(&a.rpos, 2 * n) || !scr.get(&a.rlist, 2 * n) ||
         !scr.get(&a.len, 2 * n) || !scr.get(&a.term, 2 * n) || !scr.get(&a.clist, 2 * n) ||
-        !scr.get(&a.chain_of, 8 * n) || !scr.get(&ctr, 8 + 2 * kClasses) || !scr.get(&a.err, 1) ||
-        !scr.get(&lens, n) || !scr.get(&loff, n + 1))
+        !scr.get(&a.chain_of, 8 * n) || !scr.get(&ctr, 8 + 2 * kClasses) || !scr.get(&a.err, 1))
         return cuda_err(cudaErrorMemoryAllocation, "merge workspace");
     a.ctr = ctr;
     a.cls_count = ctr + 8;
     a.cls_cursor = ctr + 8 + kClasses;
+    a.keys = d_keys;
+    a.mult = d_mult;
     EMIT_CUDA(cudaMemsetAsync(ctr, 0, (8 + 2 * kClasses) * sizeof(unsigned long long), s), "merge clear");
     EMIT_CUDA(cudaMemsetAsync(a.err, 0, sizeof(unsigned), s), "merge clear");
-    EMIT_CUDA(cudaMemsetAsync(a.hk, 0xff, hcap * sizeof(unsigned long long), s), "merge clear");
-    EMIT_CUDA(cudaMemsetAsync(a.own, 0xff, 2 * n * sizeof(unsigned), s), "merge clear");
-    // nodes in key order: lines come out sorted and arc codes compare like (key, slot)
-    if (n) {
-        size_t tb = 0;
-        EMIT_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, d_keys, keys, d_mult, mult, (int64_t)n, 0, 2 * k, s),
-                  "sort size");
-        unsigned char *tmp = nullptr;
-        if (!scr.get(&tmp, tb)) return cuda_err(cudaErrorMemoryAllocation, "sort scratch");
-        EMIT_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tb, d_keys, keys, d_mult, mult, (int64_t)n, 0, 2 * k, s),
-                  "sort");
-    }
-    a.keys = keys;
-    a.mult = mult;
+    EMIT_CUDA(cudaMemsetAsync(a.ht, 0xff, hcap * sizeof(ulonglong2), s), "merge clear");
+    EMIT_CUDA(cudaMemsetAsync(a.oo, 0xff, 2 * n * sizeof(unsigned long long), s), "merge clear");
     int launches = 0;
     k_mg_index<<<blocks(n), 256, 0, s>>>(a);
     k_mg_classify<<<blocks(n), 256, 0, s>>>(a);
     k_mg_states<<<blocks(n), 256, 0, s>>>(a);
-    k_mg_rulers<<<blocks(2 * n), 256, 0, s>>>(a);
-    launches += 4;
-    unsigned long long h[5];
+    launches += 3;
+    // rulers: at most one per state; counts stay on the device
+    if (!scr.get(&a.rn0, 2 * n) || !scr.get(&a.rn1, 2 * n) || !scr.get(&a.rl0, 2 * n) || !scr.get(&a.rl1, 2 * n))
+        return cuda_err(cudaErrorMemoryAllocation, "ruler list");
+    int sms = 0;
+    EMIT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0), "device attribute");
+    const unsigned wgrid = (unsigned)std::max(1, sms * 8);
+    k_mg_rpos<<<wgrid, 256, 0, s>>>(a);
+    k_mg_walk<<<wgrid, 256, 0, s>>>(a);
+    const int rounds = ceil_log2(std::max<uint64_t>(2 * n, 1)) + 1;
+    unsigned long long *bn[2] = {a.rn0, a.rn1}, *bl[2] = {a.rl0, a.rl1};
+    for (int r = 0; r < rounds; ++r)
+        k_mg_rjump<<<wgrid, 256, 0, s>>>(bn[r & 1], bl[r & 1], bn[(r + 1) & 1], bl[(r + 1) & 1], ctr);
+    launches += 2 + rounds;
+    const unsigned long long *rn = bn[rounds & 1], *rl = bl[rounds & 1];
+    k_mg_finish<<<blocks(2 * n), 256, 0, s>>>(a, rn, rl);
+    ++launches;
+    unsigned long long h[6];
     unsigned herr = 0;
-    EMIT_CUDA(cudaMemcpyAsync(h, ctr, sizeof(h), cudaMemcpyDeviceToHost, s), "ruler count");
+    EMIT_CUDA(cudaMemcpyAsync(h, ctr, sizeof(h), cudaMemcpyDeviceToHost, s), "cycle count");
     EMIT_CUDA(cudaMemcpyAsync(&herr, a.err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "merge status");
-    EMIT_CUDA(cudaStreamSynchronize(s), "ruler count");
-    if (herr) {
+    EMIT_CUDA(cudaStreamSynchronize(s), "cycle count");
+    if (herr & (kErrIndex | kErrNeighbour)) {
         set_error("merge: node index or neighbour lookup failed (arc without its neighbour k-molecule)");
         return SWG_ERR_BAD_INPUT;
     }
-    const uint64_t n_rul = h[0];
-    if (!scr.get(&a.rn0, n_rul) || !scr.get(&a.rn1, n_rul) || !scr.get(&a.rl0, n_rul) || !scr.get(&a.rl1, n_rul))
-        return cuda_err(cudaErrorMemoryAllocation, "ruler list");
-    const unsigned long long *rn = a.rn0, *rl = a.rl0;
-    if (n_rul) {
-        k_mg_walk<<<blocks(n_rul), 256, 0, s>>>(a, n_rul);
-        ++launches;
-        const int rounds = ceil_log2(n_rul) + 1;
-        unsigned long long *bn[2] = {a.rn0, a.rn1}, *bl[2] = {a.rl0, a.rl1};
-        for (int r = 0; r < rounds; ++r) {
-            k_mg_rjump<<<blocks(n_rul), 256, 0, s>>>(bn[r & 1], bl[r & 1], bn[(r + 1) & 1], bl[(r + 1) & 1], n_rul);
-            ++launches;
-        }
-        rn = bn[rounds & 1];
-        rl = bl[rounds & 1];
+    if (herr) {
+        set_error("merge: a walk did not end (internal error)");
+        return SWG_ERR_TIMEOUT;
     }
-    k_mg_finish<<<blocks(2 * n), 256, 0, s>>>(a, rn, rl);
-    ++launches;
-    EMIT_CUDA(cudaMemcpyAsync(h, ctr, sizeof(h), cudaMemcpyDeviceToHost, s), "cycle count");
-    EMIT_CUDA(cudaStreamSynchronize(s), "cycle count");
     const uint64_t n_cyc_states = h[1];
     if (n_cyc_states) {
         if (!scr.get(&a.cx0, 2 * n) || !scr.get(&a.cx1, 2 * n) || !scr.get(&a.cy0, 2 * n) ||
@@ -633,12 +667,33 @@ swg_status merge_graph(const unsigned long long *d_keys, const unsigned long lon
         k_mg_level<<<blocks(pairs), 256, 0, s>>>(a, pairs, t);
         ++launches;
     }
-    k_mg_line_len<<<blocks(n), 256, 0, s>>>(a, lens);
+    // the nodes left, in key order
+    const uint64_t n_lines = n - h[4] + h[3];
+    unsigned long long *skey2 = nullptr;
+    unsigned *sidx2 = nullptr;
+    uint64_t *lens = nullptr, *loff = nullptr;
+    if (!scr.get(&a.skey, n_lines) || !scr.get(&a.sidx, n_lines) || !scr.get(&skey2, n_lines) ||
+        !scr.get(&sidx2, n_lines) || !scr.get(&lens, n_lines) || !scr.get(&loff, n_lines + 1))
+        return cuda_err(cudaErrorMemoryAllocation, "line workspace");
+    k_mg_survivors<<<blocks(n), 256, 0, s>>>(a);
     ++launches;
-    swg_status st = scan_lengths(lens, loff, n, scr, s);
+    if (n_lines) {
+        size_t tb = 0;
+        EMIT_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, a.skey, skey2, a.sidx, sidx2, (int64_t)n_lines, 0,
+                                                  2 * k, s),
+                  "sort size");
+        unsigned char *tmp = nullptr;
+        if (!scr.get(&tmp, tb)) return cuda_err(cudaErrorMemoryAllocation, "sort scratch");
+        EMIT_CUDA(cub::DeviceRadixSort::SortPairs(tmp, tb, a.skey, skey2, a.sidx, sidx2, (int64_t)n_lines, 0,
+                                                  2 * k, s),
+                  "sort");
+        k_mg_line_len<<<blocks(n_lines), 256, 0, s>>>(a, sidx2, n_lines, lens);
+        ++launches;
+    }
+    swg_status st = scan_lengths(lens, loff, n_lines, scr, s);
     if (st) return st;
     uint64_t bytes = 0;
-    EMIT_CUDA(cudaMemcpyAsync(&bytes, loff + n, 8, cudaMemcpyDeviceToHost, s), "text size");
+    EMIT_CUDA(cudaMemcpyAsync(&bytes, loff + n_lines, 8, cudaMemcpyDeviceToHost, s), "text size");
     EMIT_CUDA(cudaStreamSynchronize(s), "text size");
     if (bytes + 1 > *text_cap) {
         if (*d_text) cudaFree(*d_text);
@@ -647,17 +702,17 @@ swg_status merge_graph(const unsigned long long *d_keys, const unsigned long lon
         EMIT_CUDA(cudaMalloc((void **)d_text, bytes + 1), "merged text");
         *text_cap = bytes + 1;
     }
-    k_mg_line_write<<<blocks(n), 256, 0, s>>>(a, loff, *d_text);
+    if (n_lines) k_mg_line_write<<<blocks(n_lines), 256, 0, s>>>(a, sidx2, n_lines, loff, *d_text);
     k_mg_chars<<<blocks(n), 256, 0, s>>>(a, *d_text);
     launches += 2;
     EMIT_CUDA(cudaMemsetAsync(*d_text + bytes, '\n', 1, s), "merged text");
     EMIT_CUDA(cudaGetLastError(), "merge kernels");
     EMIT_CUDA(cudaStreamSynchronize(s), "merge");
     res->text_bytes = bytes + 1;
-    res->nodes = n - h[4] + h[3];
+    res->nodes = n_lines;
     res->chains = n_chains;
     res->cycles = h[3];
-    res->rulers = n_rul;
+    res->rulers = h[0];
     res->launches = launches + 3;  // + the scan
     return SWG_OK;
 }
