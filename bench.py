@@ -66,6 +66,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-samples measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-requests measurement")
+    ap.add_argument("--no-merge", action="store_true", help="skip the merge-stage measurement")
     ap.add_argument("--algo", default="default", choices=["default", "direct", "partitioned", "bucketed"])
     ap.add_argument("--order", default="input", choices=["input", "minimizer"],
                     help="read order of the direct algorithm")
@@ -184,6 +185,46 @@ def cpu_baseline(text: bytes, n_bases: int, budget_s: float = 20.0) -> dict:
     return {"value": nb / dt, "unit": "bases/s", "cores": threads, "kind": "port",
             "sample": "first %d of %d bases (framing + count + cutoff, sorted records), %.1f s"
                       % (nb, n_bases, dt)}
+
+
+# Random accesses per k-molecule the GPU merge makes (merge.cu): index insert
+# 1, one neighbour lookup per arc (about 2), the two neighbours' flags 2, per
+# walk state one 16-byte successor load and one label store (4), the chain
+# entry 1 and the two arc-string bases 2.
+MERGE_RANDOM_PER_NODE = 12
+
+
+def merge_metrics(g, survivors: int, steps: int, warmup: int) -> dict:
+    """swg_graph_merge on the graph just built (device time from the library's
+    CUDA events, which cover its host synchronisations too)."""
+    for _ in range(max(warmup, 3)):
+        g.merge()
+    ms = []
+    for _ in range(steps):
+        g.merge()
+        ms.append(g.merge_info()["ms"])
+    info = g.merge_info()
+    m = statistics.median(ms)
+    return {"what": "merging of semi-extended k-molecules (simplifyDistNodeGraph) over the built graph, "
+                    "result = the -d file's text on the device",
+            "ms": m, "ms_all": ms, "k_molecules": survivors, "k_molecules_per_s": survivors / (m * 1e-3),
+            "nodes_left": info["nodes"], "chains": info["chains"], "cycles": info["cycles"],
+            "text_bytes": info["text_bytes"], "launches": info["launches"],
+            "random_accesses_per_k_molecule": MERGE_RANDOM_PER_NODE}
+
+
+def merge_cpu_baseline(g, k: int) -> dict:
+    """The CPU restatement of the merge (one thread) on the same k-molecules."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    keys, mult = g.copy_out(sorted=True)
+    t0 = time.perf_counter()
+    order = oracle.merge_tree_order(keys, mult.reshape(-1, 8), k)
+    oracle.merge_text(keys, mult.reshape(-1, 8), k, order=order)
+    dt = time.perf_counter() - t0
+    return {"value": keys.size / dt, "unit": "k-molecules/s", "cores": 1, "kind": "port",
+            "sample": "the whole graph: %d k-molecules (visiting order + merge + text), %.1f s"
+                      % (keys.size, dt)}
 
 
 def batched_samples(n: int = 256, seed: int = 4) -> list[dict]:
@@ -466,6 +507,9 @@ def main() -> int:
     ms_per_step = max_over_ranks(statistics.mean(step_ms), world, dev)
     value = aggregate_value(n_bases, world, ms_per_step)
     survivors, distinct = g.size(), g.distinct()
+    merge = None
+    if rank == 0 and not args.no_merge:
+        merge = merge_metrics(g, survivors, args.steps, args.warmup)
 
     # ---- end to end through the C ABI on pinned host buffers ----
     lib = swapgb.lib()
@@ -562,10 +606,12 @@ def main() -> int:
         r_red = swapgb.probe_random_access("red_add_u32", table_bytes, 1 << 31, stream.cuda_stream)
         r_pat = swapgb.probe_random_access("load16_cas128", table_bytes, 1 << 30, stream.cuda_stream)
         r_l2 = swapgb.probe_random_access("load16_cas128", 48 << 20, 1 << 30, stream.cuda_stream)
+        r_x4 = swapgb.probe_random_access("load16_x4", table_bytes, 1 << 29, stream.cuda_stream)
         # per read of length L: (L-k+1) key probes + 2(L-k) slot increments
         ops = n_occ + 2 * (n_occ - n_with_occ)
         count_ms = mean_ms[3] if used == swapgb.ALGO_BUCKETED else mean_ms[2]
         atomic = {"R_red_add_u32_per_s": r_red, "dram_load16_cas128_per_s": r_pat,
+                  "dram_load16_per_s_4_in_flight": r_x4,
                   "l2_load16_cas128_per_s": r_l2, "table_bytes": table_bytes,
                   "ops_per_step": ops, "achieved_ops_per_s": ops / (mean_ms[4] * 1e-3),
                   "frac_of_R": ops / (mean_ms[4] * 1e-3) / r_red,
@@ -579,9 +625,18 @@ def main() -> int:
     served = None
     if rank == 0 and not args.no_serve and not args.reads:
         served = served_metrics()
+    if merge and atomic:
+        achieved = MERGE_RANDOM_PER_NODE * survivors / (merge["ms"] * 1e-3)
+        peak = atomic["dram_load16_per_s_4_in_flight"]
+        merge["roofline"] = {"bound": "random access", "achieved": achieved, "peak": peak,
+                             "unit": "accesses/s", "frac": achieved / peak,
+                             "peak_source": "random 16-byte loads, four in flight per thread, over a "
+                                            "16 GiB table: probe of this run"}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(text, n_bases)
+        if merge:
+            merge["cpu_baseline"] = merge_cpu_baseline(g, K)
 
     if rank == 0:
         line = {
@@ -602,6 +657,7 @@ def main() -> int:
             "build": dict(info, phase_ms_mean=mean_ms),
             "roofline": roofline,
             "random_access": atomic,
+            "merge": merge,
             "batched": batched,
             "served": served,
             "cpu_baseline": cpu,

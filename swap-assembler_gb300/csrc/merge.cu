@@ -21,7 +21,7 @@
 // Steps (one stream): open-addressing index key -> node (16-byte entries);
 // per node the neighbour of each arc; for every mergeable node two
 // directed walk states; list ranking of the walks with a sparse ruling set
-// (every 64th state on average plus every walk head starts a ruler; a ruler
+// (one state in 16..256 — up to about 2^20 rulers — plus every walk head starts a ruler; a ruler
 // walks to the next one, then the rulers' own list is ranked by pointer
 // jumping); cycles (states no ruler reaches, or rulers whose list never
 // ends) are found, cut and ranked by pointer jumping; chains are laid out in
@@ -87,6 +87,7 @@ __device__ __forceinline__ unsigned long long agg_add_labeled(unsigned long long
 struct MergeArgs {
     int k;
     uint64_t n;
+    uint64_t rmask;  // ruler sampling: one state in rmask + 1
     const unsigned long long *keys;
     const unsigned long long *mult;  // byte s = multiplicity of slot s
     ulonglong2 *ht;                  // index: x = key (kEmptyKey when free), y = node
@@ -199,7 +200,7 @@ __device__ __forceinline__ unsigned long long walk_next(const MergeArgs &a, uint
     return kTerm | (j * 8 + (side ? 4 : 0) + 3 - first);
 }
 
-__device__ __forceinline__ bool ruler_of(uint64_t st, const ulonglong2 &pair);
+__device__ __forceinline__ bool ruler_of(const MergeArgs &a, uint64_t st, const ulonglong2 &pair);
 
 // Both walk states of a merged node, and which of them start rulers.
 __global__ void k_mg_states(MergeArgs a) {
@@ -208,7 +209,7 @@ __global__ void k_mg_states(MergeArgs a) {
     const ulonglong2 pair = make_ulonglong2(walk_next(a, i, 0), walk_next(a, i, 1));
     *reinterpret_cast<ulonglong2 *>(a.succ + 2 * i) = pair;
     for (int d = 0; d < 2; ++d) {
-        if (!ruler_of(2 * i + d, pair)) continue;
+        if (!ruler_of(a, 2 * i + d, pair)) continue;
         const unsigned p = (unsigned)agg_inc(&a.ctr[0]);
         a.rlist[p] = (unsigned)(2 * i + d);
     }
@@ -220,10 +221,12 @@ __device__ __forceinline__ ulonglong2 succ_pair(const MergeArgs &a, uint64_t st)
 }
 
 // A ruler: the first state of a walk (its twin leaves to an end) or, on
-// average, one state in 64.
-__device__ __forceinline__ bool ruler_of(uint64_t st, const ulonglong2 &pair) {
+// average, one state in rmask + 1 (16..256, chosen for at most about 2^20 rulers:
+// enough walkers to keep the SMs' warp slots busy while each walk's loads
+// wait on memory one after the other, and a ruler list small enough for L2).
+__device__ __forceinline__ bool ruler_of(const MergeArgs &a, uint64_t st, const ulonglong2 &pair) {
     const unsigned long long twin = (st & 1) ? pair.x : pair.y;
-    return (twin & kTerm) || (fmix64(st) & 63) == 0;
+    return (twin & kTerm) || (fmix64(st) & a.rmask) == 0;
 }
 
 // The ruler list position of every ruler state (read when a walk meets it).
@@ -256,7 +259,7 @@ __global__ void k_mg_walk(MergeArgs a) {
                 break;
             }
             const ulonglong2 pn = succ_pair(a, nx);
-            if (ruler_of(nx, pn)) {
+            if (ruler_of(a, nx, pn)) {
                 a.rn0[p] = a.rpos[nx];
                 a.rl0[p] = o;
                 done = true;
@@ -562,6 +565,8 @@ swg_status merge_graph(const unsigned long long *d_keys, const unsigned long lon
     std::memset(&a, 0, sizeof(a));
     a.k = k;
     a.n = n;
+    a.rmask = 15;
+    while (a.rmask < 255 && 2 * n / (a.rmask + 1) > (1ull << 20)) a.rmask = 2 * a.rmask + 1;
     unsigned long long *ctr = nullptr;
     uint64_t hcap = 1024;
     while (hcap < 2 * n) hcap *= 2;
