@@ -276,7 +276,8 @@ swg_status swg_graph_write_node_lines(const swg_graph *g, const char *path);
  * level ctz(p), levels in increasing order. A cycle of merged nodes is cut at
  * its largest key, which keeps the cycle on its two arcs. The result stays on
  * the device (as the -d file's text) until the next build. SWG_ERR_BAD_STATE
- * without a single-sample build; the graph must hold at most 2^29 k-molecules. */
+ * without a single-sample build; SWG_ERR_BAD_INPUT for an even k (the
+ * reference's k is odd, sequence.cpp:44) or more than 2^29 k-molecules. */
 swg_status swg_graph_merge(swg_graph *g);
 typedef struct swg_merge_info {
     uint64_t nodes;      /* nodes left (lines of the -d file) */

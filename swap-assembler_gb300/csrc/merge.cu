@@ -560,6 +560,10 @@ swg_status merge_graph(const unsigned long long *d_keys, const unsigned long lon
         set_error("merge: more than 2^29 k-molecules");
         return SWG_ERR_BAD_INPUT;
     }
+    if (k % 2 == 0) {  // the reference's k is odd (sequence.cpp:44): no k-mer is its own reverse complement
+        set_error("merge: k must be odd (an even k-mer can be its own reverse complement)");
+        return SWG_ERR_BAD_INPUT;
+    }
     Scratch scr(s);
     MergeArgs a;
     std::memset(&a, 0, sizeof(a));

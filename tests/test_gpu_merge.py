@@ -119,6 +119,9 @@ def test_merge_file_and_states(tmp_path):
     g.build_batch(swapgb.Opts(), [(r, case["k"], case["c"])])
     with pytest.raises(swapgb.SwgError):
         g.merge()  # batched results are per sample
+    g.build_fasta(swapgb.Opts(k=20, cutoff=2), case_text(case))
+    with pytest.raises(swapgb.SwgError):
+        g.merge()  # even k
 
 
 def test_cli_writes_contig_graph(tmp_path):
