@@ -3,11 +3,9 @@ restatement run in the same visiting order with every message applied at
 once (oracle/merge_oracle.c). The lines must be identical (the device writes
 them in key order, the restatement in visiting order, so lines are compared
 as sorted sets), and the file sizes equal."""
-import os
 import subprocess
 from pathlib import Path
 
-import numpy as np
 import pytest
 
 import oracle
