@@ -19,6 +19,7 @@ LIB_PATH = HERE / "build" / "liboracle.so"
 ORACLE_BIN = HERE / "build" / "swap_oracle"
 REF_SWAP = HERE / "_ref" / "swap"
 REF_DUMP = HERE / "_ref" / "ref_dump"
+REF_CONTIGS = HERE / "_ref" / "ref_contigs"
 
 ERRORS = {0: "ok", -1: "no record start", -2: "unterminated record", -3: "NUL byte",
           -4: "bad k", -5: "out of memory"}
@@ -199,7 +200,7 @@ def parse_node_lines(text: bytes) -> tuple[np.ndarray, np.ndarray]:
 # ---- the reference itself (only where it was compiled from its sources) ----
 
 def reference_available() -> bool:
-    return REF_SWAP.exists() and REF_DUMP.exists()
+    return REF_SWAP.exists() and REF_DUMP.exists() and REF_CONTIGS.exists()
 
 
 def run_reference(fasta_path: str, k: int, cutoff: int, outdir: str, timeout: float = 600) -> dict:
@@ -244,6 +245,32 @@ def run_reference_merge(fasta_path: str, k: int, cutoff: int, outdir: str,
     if r.returncode != 0:
         raise RuntimeError("reference merge failed: %s" % r.stdout[-2000:])
     return Path(outdir, "nodes.txt").read_bytes(), Path(outdir, "contigGraph.txt").read_bytes()
+
+
+def run_reference_contigs(merged_path: str, k: int, cutoff: int, outdir: str,
+                          timeout: float = 600) -> tuple[list[str], list[str]]:
+    """The reference's own rank-0 contig stage (graph.cpp:3629-3683) on a -d
+    file: sorted sequences of noCEcontigs.fasta and CEContig.fasta."""
+    r = subprocess.run([str(REF_CONTIGS), "-k", str(k), "-c", str(cutoff), "-i", str(merged_path),
+                        "-o", str(outdir)], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                       timeout=timeout, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference contig stage failed: %s" % r.stdout[-2000:])
+    return contig_sequences(Path(outdir, "noCEcontigs.fasta")), contig_sequences(Path(outdir, "CEContig.fasta"))
+
+
+def contig_sequences(path) -> list[str]:
+    """Sequences of a reference contig file: printContigs puts each on its
+    header line after '>procN: ' (graph.cpp:1189), masterPrintContigs on the
+    line after its header."""
+    out = []
+    for line in Path(path).read_text().splitlines():
+        line = line.strip()
+        if line.startswith(">proc"):
+            out.append(line.split(": ", 1)[1])
+        elif line and not line.startswith(">"):
+            out.append(line)
+    return sorted(out)
 
 
 def cores() -> int:

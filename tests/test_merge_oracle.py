@@ -7,6 +7,7 @@ not depend on the visiting order, and a complete merge leaves no mergeable
 node."""
 import hashlib
 import json
+import subprocess
 from pathlib import Path
 
 import numpy as np
@@ -122,3 +123,34 @@ def test_merge_tree_order_is_a_permutation():
 
 def test_merge_of_nothing_is_one_newline():
     assert oracle.merge_text(np.zeros(0, np.uint64), np.zeros((0, 8), np.uint8), 21) == b"\n"
+
+
+def _rc(s: str) -> str:
+    return s[::-1].translate(str.maketrans("ACGT", "TGCA"))
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference not compiled here")
+@pytest.mark.parametrize("case", [MERGE_CASES[0], MERGE_CASES[1], MERGE_CASES[3]] +
+                         [c for c in SYNTH_CASES if c["name"] == "c1_small"], ids=lambda c: c["name"])
+def test_reference_contig_stage_reads_the_complete_merge(case, tmp_path):
+    """Drop-in at the file seam: the reference's own contig stage, fed the
+    complete merge (the GPU's output), prints the contigs of the reference's
+    own run (noCEcontigs.fasta: arc strings only, no multiplicities) — except
+    where the reference's lost last merge splits a contig in two: each
+    contig only the reference prints is a piece of one only ours prints."""
+    k, c = case["k"], case["c"]
+    fa = tmp_path / "in.fa"
+    fa.write_bytes(case_text(case))
+    r = subprocess.run([str(oracle.REF_SWAP), "-k", str(k), "-c", str(c), "-i", str(fa), "-o",
+                        str(tmp_path / "ref"), "-d"], stdout=subprocess.DEVNULL, timeout=600)
+    assert r.returncode == 0
+    theirs = set(oracle.contig_sequences(tmp_path / "ref" / "noCEcontigs.fasta"))
+    keys, mult = oracle.records(case_text(case), k, c)
+    merged = tmp_path / "contigGraph.txt"
+    merged.write_bytes(oracle.merge_text(keys, mult, k))
+    ours_list, _ = oracle.run_reference_contigs(str(merged), k, c, str(tmp_path / "ours"))
+    ours = set(ours_list)
+    only_ours, only_theirs = ours - theirs, theirs - ours
+    assert len(only_ours) <= 1
+    for piece in only_theirs:
+        assert any(piece in s or _rc(piece) in s for s in only_ours)
