@@ -23,6 +23,8 @@
  *                                                -> swg_graph_merge
  *   distNodeGraph::gatherDistNodeGraph, -d file  graph.cpp:576-696, 3617-3621
  *                                                -> swg_graph_write_merged / swg_graph_copy_merged
+ *   distNodeGraph::masterTipsRemoval ........... graph.cpp:2194-2265 -> swg_graph_remove_tips
+ *   distNodeGraph::masterLowCoverageEdgeRemoval  graph.cpp:2267-2300 -> swg_graph_remove_low_coverage
  *
  * Packed read layout (host or device memory):
  *   packed   uint32 words; base i of the concatenated read stream sits in
@@ -295,6 +297,23 @@ swg_status swg_graph_merge_info(const swg_graph *g, swg_merge_info *info);
  * cap >= the text size (*n receives it either way). */
 swg_status swg_graph_write_merged(const swg_graph *g, const char *path);
 swg_status swg_graph_copy_merged(const swg_graph *g, char *buf, uint64_t cap, uint64_t *n);
+/* Two of the reference's rank-0 passes over the merged graph (after
+ * swg_graph_merge; the merged text is rewritten, deleted and arc-less nodes
+ * left out as gatherDistNodeGraph does):
+ * remove_tips = masterTipsRemoval (graph.cpp:2194-2265): a node with exactly
+ *   one arc, shorter than k, loses it, the far node loses its arc back, and
+ *   the node is deleted. Every node that is a tip when the pass starts is
+ *   judged on that state (the reference's one pass visiting all other nodes
+ *   first, then the tips in key order); of two tips joined only to each other
+ *   the smaller key is deleted. *removed = nodes deleted.
+ * remove_low_coverage = masterLowCoverageEdgeRemoval (graph.cpp:2267-2300):
+ *   avg = sum(len*m)/sum(len) over the arcs left (integer division); every
+ *   arc shorter than 2k with m < avg/4 is cut. *cut = arcs cut (both ends of
+ *   an edge count). With no arc left nothing is cut (the reference divides by
+ *   zero). Neither pass merges the nodes it leaves with one arc per side (the
+ *   reference's masterSimplifyNodeGraph does that next). */
+swg_status swg_graph_remove_tips(swg_graph *g, uint64_t *removed);
+swg_status swg_graph_remove_low_coverage(swg_graph *g, uint64_t *cut);
 /* Host-only writers for records already in host memory (keys[n], mult[8*n],
  * any order): the same two file formats as above. */
 swg_status swg_records_write_kmer_graph(const uint64_t *keys, const uint8_t *mult, uint64_t n,

@@ -85,6 +85,15 @@ void oracle_free_text(char *text);
 /* The visiting order the GPU merge follows (see merge_oracle.c). */
 int oracle_merge_tree_order(int k, uint64_t n, const uint64_t *keys, const uint8_t *mult, uint64_t *order);
 
+/* Rank-0 passes over a merged graph given as gathered node lines (the -d
+ * file): passes bit 0 = masterTipsRemoval (graph.cpp:2194-2265), bit 1 =
+ * masterLowCoverageEdgeRemoval (graph.cpp:2267-2300), in that order. Nodes are
+ * visited in `order` (indices of the input's lines; NULL = file order); the
+ * result is written as gathered lines in that order (+ '\n'). *count receives
+ * the tips removed plus the arcs cut. */
+int oracle_prune(int k, const char *text, uint64_t len, const uint64_t *order, int passes, char **out,
+                 uint64_t *out_len, uint64_t *count);
+
 /* Neighbour id printed in kmerGraph.txt for slot s of key K (graph.cpp:3380-3427). */
 uint64_t oracle_kmer_graph_neighbour(uint64_t key, int slot, int k);
 uint64_t oracle_revcomp(uint64_t x, int k);

@@ -508,3 +508,176 @@ int oracle_merge_tree_order(int k, uint64_t n, const uint64_t *keys, const uint8
     mgraph_free(&g);
     return rc;
 }
+
+/* ---------------------------------------------------------------------------
+ * Two of the reference's rank-0 passes over a merged graph, restated:
+ *   masterTipsRemoval            graph.cpp:2194-2265 (one pass)
+ *   masterLowCoverageEdgeRemoval graph.cpp:2267-2300
+ * The graph comes as gathered node lines (the -d file, parsed as
+ * recvBufDistNodeGraph does, graph.cpp:845-896); nodes are visited in a
+ * given order of its lines, and the result is written as gathered lines in
+ * that order (deleted and arc-less nodes skipped, graph.cpp:587-596).
+ * ------------------------------------------------------------------------- */
+
+static int parse_lines(mgraph *g, int k, const char *text, uint64_t len, uint64_t **keys_out) {
+    static const int8_t code[256] = {['A'] = 1, ['C'] = 2, ['G'] = 3, ['T'] = 4};
+    uint64_t cap = 1024, n = 0;
+    uint64_t *keys = (uint64_t *)malloc(cap * 8);
+    uint8_t(*mult)[8] = (uint8_t(*)[8])malloc(cap * 8);
+    mstr(*arcs)[8] = (mstr(*)[8])calloc(cap, sizeof(mstr[8]));
+    const char *p = text, *end = text + len;
+    int rc = 0;
+    while (!rc && p < end) {
+        while (p < end && (*p == '\n' || *p == ' ')) ++p;
+        if (p >= end || *p == 0) break;
+        if (n == cap) {
+            cap *= 2;
+            keys = (uint64_t *)realloc(keys, cap * 8);
+            mult = (uint8_t(*)[8])realloc(mult, cap * 8);
+            arcs = (mstr(*)[8])realloc(arcs, cap * sizeof(mstr[8]));
+            memset(arcs + n, 0, (cap - n) * sizeof(mstr[8]));
+        }
+        uint64_t id = 0;
+        while (p < end && *p >= '0' && *p <= '9') id = id * 10 + (uint64_t)(*p++ - '0');
+        while (p < end && *p == ' ') ++p;
+        for (int i = 0; i < 8 && !rc; ++i) {
+            const char *e = p;
+            while (e < end && *e != '#') ++e;
+            if (e >= end) {
+                rc = ORACLE_ERR_NO_RECORD;
+                break;
+            }
+            for (const char *q = p; q < e; ++q) {
+                uint8_t b = (uint8_t)(code[(unsigned char)*q] - 1);
+                if (mstr_append(&arcs[n][i], &b, 1)) rc = ORACLE_ERR_OOM;
+            }
+            p = e + 2; /* '#' and the blank after it */
+        }
+        for (int i = 0; i < 8 && !rc; ++i) {
+            int v = 0;
+            while (p < end && *p >= '0' && *p <= '9') v = v * 10 + (*p++ - '0');
+            mult[n][i] = (uint8_t)v;
+            while (p < end && *p == ' ') ++p;
+        }
+        keys[n++] = id;
+        while (p < end && *p == '\n') ++p;
+    }
+    memset(g, 0, sizeof(*g));
+    g->k = k;
+    g->n = n;
+    g->keys = keys;
+    g->mult = mult;
+    g->arcs = arcs;
+    g->deleted = (uint8_t *)calloc(n ? n : 1, 1);
+    g->locked = (uint8_t *)calloc(n ? n : 1, 1);
+    g->hcap = 16;
+    while (g->hcap < 2 * n) g->hcap *= 2;
+    g->hk = (uint64_t *)malloc(g->hcap * 8);
+    g->hv = (int64_t *)malloc(g->hcap * 8);
+    for (uint64_t h = 0; h < g->hcap; ++h) g->hv[h] = -1;
+    for (uint64_t x = 0; x < n; ++x) {
+        uint64_t h = mmix(keys[x]) & (g->hcap - 1);
+        while (g->hv[h] >= 0) h = (h + 1) & (g->hcap - 1);
+        g->hk[h] = keys[x];
+        g->hv[h] = (int64_t)x;
+    }
+    *keys_out = keys;
+    return rc;
+}
+
+static void tips_pass(mgraph *g, const uint64_t *order, uint64_t *removed) {
+    for (uint64_t t = 0; t < g->n; ++t) {
+        const uint64_t x = order[t];
+        if (g->deleted[x]) continue;
+        int num = 0, index = -1;
+        for (int i = 0; i < 8; ++i)
+            if (g->arcs[x][i].len) ++num, index = i;
+        if (num != 1 || g->arcs[x][index].len >= (uint32_t)g->k) continue;
+        uint64_t id;
+        int side;
+        arc_end(g, x, index, &id, &side);
+        const int64_t nx = mfind(g, id);
+        const int ret = nx < 0 ? -1 : src_edge(g, (uint64_t)nx, x, index < 4 ? 0 : 1);
+        if (ret < 0) { /* no arc back: only the tip's own arc goes */
+            g->mult[x][index] = 0;
+            g->arcs[x][index].len = 0;
+            continue;
+        }
+        if ((uint64_t)nx == x) continue;
+        g->mult[nx][ret] = 0;
+        g->arcs[nx][ret].len = 0;
+        g->mult[x][index] = 0;
+        g->arcs[x][index].len = 0;
+        g->deleted[x] = 1;
+        if (removed) ++*removed;
+    }
+}
+
+static void low_coverage_pass(mgraph *g, const uint64_t *order, uint64_t *cleared) {
+    uint64_t cov = 0, nuc = 0;
+    for (uint64_t x = 0; x < g->n; ++x) {
+        if (g->deleted[x]) continue;
+        for (int i = 0; i < 8; ++i) {
+            nuc += g->arcs[x][i].len;
+            cov += (uint64_t)g->arcs[x][i].len * g->mult[x][i];
+        }
+    }
+    /* the reference divides by zero when no arc is left; here nothing is cut */
+    const uint64_t avg = nuc ? cov / nuc : 0;
+    for (uint64_t t = 0; t < g->n; ++t) {
+        const uint64_t x = order[t];
+        if (g->deleted[x]) continue;
+        for (int i = 0; i < 8; ++i) {
+            /* multiplicity < 0.25 * avgCoverage, exactly: 4 * m < avg */
+            if (g->arcs[x][i].len < 2u * (uint32_t)g->k && 4ull * g->mult[x][i] < avg) {
+                if (g->arcs[x][i].len && cleared) ++*cleared;
+                g->arcs[x][i].len = 0;
+                g->mult[x][i] = 0;
+            }
+        }
+    }
+}
+
+int oracle_prune(int k, const char *text, uint64_t len, const uint64_t *order, int passes, char **out,
+                 uint64_t *out_len, uint64_t *count) {
+    *out = NULL;
+    *out_len = 0;
+    if (count) *count = 0;
+    if (k < 1 || k > 31) return ORACLE_ERR_BAD_K;
+    mgraph g;
+    uint64_t *keys = NULL;
+    int rc = parse_lines(&g, k, text, len, &keys);
+    uint64_t *ord = NULL;
+    if (!rc) {
+        ord = (uint64_t *)malloc((g.n ? g.n : 1) * 8);
+        if (!ord) rc = ORACLE_ERR_OOM;
+        for (uint64_t t = 0; !rc && t < g.n; ++t) ord[t] = order ? order[t] : t;
+    }
+    if (!rc && (passes & 1)) tips_pass(&g, ord, count);
+    if (!rc && (passes & 2)) low_coverage_pass(&g, ord, count);
+    if (!rc) {
+        uint64_t total = 2;
+        for (uint64_t x = 0; x < g.n; ++x) {
+            total += 61;
+            for (int i = 0; i < 8; ++i) total += g.arcs[x][i].len + 1;
+        }
+        char *buf = (char *)malloc(total + 64);
+        if (!buf) {
+            rc = ORACLE_ERR_OOM;
+        } else {
+            char *p = buf;
+            for (uint64_t t = 0; t < g.n; ++t) {
+                const uint64_t x = ord[t];
+                if (g.deleted[x] || !has_arc(&g, x)) continue;
+                p = put_line(p, &g, x);
+            }
+            *p++ = '\n';
+            *out = buf;
+            *out_len = (uint64_t)(p - buf);
+        }
+    }
+    free(ord);
+    mgraph_free(&g);
+    free(keys);
+    return rc;
+}

@@ -62,6 +62,9 @@ def lib() -> C.CDLL:
         L.oracle_free_text.argtypes = [P]
         L.oracle_merge_tree_order.argtypes = [i32, u64, P, P, P]
         L.oracle_merge_tree_order.restype = i32
+        L.oracle_prune.argtypes = [i32, C.c_char_p, u64, P, i32, C.POINTER(C.c_void_p), C.POINTER(u64),
+                                   C.POINTER(u64)]
+        L.oracle_prune.restype = i32
         _lib = L
     return _lib
 
@@ -183,6 +186,57 @@ def merge_text(keys: np.ndarray, mult: np.ndarray, k: int, order=None,
         lib().oracle_free_text(ptr)
 
 
+PRUNE_TIPS = 1
+PRUNE_LOW_COVERAGE = 2
+
+
+def prune_text(text: bytes, k: int, passes: int, order=None) -> tuple[bytes, int]:
+    """masterTipsRemoval (passes & 1) then masterLowCoverageEdgeRemoval
+    (passes & 2) on a merged graph given as gathered node lines, nodes visited
+    in `order` (line indices; default file order). Returns the resulting
+    gathered lines and the tips removed + arcs cut."""
+    ptr, n, cnt = C.c_void_p(), C.c_uint64(), C.c_uint64()
+    if order is not None:
+        order = np.ascontiguousarray(order, dtype=np.uint64)
+    e = lib().oracle_prune(k, text, len(text), order.ctypes.data if order is not None else None, passes,
+                           C.byref(ptr), C.byref(n), C.byref(cnt))
+    if e:
+        raise OracleError(e)
+    try:
+        return (C.string_at(ptr.value, n.value) if n.value else b""), cnt.value
+    finally:
+        lib().oracle_free_text(ptr)
+
+
+def tips_last_order(text: bytes, k: int) -> np.ndarray:
+    """The GPU's visiting order for the tip pass: every node that is not a tip
+    (in key order), then the tips in key order; as line indices of `text`."""
+    keys, tip = [], []
+    for line in text.split(b"\n"):
+        if not line.strip():
+            continue
+        head, rest = line.split(b" ", 1)
+        arcs = [f.strip() for f in rest.split(b"#")[:8]]
+        live = [a for a in arcs if a]
+        keys.append(int(head))
+        tip.append(len(live) == 1 and len(live[0]) < k)
+    idx = sorted(range(len(keys)), key=lambda i: (tip[i], keys[i]))
+    return np.array(idx, dtype=np.uint64)
+
+
+def run_reference_prune(merged_path: str, k: int, cutoff: int, outdir: str,
+                        timeout: float = 600) -> tuple[bytes, bytes, bytes]:
+    """The reference's masterTipsRemoval and masterLowCoverageEdgeRemoval on a
+    -d file: its graph (gathered lines, node map order) before, after the tip
+    pass and after the low-coverage pass."""
+    r = subprocess.run([str(HERE / "_ref" / "ref_prune"), "-k", str(k), "-c", str(cutoff), "-i",
+                        str(merged_path), "-o", str(outdir)], stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, timeout=timeout, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference prune failed: %s" % r.stdout[-2000:])
+    return tuple(Path(outdir, f).read_bytes() for f in ("before.txt", "tips.txt", "lowcov.txt"))
+
+
 def parse_node_lines(text: bytes) -> tuple[np.ndarray, np.ndarray]:
     """Keys and 8 multiplicities from node lines (graph.cpp:569 layout), in
     file order."""
@@ -200,7 +254,7 @@ def parse_node_lines(text: bytes) -> tuple[np.ndarray, np.ndarray]:
 # ---- the reference itself (only where it was compiled from its sources) ----
 
 def reference_available() -> bool:
-    return REF_SWAP.exists() and REF_DUMP.exists() and REF_CONTIGS.exists()
+    return REF_SWAP.exists() and REF_DUMP.exists() and REF_CONTIGS.exists() and (HERE / "_ref" / "ref_prune").exists()
 
 
 def run_reference(fasta_path: str, k: int, cutoff: int, outdir: str, timeout: float = 600) -> dict:

@@ -67,7 +67,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict[str, Path]:
     jobs.append((OBJ / "framing.o", [fr, *headers],
                  [nvcc, *ARCH, "-lineinfo", "-Xcompiler", "-fPIC", *common, "-c", str(fr), "-o",
                   str(OBJ / "framing.o")]))
-    for name in ("emit.cu", "merge.cu"):
+    for name in ("emit.cu", "merge.cu", "prune.cu"):
         src = CSRC / name
         o = OBJ / (name[:-3] + ".o")
         jobs.append((o, [src, CSRC / "text_dev.cuh", *headers],
@@ -95,7 +95,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict[str, Path]:
         list(ex.map(lambda j: _run(j[2]), todo))
 
     lib = PKG / "libswapgb.so"
-    lib_objs = [OBJ / n for n in ("kernels.o", "framing.o", "emit.o", "merge.o", "noalloc.o", "api.o", "reads.o",
+    lib_objs = [OBJ / n for n in ("kernels.o", "framing.o", "emit.o", "merge.o", "prune.o", "noalloc.o", "api.o", "reads.o",
                                   "writers.o", "server.o", "autotune.o")]
     if _stale(lib, lib_objs):
         _run([nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, lib_objs), "-lpthread"])

@@ -138,9 +138,8 @@ struct swg_graph {
     uint64_t seg_cursor_cap = 0;
     unsigned long long *d_bigmeta = nullptr;  // bucketed: big-bucket ranges for the global table
     uint64_t bigmeta_cap = 0;
-    // merged graph (swg_graph_merge): the -d file's text on the device
-    char *d_mtext = nullptr;
-    uint64_t mtext_cap = 0;
+    // merged graph (swg_graph_merge): the -d file's text and its lines on the device
+    swg::MergedGraph mg;
     bool merged = false;
     swg::MergeResult mres;
     float merge_ms = 0;
@@ -1169,7 +1168,7 @@ void swg_graph_free(swg_graph *g) {
     cudaFree(g->d_out2_mult);
     cudaFree(g->d_seg_cursor);
     cudaFree(g->d_bigmeta);
-    cudaFree(g->d_mtext);
+    swg::merged_free(&g->mg);
     cudaFree(g->d_hll_seg);
     cudaFree(g->d_bucket);
     cudaFree(g->d_poff);
@@ -1430,8 +1429,7 @@ swg_status swg_graph_merge(swg_graph *g) {
     g->merged = false;
     cudaEvent_t e0 = g->ev[0], e1 = g->ev[1];
     SWG_CUDA(cudaEventRecord(e0, g->own), "merge timing");
-    st = swg::merge_graph(g->d_out_keys, g->d_out_mult, g->n_out, g->k, g->own, &g->d_mtext, &g->mtext_cap,
-                          &g->mres);
+    st = swg::merge_graph(g->d_out_keys, g->d_out_mult, g->n_out, g->k, g->own, &g->mg, &g->mres);
     if (st) return st;
     SWG_CUDA(cudaEventRecord(e1, g->own), "merge timing");
     SWG_CUDA(cudaEventSynchronize(e1), "merge timing");
@@ -1452,10 +1450,10 @@ swg_status swg_graph_merge_info(const swg_graph *g, swg_merge_info *info) {
     if (!g || !info) return SWG_ERR_BAD_INPUT;
     swg_status st = merged_state(g);
     if (st) return st;
-    info->nodes = g->mres.nodes;
+    info->nodes = g->mg.nodes;
     info->chains = g->mres.chains;
     info->cycles = g->mres.cycles;
-    info->text_bytes = g->mres.text_bytes;
+    info->text_bytes = g->mg.text_bytes;
     info->ms = g->merge_ms;
     info->launches = g->mres.launches;
     return SWG_OK;
@@ -1465,13 +1463,13 @@ swg_status swg_graph_copy_merged(const swg_graph *g, char *buf, uint64_t cap, ui
     if (!g || !n) return SWG_ERR_BAD_INPUT;
     swg_status st = merged_state(g);
     if (st) return st;
-    *n = g->mres.text_bytes;
+    *n = g->mg.text_bytes;
     if (cap < *n || (*n && !buf)) {
         swg::set_error("buffer smaller than the merged text");
         return SWG_ERR_BAD_INPUT;
     }
     SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
-    SWG_CUDA(cudaMemcpyAsync(buf, g->d_mtext, *n, cudaMemcpyDeviceToHost, g->own), "merged text copy");
+    SWG_CUDA(cudaMemcpyAsync(buf, g->mg.text, *n, cudaMemcpyDeviceToHost, g->own), "merged text copy");
     SWG_CUDA(cudaStreamSynchronize(g->own), "merged text copy");
     return SWG_OK;
 }
@@ -1481,7 +1479,30 @@ swg_status swg_graph_write_merged(const swg_graph *g, const char *path) {
     swg_status st = merged_state(g);
     if (st) return st;
     SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
-    return swg::stream_to_file(g->d_mtext, g->mres.text_bytes, path, g->own);
+    return swg::stream_to_file(g->mg.text, g->mg.text_bytes, path, g->own);
+}
+
+// Rank-0 passes of the reference over the merged graph (prune.cu).
+swg_status swg_graph_remove_tips(swg_graph *g, uint64_t *removed) {
+    if (!g) return SWG_ERR_BAD_INPUT;
+    swg_status st = merged_state(g);
+    if (st) return st;
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    uint64_t n = 0;
+    st = swg::prune_tips(&g->mg, g->own, &n);
+    if (removed) *removed = n;
+    return st;
+}
+
+swg_status swg_graph_remove_low_coverage(swg_graph *g, uint64_t *cut) {
+    if (!g) return SWG_ERR_BAD_INPUT;
+    swg_status st = merged_state(g);
+    if (st) return st;
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    uint64_t n = 0;
+    st = swg::prune_low_coverage(&g->mg, g->own, &n);
+    if (cut) *cut = n;
+    return st;
 }
 
 static swg_status sorted_copy(const uint64_t *keys, const uint8_t *mult, uint64_t n,

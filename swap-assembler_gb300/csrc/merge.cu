@@ -490,23 +490,36 @@ __global__ void k_mg_line_len(MergeArgs a, const unsigned *__restrict__ order, u
     out[q] = l;
 }
 
+// Line position of every node left.
+__global__ void k_mg_pos(const unsigned *__restrict__ order, uint64_t n_lines, unsigned *__restrict__ pos_of) {
+    const uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n_lines) pos_of[order[q]] = (unsigned)q;
+}
+
 __global__ void k_mg_line_write(MergeArgs a, const unsigned *__restrict__ order, uint64_t n_lines,
-                                const uint64_t *__restrict__ off, char *__restrict__ text) {
+                                const uint64_t *__restrict__ off, char *__restrict__ text,
+                                const unsigned *__restrict__ pos_of, MergedGraph mg) {
     const uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n_lines) return;
     const uint64_t j = order[q];
     const uint64_t m = a.mult[j];
     char *const start = text + off[q];
     char *p = put_u64(start, a.keys[j]);
+    mg.key[q] = a.keys[j];
+    mg.del[q] = 0;
     unsigned mm[8];
     uint64_t vlen = 69;
+    const uint64_t key = a.keys[j], rk = rc_dev(key, a.k);
     for (int s = 0; s < 8; ++s) {
         *p++ = ' ';
         mm[s] = mbyte(m, s);
+        uint64_t l = 0;
+        unsigned back = kNone;
         if (mm[s]) {
             *p = "ACGT"[s & 3];
             const unsigned v = a.nb[j * 8 + s];
-            uint64_t l = 1;
+            mg.src[8 * q + s] = (unsigned long long)(p - text);
+            l = 1;
             if (is_m(a, v >> 1)) {
                 const uint64_t st = first_state(v);
                 const uint64_t mine = j * 8 + s, other = a.term[st] & ~kTerm;
@@ -517,10 +530,20 @@ __global__ void k_mg_line_write(MergeArgs a, const unsigned *__restrict__ order,
                 else a.ch_drev[id] = dest;
                 mm[s] = a.ent[a.ch_eoff[id]];
                 l += a.len[st];
+                back = pos_of[other >> 3] * 8u + (unsigned)(other & 7);
+            } else {  // one base to the next node left: its arc back, as walk_next finds it
+                const uint64_t o = s < 4 ? key : rk;
+                const unsigned first = (unsigned)(o >> (2 * (a.k - 1))) & 3u;
+                back = pos_of[v >> 1] * 8u + ((v & 1u) ? 4u : 0u) + 3u - first;
             }
             p += l;
             vlen += l;
+        } else {
+            mg.src[8 * q + s] = 0;
         }
+        mg.len[8 * q + s] = (unsigned)l;
+        mg.mult[8 * q + s] = (unsigned char)mm[s];
+        mg.back[8 * q + s] = back;
         *p++ = '#';
     }
     for (int s = 0; s < 8; ++s) {
@@ -553,8 +576,60 @@ int ceil_log2(uint64_t v) {
 
 }  // namespace
 
+// Grows the merged graph's buffers (the text, the spare text for rewrites,
+// the per-line arrays) to hold `bytes` of text and `lines` lines.
+swg_status merged_reserve(MergedGraph *m, uint64_t bytes, uint64_t lines) {
+    if (bytes > m->text_cap) {
+        cudaFree(m->text);
+        cudaFree(m->text2);
+        m->text = m->text2 = nullptr;
+        m->text_cap = m->text2_cap = 0;
+        EMIT_CUDA(cudaMalloc((void **)&m->text, bytes), "merged text");
+        m->text_cap = bytes;
+    }
+    if (lines > m->line_cap || !m->key) {
+        const uint64_t c = std::max<uint64_t>(lines, 1);
+        cudaFree(m->key);
+        cudaFree(m->len);
+        cudaFree(m->mult);
+        cudaFree(m->src);
+        cudaFree(m->src2);
+        cudaFree(m->back);
+        cudaFree(m->del);
+        m->key = nullptr;
+        m->len = nullptr;
+        m->mult = nullptr;
+        m->src = m->src2 = nullptr;
+        m->back = nullptr;
+        m->del = nullptr;
+        m->line_cap = 0;
+        EMIT_CUDA(cudaMalloc((void **)&m->key, c * 8), "merged lines");
+        EMIT_CUDA(cudaMalloc((void **)&m->len, c * 32), "merged lines");
+        EMIT_CUDA(cudaMalloc((void **)&m->mult, c * 8), "merged lines");
+        EMIT_CUDA(cudaMalloc((void **)&m->src, c * 64), "merged lines");
+        EMIT_CUDA(cudaMalloc((void **)&m->src2, c * 64), "merged lines");
+        EMIT_CUDA(cudaMalloc((void **)&m->back, c * 32), "merged lines");
+        EMIT_CUDA(cudaMalloc((void **)&m->del, c), "merged lines");
+        m->line_cap = c;
+    }
+    return SWG_OK;
+}
+
+void merged_free(MergedGraph *m) {
+    cudaFree(m->text);
+    cudaFree(m->text2);
+    cudaFree(m->key);
+    cudaFree(m->len);
+    cudaFree(m->mult);
+    cudaFree(m->src);
+    cudaFree(m->src2);
+    cudaFree(m->back);
+    cudaFree(m->del);
+    *m = MergedGraph();
+}
+
 swg_status merge_graph(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n, int k,
-                       cudaStream_t s, char **d_text, uint64_t *text_cap, MergeResult *res) {
+                       cudaStream_t s, MergedGraph *mg, MergeResult *res) {
     *res = MergeResult();
     if (n >= (1ull << 29)) {
         set_error("merge: more than 2^29 k-molecules");
@@ -704,20 +779,24 @@ swg_status merge_graph(const unsigned long long *d_keys, const unsigned long lon
     uint64_t bytes = 0;
     EMIT_CUDA(cudaMemcpyAsync(&bytes, loff + n_lines, 8, cudaMemcpyDeviceToHost, s), "text size");
     EMIT_CUDA(cudaStreamSynchronize(s), "text size");
-    if (bytes + 1 > *text_cap) {
-        if (*d_text) cudaFree(*d_text);
-        *d_text = nullptr;
-        *text_cap = 0;
-        EMIT_CUDA(cudaMalloc((void **)d_text, bytes + 1), "merged text");
-        *text_cap = bytes + 1;
+    swg_status gst = merged_reserve(mg, bytes + 1, n_lines);
+    if (gst) return gst;
+    mg->k = k;
+    mg->lines = n_lines;
+    unsigned *pos_of = nullptr;
+    if (!scr.get(&pos_of, n)) return cuda_err(cudaErrorMemoryAllocation, "line positions");
+    if (n_lines) {
+        k_mg_pos<<<blocks(n_lines), 256, 0, s>>>(sidx2, n_lines, pos_of);
+        k_mg_line_write<<<blocks(n_lines), 256, 0, s>>>(a, sidx2, n_lines, loff, mg->text, pos_of, *mg);
     }
-    if (n_lines) k_mg_line_write<<<blocks(n_lines), 256, 0, s>>>(a, sidx2, n_lines, loff, *d_text);
-    k_mg_chars<<<blocks(n), 256, 0, s>>>(a, *d_text);
-    launches += 2;
-    EMIT_CUDA(cudaMemsetAsync(*d_text + bytes, '\n', 1, s), "merged text");
+    k_mg_chars<<<blocks(n), 256, 0, s>>>(a, mg->text);
+    launches += 3;
+    EMIT_CUDA(cudaMemsetAsync(mg->text + bytes, '\n', 1, s), "merged text");
     EMIT_CUDA(cudaGetLastError(), "merge kernels");
     EMIT_CUDA(cudaStreamSynchronize(s), "merge");
     res->text_bytes = bytes + 1;
+    mg->text_bytes = bytes + 1;
+    mg->nodes = n_lines;
     res->nodes = n_lines;
     res->chains = n_chains;
     res->cycles = h[3];

@@ -195,14 +195,35 @@ uint64_t revcomp_host(uint64_t x, int k);
 // writers: records on the device, any order.
 // Device text -> file through two pinned 64 MiB buffers (emit.cu).
 swg_status stream_to_file(const char *d_text, uint64_t bytes, const char *path, cudaStream_t s);
-// Merging of semi-extended k-molecules (merge.cu): the -d file's text
-// (gathered node lines + final '\n') into *d_text (grown as needed).
+// The merged graph on the device: the -d file's text (gathered node lines in
+// key order + final '\n') and, per line, its node key and per arc slot the
+// arc's length, multiplicity, offset of its string in the text and the arc
+// at the far end pointing back (far line * 8 + slot; ~0u for an empty slot).
+struct MergedGraph {
+    int k = 0;
+    char *text = nullptr, *text2 = nullptr;  // current text, spare for rewrites
+    uint64_t text_cap = 0, text2_cap = 0, text_bytes = 0;
+    uint64_t lines = 0, line_cap = 0, nodes = 0;  // lines held; nodes printed
+    unsigned long long *key = nullptr;
+    unsigned *len = nullptr;
+    unsigned char *mult = nullptr;
+    unsigned long long *src = nullptr, *src2 = nullptr;
+    unsigned *back = nullptr;
+    unsigned char *del = nullptr;  // deleted by a pass
+};
+void merged_free(MergedGraph *m);
+swg_status merged_reserve(MergedGraph *m, uint64_t bytes, uint64_t lines);
+// Merging of semi-extended k-molecules (merge.cu) into *mg.
 struct MergeResult {
     uint64_t text_bytes = 0, nodes = 0, chains = 0, cycles = 0, rulers = 0;
     int launches = 0;
 };
 swg_status merge_graph(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n, int k,
-                       cudaStream_t s, char **d_text, uint64_t *text_cap, MergeResult *res);
+                       cudaStream_t s, MergedGraph *mg, MergeResult *res);
+// masterTipsRemoval / masterLowCoverageEdgeRemoval on the merged graph
+// (prune.cu); the text is rewritten. *count = tips removed / arcs cut.
+swg_status prune_tips(MergedGraph *mg, cudaStream_t s, uint64_t *count);
+swg_status prune_low_coverage(MergedGraph *mg, cudaStream_t s, uint64_t *count);
 swg_status emit_node_lines(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n,
                            int k, const char *path, cudaStream_t s);
 swg_status emit_kmer_graph(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n, int k,

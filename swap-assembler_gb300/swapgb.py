@@ -137,6 +137,8 @@ def lib() -> C.CDLL:
             "swg_graph_merge_info": (i32, [P, C.POINTER(MergeInfo)]),
             "swg_graph_write_merged": (i32, [P, C.c_char_p]),
             "swg_graph_copy_merged": (i32, [P, P, u64, pu64]),
+            "swg_graph_remove_tips": (i32, [P, pu64]),
+            "swg_graph_remove_low_coverage": (i32, [P, pu64]),
             "swg_records_write_kmer_graph": (i32, [P, P, u64, i32, C.c_char_p]),
             "swg_records_write_node_lines": (i32, [P, P, u64, C.c_char_p]),
             "swg_graph_last_timings": (i32, [P, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
@@ -316,6 +318,18 @@ class Graph:
         _check(lib().swg_graph_copy_merged(self._h, C.addressof(buf), n.value, C.byref(n)),
                "swg_graph_copy_merged")
         return buf.raw[: n.value]
+
+    def remove_tips(self) -> int:
+        """masterTipsRemoval on the merged graph; returns the nodes deleted."""
+        n = C.c_uint64()
+        _check(lib().swg_graph_remove_tips(self._h, C.byref(n)), "swg_graph_remove_tips")
+        return n.value
+
+    def remove_low_coverage(self) -> int:
+        """masterLowCoverageEdgeRemoval on the merged graph; returns the arcs cut."""
+        n = C.c_uint64()
+        _check(lib().swg_graph_remove_low_coverage(self._h, C.byref(n)), "swg_graph_remove_low_coverage")
+        return n.value
 
     def write_merged(self, path: str) -> None:
         _check(lib().swg_graph_write_merged(self._h, str(path).encode()), "swg_graph_write_merged")

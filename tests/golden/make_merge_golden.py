@@ -13,7 +13,18 @@ against the project's single-rank MPI shim). Stored next to this script:
                           node's index among the k-molecules sorted by key
 
 With the order the CPU restatement replays the reference's merge without the
-reference. Run from the repository root where the reference tree exists:
+reference. The same script stores, per case, the reference's tip and
+low-coverage passes (oracle/ref_prune.cpp: masterTipsRemoval and
+masterLowCoverageEdgeRemoval, graph.cpp:2194-2300) run on the complete merge
+of the case (oracle.merge_text, deterministic):
+
+  <name>.prune_order.npy  the order those passes visit the nodes (the node map's
+                          iteration order after recvBufDistNodeGraph) as
+                          indices of the complete merge's lines
+  merge_cases.json        also the SHA-256 and size of the graph after the
+                          tip pass and after the low-coverage pass
+
+Run from the repository root where the reference tree exists:
     python tests/golden/make_merge_golden.py
 """
 from __future__ import annotations
@@ -61,7 +72,20 @@ def main() -> None:
                 merged_bytes=len(merged),
                 merged_lines=merged.count(b"\n") - 1,
             )
-            print(case["name"], out[case["name"]]["nodes"], out[case["name"]]["merged_lines"])
+            full = oracle.merge_text(*oracle.records(text, case["k"], case["c"]), case["k"])
+            mp = tmp / (case["name"] + ".merged.txt")
+            mp.write_bytes(full)
+            before, tips, low = oracle.run_reference_prune(str(mp), case["k"], case["c"],
+                                                           str(tmp / (case["name"] + "_prune")))
+            index = {l.split(b" ", 1)[0]: i for i, l in enumerate(l for l in full.split(b"\n") if l)}
+            porder = np.array([index[l.split(b" ", 1)[0]] for l in before.split(b"\n") if l],
+                              dtype=np.uint32)
+            np.save(HERE / (case["name"] + ".prune_order.npy"), porder)
+            out[case["name"]].update(
+                tips_sha256=hashlib.sha256(tips).hexdigest(), tips_bytes=len(tips),
+                lowcov_sha256=hashlib.sha256(low).hexdigest(), lowcov_bytes=len(low))
+            print(case["name"], out[case["name"]]["nodes"], out[case["name"]]["merged_lines"],
+                  tips.count(b"\n") - 1, low.count(b"\n") - 1)
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
     (HERE / "merge_cases.json").write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")

@@ -140,3 +140,52 @@ def test_cli_writes_contig_graph(tmp_path):
                         "-d", "-s"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=300)
     assert r.returncode == 0, r.stdout
     assert (out2 / "kmerGraph.txt").exists() and not (out2 / "contigGraph.txt").exists()
+
+
+PRUNE_CASES = MERGE_CASES + [c for c in SYNTH_CASES if c["name"] in ("c1_small", "c3_small", "k25_c1")]
+
+
+@pytest.mark.parametrize("case", PRUNE_CASES, ids=lambda c: c["name"])
+def test_tip_and_low_coverage_passes_match_oracle(case):
+    """swg_graph_remove_tips / _low_coverage on the merged graph against the
+    restatement of masterTipsRemoval / masterLowCoverageEdgeRemoval visiting
+    every non-tip first and then the tips in key order."""
+    k, c = case["k"], case["c"]
+    g = swapgb.Graph()
+    g.build_fasta(swapgb.Opts(k=k, cutoff=c), case_text(case))
+    g.merge()
+    before = g.merged_text()
+    order = oracle.tips_last_order(before, k)
+    removed = g.remove_tips()
+    tips = g.merged_text()
+    want, n = oracle.prune_text(before, k, oracle.PRUNE_TIPS, order)
+    assert removed == n
+    assert _lines(tips) == _lines(want) and len(tips) == len(want)
+    assert g.merge_info()["nodes"] == len(_lines(tips))
+    cut = g.remove_low_coverage()
+    low = g.merged_text()
+    want2, n2 = oracle.prune_text(before, k, oracle.PRUNE_TIPS | oracle.PRUNE_LOW_COVERAGE, order)
+    assert cut == n2 - n
+    assert _lines(low) == _lines(want2) and len(low) == len(want2)
+    firsts = [int(l.split(b" ", 1)[0]) for l in low.split(b"\n") if l]
+    assert firsts == sorted(firsts)
+
+
+def test_prune_states_and_repeat():
+    """The passes need a merged graph; a second tip pass removes the tips the
+    first one left (nodes whose other arcs went with the first tips), as the
+    restatement's second pass does."""
+    k = 21
+    g = swapgb.Graph()
+    g.build_fasta(swapgb.Opts(k=k, cutoff=1), case_text(MERGE_CASES[0]))
+    with pytest.raises(swapgb.SwgError):
+        g.remove_tips()  # not merged
+    g.merge()
+    before = g.merged_text()
+    assert g.remove_tips() > 0
+    once = g.merged_text()
+    want1, _ = oracle.prune_text(before, k, oracle.PRUNE_TIPS, oracle.tips_last_order(before, k))
+    assert _lines(once) == _lines(want1)
+    second = g.remove_tips()
+    want2, n2 = oracle.prune_text(once, k, oracle.PRUNE_TIPS, oracle.tips_last_order(once, k))
+    assert second == n2 and _lines(g.merged_text()) == _lines(want2)

@@ -154,3 +154,40 @@ def test_reference_contig_stage_reads_the_complete_merge(case, tmp_path):
     assert len(only_ours) <= 1
     for piece in only_theirs:
         assert any(piece in s or _rc(piece) in s for s in only_ours)
+
+
+# ---- masterTipsRemoval / masterLowCoverageEdgeRemoval on the complete merge
+
+@pytest.mark.parametrize("case", MERGE_CASES, ids=lambda c: c["name"])
+def test_prune_replays_reference_fixture(case):
+    g = MERGE_GOLDEN[case["name"]]
+    k = case["k"]
+    full = oracle.merge_text(*oracle.records(case_text(case), k, case["c"]), k)
+    order = np.load(GOLDEN / (case["name"] + ".prune_order.npy")).astype(np.uint64)
+    tips, _ = oracle.prune_text(full, k, oracle.PRUNE_TIPS, order)
+    assert len(tips) == g["tips_bytes"] and hashlib.sha256(tips).hexdigest() == g["tips_sha256"]
+    low, _ = oracle.prune_text(full, k, oracle.PRUNE_TIPS | oracle.PRUNE_LOW_COVERAGE, order)
+    assert len(low) == g["lowcov_bytes"] and hashlib.sha256(low).hexdigest() == g["lowcov_sha256"]
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference not compiled here")
+@pytest.mark.parametrize("case", [c for c in SYNTH_CASES if c["name"] in ("c1_small", "c3_small", "k25_c1")],
+                         ids=lambda c: c["name"])
+def test_prune_replays_live_reference(case, tmp_path):
+    k = case["k"]
+    full = oracle.merge_text(*oracle.records(case_text(case), k, case["c"]), k)
+    mp = tmp_path / "merged.txt"
+    mp.write_bytes(full)
+    before, tips, low = oracle.run_reference_prune(str(mp), k, case["c"], str(tmp_path / "o"))
+    assert oracle.prune_text(before, k, oracle.PRUNE_TIPS)[0] == tips
+    assert oracle.prune_text(before, k, oracle.PRUNE_TIPS | oracle.PRUNE_LOW_COVERAGE)[0] == low
+
+
+def test_prune_low_coverage_cuts_something():
+    """At least one fixture exercises the low-coverage cut (not only tips)."""
+    case = MERGE_CASES[1]
+    k = case["k"]
+    full = oracle.merge_text(*oracle.records(case_text(case), k, case["c"]), k)
+    tips, n_tips = oracle.prune_text(full, k, oracle.PRUNE_TIPS)
+    both, n_both = oracle.prune_text(full, k, oracle.PRUNE_TIPS | oracle.PRUNE_LOW_COVERAGE)
+    assert n_tips > 0 and n_both > n_tips and both != tips
