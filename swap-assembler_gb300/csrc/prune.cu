@@ -138,14 +138,32 @@ __global__ void k_pr_write(MergedGraph m, const uint64_t *__restrict__ off, char
     *p = '\n';
 }
 
-// A block per arc slot (grid-stride): the arc's string from the old text to
-// the new one.
-__global__ void k_pr_copy(MergedGraph m, const char *__restrict__ from, char *__restrict__ to) {
-    for (uint64_t a = blockIdx.x; a < 8 * m.lines; a += gridDim.x) {
-        const unsigned l = m.len[a];
-        if (!l) continue;
-        const char *src = from + m.src[a];
-        char *dst = to + m.src2[a];
+// The arc strings move from the old text to the new one in 4 KiB chunks, a
+// block per chunk, so that a few very long arcs (whole chains) spread over
+// the GPU too: chunk counts per arc slot, their prefix, then each block finds
+// its arc by binary search in the prefix.
+constexpr unsigned kChunk = 4096;
+
+__global__ void k_pr_chunks(MergedGraph m, uint64_t *__restrict__ chunks) {
+    const uint64_t a = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < 8 * m.lines) chunks[a] = (m.len[a] + kChunk - 1) / kChunk;
+}
+
+__global__ void k_pr_copy(MergedGraph m, const uint64_t *__restrict__ first, uint64_t n_chunks,
+                          const char *__restrict__ from, char *__restrict__ to) {
+    const uint64_t arcs = 8 * m.lines;
+    for (uint64_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        uint64_t lo = 0, hi = arcs;  // the last arc whose first chunk is <= c
+        while (hi - lo > 1) {
+            const uint64_t mid = (lo + hi) / 2;
+            if (first[mid] <= c) lo = mid;
+            else hi = mid;
+        }
+        const uint64_t at = (c - first[lo]) * kChunk;
+        const uint64_t rest = m.len[lo] - at;
+        const unsigned l = rest < kChunk ? (unsigned)rest : kChunk;
+        const char *src = from + m.src[lo] + at;
+        char *dst = to + m.src2[lo] + at;
         for (unsigned i = threadIdx.x; i < l; i += blockDim.x) dst[i] = src[i];
     }
 }
@@ -175,8 +193,19 @@ swg_status rewrite(MergedGraph *m, cudaStream_t s, Scratch &scr) {
         m->text2_cap = bytes;
     }
     if (m->lines) {
+        uint64_t *chunks = nullptr, *first = nullptr;
+        if (!scr.get(&chunks, 8 * m->lines) || !scr.get(&first, 8 * m->lines + 1))
+            return cuda_err(cudaErrorMemoryAllocation, "rewrite workspace");
         k_pr_write<<<blocks(m->lines), 256, 0, s>>>(*m, off, m->text2);
-        k_pr_copy<<<(unsigned)std::min<uint64_t>(8 * m->lines, 1u << 20), 128, 0, s>>>(*m, m->text, m->text2);
+        k_pr_chunks<<<blocks(8 * m->lines), 256, 0, s>>>(*m, chunks);
+        st = scan_lengths(chunks, first, 8 * m->lines, scr, s);
+        if (st) return st;
+        uint64_t n_chunks = 0;
+        EMIT_CUDA(cudaMemcpyAsync(&n_chunks, first + 8 * m->lines, 8, cudaMemcpyDeviceToHost, s), "chunks");
+        EMIT_CUDA(cudaStreamSynchronize(s), "chunks");
+        if (n_chunks)
+            k_pr_copy<<<(unsigned)std::min<uint64_t>(n_chunks, 1u << 20), 256, 0, s>>>(*m, first, n_chunks,
+                                                                                      m->text, m->text2);
     }
     EMIT_CUDA(cudaMemsetAsync(m->text2 + h[0], '\n', 1, s), "merged text");
     EMIT_CUDA(cudaGetLastError(), "rewrite kernels");
