@@ -429,7 +429,7 @@ swg_status build_direct(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStrea
 }
 
 // Hash-partitioned counting: every occurrence becomes an 8-byte record
-// {low bits of mix64(key), arc code}, scattered to the partition named by the
+// {low bits of rmix64(key), arc code}, scattered to the partition named by the
 // top bits; each partition is then counted in a table slice sized by its
 // record count (an upper bound on its distinct keys) that stays resident in
 // L2, several partitions (a wave) at a time, and compacted straight from L2.

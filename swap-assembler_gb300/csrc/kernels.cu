@@ -398,15 +398,19 @@ __device__ __forceinline__ uint64_t code_inc(unsigned code) {
     return inc;
 }
 
-// Inverse of mix64 (each xor-shift by 33 is its own inverse on 64 bits; the
-// multipliers are the inverses of mix64's modulo 2^64).
-__device__ __forceinline__ uint64_t unmix64(uint64_t x) {
-    x ^= x >> 33;
-    x *= 0x9cb4b2f8129337dbull;
-    x ^= x >> 33;
-    x *= 0x4f74430c22a54005ull;
-    x ^= x >> 33;
-    return x;
+// Record hash of the level-1 scatter (bucketed and partitioned builds): a
+// bijection on 64 bits, cheaper than mix64 on the per-occurrence path. An odd
+// multiplier carries every key bit into the top bits (the partition and the
+// bucket); folding the high half into the low half gives the low bits (the
+// table slot) every key bit too. rmix64's inverse: undo the fold (the high
+// half is unchanged), multiply by the multiplier's inverse modulo 2^64.
+__device__ __forceinline__ uint64_t rmix64(uint64_t x) {
+    x *= 0x9e3779b97f4a7c15ull;
+    return x ^ (x >> 32);
+}
+__device__ __forceinline__ uint64_t runmix64(uint64_t x) {
+    x ^= x >> 32;
+    return x * 0xf1de83e19937733dull;
 }
 
 // ---------------------------------------------------------------------
@@ -748,7 +752,7 @@ __global__ void __launch_bounds__(kCBlock) k_compact(BuildArgs a) {
 }
 
 // ---------------------------------------------------------------------
-// Partitioned build. A record is {the low 64-bits bits of h = mix64(key),
+// Partitioned build. A record is {the low 64-bits bits of h = rmix64(key),
 // shifted left by 8 | arc code}; the partition is the top `bits` bits of h,
 // so h (a bijection of the key) is whole again in the partition's pass.
 constexpr int kMaxSlots = 64;
@@ -863,7 +867,7 @@ __global__ void __launch_bounds__(256) k_p1_count(BuildArgs a, PartArgs pa) {
                 uint64_t key;
                 unsigned code;
                 walk_emit(a, st, key, code);
-                atomicAdd(&hist[mix64(key) >> shift], 1u);
+                atomicAdd(&hist[rmix64(key) >> shift], 1u);
             }
         }
     }
@@ -896,7 +900,7 @@ __global__ void __launch_bounds__(256) k_p1_sample(BuildArgs a, PartArgs pa, Buc
                 uint64_t key;
                 unsigned code;
                 walk_emit(a, st, key, code);
-                const uint64_t h = mix64(key);
+                const uint64_t h = rmix64(key);
                 atomicAdd(&hist[h >> shift], 1u);
                 atomicAdd(&b.cursor2[h >> bshift], 1ull);
             }
@@ -982,7 +986,7 @@ __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs p
                     uint64_t key;
                     unsigned code;
                     walk_emit(a, st, key, code);
-                    const uint64_t h = mix64(key);
+                    const uint64_t h = rmix64(key);
                     const unsigned part = (unsigned)(h >> shift);
                     rec[j] = ((h << pa.bits) >> (pa.bits - 8)) | code;  // low 64-b1 bits << 8
                     pr[j] = part | (atomicAdd(&hist[part], 1u) << 16);
@@ -1123,7 +1127,7 @@ __global__ void __launch_bounds__(kCBlock) k_part_compact(BuildArgs a, PartArgs 
                 *reinterpret_cast<ulonglong2 *>(e) = make_ulonglong2(0ull, 0ull);
                 nused++;
                 if (w != 0) {
-                    keys[it] = unmix64(v.x);
+                    keys[it] = runmix64(v.x);
                     cnts[it] = w;
                     keep |= 1u << it;
                     nkeep++;
@@ -1687,7 +1691,7 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
                 h = keys[sl];
                 if (!over) {
                     if (tb) {  // the sample's own cutoff, per-sample counts
-                        const uint32_t smp = (uint32_t)(unmix64(h) >> (64 - tb));
+                        const uint32_t smp = (uint32_t)(runmix64(h) >> (64 - tb));
                         const int cs = a.segs[smp].cutoff;
                         m = bucket_mult(cnt, sl, (cs > 0 && cs < 256) ? (0x8000u - (unsigned)cs) * 0x00010001u : 0u,
                                         cs >= 256);
@@ -1707,7 +1711,7 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
                 at = __shfl_sync(kFull, at, __ffs(kept) - 1);
                 if (m) {
                     const uint64_t pos = rb + at + __popc(kept & ((1u << lane) - 1));
-                    b.stage_keys[pos] = unmix64(h);
+                    b.stage_keys[pos] = runmix64(h);
                     b.rec2[pos] = m;
                 }
             }
@@ -1828,7 +1832,7 @@ __global__ void __launch_bounds__(kCBlock) k_big_compact(BuildArgs a, const Entr
         int cc = c;
         uint32_t smp = 0;
         if (a.tag_bits) {  // tagged batch: the sample's own cutoff, per-sample counts
-            smp = (uint32_t)(unmix64(e.x) >> (64 - a.tag_bits));
+            smp = (uint32_t)(runmix64(e.x) >> (64 - a.tag_bits));
             cc = a.segs[smp].cutoff;
             th = cc <= 0 ? 0u : (cc >= 256 ? 0u : (uint32_t)cc * 0x01010101u);
         }
@@ -1843,7 +1847,7 @@ __global__ void __launch_bounds__(kCBlock) k_big_compact(BuildArgs a, const Entr
             if (v) atomicAdd(&a.seg_counts[2 * smp + 1], 1ull);
         }
         if (v) {
-            keys[it] = unmix64(e.x);
+            keys[it] = runmix64(e.x);
             cnts[it] = v;
             keep |= 1u << it;
             nkeep++;
