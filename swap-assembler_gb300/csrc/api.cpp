@@ -1490,7 +1490,8 @@ swg_status swg_graph_remove_tips(swg_graph *g, uint64_t *removed) {
     SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
     uint64_t n = 0;
     st = swg::prune_tips(&g->mg, g->own, &n);
-    if (removed) *removed = n;
+    if (st) g->merged = false;  // lines edited, text not rewritten: drop both
+    if (removed) *removed = st ? 0 : n;
     return st;
 }
 
@@ -1501,7 +1502,8 @@ swg_status swg_graph_remove_low_coverage(swg_graph *g, uint64_t *cut) {
     SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
     uint64_t n = 0;
     st = swg::prune_low_coverage(&g->mg, g->own, &n);
-    if (cut) *cut = n;
+    if (st) g->merged = false;  // lines edited, text not rewritten: drop both
+    if (cut) *cut = st ? 0 : n;
     return st;
 }
 
