@@ -25,6 +25,7 @@
  *                                                -> swg_graph_write_merged / swg_graph_copy_merged
  *   distNodeGraph::masterTipsRemoval ........... graph.cpp:2194-2265 -> swg_graph_remove_tips
  *   distNodeGraph::masterLowCoverageEdgeRemoval  graph.cpp:2267-2300 -> swg_graph_remove_low_coverage
+ *   distNodeGraph::masterSimplifyNodeGraph ..... graph.cpp:2089-2192 -> swg_graph_simplify
  *
  * Packed read layout (host or device memory):
  *   packed   uint32 words; base i of the concatenated read stream sits in
@@ -314,6 +315,15 @@ swg_status swg_graph_copy_merged(const swg_graph *g, char *buf, uint64_t cap, ui
  *   reference's masterSimplifyNodeGraph does that next). */
 swg_status swg_graph_remove_tips(swg_graph *g, uint64_t *removed);
 swg_status swg_graph_remove_low_coverage(swg_graph *g, uint64_t *cut);
+/* masterSimplifyNodeGraph (graph.cpp:2089-2192) on the merged graph, as the
+ * reference runs it after those passes: a node left with exactly one arc on
+ * each side whose neighbours are not itself is merged into its neighbours;
+ * each end arc of a chain of such nodes becomes the concatenation of the
+ * chain's arcs, with the weighted average multiplicity in size_t arithmetic
+ * (graph.cpp:2157-2163) taken in swg_graph_merge's visiting order (chain
+ * positions from the smaller end arc, node p at level ctz(p)); a cycle of such
+ * nodes is cut at its largest key. *merged = nodes merged away. */
+swg_status swg_graph_simplify(swg_graph *g, uint64_t *merged);
 /* Host-only writers for records already in host memory (keys[n], mult[8*n],
  * any order): the same two file formats as above. */
 swg_status swg_records_write_kmer_graph(const uint64_t *keys, const uint8_t *mult, uint64_t n,

@@ -94,6 +94,14 @@ int oracle_merge_tree_order(int k, uint64_t n, const uint64_t *keys, const uint8
 int oracle_prune(int k, const char *text, uint64_t len, const uint64_t *order, int passes, char **out,
                  uint64_t *out_len, uint64_t *count);
 
+/* masterSimplifyNodeGraph (graph.cpp:2089-2192) once over gathered lines,
+ * visiting them in `order` (NULL = file order); *merged = nodes merged away. */
+int oracle_simplify_lines(int k, const char *text, uint64_t len, const uint64_t *order, char **out,
+                          uint64_t *out_len, uint64_t *merged);
+/* The GPU's visiting order for that pass (chains numbered from their smaller
+ * end arc, level ctz(position)), as line indices; *n = lines. */
+int oracle_lines_tree_order(int k, const char *text, uint64_t len, uint64_t *order, uint64_t cap, uint64_t *n);
+
 /* Neighbour id printed in kmerGraph.txt for slot s of key K (graph.cpp:3380-3427). */
 uint64_t oracle_kmer_graph_neighbour(uint64_t key, int slot, int k);
 uint64_t oracle_revcomp(uint64_t x, int k);

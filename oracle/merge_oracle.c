@@ -681,3 +681,201 @@ int oracle_prune(int k, const char *text, uint64_t len, const uint64_t *order, i
     free(keys);
     return rc;
 }
+
+/* ---------------------------------------------------------------------------
+ * masterSimplifyNodeGraph (graph.cpp:2089-2192) over gathered lines: in the
+ * given order, a node left with exactly one arc on each side whose two
+ * neighbours both hold an arc back to it (getSrcNodeEdge, graph.cpp:250-309)
+ * and neither of which is itself is merged away; each neighbour's arc back
+ * gets the node's other arc appended, its multiplicity the weighted average
+ * in size_t arithmetic (graph.cpp:2157-2163, no int step here).
+ * ------------------------------------------------------------------------- */
+
+static void master_append(mgraph *g, uint64_t d, int slot, const mstr *s, uint8_t m) {
+    mstr *a = &g->arcs[d][slot];
+    const uint64_t sum = (uint64_t)g->mult[d][slot] * a->len + (uint64_t)m * s->len;
+    g->mult[d][slot] = (uint8_t)(sum / (a->len + s->len));
+    if (mstr_append(a, s->s, s->len)) g->err = ORACLE_ERR_OOM;
+}
+
+static void simplify_master(mgraph *g, const uint64_t *order, uint64_t *merged) {
+    for (uint64_t t = 0; t < g->n && !g->err; ++t) {
+        const uint64_t x = order[t];
+        if (g->deleted[x]) continue;
+        int ls, rs, lc, rc;
+        one_sided(g, x, &ls, &rs, &lc, &rc);
+        if (lc != 1 || rc != 1) continue;
+        uint64_t rid, lid;
+        int rsd, lsd;
+        arc_end(g, x, rs, &rid, &rsd);
+        arc_end(g, x, ls, &lid, &lsd);
+        const int64_t ri = mfind(g, rid), li = mfind(g, lid);
+        if (ri < 0 || li < 0) continue; /* a missing neighbour holds no arc back */
+        const int rret = src_edge(g, (uint64_t)ri, x, 0), lret = src_edge(g, (uint64_t)li, x, 1);
+        if (rret < 0 || lret < 0) continue;
+        if ((uint64_t)li == x || (uint64_t)ri == x) continue;
+        mstr xl = g->arcs[x][ls], xr = g->arcs[x][rs]; /* read before ri/li change */
+        master_append(g, (uint64_t)ri, rret, &xl, g->mult[x][ls]);
+        master_append(g, (uint64_t)li, lret, &xr, g->mult[x][rs]);
+        g->deleted[x] = 1;
+        if (merged) ++*merged;
+    }
+}
+
+/* The GPU's visiting order on a graph of arbitrary arcs: as
+ * oracle_merge_tree_order, the chain end's arc back found by getSrcNodeEdge. */
+static int tree_order_graph(mgraph *g, uint64_t *order) {
+    const uint64_t n = g->n;
+    int rc = 0;
+    uint8_t *mg = (uint8_t *)calloc(n ? n : 1, 1);
+    int8_t *ls = (int8_t *)malloc(n ? n : 1), *rs = (int8_t *)malloc(n ? n : 1);
+    tord *to = (tord *)malloc((n ? n : 1) * sizeof(tord));
+    uint8_t *seen = (uint8_t *)calloc(n ? n : 1, 1);
+    uint64_t *cyc = (uint64_t *)malloc((n ? n : 1) * sizeof(uint64_t));
+    if (!mg || !ls || !rs || !to || !seen || !cyc) rc = ORACLE_ERR_OOM;
+    for (uint64_t x = 0; !rc && x < n; ++x) {
+        int l, r, lc, rcnt;
+        one_sided(g, x, &l, &r, &lc, &rcnt);
+        ls[x] = (int8_t)l;
+        rs[x] = (int8_t)r;
+        if (g->deleted[x] || lc != 1 || rcnt != 1) continue;
+        int s1, s2;
+        const int64_t a = step(g, x, l, &s1), b = step(g, x, r, &s2);
+        if (a < 0 || b < 0) continue;
+        if (src_edge(g, (uint64_t)b, x, 0) < 0 || src_edge(g, (uint64_t)a, x, 1) < 0) continue;
+        mg[x] = (uint64_t)a != x && (uint64_t)b != x;
+    }
+    uint64_t nt = 0, ncyc = 0;
+    for (int pass = 0; !rc && pass < 2; ++pass) {
+        for (uint64_t x = 0; !rc && x < n; ++x) {
+            if (pass == 0 && (mg[x] || g->deleted[x])) continue;
+            if (pass == 1 && (!mg[x] || seen[x])) continue;
+            uint64_t start = x;
+            if (pass == 1) {
+                uint64_t best = x, cur = x;
+                int dslot = rs[x];
+                for (;;) {
+                    int side;
+                    const int64_t y = step(g, cur, dslot, &side);
+                    if ((uint64_t)y == x) break;
+                    if (g->keys[y] > g->keys[best]) best = (uint64_t)y;
+                    dslot = side ? rs[y] : ls[y];
+                    cur = (uint64_t)y;
+                }
+                start = best;
+                mg[start] = 0;
+                seen[start] = 1;
+                cyc[ncyc++] = start;
+            }
+            for (int slot = 0; slot < 8 && !rc; ++slot) {
+                if (!g->arcs[start][slot].len) continue;
+                int side;
+                const int64_t y = step(g, start, slot, &side);
+                if (y < 0 || !mg[y]) continue;
+                uint64_t m = 0, cur = (uint64_t)y, ekey = 0, eslot = 0;
+                int dir = side;
+                for (;;) {
+                    ++m;
+                    const int out = dir ? rs[cur] : ls[cur];
+                    int s2;
+                    const int64_t z = step(g, cur, out, &s2);
+                    if (!mg[z]) {
+                        ekey = g->keys[z];
+                        eslot = (uint64_t)src_edge(g, (uint64_t)z, cur, dir ? 0 : 1);
+                        break;
+                    }
+                    dir = s2;
+                    cur = (uint64_t)z;
+                }
+                const int fwd = g->keys[start] < ekey || (g->keys[start] == ekey && (uint64_t)slot < eslot);
+                if (!fwd) continue;
+                cur = (uint64_t)y;
+                dir = side;
+                for (uint64_t p = 1; p <= m; ++p) {
+                    to[nt].level = (uint64_t)ctz64(p);
+                    to[nt].ckey = g->keys[start];
+                    to[nt].cslot = (uint64_t)slot;
+                    to[nt].pos = p;
+                    to[nt].node = cur;
+                    ++nt;
+                    seen[cur] = 1;
+                    const int out = dir ? rs[cur] : ls[cur];
+                    int s2;
+                    const int64_t z = step(g, cur, out, &s2);
+                    dir = s2;
+                    cur = (uint64_t)z;
+                }
+            }
+        }
+    }
+    if (!rc) {
+        qsort(to, nt, sizeof(tord), tord_cmp);
+        uint64_t o = 0;
+        for (uint64_t x = 0; x < n; ++x)
+            if (!mg[x] && !seen[x]) order[o++] = x;
+        for (uint64_t i = 0; i < nt; ++i) order[o++] = to[i].node;
+        for (uint64_t i = 0; i < ncyc; ++i) order[o++] = cyc[i];
+        if (o != n) rc = -13;
+    }
+    free(cyc);
+    free(mg);
+    free(ls);
+    free(rs);
+    free(to);
+    free(seen);
+    return rc;
+}
+
+static int lines_out(mgraph *g, const uint64_t *ord, char **out, uint64_t *out_len) {
+    uint64_t total = 2;
+    for (uint64_t x = 0; x < g->n; ++x) {
+        total += 61;
+        for (int i = 0; i < 8; ++i) total += g->arcs[x][i].len + 1;
+    }
+    char *buf = (char *)malloc(total + 64);
+    if (!buf) return ORACLE_ERR_OOM;
+    char *p = buf;
+    for (uint64_t t = 0; t < g->n; ++t) {
+        const uint64_t x = ord[t];
+        if (g->deleted[x] || !has_arc(g, x)) continue;
+        p = put_line(p, g, x);
+    }
+    *p++ = '\n';
+    *out = buf;
+    *out_len = (uint64_t)(p - buf);
+    return 0;
+}
+
+int oracle_simplify_lines(int k, const char *text, uint64_t len, const uint64_t *order, char **out,
+                          uint64_t *out_len, uint64_t *merged) {
+    *out = NULL;
+    *out_len = 0;
+    if (merged) *merged = 0;
+    if (k < 1 || k > 31) return ORACLE_ERR_BAD_K;
+    mgraph g;
+    uint64_t *keys = NULL;
+    int rc = parse_lines(&g, k, text, len, &keys);
+    uint64_t *ord = (uint64_t *)malloc((g.n ? g.n : 1) * 8);
+    if (!ord) rc = ORACLE_ERR_OOM;
+    for (uint64_t t = 0; !rc && t < g.n; ++t) ord[t] = order ? order[t] : t;
+    if (!rc) simplify_master(&g, ord, merged);
+    if (!rc) rc = g.err;
+    if (!rc) rc = lines_out(&g, ord, out, out_len);
+    free(ord);
+    mgraph_free(&g);
+    free(keys);
+    return rc;
+}
+
+int oracle_lines_tree_order(int k, const char *text, uint64_t len, uint64_t *order, uint64_t cap, uint64_t *n) {
+    if (k < 1 || k > 31) return ORACLE_ERR_BAD_K;
+    mgraph g;
+    uint64_t *keys = NULL;
+    int rc = parse_lines(&g, k, text, len, &keys);
+    *n = g.n;
+    if (!rc && cap < g.n) rc = ORACLE_ERR_OOM;
+    if (!rc) rc = tree_order_graph(&g, order);
+    mgraph_free(&g);
+    free(keys);
+    return rc;
+}

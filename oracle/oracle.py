@@ -65,6 +65,11 @@ def lib() -> C.CDLL:
         L.oracle_prune.argtypes = [i32, C.c_char_p, u64, P, i32, C.POINTER(C.c_void_p), C.POINTER(u64),
                                    C.POINTER(u64)]
         L.oracle_prune.restype = i32
+        L.oracle_simplify_lines.argtypes = [i32, C.c_char_p, u64, P, C.POINTER(C.c_void_p), C.POINTER(u64),
+                                            C.POINTER(u64)]
+        L.oracle_simplify_lines.restype = i32
+        L.oracle_lines_tree_order.argtypes = [i32, C.c_char_p, u64, P, u64, C.POINTER(u64)]
+        L.oracle_lines_tree_order.restype = i32
         _lib = L
     return _lib
 
@@ -208,6 +213,46 @@ def prune_text(text: bytes, k: int, passes: int, order=None) -> tuple[bytes, int
         lib().oracle_free_text(ptr)
 
 
+def simplify_text(text: bytes, k: int, order=None) -> tuple[bytes, int]:
+    """masterSimplifyNodeGraph once over gathered lines, visiting them in
+    `order` (line indices; default file order). Returns the resulting lines
+    and the nodes merged away."""
+    ptr, n, cnt = C.c_void_p(), C.c_uint64(), C.c_uint64()
+    if order is not None:
+        order = np.ascontiguousarray(order, dtype=np.uint64)
+    e = lib().oracle_simplify_lines(k, text, len(text), order.ctypes.data if order is not None else None,
+                                    C.byref(ptr), C.byref(n), C.byref(cnt))
+    if e:
+        raise OracleError(e)
+    try:
+        return (C.string_at(ptr.value, n.value) if n.value else b""), cnt.value
+    finally:
+        lib().oracle_free_text(ptr)
+
+
+def lines_tree_order(text: bytes, k: int) -> np.ndarray:
+    """The GPU's visiting order of masterSimplifyNodeGraph over these lines."""
+    cap = max(text.count(b"\n"), 1)
+    order = np.zeros(cap, dtype=np.uint64)
+    n = C.c_uint64()
+    e = lib().oracle_lines_tree_order(k, text, len(text), order.ctypes.data, cap, C.byref(n))
+    if e:
+        raise OracleError(e)
+    return order[: n.value]
+
+
+def run_reference_simplify(lines_path: str, k: int, cutoff: int, outdir: str,
+                           timeout: float = 600) -> tuple[bytes, bytes]:
+    """The reference's masterSimplifyNodeGraph on gathered lines: its graph
+    before (node map order) and after the pass."""
+    r = subprocess.run([str(HERE / "_ref" / "ref_simplify"), "-k", str(k), "-c", str(cutoff), "-i",
+                        str(lines_path), "-o", str(outdir)], stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, timeout=timeout, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference simplify failed: %s" % r.stdout[-2000:])
+    return Path(outdir, "before.txt").read_bytes(), Path(outdir, "after.txt").read_bytes()
+
+
 def tips_last_order(text: bytes, k: int) -> np.ndarray:
     """The GPU's visiting order for the tip pass: every node that is not a tip
     (in key order), then the tips in key order; as line indices of `text`."""
@@ -254,7 +299,7 @@ def parse_node_lines(text: bytes) -> tuple[np.ndarray, np.ndarray]:
 # ---- the reference itself (only where it was compiled from its sources) ----
 
 def reference_available() -> bool:
-    return REF_SWAP.exists() and REF_DUMP.exists() and REF_CONTIGS.exists() and (HERE / "_ref" / "ref_prune").exists()
+    return REF_SWAP.exists() and REF_DUMP.exists() and REF_CONTIGS.exists() and (HERE / "_ref" / "ref_prune").exists() and (HERE / "_ref" / "ref_simplify").exists()
 
 
 def run_reference(fasta_path: str, k: int, cutoff: int, outdir: str, timeout: float = 600) -> dict:

@@ -1507,6 +1507,18 @@ swg_status swg_graph_remove_low_coverage(swg_graph *g, uint64_t *cut) {
     return st;
 }
 
+swg_status swg_graph_simplify(swg_graph *g, uint64_t *merged) {
+    if (!g) return SWG_ERR_BAD_INPUT;
+    swg_status st = merged_state(g);
+    if (st) return st;
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    uint64_t n = 0;
+    st = swg::simplify_lines(&g->mg, g->own, &n);
+    if (st) g->merged = false;  // lines edited, text not rewritten: drop both
+    if (merged) *merged = st ? 0 : n;
+    return st;
+}
+
 static swg_status sorted_copy(const uint64_t *keys, const uint8_t *mult, uint64_t n,
                               std::vector<uint64_t> &k, std::vector<uint64_t> &m) {
     if (n && (!keys || !mult)) return SWG_ERR_BAD_INPUT;

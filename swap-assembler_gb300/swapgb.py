@@ -139,6 +139,7 @@ def lib() -> C.CDLL:
             "swg_graph_copy_merged": (i32, [P, P, u64, pu64]),
             "swg_graph_remove_tips": (i32, [P, pu64]),
             "swg_graph_remove_low_coverage": (i32, [P, pu64]),
+            "swg_graph_simplify": (i32, [P, pu64]),
             "swg_records_write_kmer_graph": (i32, [P, P, u64, i32, C.c_char_p]),
             "swg_records_write_node_lines": (i32, [P, P, u64, C.c_char_p]),
             "swg_graph_last_timings": (i32, [P, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
@@ -329,6 +330,12 @@ class Graph:
         """masterLowCoverageEdgeRemoval on the merged graph; returns the arcs cut."""
         n = C.c_uint64()
         _check(lib().swg_graph_remove_low_coverage(self._h, C.byref(n)), "swg_graph_remove_low_coverage")
+        return n.value
+
+    def simplify(self) -> int:
+        """masterSimplifyNodeGraph on the merged graph; returns the nodes merged away."""
+        n = C.c_uint64()
+        _check(lib().swg_graph_simplify(self._h, C.byref(n)), "swg_graph_simplify")
         return n.value
 
     def write_merged(self, path: str) -> None:

@@ -24,6 +24,13 @@ of the case (oracle.merge_text, deterministic):
   merge_cases.json        also the SHA-256 and size of the graph after the
                           tip pass and after the low-coverage pass
 
+and the reference's masterSimplifyNodeGraph (oracle/ref_simplify.cpp,
+graph.cpp:2089-2192) run on the restatement's tip pass over the complete
+merge (every non-tip first, then the tips in key order — deterministic):
+
+  <name>.simplify_order.npy  its visiting order as line indices of that input
+  merge_cases.json           the SHA-256 and size of its output
+
 Run from the repository root where the reference tree exists:
     python tests/golden/make_merge_golden.py
 """
@@ -84,6 +91,16 @@ def main() -> None:
             out[case["name"]].update(
                 tips_sha256=hashlib.sha256(tips).hexdigest(), tips_bytes=len(tips),
                 lowcov_sha256=hashlib.sha256(low).hexdigest(), lowcov_bytes=len(low))
+            tips_in, _ = oracle.prune_text(full, case["k"], oracle.PRUNE_TIPS,
+                                           oracle.tips_last_order(full, case["k"]))
+            tp = tmp / (case["name"] + ".tips.txt")
+            tp.write_bytes(tips_in)
+            sb, sa = oracle.run_reference_simplify(str(tp), case["k"], case["c"],
+                                                   str(tmp / (case["name"] + "_simplify")))
+            tindex = {l.split(b" ", 1)[0]: i for i, l in enumerate(l for l in tips_in.split(b"\n") if l)}
+            sorder = np.array([tindex[l.split(b" ", 1)[0]] for l in sb.split(b"\n") if l], dtype=np.uint32)
+            np.save(HERE / (case["name"] + ".simplify_order.npy"), sorder)
+            out[case["name"]].update(simplify_sha256=hashlib.sha256(sa).hexdigest(), simplify_bytes=len(sa))
             print(case["name"], out[case["name"]]["nodes"], out[case["name"]]["merged_lines"],
                   tips.count(b"\n") - 1, low.count(b"\n") - 1)
     finally:

@@ -189,3 +189,54 @@ def test_prune_states_and_repeat():
     second = g.remove_tips()
     want2, n2 = oracle.prune_text(once, k, oracle.PRUNE_TIPS, oracle.tips_last_order(once, k))
     assert second == n2 and _lines(g.merged_text()) == _lines(want2)
+
+
+@pytest.mark.parametrize("case", PRUNE_CASES, ids=lambda c: c["name"])
+def test_simplify_after_the_passes_matches_oracle(case):
+    """The reference's sequence tip pass -> masterSimplifyNodeGraph ->
+    low-coverage pass -> masterSimplifyNodeGraph on the merged graph: each
+    GPU step equals the restatement (the simplify in the GPU's visiting order
+    of the lines, oracle_lines_tree_order)."""
+    k, c = case["k"], case["c"]
+    g = swapgb.Graph()
+    g.build_fasta(swapgb.Opts(k=k, cutoff=c), case_text(case))
+    g.merge()
+    g.remove_tips()
+    tips = g.merged_text()
+    merged = g.simplify()
+    want, n = oracle.simplify_text(tips, k, oracle.lines_tree_order(tips, k))
+    got = g.merged_text()
+    assert merged == n
+    assert _lines(got) == _lines(want) and len(got) == len(want)
+    assert g.merge_info()["nodes"] == len(_lines(got))
+    g.remove_low_coverage()
+    low = g.merged_text()
+    g.simplify()
+    want2, _ = oracle.simplify_text(low, k, oracle.lines_tree_order(low, k))
+    assert _lines(g.merged_text()) == _lines(want2)
+    # nothing left to merge
+    assert g.simplify() == 0
+
+
+def test_simplify_cycles():
+    """A cycle left when a tip that held its only branch goes: cut at its
+    largest key, as the restatement's visiting order does."""
+    import random
+    rng = random.Random(9)
+    g0 = "".join(rng.choice("ACGT") for _ in range(2000))
+    reads = [g0[i:i + 100] if i + 100 <= 2000 else g0[i:] + g0[:i + 100 - 2000] for i in range(0, 2000, 5)]
+    # three short spurs off the circle: tips once merged; without them the
+    # three branch nodes form a cycle of one-arc-per-side nodes
+    for at in (300, 900, 1500):
+        spur = g0[at:at + 30] + "".join(rng.choice("ACGT") for _ in range(5))
+        reads += [spur] * 6
+    text = "".join(">r%d\n%s\n" % (i, r) for i, r in enumerate(reads)).encode()
+    for k in (21, 25):
+        g = swapgb.Graph()
+        g.build_fasta(swapgb.Opts(k=k, cutoff=2), text)
+        g.merge()
+        g.remove_tips()
+        tips = g.merged_text()
+        assert g.simplify() == 2
+        want, _ = oracle.simplify_text(tips, k, oracle.lines_tree_order(tips, k))
+        assert _lines(g.merged_text()) == _lines(want) and len(_lines(want)) == 1

@@ -191,3 +191,42 @@ def test_prune_low_coverage_cuts_something():
     tips, n_tips = oracle.prune_text(full, k, oracle.PRUNE_TIPS)
     both, n_both = oracle.prune_text(full, k, oracle.PRUNE_TIPS | oracle.PRUNE_LOW_COVERAGE)
     assert n_tips > 0 and n_both > n_tips and both != tips
+
+
+# ---- masterSimplifyNodeGraph over the lines left by a pass
+
+@pytest.mark.parametrize("case", MERGE_CASES, ids=lambda c: c["name"])
+def test_simplify_replays_reference_fixture(case):
+    g = MERGE_GOLDEN[case["name"]]
+    k = case["k"]
+    full = oracle.merge_text(*oracle.records(case_text(case), k, case["c"]), k)
+    tips, _ = oracle.prune_text(full, k, oracle.PRUNE_TIPS, oracle.tips_last_order(full, k))
+    order = np.load(GOLDEN / (case["name"] + ".simplify_order.npy")).astype(np.uint64)
+    out, _ = oracle.simplify_text(tips, k, order)
+    assert len(out) == g["simplify_bytes"] and hashlib.sha256(out).hexdigest() == g["simplify_sha256"]
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference not compiled here")
+@pytest.mark.parametrize("case", [c for c in SYNTH_CASES if c["name"] in ("c1_small", "c3_small", "k25_c1")],
+                         ids=lambda c: c["name"])
+def test_simplify_replays_live_reference(case, tmp_path):
+    k = case["k"]
+    full = oracle.merge_text(*oracle.records(case_text(case), k, case["c"]), k)
+    tips, _ = oracle.prune_text(full, k, oracle.PRUNE_TIPS)
+    tp = tmp_path / "tips.txt"
+    tp.write_bytes(tips)
+    before, after = oracle.run_reference_simplify(str(tp), k, case["c"], str(tmp_path / "o"))
+    assert oracle.simplify_text(before, k)[0] == after
+
+
+def test_simplify_order_is_a_permutation_and_merges_as_many():
+    case = MERGE_CASES[0]
+    k = case["k"]
+    full = oracle.merge_text(*oracle.records(case_text(case), k, case["c"]), k)
+    tips, _ = oracle.prune_text(full, k, oracle.PRUNE_TIPS)
+    order = oracle.lines_tree_order(tips, k)
+    n = len([l for l in tips.split(b"\n") if l])
+    assert np.array_equal(np.sort(order), np.arange(n, dtype=np.uint64))
+    a, na = oracle.simplify_text(tips, k)
+    b, nb = oracle.simplify_text(tips, k, order)
+    assert na == nb > 0 and len(a) == len(b)
