@@ -205,13 +205,18 @@ def merge_metrics(g, survivors: int, steps: int, warmup: int) -> dict:
         ms.append(g.merge_info()["ms"])
     info = g.merge_info()
     m = statistics.median(ms)
-    # the two rank-0 passes on the merged graph (wall time of each call: the
+    # the reference's rank-0 sequence on the merged graph: tip pass,
+    # simplify, low-coverage pass, simplify (wall time of each call: the
     # kernels, the text rewrite and its host synchronisations)
     t0 = time.perf_counter()
     tips = g.remove_tips()
     t1 = time.perf_counter()
-    cut = g.remove_low_coverage()
+    s1 = g.simplify()
     t2 = time.perf_counter()
+    cut = g.remove_low_coverage()
+    t3 = time.perf_counter()
+    s2 = g.simplify()
+    t4 = time.perf_counter()
     return {"what": "merging of semi-extended k-molecules (simplifyDistNodeGraph) over the built graph, "
                     "result = the -d file's text on the device",
             "ms": m, "ms_all": ms, "k_molecules": survivors, "k_molecules_per_s": survivors / (m * 1e-3),
@@ -219,8 +224,10 @@ def merge_metrics(g, survivors: int, steps: int, warmup: int) -> dict:
             "text_bytes": info["text_bytes"], "launches": info["launches"],
             "random_accesses_per_k_molecule": MERGE_RANDOM_PER_NODE,
             "tips": {"wall_ms": (t1 - t0) * 1e3, "removed": tips},
-            "low_coverage": {"wall_ms": (t2 - t1) * 1e3, "arcs_cut": cut,
-                             "nodes_left": g.merge_info()["nodes"]}}
+            "simplify_after_tips": {"wall_ms": (t2 - t1) * 1e3, "merged": s1},
+            "low_coverage": {"wall_ms": (t3 - t2) * 1e3, "arcs_cut": cut},
+            "simplify_after_low_coverage": {"wall_ms": (t4 - t3) * 1e3, "merged": s2,
+                                            "nodes_left": g.merge_info()["nodes"]}}
 
 
 def merge_cpu_baseline(g, k: int) -> dict:

@@ -1,6 +1,8 @@
-// Two of the reference's rank-0 passes over the merged graph, on the device:
-// masterTipsRemoval (graph.cpp:2194-2265) and masterLowCoverageEdgeRemoval
-// (graph.cpp:2267-2300). They work on the merged graph's lines (node key, per
+// The reference's rank-0 passes over the merged graph that follow the merge,
+// on the device: masterTipsRemoval (graph.cpp:2194-2265),
+// masterLowCoverageEdgeRemoval (graph.cpp:2267-2300) and the re-merge the
+// reference runs after each, masterSimplifyNodeGraph (graph.cpp:2089-2192,
+// described with its kernels below). They work on the merged graph's lines (node key, per
 // arc slot its length, multiplicity, string offset and the far end's arc
 // back) and then rewrite its text (gathered node lines in key order, deleted
 // and arc-less nodes left out as gatherDistNodeGraph does, graph.cpp:587-596).
