@@ -278,7 +278,9 @@ swg_status swg_graph_write_node_lines(const swg_graph *g, const char *path);
  * nodes numbered 1..m from its smaller end arc (key, then slot), node p at
  * level ctz(p), levels in increasing order. A cycle of merged nodes is cut at
  * its largest key, which keeps the cycle on its two arcs. The result stays on
- * the device (as the -d file's text) until the next build. SWG_ERR_BAD_STATE
+ * the device (as the -d file's text) until the next build; the handle keeps
+ * the merge's device workspace in its own memory pool until swg_graph_free, so
+ * later merges and passes need not map it again. SWG_ERR_BAD_STATE
  * without a single-sample build; SWG_ERR_BAD_INPUT for an even k (the
  * reference's k is odd, sequence.cpp:44) or more than 2^29 k-molecules. */
 swg_status swg_graph_merge(swg_graph *g);

@@ -1427,6 +1427,16 @@ swg_status swg_graph_merge(swg_graph *g) {
     if (st) return st;
     SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
     g->merged = false;
+    if (!g->mg.pool) {  // the handle's own pool: merge scratch stays mapped between calls
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = g->device;
+        SWG_CUDA(cudaMemPoolCreate(&g->mg.pool, &props), "merge memory pool");
+        uint64_t keep = ~0ull;
+        SWG_CUDA(cudaMemPoolSetAttribute(g->mg.pool, cudaMemPoolAttrReleaseThreshold, &keep), "merge memory pool");
+    }
     cudaEvent_t e0 = g->ev[0], e1 = g->ev[1];
     SWG_CUDA(cudaEventRecord(e0, g->own), "merge timing");
     st = swg::merge_graph(g->d_out_keys, g->d_out_mult, g->n_out, g->k, g->own, &g->mg, &g->mres);

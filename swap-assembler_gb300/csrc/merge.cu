@@ -625,6 +625,7 @@ void merged_free(MergedGraph *m) {
     cudaFree(m->src2);
     cudaFree(m->back);
     cudaFree(m->del);
+    if (m->pool) cudaMemPoolDestroy(m->pool);
     *m = MergedGraph();
 }
 
@@ -639,7 +640,7 @@ swg_status merge_graph(const unsigned long long *d_keys, const unsigned long lon
         set_error("merge: k must be odd (an even k-mer can be its own reverse complement)");
         return SWG_ERR_BAD_INPUT;
     }
-    Scratch scr(s);
+    Scratch scr(s, mg->pool);
     MergeArgs a;
     std::memset(&a, 0, sizeof(a));
     a.k = k;

@@ -498,7 +498,7 @@ int sm_ceil_log2(uint64_t v) {
 }  // namespace
 
 swg_status prune_tips(MergedGraph *m, cudaStream_t s, uint64_t *count) {
-    Scratch scr(s);
+    Scratch scr(s, m->pool);
     unsigned char *tip = nullptr;
     unsigned long long *ctr = nullptr;
     if (!scr.get(&tip, m->lines) || !scr.get(&ctr, 1)) return cuda_err(cudaErrorMemoryAllocation, "tips workspace");
@@ -513,7 +513,7 @@ swg_status prune_tips(MergedGraph *m, cudaStream_t s, uint64_t *count) {
 
 swg_status simplify_lines(MergedGraph *m, cudaStream_t s, uint64_t *count) {
     *count = 0;
-    Scratch scr(s);
+    Scratch scr(s, m->pool);
     const uint64_t L = m->lines;
     SimplifyArgs a{};
     a.m = *m;
@@ -586,7 +586,7 @@ swg_status simplify_lines(MergedGraph *m, cudaStream_t s, uint64_t *count) {
 }
 
 swg_status prune_low_coverage(MergedGraph *m, cudaStream_t s, uint64_t *count) {
-    Scratch scr(s);
+    Scratch scr(s, m->pool);
     unsigned long long *ctr = nullptr;
     if (!scr.get(&ctr, 3)) return cuda_err(cudaErrorMemoryAllocation, "low-coverage workspace");
     EMIT_CUDA(cudaMemsetAsync(ctr, 0, 24, s), "low coverage");

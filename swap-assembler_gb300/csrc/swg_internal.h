@@ -210,6 +210,7 @@ struct MergedGraph {
     unsigned long long *src = nullptr, *src2 = nullptr;
     unsigned *back = nullptr;
     unsigned char *del = nullptr;  // deleted by a pass
+    cudaMemPool_t pool = nullptr;   // scratch of the merge and the passes, kept for reuse
 };
 void merged_free(MergedGraph *m);
 swg_status merged_reserve(MergedGraph *m, uint64_t bytes, uint64_t lines);

@@ -57,16 +57,21 @@ __device__ __forceinline__ uint64_t neighbour_dev(uint64_t key, int slot, int k)
 }
 
 // Stream-ordered device scratch, freed on every return path.
+// With a pool, from that pool (one that keeps its memory for reuse).
 struct Scratch {
     cudaStream_t s;
+    cudaMemPool_t pool;
     void *p[48] = {};
     int n = 0;
-    explicit Scratch(cudaStream_t st) : s(st) {}
+    explicit Scratch(cudaStream_t st, cudaMemPool_t mp = nullptr) : s(st), pool(mp) {}
     template <typename T>
     bool get(T **out, uint64_t count) {
         *out = nullptr;
         if (n == 48) return false;
-        if (cudaMallocAsync((void **)out, std::max<uint64_t>(count, 1) * sizeof(T), s) != cudaSuccess) {
+        const size_t bytes = std::max<uint64_t>(count, 1) * sizeof(T);
+        const cudaError_t e = pool ? cudaMallocFromPoolAsync((void **)out, bytes, pool, s)
+                                   : cudaMallocAsync((void **)out, bytes, s);
+        if (e != cudaSuccess) {
             cudaGetLastError();
             return false;
         }
