@@ -97,6 +97,50 @@ def test_abi_exports_every_declared_symbol():
         assert hasattr(lib, name)
 
 
+C_CALLER = r"""
+#include <stdio.h>
+#include <stdlib.h>
+#include "swapgb.h"
+int main(int argc, char **argv) {
+    swg_reads *reads = NULL;
+    if (argc < 2 || swg_reads_from_fasta_file(argv[1], 31, &reads) != SWG_OK) return 1;
+    const uint32_t *packed; const uint64_t *off; const uint32_t *len;
+    uint64_t n_words, n_reads, n_bases;
+    swg_reads_view(reads, &packed, &n_words, &off, &len, &n_reads, &n_bases);
+    swg_opts o = {0};
+    o.k = 31; o.cutoff = 5;
+    swg_graph *g = NULL;
+    swg_status st = swg_build(&o, packed, n_words, off, len, n_reads, &g);
+    swg_reads_free(reads);
+    if (st != SWG_OK) { printf("%s\n", swg_last_error()); return 1; }
+    uint64_t n = 0, bytes = 0, removed = 0, merged = 0, cut = 0;
+    swg_graph_size(g, &n);
+    uint64_t *keys = malloc(8 * n); uint8_t *mult = malloc(8 * n);
+    swg_graph_copy_out(g, keys, mult, n, 0, &n);
+    swg_graph_merge(g);
+    swg_graph_copy_merged(g, NULL, 0, &bytes);
+    swg_graph_remove_tips(g, &removed); swg_graph_simplify(g, &merged);
+    swg_graph_remove_low_coverage(g, &cut); swg_graph_simplify(g, &merged);
+    swg_merge_info mi; swg_graph_merge_info(g, &mi);
+    swg_graph_write_merged(g, "contigGraph.txt");
+    swg_graph_free(g); free(keys); free(mult);
+    return 0;
+}
+"""
+
+
+def test_header_is_plain_c_and_links(tmp_path):
+    """A C caller (no C++, no CUDA headers) compiles against include/swapgb.h
+    with warnings as errors and links against libswapgb.so."""
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-Werror", "-I" + str(ROOT / "include"),
+                        str(src), "-L" + str(swapgb.LIB_PATH.parent), "-lswapgb",
+                        "-Wl,-rpath," + str(swapgb.LIB_PATH.parent), "-o", str(tmp_path / "caller")],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout
+
+
 def test_status_strings():
     lib = swapgb.lib()
     for s in range(11):
