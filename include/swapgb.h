@@ -26,6 +26,7 @@
  *   distNodeGraph::masterTipsRemoval ........... graph.cpp:2194-2265 -> swg_graph_remove_tips
  *   distNodeGraph::masterLowCoverageEdgeRemoval  graph.cpp:2267-2300 -> swg_graph_remove_low_coverage
  *   distNodeGraph::masterSimplifyNodeGraph ..... graph.cpp:2089-2192 -> swg_graph_simplify
+ *   distNodeGraph::printContigs ................ graph.cpp:1139-1202 -> swg_graph_write_contigs
  *
  * Packed read layout (host or device memory):
  *   packed   uint32 words; base i of the concatenated read stream sits in
@@ -326,6 +327,13 @@ swg_status swg_graph_remove_low_coverage(swg_graph *g, uint64_t *cut);
  * positions from the smaller end arc, node p at level ctz(p)); a cycle of such
  * nodes is cut at its largest key. *merged = nodes merged away. */
 swg_status swg_graph_simplify(swg_graph *g, uint64_t *merged);
+/* The reference's printContigs (graph.cpp:1139-1202, noCEcontigs.fasta) on the
+ * merged graph as it stands: every arc of at least 100 - k bases
+ * (Contig_Length, sequence.h:15), once, from the end whose key is not smaller
+ * than the far end's, as the line ">proc0: " + that node's k-mer (its reverse
+ * complement for slots 4-7) + the arc string; nodes in key order. *n =
+ * contigs written. */
+swg_status swg_graph_write_contigs(swg_graph *g, const char *path, uint64_t *n);
 /* Host-only writers for records already in host memory (keys[n], mult[8*n],
  * any order): the same two file formats as above. */
 swg_status swg_records_write_kmer_graph(const uint64_t *keys, const uint8_t *mult, uint64_t n,

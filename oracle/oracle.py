@@ -253,6 +253,41 @@ def run_reference_simplify(lines_path: str, k: int, cutoff: int, outdir: str,
     return Path(outdir, "before.txt").read_bytes(), Path(outdir, "after.txt").read_bytes()
 
 
+CONTIG_LENGTH = 100  # sequence.h:15
+
+
+def _rc_str(s: str) -> str:
+    return s[::-1].translate(str.maketrans("ACGT", "TGCA"))
+
+
+def contigs_of_lines(text: bytes, k: int) -> list[str]:
+    """printContigs (graph.cpp:1139-1202) over gathered node lines: for every
+    arc of at least Contig_Length - k bases whose node key is not smaller than
+    the canonical id of the arc's last k bases, the node's k-mer (reverse
+    complemented for slots 4-7) + the arc string. Sorted."""
+    out = []
+    for line in text.split(b"\n"):
+        if not line.strip():
+            continue
+        head, rest = line.split(b" ", 1)
+        key = int(head)
+        arcs = [f.strip().decode() for f in rest.split(b"#")[:8]]
+        kmer = "".join("ACGT"[(key >> (2 * (k - 1 - i))) & 3] for i in range(k))
+        for i, a in enumerate(arcs):
+            if not a or len(a) < CONTIG_LENGTH - k:
+                continue
+            d = (kmer if i < 4 else _rc_str(kmer)) + a
+            last = d[-k:]
+            canon = max(last, _rc_str(last))
+            nid = 0
+            for ch in canon:
+                nid = nid * 4 + "ACGT".index(ch)
+            if key < nid:
+                continue
+            out.append(d)
+    return sorted(out)
+
+
 def tips_last_order(text: bytes, k: int) -> np.ndarray:
     """The GPU's visiting order for the tip pass: every node that is not a tip
     (in key order), then the tips in key order; as line indices of `text`."""

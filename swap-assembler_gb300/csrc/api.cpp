@@ -1529,6 +1529,17 @@ swg_status swg_graph_simplify(swg_graph *g, uint64_t *merged) {
     return st;
 }
 
+swg_status swg_graph_write_contigs(swg_graph *g, const char *path, uint64_t *n) {
+    if (!g || !path) return SWG_ERR_BAD_INPUT;
+    swg_status st = merged_state(g);
+    if (st) return st;
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    uint64_t c = 0;
+    st = swg::write_contigs(&g->mg, path, g->own, &c);
+    if (n) *n = st ? 0 : c;
+    return st;
+}
+
 static swg_status sorted_copy(const uint64_t *keys, const uint8_t *mult, uint64_t n,
                               std::vector<uint64_t> &k, std::vector<uint64_t> &m) {
     if (n && (!keys || !mult)) return SWG_ERR_BAD_INPUT;

@@ -495,6 +495,63 @@ int sm_ceil_log2(uint64_t v) {
     return r;
 }
 
+
+// ---- printContigs (graph.cpp:1139-1202): every arc of at least
+// Contig_Length - k bases (Contig_Length = 100, sequence.h:15) is printed
+// once, from the end whose key is not smaller than the far end's, as
+// ">proc0: " + the node's k-mer oriented for the arc's side + the arc string.
+constexpr int kContigLength = 100;
+
+__device__ __forceinline__ bool ct_prints(const MergedGraph &m, uint64_t a) {
+    const uint64_t q = a >> 3;
+    const unsigned l = m.len[a];
+    if (m.del[q] || l == 0 || (int)l < kContigLength - m.k) return false;
+    return m.key[q] >= m.key[m.back[a] >> 3];
+}
+
+__global__ void k_ct_len(MergedGraph m, uint64_t *__restrict__ out, unsigned long long *count) {
+    const uint64_t a = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= 8 * m.lines) return;
+    const bool p = ct_prints(m, a);
+    out[a] = p ? 8 + (uint64_t)m.k + m.len[a] + 1 : 0;
+    if (p) agg_add(count, 1);
+}
+
+__global__ void k_ct_write(MergedGraph m, const uint64_t *__restrict__ off, char *__restrict__ text) {
+    const uint64_t a = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= 8 * m.lines || off[a + 1] == off[a]) return;
+    char *p = text + off[a];
+    const char head[8] = {'>', 'p', 'r', 'o', 'c', '0', ':', ' '};
+    for (int i = 0; i < 8; ++i) *p++ = head[i];
+    const uint64_t key = m.key[a >> 3];
+    const uint64_t o = (a & 7) < 4 ? key : rc_dev(key, m.k);
+    for (int i = m.k - 1; i >= 0; --i) *p++ = "ACGT"[(o >> (2 * i)) & 3];
+    p[m.len[a]] = '\n';  // the arc string itself is copied in chunks
+}
+
+__global__ void k_ct_chunks(MergedGraph m, const uint64_t *__restrict__ off, uint64_t *__restrict__ chunks) {
+    const uint64_t a = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < 8 * m.lines) chunks[a] = off[a + 1] == off[a] ? 0 : (m.len[a] + kChunk - 1) / kChunk;
+}
+
+__global__ void k_ct_copy(MergedGraph m, const uint64_t *__restrict__ off, const uint64_t *__restrict__ first,
+                          uint64_t n_chunks, char *__restrict__ out) {
+    const uint64_t arcs = 8 * m.lines;
+    for (uint64_t c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        uint64_t lo = 0, hi = arcs;
+        while (hi - lo > 1) {
+            const uint64_t mid = (lo + hi) / 2;
+            if (first[mid] <= c) lo = mid;
+            else hi = mid;
+        }
+        const uint64_t at = (c - first[lo]) * kChunk;
+        const uint64_t rest = m.len[lo] - at;
+        const unsigned l = rest < kChunk ? (unsigned)rest : kChunk;
+        const char *a = m.text + m.src[lo] + at;
+        char *b = out + off[lo] + 8 + m.k + at;
+        for (unsigned i = threadIdx.x; i < l; i += blockDim.x) b[i] = a[i];
+    }
+}
 }  // namespace
 
 swg_status prune_tips(MergedGraph *m, cudaStream_t s, uint64_t *count) {
@@ -583,6 +640,42 @@ swg_status simplify_lines(MergedGraph *m, cudaStream_t s, uint64_t *count) {
     x.arc = a.xarc;
     x.at = a.xat;
     return rewrite(m, s, scr, x);
+}
+
+swg_status write_contigs(MergedGraph *m, const char *path, cudaStream_t s, uint64_t *count) {
+    *count = 0;
+    Scratch scr(s, m->pool);
+    const uint64_t arcs = 8 * m->lines;
+    uint64_t *len = nullptr, *off = nullptr, *chunks = nullptr, *first = nullptr;
+    unsigned long long *ctr = nullptr;
+    if (!scr.get(&len, arcs) || !scr.get(&off, arcs + 1) || !scr.get(&chunks, arcs) ||
+        !scr.get(&first, arcs + 1) || !scr.get(&ctr, 1))
+        return cuda_err(cudaErrorMemoryAllocation, "contig workspace");
+    EMIT_CUDA(cudaMemsetAsync(ctr, 0, 8, s), "contigs");
+    if (arcs) k_ct_len<<<blocks(arcs), 256, 0, s>>>(*m, len, ctr);
+    swg_status st = scan_lengths(len, off, arcs, scr, s);
+    if (st) return st;
+    uint64_t h[2] = {0, 0};
+    EMIT_CUDA(cudaMemcpyAsync(&h[0], off + arcs, 8, cudaMemcpyDeviceToHost, s), "contigs");
+    EMIT_CUDA(cudaMemcpyAsync(&h[1], ctr, 8, cudaMemcpyDeviceToHost, s), "contigs");
+    EMIT_CUDA(cudaStreamSynchronize(s), "contigs");
+    char *text = nullptr;
+    if (!scr.get(&text, h[0])) return cuda_err(cudaErrorMemoryAllocation, "contig text");
+    if (arcs) {
+        k_ct_write<<<blocks(arcs), 256, 0, s>>>(*m, off, text);
+        k_ct_chunks<<<blocks(arcs), 256, 0, s>>>(*m, off, chunks);
+        st = scan_lengths(chunks, first, arcs, scr, s);
+        if (st) return st;
+        uint64_t n_chunks = 0;
+        EMIT_CUDA(cudaMemcpyAsync(&n_chunks, first + arcs, 8, cudaMemcpyDeviceToHost, s), "contigs");
+        EMIT_CUDA(cudaStreamSynchronize(s), "contigs");
+        if (n_chunks)
+            k_ct_copy<<<(unsigned)std::min<uint64_t>(n_chunks, 1u << 20), 256, 0, s>>>(*m, off, first, n_chunks,
+                                                                                      text);
+    }
+    EMIT_CUDA(cudaGetLastError(), "contig kernels");
+    *count = h[1];
+    return stream_to_file(text, h[0], path, s);
 }
 
 swg_status prune_low_coverage(MergedGraph *m, cudaStream_t s, uint64_t *count) {

@@ -12,6 +12,8 @@
 //   contigGraph.txt with -d and without -s (graph.cpp:3617-3621), the graph
 //                  after merging its semi-extended k-molecules (the merge of
 //                  simplifyDistNodeGraph, graph.cpp:1392-1566, run on the GPU);
+//   noCEcontigs.fasta with it: the contigs of the merged graph as the
+//                  reference's printContigs writes them (graph.cpp:1139-1202);
 //   logtime.txt    phase times.
 // stdout carries the reference's graph totals (graph.cpp:1621-1625).
 // Unlike the reference, every failure exits with a nonzero status.
@@ -158,6 +160,10 @@ int main(int argc, char **argv) {
         if ((st = swg_graph_merge_info(g, &minfo))) return fail(st, "merge info");
         if ((st = swg_graph_write_merged(g, (out + "/contigGraph.txt").c_str())))
             return fail(st, "writing contigGraph.txt");
+        uint64_t contigs = 0;
+        if ((st = swg_graph_write_contigs(g, (out + "/noCEcontigs.fasta").c_str(), &contigs)))
+            return fail(st, "writing noCEcontigs.fasta");
+        std::printf(">proc0: %llu contigs\n", (unsigned long long)contigs);
     }
     const double t3 = now_s();
     float ms[5];

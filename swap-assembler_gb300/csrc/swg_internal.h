@@ -227,6 +227,8 @@ swg_status prune_tips(MergedGraph *mg, cudaStream_t s, uint64_t *count);
 swg_status prune_low_coverage(MergedGraph *mg, cudaStream_t s, uint64_t *count);
 // masterSimplifyNodeGraph on the merged graph (prune.cu); *count = nodes merged away.
 swg_status simplify_lines(MergedGraph *mg, cudaStream_t s, uint64_t *count);
+// printContigs of the merged graph into a file (prune.cu); *count = contigs.
+swg_status write_contigs(MergedGraph *mg, const char *path, cudaStream_t s, uint64_t *count);
 swg_status emit_node_lines(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n,
                            int k, const char *path, cudaStream_t s);
 swg_status emit_kmer_graph(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n, int k,

@@ -140,6 +140,7 @@ def lib() -> C.CDLL:
             "swg_graph_remove_tips": (i32, [P, pu64]),
             "swg_graph_remove_low_coverage": (i32, [P, pu64]),
             "swg_graph_simplify": (i32, [P, pu64]),
+            "swg_graph_write_contigs": (i32, [P, C.c_char_p, pu64]),
             "swg_records_write_kmer_graph": (i32, [P, P, u64, i32, C.c_char_p]),
             "swg_records_write_node_lines": (i32, [P, P, u64, C.c_char_p]),
             "swg_graph_last_timings": (i32, [P, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
@@ -336,6 +337,12 @@ class Graph:
         """masterSimplifyNodeGraph on the merged graph; returns the nodes merged away."""
         n = C.c_uint64()
         _check(lib().swg_graph_simplify(self._h, C.byref(n)), "swg_graph_simplify")
+        return n.value
+
+    def write_contigs(self, path: str) -> int:
+        """printContigs of the merged graph into `path`; returns the contigs written."""
+        n = C.c_uint64()
+        _check(lib().swg_graph_write_contigs(self._h, str(path).encode(), C.byref(n)), "swg_graph_write_contigs")
         return n.value
 
     def write_merged(self, path: str) -> None:

@@ -134,6 +134,7 @@ def test_cli_writes_contig_graph(tmp_path):
     keys, mult = oracle.records(case_text(case), case["k"], case["c"])
     assert _lines(got) == _lines(oracle.merge_text(keys, mult, case["k"]))
     assert "Simplify DistGraph" in (out / "logtime.txt").read_text()
+    assert oracle.contig_sequences(out / "noCEcontigs.fasta") == oracle.contigs_of_lines(got, case["k"])
     # with -s the reference stops after kmerGraph.txt: no merge
     out2 = tmp_path / "o2"
     r = subprocess.run([str(SWAP), "-k", str(case["k"]), "-c", str(case["c"]), "-i", str(fa), "-o", str(out2),
@@ -240,3 +241,22 @@ def test_simplify_cycles():
         assert g.simplify() == 2
         want, _ = oracle.simplify_text(tips, k, oracle.lines_tree_order(tips, k))
         assert _lines(g.merged_text()) == _lines(want) and len(_lines(want)) == 1
+
+
+@pytest.mark.parametrize("case", PRUNE_CASES[:4], ids=lambda c: c["name"])
+def test_contigs_match_oracle(case, tmp_path):
+    """swg_graph_write_contigs (printContigs) on the merged graph, and again
+    after the tip pass and re-merge, against the restatement on the same
+    lines; the file holds exactly the '>proc0: ' lines."""
+    k, c = case["k"], case["c"]
+    g = swapgb.Graph()
+    g.build_fasta(swapgb.Opts(k=k, cutoff=c), case_text(case))
+    g.merge()
+    for step in range(2):
+        p = tmp_path / ("contigs%d.fasta" % step)
+        n = g.write_contigs(str(p))
+        body = p.read_bytes()
+        assert body.count(b"\n") == n and all(l.startswith(b">proc0: ") for l in body.split(b"\n") if l)
+        assert oracle.contig_sequences(p) == oracle.contigs_of_lines(g.merged_text(), k)
+        g.remove_tips()
+        g.simplify()

@@ -230,3 +230,18 @@ def test_simplify_order_is_a_permutation_and_merges_as_many():
     a, na = oracle.simplify_text(tips, k)
     b, nb = oracle.simplify_text(tips, k, order)
     assert na == nb > 0 and len(a) == len(b)
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference not compiled here")
+@pytest.mark.parametrize("case", MERGE_CASES[:2] + [c for c in SYNTH_CASES if c["name"] == "c1_small"],
+                         ids=lambda c: c["name"])
+def test_contigs_of_the_complete_merge_match_the_reference_writer(case, tmp_path):
+    """printContigs restated (oracle.contigs_of_lines) equals the reference's
+    own noCEcontigs.fasta on the same merged graph (its contig stage run on
+    the complete merge; its masterSimplifyNodeGraph finds nothing to merge)."""
+    k = case["k"]
+    full = oracle.merge_text(*oracle.records(case_text(case), k, case["c"]), k)
+    mp = tmp_path / "merged.txt"
+    mp.write_bytes(full)
+    theirs, _ = oracle.run_reference_contigs(str(mp), k, case["c"], str(tmp_path / "o"))
+    assert oracle.contigs_of_lines(full, k) == theirs
