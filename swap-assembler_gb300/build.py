@@ -98,7 +98,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict[str, Path]:
     lib_objs = [OBJ / n for n in ("kernels.o", "framing.o", "emit.o", "merge.o", "prune.o", "noalloc.o", "api.o", "reads.o",
                                   "writers.o", "server.o", "autotune.o")]
     if _stale(lib, lib_objs):
-        _run([nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, lib_objs), "-lpthread"])
+        _run([nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, lib_objs), "-lpthread", "-ldl"])
     synth = PKG / "libswgsynth.so"
     if _stale(synth, [synth_o]):
         _run(["g++", "-shared", "-pthread", "-o", str(synth), str(synth_o)])

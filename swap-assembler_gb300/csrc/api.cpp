@@ -20,6 +20,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "swg_internal.h"
 
 namespace swg {
@@ -240,8 +242,18 @@ bool bucketed_fits(const swg_graph *g, uint64_t occurrences) {
     return need <= 0.8 * ((double)free_b + held);
 }
 
+// NVTX range over one call, named after the reference's phase it replaces
+// (visible to a profiler; no cost without one).
+struct Phase {
+    explicit Phase(const char *name) { nvtxRangePushA(name); }
+    ~Phase() { nvtxRangePop(); }
+    Phase(const Phase &) = delete;
+    Phase &operator=(const Phase &) = delete;
+};
+
 swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, uint64_t n_words,
                       const uint64_t *off, const uint32_t *len, uint64_t n_reads) {
+    Phase phase("constructDistNodeGraph + cutoffGraph");
     swg_status st = check_opts(o);
     if (st) return st;
     if (n_reads >= 0xffffffffull) {
@@ -1218,6 +1230,7 @@ swg_status swg_graph_build(swg_graph *g, const swg_opts *o, const uint32_t *pack
 }
 
 swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *text, uint64_t len) {
+    Phase phase("constructKmerGraph framing + build");
     if (!g) return SWG_ERR_BAD_INPUT;
     swg_status st = check_opts(o);
     if (st) return st;
@@ -1404,6 +1417,7 @@ static swg_status writable(const swg_graph *g) {
 }
 
 swg_status swg_graph_write_kmer_graph(const swg_graph *g, const char *path) {
+    Phase phase("printKmerGraph");
     if (!g || !path) return SWG_ERR_BAD_INPUT;
     swg_status st = writable(g);
     if (st) return st;
@@ -1412,6 +1426,7 @@ swg_status swg_graph_write_kmer_graph(const swg_graph *g, const char *path) {
 }
 
 swg_status swg_graph_write_node_lines(const swg_graph *g, const char *path) {
+    Phase phase("printLocalNodeGraph");
     if (!g || !path) return SWG_ERR_BAD_INPUT;
     swg_status st = writable(g);
     if (st) return st;
@@ -1422,6 +1437,7 @@ swg_status swg_graph_write_node_lines(const swg_graph *g, const char *path) {
 // Merging of semi-extended k-molecules (merge.cu) over the built graph; the
 // result is the -d file's text, kept on the device until the next build.
 swg_status swg_graph_merge(swg_graph *g) {
+    Phase phase("simplifyDistNodeGraph");
     if (!g) return SWG_ERR_BAD_INPUT;
     swg_status st = writable(g);
     if (st) return st;
@@ -1494,6 +1510,7 @@ swg_status swg_graph_write_merged(const swg_graph *g, const char *path) {
 
 // Rank-0 passes of the reference over the merged graph (prune.cu).
 swg_status swg_graph_remove_tips(swg_graph *g, uint64_t *removed) {
+    Phase phase("masterTipsRemoval");
     if (!g) return SWG_ERR_BAD_INPUT;
     swg_status st = merged_state(g);
     if (st) return st;
@@ -1506,6 +1523,7 @@ swg_status swg_graph_remove_tips(swg_graph *g, uint64_t *removed) {
 }
 
 swg_status swg_graph_remove_low_coverage(swg_graph *g, uint64_t *cut) {
+    Phase phase("masterLowCoverageEdgeRemoval");
     if (!g) return SWG_ERR_BAD_INPUT;
     swg_status st = merged_state(g);
     if (st) return st;
@@ -1518,6 +1536,7 @@ swg_status swg_graph_remove_low_coverage(swg_graph *g, uint64_t *cut) {
 }
 
 swg_status swg_graph_simplify(swg_graph *g, uint64_t *merged) {
+    Phase phase("masterSimplifyNodeGraph");
     if (!g) return SWG_ERR_BAD_INPUT;
     swg_status st = merged_state(g);
     if (st) return st;
@@ -1530,6 +1549,7 @@ swg_status swg_graph_simplify(swg_graph *g, uint64_t *merged) {
 }
 
 swg_status swg_graph_write_contigs(swg_graph *g, const char *path, uint64_t *n) {
+    Phase phase("printContigs");
     if (!g || !path) return SWG_ERR_BAD_INPUT;
     swg_status st = merged_state(g);
     if (st) return st;

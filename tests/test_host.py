@@ -1,5 +1,6 @@
 """Host-side parts of the library that need no GPU: FASTA framing and 2-bit
 packing, the output writers, the C-ABI surface and the command line."""
+import os
 import re
 import subprocess
 from pathlib import Path
@@ -139,6 +140,31 @@ def test_header_is_plain_c_and_links(tmp_path):
                         "-Wl,-rpath," + str(swapgb.LIB_PATH.parent), "-o", str(tmp_path / "caller")],
                        stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     assert r.returncode == 0, r.stdout
+
+
+def test_host_code_under_address_and_undefined_sanitizers(tmp_path):
+    """The host FASTA framing/packing (multi-threaded) and the text writers,
+    compiled with -fsanitize=address,undefined, over the golden known-answer
+    inputs, malformed inputs and random records: no sanitizer report."""
+    import shutil
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    cuda_inc = os.environ.get("CUDA_HOME", "/usr/local/cuda") + "/include"
+    csrc = ROOT / "swap-assembler_gb300" / "csrc"
+    exe = tmp_path / "host_sanitize"
+    r = subprocess.run(["g++", "-std=c++17", "-fsanitize=address,undefined", "-fno-sanitize-recover=all", "-g",
+                        "-O1", "-I" + str(ROOT / "include"), "-I" + str(csrc), "-I" + cuda_inc,
+                        str(csrc / "reads.cpp"), str(csrc / "writers.cpp"),
+                        str(ROOT / "tests" / "sanitize" / "host_sanitize.cpp"), "-lpthread", "-o", str(exe)],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, stdin=subprocess.DEVNULL)
+    if r.returncode != 0 and "sanitize" in r.stdout:
+        pytest.skip("sanitizer runtime not available: " + r.stdout[-300:])
+    assert r.returncode == 0, r.stdout
+    inputs = sorted(str(p) for p in (ROOT / "tests" / "golden").glob("*.fa"))
+    env = dict(os.environ, SWG_SANITIZE_OUT=str(tmp_path))
+    r = subprocess.run([str(exe), *inputs], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                       env=env, stdin=subprocess.DEVNULL, timeout=600)
+    assert r.returncode == 0 and "clean" in r.stdout, r.stdout[-3000:]
 
 
 def test_status_strings():
