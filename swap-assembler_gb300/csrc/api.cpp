@@ -147,6 +147,16 @@ struct swg_graph {
     float merge_ms = 0;
     unsigned *d_hll_seg = nullptr;
     uint64_t hll_seg_cap = 0;
+    // streamed FASTA build: the copy stream, one event per text piece, and
+    // the framing arrays that grow as pieces land
+    cudaStream_t copy = nullptr, frame = nullptr;
+    std::vector<cudaEvent_t> piece_ev;
+    uint64_t *d_sfw = nullptr;  // block counts | block bases | scan scratch | totals
+    uint64_t sfw_cap = 0;
+    uint64_t *d_nl = nullptr;
+    uint64_t nl_cap = 0;
+    uint64_t *d_keep = nullptr, *d_words = nullptr, *d_ridx = nullptr, *d_woff = nullptr;
+    uint64_t keep_cap = 0, words_cap = 0, ridx_cap = 0, woff_cap = 0;
 };
 
 namespace {
@@ -864,11 +874,21 @@ swg_status batch_impl(swg_graph *g, const swg_opts *o, const swg_sample *sm, uin
 // them. A partition or bucket that outgrows its region (a sampling miss) sets
 // a status bit, the later kernels skip their work, and the build reruns with
 // exact counts (counted = true).
-swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s,
-                          double load, bool counted) {
+struct BucketPlan {
+    int b1 = 0, b2 = 0;
+    uint64_t P = 0, NB = 0;
+    swg::PartArgs pa;
+    swg::BucketArgs bk;
+    unsigned long long *scr = nullptr, *sampled = nullptr;
+};
+
+// Sizes the bucketed build for N occurrences, allocates its workspace and
+// lays out the level-1 partition and bucket regions: from exact counts over
+// the reads of a (counted), else from a sample of them (every stride-th
+// batch, once N reaches 64M occurrences).
+swg_status bucketed_plan(swg_graph *g, const BuildArgs &a, uint64_t N, bool counted, uint32_t stride,
+                         cudaStream_t s, BucketPlan &pl) {
     swg_status st;
-    g->algorithm = SWG_ALGO_BUCKETED;
-    const uint64_t N = a.total_occ;
     // level-1 partitions: 256, 512 past 400M occurrences (a level-1 round of
     // 4096 records still writes runs of 8), 1024 only past 6.4G
     int b1 = N <= (400ull << 20) ? 8 : (N <= (6400ull << 20) ? 9 : 10);
@@ -940,10 +960,10 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
         g->launches += swg::launch_part_prefix(pa, s);
     } else {
         SWG_CUDA(cudaMemsetAsync(bk.cursor2, 0, NB * 8, s), "clear bucket samples");
-        // from 64M occurrences every 16th batch of reads is sampled; smaller
-        // inputs get uniform regions (an empty sample), whose slack covers
-        // their spread (a skewed one recounts)
-        if (N >= (64ull << 20)) g->launches += swg::launch_p1_sample(a, pa, bk, 16, s);
+        // from 64M occurrences every stride-th batch of reads is sampled;
+        // smaller inputs get uniform regions (an empty sample), whose slack
+        // covers their spread (a skewed one recounts)
+        if (N >= (64ull << 20)) g->launches += swg::launch_p1_sample(a, pa, bk, stride, s);
         g->launches += swg::launch_part_caps(pa, N, sampled, s);
         // bucket regions from the same sample (surv serves as scratch)
         g->launches += swg::launch_bucket_caps(bk.cursor2, sampled, N, NB, bk.surv, s);
@@ -953,9 +973,45 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
                                          reinterpret_cast<uint64_t *>(bk.off2 + NB), s);
         SWG_CUDA(cudaMemcpyAsync(bk.cursor2, bk.off2, NB * 8, cudaMemcpyDeviceToDevice, s), "bucket cursors");
     }
+    pl.b1 = b1;
+    pl.b2 = b2;
+    pl.P = P;
+    pl.NB = NB;
+    pl.pa = pa;
+    pl.bk = bk;
+    pl.scr = scr;
+    pl.sampled = sampled;
+    return SWG_OK;
+}
+
+swg_status bucketed_finish(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s, double load,
+                           bool counted, BucketPlan &pl);
+
+swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s,
+                          double load, bool counted) {
+    swg_status st;
+    g->algorithm = SWG_ALGO_BUCKETED;
+    BucketPlan pl;
+    if ((st = bucketed_plan(g, a, a.total_occ, counted, 16, s, pl))) return st;
     SWG_CUDA(cudaEventRecord(g->ev[1], s), "event");
-    g->launches += swg::launch_part_scatter(a, pa, s);
+    g->launches += swg::launch_part_scatter(a, pl.pa, s);
     SWG_CUDA(cudaEventRecord(g->ev[2], s), "event");
+    return bucketed_finish(g, o, a, s, load, counted, pl);
+}
+
+// Everything after the level-1 scatter: level-2 scatter, bucket counting,
+// survivor packing, the big buckets; an overflowed region reruns the build
+// with exact counts.
+swg_status bucketed_finish(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStream_t s, double load,
+                           bool counted, BucketPlan &pl) {
+    swg_status st;
+    g->algorithm = SWG_ALGO_BUCKETED;
+    const uint64_t N = a.total_occ;
+    const int b1 = pl.b1, b2 = pl.b2;
+    const uint64_t P = pl.P, NB = pl.NB;
+    swg::BucketArgs &bk = pl.bk;
+    unsigned long long *scr = pl.scr;
+    (void)P;
     g->launches += swg::launch_chunk_prefix(bk, s);
     if (counted) {  // exact bucket regions
         SWG_CUDA(cudaMemsetAsync(bk.cursor2, 0, NB * 8, s), "clear bucket counts");
@@ -1074,6 +1130,244 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     return SWG_OK;
 }
 
+// Grows a device array to want elements, keeping its first keep. Called
+// only where the stream that uses the array is idle (after a synchronize).
+template <typename T>
+swg_status grow_keep(T **p, uint64_t *cap, uint64_t want, uint64_t keep, const char *what) {
+    if (*p && *cap >= want) return SWG_OK;
+    T *q = nullptr;
+    const uint64_t n = std::max<uint64_t>(want, 1);
+    cudaError_t e = cudaMalloc((void **)&q, n * sizeof(T));
+    if (e == cudaSuccess && *p && keep) e = cudaMemcpy(q, *p, keep * sizeof(T), cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(q);
+        return cuda_fail(e, what);
+    }
+    cudaFree(*p);
+    *p = q;
+    *cap = n;
+    return SWG_OK;
+}
+
+constexpr uint64_t kStreamMin = 96ull << 20;    // shorter texts go up and are framed in one piece
+constexpr uint64_t kStreamPiece = 64ull << 20;  // target bytes per piece
+constexpr uint64_t kStreamMaxPieces = 16;
+
+// Streamed FASTA build (texts of kStreamMin bytes and more). The text goes
+// up in pieces on a copy stream; a framing stream frames each piece as it
+// lands — newline counts, newline positions, the records completed so far,
+// their packing — and, on the bucketed path, the build stream scatters that
+// piece's reads to the level-1 partitions while the next pieces are copied
+// and framed. The framing stream's host round trips (record and word totals)
+// never wait for a scatter. The partition and bucket regions are sized from
+// the first piece: its occurrences per text byte scale to the whole text (a
+// region that the estimate or the sample misses overflows, and the build
+// recounts exactly, as the one-shot build does), and its reads are the
+// sample. Any piece with a read longer than the bucketed build takes,
+// another algorithm or read order, or a graph the bucketed workspace does not
+// fit, falls back to the one-shot build over the reads framed here. Results
+// are those of the one-shot build.
+swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *first, uint64_t n,
+                                cudaStream_t s) {
+    swg_status st;
+    const uint64_t nc = swg::framing_chunks(n);
+    uint64_t C = std::min<uint64_t>(kStreamMaxPieces, std::max<uint64_t>(2, n / kStreamPiece));
+    if (const char *e = std::getenv("SWG_STREAM_PIECES"))  // at most 16: the first piece is the sample
+        C = std::min<uint64_t>(kStreamMaxPieces, std::max(2, std::atoi(e)));
+    std::vector<uint64_t> cut(C + 1);  // piece c: bytes [cut[c], cut[c+1]), on framing-chunk bounds
+    for (uint64_t c = 0; c < C; ++c) cut[c] = nc * c / C * swg::kFramingChunk;
+    cut[C] = n;
+    if (!g->copy) SWG_CUDA(cudaStreamCreateWithFlags(&g->copy, cudaStreamNonBlocking), "copy stream");
+    if (!g->frame) {  // the framing stream's blocks go first as the scatter's retire
+        int least = 0, greatest = 0;
+        SWG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+        SWG_CUDA(cudaStreamCreateWithPriority(&g->frame, cudaStreamNonBlocking, greatest), "framing stream");
+    }
+    cudaStream_t F = g->frame;
+    while (g->piece_ev.size() < 2 * C) {  // copied [C] | packed [C]
+        cudaEvent_t e = nullptr;
+        SWG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "piece event");
+        g->piece_ev.push_back(e);
+    }
+    cudaEvent_t *copied = g->piece_ev.data(), *packed_ev = copied + C;
+    // +64: the packing kernel's aligned 16-byte loads read up to 31 bytes past a record
+    if ((st = ensure(&g->d_text, &g->text_cap, n + 64, "FASTA text"))) return st;
+    // the copies and the framing wait for earlier work on the build stream
+    SWG_CUDA(cudaEventRecord(g->ev[6], s), "event");
+    SWG_CUDA(cudaStreamWaitEvent(g->copy, g->ev[6], 0), "copy stream wait");
+    SWG_CUDA(cudaStreamWaitEvent(F, g->ev[6], 0), "framing stream wait");
+    for (uint64_t c = 0; c < C; ++c) {
+        SWG_CUDA(cudaMemcpyAsync(g->d_text + cut[c], first + cut[c], cut[c + 1] - cut[c],
+                                 cudaMemcpyHostToDevice, g->copy),
+                 "copy FASTA piece");
+        SWG_CUDA(cudaEventRecord(copied[c], g->copy), "piece event");
+    }
+    // the caller's buffer is read until the last copy ends, and the framing
+    // stream's work must end before the arrays it writes are reused: no
+    // return before both streams are idle
+    struct Drain {
+        cudaStream_t c, f;
+        ~Drain() {
+            cudaStreamSynchronize(c);
+            cudaStreamSynchronize(f);
+        }
+    } drain{g->copy, F};
+    // workspace: block counts [nc] | block bases [nc] | scan scratch [S] | totals [8]
+    // totals: newlines, reads, words, occurrences, longest read, NUL flag
+    const uint64_t S = std::max(swg::gscan_scratch(nc), swg::gscan_scratch(n / 2 + 1));
+    if ((st = ensure(&g->d_sfw, &g->sfw_cap, 2 * nc + S + 8, "framing workspace"))) return st;
+    uint64_t *counts = g->d_sfw, *cbase = counts + nc, *scratch = cbase + nc, *tot = scratch + S;
+    auto *acc = reinterpret_cast<unsigned long long *>(tot + 3);
+    unsigned *nul_flag = reinterpret_cast<unsigned *>(tot + 5);
+    SWG_CUDA(cudaMemsetAsync(tot, 0, 8 * 8, F), "clear framing totals");
+
+    // build state, as build_impl sets it
+    g->built = false;
+    g->merged = false;
+    g->n_samples = 0;
+    g->k = o->k;
+    g->cutoff = o->cutoff;
+    g->launches = 0;
+    g->retries = 0;
+    g->estimate = 0;
+    const double load = o->load_factor > 0 ? o->load_factor : 0.6;
+    SWG_CUDA(cudaEventRecord(g->ev[0], s), "event");
+    SWG_CUDA(cudaMemsetAsync(g->d_ctl, 0, sizeof(Control), s), "memset control");
+    BuildArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.k = o->k;
+    a.cutoff = o->cutoff;
+    a.hll = g->d_hll;
+    a.status = &g->d_ctl->status;
+    a.counters = g->d_ctl->counters;
+    BucketPlan pl;
+    bool stream = o->algorithm == SWG_ALGO_BUCKETED ||
+                  (o->algorithm == SWG_ALGO_DEFAULT && o->read_order == SWG_ORDER_INPUT);
+    int launches = 0;
+    uint64_t NL = 0, R = 0, reads = 0, words = 0, occ = 0, longest = 0;
+    for (uint64_t c = 0; c < C; ++c) {
+        SWG_CUDA(cudaStreamWaitEvent(F, copied[c], 0), "piece wait");
+        const uint64_t j0 = cut[c] / swg::kFramingChunk, end = cut[c + 1];
+        launches += swg::launch_nl_count(g->d_text, end, counts, nul_flag, F, j0);
+        launches += swg::launch_gscan(counts, cbase, swg::framing_chunks(end), scratch, tot, F);
+        uint64_t h[6] = {0, 0, 0, 0, 0, 0};
+        SWG_CUDA(cudaMemcpyAsync(h, tot, sizeof(h), cudaMemcpyDeviceToHost, F), "read newline count");
+        SWG_CUDA(cudaStreamSynchronize(F), "framing count");
+        if ((unsigned)h[5]) {
+            swg::set_error("NUL byte in the FASTA input");
+            return SWG_ERR_BAD_INPUT;
+        }
+        const uint64_t NLc = h[0], Rc = NLc / 2;
+        // capacities from the first piece, scaled to the whole text with slack
+        const double scale = (double)n / (double)end;
+        const uint64_t nl_want = std::max<uint64_t>(NLc, (uint64_t)(scale * 1.1 * (double)NLc) + 1024);
+        if ((st = grow_keep(&g->d_nl, &g->nl_cap, g->nl_cap >= NLc ? NLc : nl_want, NL, "newline positions")))
+            return st;
+        const uint64_t r_want = std::max<uint64_t>(Rc, (uint64_t)(scale * 1.1 * (double)Rc) + 1024);
+        const uint64_t rw = g->keep_cap >= Rc ? Rc : r_want;
+        if ((st = grow_keep(&g->d_keep, &g->keep_cap, rw, R, "record flags")) ||
+            (st = grow_keep(&g->d_words, &g->words_cap, rw, R, "record words")) ||
+            (st = grow_keep(&g->d_ridx, &g->ridx_cap, rw, R, "read index")) ||
+            (st = grow_keep(&g->d_woff, &g->woff_cap, rw, R, "word offsets")))
+            return st;
+        launches += swg::launch_nl_pos(g->d_text, end, cbase, g->d_nl, F, j0);
+        launches += swg::launch_rec_len(g->d_nl, Rc, o->k, g->d_keep, g->d_words, F, R, acc);
+        // this piece's records only: prefixes from 0, the totals so far added when packing
+        launches += swg::launch_gscan(g->d_keep + R, g->d_ridx + R, Rc - R, scratch, tot + 1, F);
+        launches += swg::launch_gscan(g->d_words + R, g->d_woff + R, Rc - R, scratch, tot + 2, F);
+        SWG_CUDA(cudaGetLastError(), "framing launch");
+        SWG_CUDA(cudaMemcpyAsync(h, tot, sizeof(h), cudaMemcpyDeviceToHost, F), "read framing totals");
+        SWG_CUDA(cudaStreamSynchronize(F), "framing scan");
+        const uint64_t reads_c = reads + h[1], words_c = words + h[2], occ_c = h[3];
+        longest = std::max<uint64_t>(longest, h[4]);
+        // the reads' arrays grow only with the build stream idle: its
+        // scatters of earlier pieces read them
+        const bool grow_packed = g->packed_cap < words_c + 4 || !g->d_packed;
+        const bool grow_reads = g->reads_cap < reads_c || !g->d_off || !g->d_len;
+        if (grow_packed || grow_reads) SWG_CUDA(cudaStreamSynchronize(s), "build stream");
+        if (grow_packed) {
+            const uint64_t p_want = std::max<uint64_t>(words_c + 4, (uint64_t)(scale * 1.1 * (double)words_c) + 1024);
+            if ((st = grow_keep(&g->d_packed, &g->packed_cap, p_want, words, "packed reads"))) return st;
+        }
+        if (grow_reads) {
+            const uint64_t rd_want = std::max<uint64_t>(reads_c, (uint64_t)(scale * 1.1 * (double)reads_c) + 1024);
+            uint64_t c1 = g->reads_cap, c2 = g->reads_cap;
+            if ((st = grow_keep(&g->d_off, &c1, rd_want, reads, "read offsets")) ||
+                (st = grow_keep(&g->d_len, &c2, rd_want, reads, "read lengths")))
+                return st;
+            g->reads_cap = std::min(c1, c2);
+        }
+        launches += swg::launch_rec_pack(g->d_text, g->d_nl, Rc, o->k, g->d_ridx, g->d_woff, g->d_off,
+                                         g->d_len, g->d_packed, F, R, reads, words);
+        SWG_CUDA(cudaGetLastError(), "pack launch");
+        SWG_CUDA(cudaEventRecord(packed_ev[c], F), "packed event");
+        if (stream && o->algorithm == SWG_ALGO_DEFAULT && longest > kBucketedMaxRead) stream = false;
+        if (stream && c == 0) {
+            // the first piece sizes the build: its occurrences per byte, and its reads as the sample
+            const uint64_t N_est = occ_c ? (uint64_t)(scale * (double)occ_c * 1.02) + 65536 : 0;
+            if (!N_est || (o->algorithm == SWG_ALGO_DEFAULT && !bucketed_fits(g, N_est))) {
+                stream = false;
+            } else {
+                SWG_CUDA(cudaStreamWaitEvent(s, packed_ev[0], 0), "build stream wait");
+                BuildArgs a0 = a;
+                a0.packed = g->d_packed;
+                a0.n_words = words_c;
+                a0.read_off = g->d_off;
+                a0.read_len = g->d_len;
+                a0.n_reads = reads_c;
+                a0.total_occ = occ_c;
+                g->algorithm = SWG_ALGO_BUCKETED;
+                const uint32_t stride = (uint32_t)std::max<uint64_t>(1, 16 / C);
+                if ((st = bucketed_plan(g, a0, N_est, false, stride, s, pl))) return st;
+                SWG_CUDA(cudaEventRecord(g->ev[1], s), "event");
+            }
+        }
+        if (stream && reads_c > reads) {  // this piece's reads to the level-1 partitions
+            SWG_CUDA(cudaStreamWaitEvent(s, packed_ev[c], 0), "build stream wait");
+            BuildArgs ac = a;
+            ac.packed = g->d_packed;
+            ac.n_words = words_c;
+            ac.read_off = g->d_off + reads;
+            ac.read_len = g->d_len + reads;
+            ac.n_reads = reads_c - reads;
+            ac.total_occ = occ_c - occ;
+            SWG_CUDA(cudaMemsetAsync(&g->d_ctl->work[1], 0, sizeof(unsigned long long), s), "clear work");
+            g->launches += swg::launch_part_scatter(ac, pl.pa, s, false);
+            SWG_CUDA(cudaGetLastError(), "scatter launch");
+        }
+        NL = NLc;
+        R = Rc;
+        reads = reads_c;
+        words = words_c;
+        occ = occ_c;
+    }
+    // the build stream goes on after all framing
+    SWG_CUDA(cudaStreamWaitEvent(s, packed_ev[C - 1], 0), "build stream wait");
+    if (NL & 1) {
+        swg::set_error("the last record has a header line but no sequence line");
+        return SWG_ERR_BAD_INPUT;
+    }
+    if (stream && o->algorithm == SWG_ALGO_DEFAULT && !bucketed_fits(g, occ)) stream = false;
+    if (!stream) {  // the one-shot build over the reads framed here
+        st = build_impl(g, o, g->d_packed, words, g->d_off, g->d_len, reads);
+        if (st == SWG_OK) g->launches += launches;
+        return st;
+    }
+    SWG_CUDA(cudaEventRecord(g->ev[2], s), "event");
+    a.packed = g->d_packed;
+    a.n_words = words;
+    a.read_off = g->d_off;
+    a.read_len = g->d_len;
+    a.n_reads = reads;
+    a.total_occ = occ;
+    g->occurrences = occ;
+    g->h_ctl->max_len = (unsigned)longest;
+    pl.bk.n_rec = occ;
+    g->launches += launches;
+    return bucketed_finish(g, o, a, s, load, false, pl);
+}
+
 swg_status fetch_sorted(const swg_graph *g, std::vector<uint64_t> &keys,
                         std::vector<uint64_t> &mult) {
     if (!g || !g->built || g->n_samples) {
@@ -1187,6 +1481,18 @@ void swg_graph_free(swg_graph *g) {
     cudaFree(g->d_plen);
     cudaFree(g->d_records);
     cudaFree(g->d_slices);
+    cudaFree(g->d_sfw);
+    cudaFree(g->d_nl);
+    cudaFree(g->d_keep);
+    cudaFree(g->d_words);
+    cudaFree(g->d_ridx);
+    cudaFree(g->d_woff);
+    if (g->copy) cudaStreamSynchronize(g->copy);
+    if (g->frame) cudaStreamSynchronize(g->frame);
+    for (auto &e : g->piece_ev)
+        if (e) cudaEventDestroy(e);
+    if (g->copy) cudaStreamDestroy(g->copy);
+    if (g->frame) cudaStreamDestroy(g->frame);
     if (g->h_part) cudaFreeHost(g->h_part);
     if (g->h_ctl) cudaFreeHost(g->h_ctl);
     if (g->h_hll) cudaFreeHost(g->h_hll);
@@ -1250,6 +1556,7 @@ swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *te
     const uint64_t n = len - (uint64_t)(first - text);
     SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
     cudaStream_t s = stream_of(g, o);
+    if (n >= kStreamMin && !std::getenv("SWG_NO_STREAM")) return build_fasta_streamed(g, o, first, n, s);
     // +64: the packing kernel's aligned 16-byte loads read up to 31 bytes past a record
     if ((st = ensure(&g->d_text, &g->text_cap, n + 64, "FASTA text"))) return st;
     SWG_CUDA(cudaMemcpyAsync(g->d_text, first, n, cudaMemcpyHostToDevice, s), "copy FASTA text");

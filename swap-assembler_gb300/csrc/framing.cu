@@ -3,7 +3,7 @@
 // Same framing as the host path (and the reference, kmerGraph.cpp:113-114,
 // 160-233): from the first '>', lines alternate header / ONE sequence line;
 // acgt upper-cased, any other byte read as 'A'; sequences shorter than k
-// dropped. Steps: newlines per 4 KiB chunk -> scan -> every newline's
+// dropped. Steps: newlines per 16 KiB chunk -> scan -> every newline's
 // position -> record r = (line 2r, line 2r+1) -> keep sequences of length >= k
 // -> scan of kept reads and of their 16-base words -> pack. Every read starts
 // on a word boundary of the packed stream (read_off is a multiple of 16), so
@@ -22,6 +22,7 @@ constexpr int kFBlock = 256;
 constexpr int kFVec = 4;                                    // 16-byte loads per thread
 constexpr int kFBytes = 16 * kFVec;                         // bytes per thread
 constexpr uint64_t kFChunk = (uint64_t)kFBlock * kFBytes;  // bytes per block
+static_assert(kFChunk == kFramingChunk, "the streamed build splits the text on framing chunks");
 constexpr int kGItems = 8;
 constexpr uint64_t kGChunk = (uint64_t)kFBlock * kGItems;  // items per scan block
 
@@ -56,13 +57,14 @@ __device__ __forceinline__ void load_words(const unsigned char *__restrict__ t, 
 // 0xff in every byte of x equal to '\n'.
 __device__ __forceinline__ uint32_t nl_mask(uint32_t x) { return __vcmpeq4(x, 0x0a0a0a0au); }
 
-// Newlines per chunk; any NUL byte raises flag.
+// Newlines per chunk (chunks j0 + blockIdx.x); any NUL byte raises flag.
 __global__ void __launch_bounds__(kFBlock) k_nl_count(const unsigned char *__restrict__ t, uint64_t n,
                                                       uint64_t *__restrict__ counts,
-                                                      unsigned *__restrict__ flag) {
+                                                      unsigned *__restrict__ flag, uint64_t j0) {
     __shared__ uint64_t wb[kFBlock / 32];
+    const uint64_t j = j0 + blockIdx.x;
     uint32_t w[kFBytes / 4];
-    load_words(t, n, (uint64_t)blockIdx.x * kFChunk + (uint64_t)threadIdx.x * kFBytes, w);
+    load_words(t, n, j * kFChunk + (uint64_t)threadIdx.x * kFBytes, w);
     unsigned c = 0, z = 0;
 #pragma unroll
     for (int q = 0; q < kFBytes / 4; ++q) {
@@ -71,22 +73,23 @@ __global__ void __launch_bounds__(kFBlock) k_nl_count(const unsigned char *__res
     }
     uint64_t total;
     block_exclusive_scan<kFBlock>(c, wb, &total);
-    if (threadIdx.x == 0) counts[blockIdx.x] = total;
+    if (threadIdx.x == 0) counts[j] = total;
     if (z) atomicOr(flag, 1u);
 }
 
-// Position of every newline, in order.
+// Position of every newline of chunks j0 + blockIdx.x, in order.
 __global__ void __launch_bounds__(kFBlock) k_nl_pos(const unsigned char *__restrict__ t, uint64_t n,
                                                     const uint64_t *__restrict__ chunk_base,
-                                                    uint64_t *__restrict__ nl) {
+                                                    uint64_t *__restrict__ nl, uint64_t j0) {
     __shared__ uint64_t wb[kFBlock / 32];
-    const uint64_t base = (uint64_t)blockIdx.x * kFChunk + (uint64_t)threadIdx.x * kFBytes;
+    const uint64_t j = j0 + blockIdx.x;
+    const uint64_t base = j * kFChunk + (uint64_t)threadIdx.x * kFBytes;
     uint32_t w[kFBytes / 4];
     load_words(t, n, base, w);
     unsigned c = 0;
 #pragma unroll
     for (int q = 0; q < kFBytes / 4; ++q) c += __popc(nl_mask(w[q])) >> 3;
-    uint64_t pos = chunk_base[blockIdx.x] + block_exclusive_scan<kFBlock>(c, wb, nullptr);
+    uint64_t pos = chunk_base[j] + block_exclusive_scan<kFBlock>(c, wb, nullptr);
 #pragma unroll
     for (int q = 0; q < kFBytes / 4; ++q) {
         uint32_t m = nl_mask(w[q]);
@@ -152,16 +155,36 @@ __global__ void __launch_bounds__(kFBlock) k_gscan_write(const uint64_t *in, uin
     }
 }
 
-// Record r: header line 2r, sequence line 2r+1 (line 0 starts at byte 0).
-__global__ void k_rec_len(const uint64_t *__restrict__ nl, uint64_t n_rec, int k,
-                          uint64_t *__restrict__ keep, uint64_t *__restrict__ words) {
-    const uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= n_rec) return;
-    const uint64_t start = nl[2 * r] + 1, end = nl[2 * r + 1];
-    const uint64_t L = end - start;
-    const bool ok = L >= (uint64_t)k;
-    keep[r] = ok ? 1 : 0;
-    words[r] = ok ? (L + 15) / 16 : 0;
+// Records r0 <= r < r1: header line 2r, sequence line 2r+1 (line 0 starts at
+// byte 0). With acc, the kept reads' k-mer occurrences are added to acc[0]
+// and their longest length maxed into acc[1].
+__global__ void k_rec_len(const uint64_t *__restrict__ nl, uint64_t r0, uint64_t r1, int k,
+                          uint64_t *__restrict__ keep, uint64_t *__restrict__ words,
+                          unsigned long long *__restrict__ acc) {
+    const uint64_t r = r0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long occ = 0, mx = 0;
+    if (r < r1) {
+        const uint64_t start = nl[2 * r] + 1, end = nl[2 * r + 1];
+        const uint64_t L = end - start;
+        const bool ok = L >= (uint64_t)k;
+        keep[r] = ok ? 1 : 0;
+        words[r] = ok ? (L + 15) / 16 : 0;
+        if (ok) {
+            occ = L - (uint64_t)k + 1;
+            mx = L;
+        }
+    }
+    if (!acc) return;
+#pragma unroll
+    for (int d = 16; d; d >>= 1) {  // blockDim is a multiple of 32: whole warps
+        occ += __shfl_down_sync(0xffffffffu, occ, d);
+        const unsigned long long y = __shfl_down_sync(0xffffffffu, mx, d);
+        mx = y > mx ? y : mx;
+    }
+    if ((threadIdx.x & 31) == 0 && occ) {
+        atomicAdd(&acc[0], occ);
+        atomicMax(&acc[1], mx);
+    }
 }
 
 __device__ __forceinline__ uint32_t code_of(unsigned char ch) {
@@ -183,9 +206,11 @@ __device__ __forceinline__ uint32_t code_of(unsigned char ch) {
 // byte mapped through a 256-entry table. The text buffer has 64 bytes of
 // slack past its end.
 __global__ void __launch_bounds__(256) k_rec_pack(const unsigned char *__restrict__ t,
-                                                  const uint64_t *__restrict__ nl, uint64_t n_rec, int k,
+                                                  const uint64_t *__restrict__ nl, uint64_t r0,
+                                                  uint64_t n_rec, int k,
                                                   const uint64_t *__restrict__ read_idx,
                                                   const uint64_t *__restrict__ word_off,
+                                                  uint64_t read_base, uint64_t word_base,
                                                   uint64_t *__restrict__ off, uint32_t *__restrict__ len,
                                                   uint32_t *__restrict__ packed) {
     __shared__ unsigned char lut[256];
@@ -196,7 +221,7 @@ __global__ void __launch_bounds__(256) k_rec_pack(const unsigned char *__restric
     __syncthreads();
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t g0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; g0 < n_rec;
+    for (uint64_t g0 = r0 + (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; g0 < n_rec;
          g0 += nwarps * 32) {
         const uint64_t r = g0 + lane;
         uint64_t my_start = 0, my_w0 = 0;
@@ -207,8 +232,8 @@ __global__ void __launch_bounds__(256) k_rec_pack(const unsigned char *__restric
             if (L >= (uint64_t)k) {
                 my_len = (uint32_t)L;
                 my_nw = (uint32_t)((L + 15) / 16);
-                my_w0 = word_off[r];
-                const uint64_t ri = read_idx[r];
+                my_w0 = word_base + word_off[r];
+                const uint64_t ri = read_base + read_idx[r];
                 off[ri] = my_w0 * 16;
                 len[ri] = my_len;
             }
@@ -281,37 +306,39 @@ int launch_gscan(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t *scratc
 }
 
 int launch_nl_count(const unsigned char *t, uint64_t n, uint64_t *counts, unsigned *flag,
-                    cudaStream_t s) {
+                    cudaStream_t s, uint64_t j0) {
     const uint64_t nc = framing_chunks(n);
-    if (!nc) return 0;
-    k_nl_count<<<(unsigned)nc, kFBlock, 0, s>>>(t, n, counts, flag);
+    if (nc <= j0) return 0;
+    k_nl_count<<<(unsigned)(nc - j0), kFBlock, 0, s>>>(t, n, counts, flag, j0);
     return 1;
 }
 
 int launch_nl_pos(const unsigned char *t, uint64_t n, const uint64_t *chunk_base, uint64_t *nl,
-                  cudaStream_t s) {
+                  cudaStream_t s, uint64_t j0) {
     const uint64_t nc = framing_chunks(n);
-    if (!nc) return 0;
-    k_nl_pos<<<(unsigned)nc, kFBlock, 0, s>>>(t, n, chunk_base, nl);
+    if (nc <= j0) return 0;
+    k_nl_pos<<<(unsigned)(nc - j0), kFBlock, 0, s>>>(t, n, chunk_base, nl, j0);
     return 1;
 }
 
 int launch_rec_len(const uint64_t *nl, uint64_t n_rec, int k, uint64_t *keep, uint64_t *words,
-                   cudaStream_t s) {
-    if (!n_rec) return 0;
-    k_rec_len<<<(unsigned)((n_rec + 255) / 256), 256, 0, s>>>(nl, n_rec, k, keep, words);
+                   cudaStream_t s, uint64_t r0, unsigned long long *acc) {
+    if (n_rec <= r0) return 0;
+    k_rec_len<<<(unsigned)((n_rec - r0 + 255) / 256), 256, 0, s>>>(nl, r0, n_rec, k, keep, words, acc);
     return 1;
 }
 
 int launch_rec_pack(const unsigned char *t, const uint64_t *nl, uint64_t n_rec, int k,
                     const uint64_t *read_idx, const uint64_t *word_off, uint64_t *off,
-                    uint32_t *len, uint32_t *packed, cudaStream_t s) {
-    if (!n_rec) return 0;
+                    uint32_t *len, uint32_t *packed, cudaStream_t s, uint64_t r0, uint64_t read_base,
+                    uint64_t word_base) {
+    if (n_rec <= r0) return 0;
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const uint64_t blocks = std::min<uint64_t>((n_rec + 255) / 256, (uint64_t)std::max(sms, 1) * 16);
-    k_rec_pack<<<(unsigned)blocks, 256, 0, s>>>(t, nl, n_rec, k, read_idx, word_off, off, len, packed);
+    const uint64_t blocks = std::min<uint64_t>((n_rec - r0 + 255) / 256, (uint64_t)std::max(sms, 1) * 16);
+    k_rec_pack<<<(unsigned)blocks, 256, 0, s>>>(t, nl, r0, n_rec, k, read_idx, word_off, read_base, word_base,
+                                                off, len, packed);
     return 1;
 }
 

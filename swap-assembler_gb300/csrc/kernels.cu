@@ -1627,6 +1627,7 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
             }
 #pragma unroll
             for (int i = 0; i < kBkBatch; ++i) {
+                if (base + (uint64_t)i * kNT >= re) break;  // no thread of the block has a record left
                 const bool valid = !full && base + (uint64_t)i * kNT + threadIdx.x < re;
                 bool fresh = false;
                 uint32_t slot = 0;
@@ -2076,21 +2077,22 @@ int scatter_shape() {
 }
 
 template <int NT, int IT, int MINB>
-int launch_p1_scatter_shape(const BuildArgs &a, const PartArgs &p, cudaStream_t s) {
+int launch_p1_scatter_shape(const BuildArgs &a, const PartArgs &p, cudaStream_t s, bool persistent) {
     auto kern = k_p1_scatter<NT, IT, MINB>;
     const size_t smem = p1_scatter_smem(p.n_parts, NT * IT);
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    const uint64_t grid = std::min<uint64_t>((a.n_reads + NT - 1) / NT, resident_grid(kern, NT, smem));
+    const uint64_t batches = (a.n_reads + NT - 1) / NT;
+    const uint64_t grid = persistent ? std::min<uint64_t>(batches, resident_grid(kern, NT, smem)) : batches;
     kern<<<(unsigned)grid, NT, smem, s>>>(a, p);
     return 1;
 }
 
-int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s) {
+int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s, bool persistent) {
     if (a.total_occ == 0 || a.n_reads == 0) return 0;
     switch (scatter_shape()) {
-        case 1: return launch_p1_scatter_shape<512, 8, 2>(a, p, s);
-        case 2: return launch_p1_scatter_shape<256, 8, 4>(a, p, s);
-        default: return launch_p1_scatter_shape<256, 16, 3>(a, p, s);
+        case 1: return launch_p1_scatter_shape<512, 8, 2>(a, p, s, persistent);
+        case 2: return launch_p1_scatter_shape<256, 8, 4>(a, p, s, persistent);
+        default: return launch_p1_scatter_shape<256, 16, 3>(a, p, s, persistent);
     }
 }
 

@@ -149,7 +149,10 @@ int launch_bucket_caps(const unsigned long long *counts, const unsigned long lon
                        uint64_t nb, unsigned long long *caps, cudaStream_t s);
 int launch_big_multi(const BuildArgs &a, const BucketArgs &b, const unsigned long long *meta, uint32_t n,
                      uint64_t records, Entry *table, uint64_t cap, cudaStream_t s);
-int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s);
+// persistent: at most the resident blocks, each taking read batches until
+// none is left; else one block per batch (blocks retire as they finish, so
+// other streams' kernels get SMs during the scatter)
+int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s, bool persistent = true);
 int launch_part_wave(const BuildArgs &a, const PartArgs &p, uint32_t p0, uint32_t n,
                      uint64_t rec_begin, uint64_t rec_end, cudaStream_t s);
 // Device FASTA framing (framing.cu).
@@ -157,15 +160,21 @@ uint64_t framing_chunks(uint64_t n);
 uint64_t gscan_scratch(uint64_t n);
 int launch_gscan(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t *scratch, uint64_t *total,
                  cudaStream_t s);
+// The text's 16 KiB chunks from j0 up to the end n; records from r0 up to
+// n_rec (a streamed build frames the text a piece at a time); a record's
+// read index and first word are read_base + read_idx[r], word_base +
+// word_off[r].
 int launch_nl_count(const unsigned char *t, uint64_t n, uint64_t *counts, unsigned *flag,
-                    cudaStream_t s);
+                    cudaStream_t s, uint64_t j0 = 0);
 int launch_nl_pos(const unsigned char *t, uint64_t n, const uint64_t *chunk_base, uint64_t *nl,
-                  cudaStream_t s);
+                  cudaStream_t s, uint64_t j0 = 0);
 int launch_rec_len(const uint64_t *nl, uint64_t n_rec, int k, uint64_t *keep, uint64_t *words,
-                   cudaStream_t s);
+                   cudaStream_t s, uint64_t r0 = 0, unsigned long long *acc = nullptr);
 int launch_rec_pack(const unsigned char *t, const uint64_t *nl, uint64_t n_rec, int k,
                     const uint64_t *read_idx, const uint64_t *word_off, uint64_t *off,
-                    uint32_t *len, uint32_t *packed, cudaStream_t s);
+                    uint32_t *len, uint32_t *packed, cudaStream_t s, uint64_t r0 = 0,
+                    uint64_t read_base = 0, uint64_t word_base = 0);
+constexpr uint64_t kFramingChunk = 16384;  // bytes per block of k_nl_count / k_nl_pos
 int launch_chunk_prefix(const BucketArgs &b, cudaStream_t s);
 int launch_sub_hist(const BucketArgs &b, cudaStream_t s);
 int launch_sub_scatter(const BucketArgs &b, cudaStream_t s);

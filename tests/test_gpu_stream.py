@@ -1,0 +1,122 @@
+"""The streamed FASTA build: a text of 96 MiB or more goes up in pieces, each
+framed and scattered to the level-1 partitions as it lands, with the regions
+sized from the first piece. Its graph must equal the one-shot build's (the
+text copied whole, framed, then built; SWG_NO_STREAM selects it) bit for bit:
+on plain inputs of 2 and 4 pieces, with each algorithm, with a read too long
+for the bucketed build in a later piece (the fallback), with the multi-line
+quirk shifting the header/sequence alternation mid-text, on a reused handle,
+and with the same errors for a NUL byte or an unpaired last header."""
+import os
+
+import numpy as np
+import pytest
+
+import swapgb
+
+pytestmark = pytest.mark.gpu
+
+STREAM_MIN = 96 << 20
+
+
+def synth(seed: int, n_reads: int, genome_len: int = 2_000_000) -> bytes:
+    return swapgb.synth_fasta(seed=seed, genome_len=genome_len, n_reads=n_reads, read_len=100)
+
+
+def build(text: bytes, opts: swapgb.Opts, streamed: bool, g: swapgb.Graph | None = None):
+    if streamed:
+        os.environ.pop("SWG_NO_STREAM", None)
+    else:
+        os.environ["SWG_NO_STREAM"] = "1"
+    try:
+        g = (g or swapgb.Graph()).build_fasta(opts, text)
+    finally:
+        os.environ.pop("SWG_NO_STREAM", None)
+    keys, mult = g.copy_out(sorted=True)
+    return g, keys, mult
+
+
+def assert_same(text: bytes, opts: swapgb.Opts) -> dict:
+    assert len(text) >= STREAM_MIN
+    gs, ks, ms = build(text, opts, True)
+    go, ko, mo = build(text, opts, False)
+    si, oi = gs.info(), go.info()
+    assert ks.size == ko.size and np.array_equal(ks, ko)
+    assert np.array_equal(ms, mo)
+    for key in ("occurrences", "distinct", "survivors"):
+        assert si[key] == oi[key], (key, si, oi)
+    return si
+
+
+@pytest.fixture(scope="module")
+def text2():
+    # 1.1M x 100 bp reads: about 120 MB of text, two pieces
+    return synth(41, 1_100_000)
+
+
+def test_two_pieces_equal_one_shot(text2):
+    info = assert_same(text2, swapgb.Opts(k=31, cutoff=5))
+    assert info["algorithm"] == swapgb.ALGO_BUCKETED and info["survivors"] > 0
+    assert info["estimate"] == 0  # the first piece's sample sized every region
+
+
+def test_four_pieces_equal_one_shot_and_host_framing():
+    text = synth(42, 2_600_000, genome_len=5_000_000)  # about 286 MB
+    assert len(text) >= 4 * (64 << 20)
+    opts = swapgb.Opts(k=21, cutoff=2)
+    assert assert_same(text, opts)["estimate"] == 0
+    _, ks, ms = build(text, opts, True)
+    gh = swapgb.Graph().build_reads(opts, swapgb.reads_from_fasta(text, 21))
+    kh, mh = gh.copy_out(sorted=True)
+    assert np.array_equal(ks, kh) and np.array_equal(ms, mh)
+
+
+@pytest.mark.parametrize("algo", [swapgb.ALGO_BUCKETED, swapgb.ALGO_DIRECT, swapgb.ALGO_PARTITIONED])
+def test_each_algorithm(text2, algo):
+    assert_same(text2, swapgb.Opts(k=31, cutoff=3, algorithm=algo))
+
+
+def test_minimizer_order_falls_back(text2):
+    assert_same(text2, swapgb.Opts(k=31, cutoff=3, read_order=swapgb.ORDER_MINIMIZER))
+
+
+def test_long_read_in_a_later_piece_falls_back(text2):
+    rng = np.random.default_rng(3)
+    long_read = bytes(np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, 20_000)])
+    text = text2 + b">long\n" + long_read + b"\n"
+    info = assert_same(text, swapgb.Opts(k=31, cutoff=1))
+    assert info["algorithm"] != swapgb.ALGO_BUCKETED  # the one-shot default takes the direct build
+
+
+def test_multiline_record_shifts_the_alternation(text2):
+    # a sequence split over two lines: from there on the reference reads
+    # every header as a sequence and every sequence as a header (one more
+    # line at the end keeps the line count even: the old last sequence line
+    # is that record's header)
+    half = len(text2) // 2
+    cut = text2.index(b"\n>", half) + 1
+    ml = b">ml\n" + b"ACGTTGCA" * 10 + b"\n" + b"TTGCAACG" * 10 + b"\n"
+    text = text2[:cut] + ml + text2[cut:] + b"GATTACA" * 12 + b"\n"
+    opts = swapgb.Opts(k=19, cutoff=1)
+    shifted = assert_same(text, opts)
+    plain = build(text2, opts, True)[0].info()
+    # the second half's sequences are headers now, its headers too short to count
+    assert shifted["occurrences"] < 0.6 * plain["occurrences"]
+
+
+def test_handle_reuse_across_streamed_builds(text2):
+    opts = swapgb.Opts(k=31, cutoff=2)
+    other = synth(43, 1_000_000, genome_len=3_000_000)
+    g, _, _ = build(other, opts, True)
+    g, ks, ms = build(text2, opts, True, g)
+    _, ko, mo = build(text2, opts, False)
+    assert np.array_equal(ks, ko) and np.array_equal(ms, mo)
+
+
+def test_errors_match_one_shot(text2):
+    bad_nul = text2[:-50] + b"\x00" + text2[-49:]
+    unpaired = text2 + b">no_sequence\n"
+    for bad in (bad_nul, unpaired):
+        for streamed in (True, False):
+            with pytest.raises(swapgb.SwgError) as e:
+                build(bad, swapgb.Opts(k=31, cutoff=5), streamed)
+            assert e.value.status == 1
