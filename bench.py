@@ -230,8 +230,18 @@ def merge_metrics(g, survivors: int, steps: int, warmup: int) -> dict:
                                             "nodes_left": g.merge_info()["nodes"]}}
 
 
+MERGE_CPU_MAX = 8_000_000  # k-molecules: about 40 s for the one-thread restatement
+
+
 def merge_cpu_baseline(g, k: int) -> dict:
-    """The CPU restatement of the merge (one thread) on the same k-molecules."""
+    """The CPU restatement of the merge (one thread) on the same k-molecules.
+    The merge needs the whole graph (chains run through it), so a graph past
+    MERGE_CPU_MAX k-molecules is not timed: it would take minutes."""
+    n = g.size()
+    if n > MERGE_CPU_MAX:
+        return {"value": None, "unit": "k-molecules/s", "cores": 1, "kind": "port",
+                "sample": "not run: %d k-molecules, past the %d that finish in about 40 s"
+                          % (n, MERGE_CPU_MAX)}
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
     keys, mult = g.copy_out(sorted=True)
@@ -560,7 +570,7 @@ def main() -> int:
                                           h_off.numel()), "swg_graph_build")
         return copy_out_e2e()
 
-    def timed(fn) -> tuple[float, int]:
+    def timed(fn) -> tuple[float, int, list[float]]:
         for _ in range(2):
             fn()
         torch.cuda.synchronize()
@@ -569,10 +579,10 @@ def main() -> int:
             t0 = time.perf_counter()
             n = fn()
             ts.append(time.perf_counter() - t0)
-        return max_over_ranks(statistics.mean(ts), world, dev), n
+        return max_over_ranks(statistics.mean(ts), world, dev), n, [round(t * 1e3, 3) for t in ts]
 
-    e2e_s, n_e2e = timed(e2e_fasta)
-    e2e_p_s, _ = timed(e2e_packed)
+    e2e_s, n_e2e, e2e_steps = timed(e2e_fasta)
+    e2e_p_s, _, e2e_p_steps = timed(e2e_packed)
     h2d = h_text.numel()
     h2d_p = h_packed.numel() * 4 + h_off.numel() * 8 + h_len.numel() * 4
     d2h = n_e2e * 16
@@ -663,12 +673,13 @@ def main() -> int:
             "data": "synthetic (seeded generator, no dataset)", "config": dict(config_dict(args.algo, args.order),
                                                                     algorithm_used={1: "direct", 2: "partitioned", 3: "bucketed"}[used]),
             "e2e": {"value": aggregate_value(n_bases, world, e2e_s * 1e3), "unit": "bases/s",
-                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "wall_ms_steps": e2e_steps,
                     "path": "swg_graph_build_fasta on the pinned FASTA text (framing + packing on "
-                            "the device) + swg_graph_copy_out"},
+                            "the device; texts of 96 MiB and more stream up in pieces) + "
+                            "swg_graph_copy_out"},
             "e2e_packed": {"value": aggregate_value(n_bases, world, e2e_p_s * 1e3),
                            "unit": "bases/s", "h2d_bytes_per_step": h2d_p,
-                           "d2h_bytes_per_step": d2h,
+                           "d2h_bytes_per_step": d2h, "wall_ms_steps": e2e_p_steps,
                            "path": "swg_graph_build on pinned host packed reads + swg_graph_copy_out"},
             "gpu_launches": launches,
             "build": dict(info, phase_ms_mean=mean_ms),
