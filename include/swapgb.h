@@ -160,7 +160,12 @@ swg_status swg_graph_build_device(swg_graph *g, const swg_opts *o, const uint32_
 /* Build from a FASTA held in HOST memory, framed and packed ON THE DEVICE: the
  * text is copied to the GPU, lines are found and paired there with the same
  * framing as swg_reads_from_fasta (same errors), reads are 2-bit packed, then
- * built as swg_graph_build_device. */
+ * built as swg_graph_build_device. A text of 96 MiB or more is copied in
+ * pieces, each framed and scattered while the rest is still copying (the
+ * result is the same); from pinned host memory (cudaHostAlloc) the copies
+ * overlap the work. The call returns after every copy from `text` has ended.
+ * Environment: SWG_NO_STREAM=1 copies and frames the text in one piece;
+ * SWG_STREAM_PIECES=2..16 sets the number of pieces. */
 swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *text, uint64_t len);
 /* Convenience: create + build from host packed reads. */
 swg_status swg_build(const swg_opts *o, const uint32_t *packed, uint64_t n_words,
