@@ -120,3 +120,16 @@ def test_errors_match_one_shot(text2):
             with pytest.raises(swapgb.SwgError) as e:
                 build(bad, swapgb.Opts(k=31, cutoff=5), streamed)
             assert e.value.status == 1
+
+
+def test_sample_miss_recounts_exactly(text2):
+    # 200k reads of one dinucleotide repeat, all in the second piece: the
+    # first piece's sample cannot see the two hot k-mers, their bucket
+    # outgrows its region, and the streamed build recounts with exact counts
+    hot = b"".join(b">t%d\n" % i + b"AC" * 50 + b"\n" for i in range(200_000))
+    text = text2 + hot
+    opts = swapgb.Opts(k=31, cutoff=3)
+    info = assert_same(text, opts)
+    assert info["estimate"] == 1  # the exact-count rerun ran
+    gs, ks, ms = build(text, opts, True)
+    assert (ms == 255).any()  # the hot k-mers saturate
