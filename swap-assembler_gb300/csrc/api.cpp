@@ -1362,7 +1362,6 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
     a.n_reads = reads;
     a.total_occ = occ;
     g->occurrences = occ;
-    g->h_ctl->max_len = (unsigned)longest;
     pl.bk.n_rec = occ;
     g->launches += launches;
     return bucketed_finish(g, o, a, s, load, false, pl);
