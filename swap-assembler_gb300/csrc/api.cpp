@@ -1175,8 +1175,14 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
     uint64_t C = std::min<uint64_t>(kStreamMaxPieces, std::max<uint64_t>(2, n / kStreamPiece));
     if (const char *e = std::getenv("SWG_STREAM_PIECES"))  // at most 16: the first piece is the sample
         C = std::min<uint64_t>(kStreamMaxPieces, std::max(2, std::atoi(e)));
-    std::vector<uint64_t> cut(C + 1);  // piece c: bytes [cut[c], cut[c+1]), on framing-chunk bounds
-    for (uint64_t c = 0; c < C; ++c) cut[c] = nc * c / C * swg::kFramingChunk;
+    // piece c: bytes [cut[c], cut[c+1]), on framing-chunk bounds. The first
+    // piece, whose copy nothing overlaps, is half a piece but at least 1/16
+    // of the text (its reads are the sample: at least 1/16 of all reads)
+    std::vector<uint64_t> cut(C + 1);
+    const uint64_t first_blocks = std::max<uint64_t>(1, std::max(nc / (2 * C), nc / 16));
+    cut[0] = 0;
+    for (uint64_t c = 1; c < C; ++c)
+        cut[c] = (first_blocks + (nc - first_blocks) * (c - 1) / (C - 1)) * swg::kFramingChunk;
     cut[C] = n;
     if (!g->copy) SWG_CUDA(cudaStreamCreateWithFlags(&g->copy, cudaStreamNonBlocking), "copy stream");
     if (!g->frame) {  // the framing stream's blocks go first as the scatter's retire
@@ -1318,7 +1324,8 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
                 a0.n_reads = reads_c;
                 a0.total_occ = occ_c;
                 g->algorithm = SWG_ALGO_BUCKETED;
-                const uint32_t stride = (uint32_t)std::max<uint64_t>(1, 16 / C);
+                // every stride-th batch of the first piece: 1/16 to 1/8 of all reads
+                const uint32_t stride = (uint32_t)std::max<uint64_t>(1, 16 * first_blocks / nc);
                 if ((st = bucketed_plan(g, a0, N_est, false, stride, s, pl))) return st;
                 SWG_CUDA(cudaEventRecord(g->ev[1], s), "event");
             }
