@@ -81,11 +81,12 @@ def parse_args():
     return args
 
 
-def config_dict(algo: str = "default", order: str = "input") -> dict:
-    return {"algorithm": algo, "read_order": order, "workload": DESC,
-            "genome_bp": WORKLOAD["genome_len"], "reads": WORKLOAD["n_reads"],
+def config_dict() -> dict:
+    """The workload, the same for both arms (what each arm runs on it is in
+    its "arm" key)."""
+    return {"workload": DESC, "genome_bp": WORKLOAD["genome_len"], "reads": WORKLOAD["n_reads"],
             "read_len": WORKLOAD["read_len"], "k": K, "c": CUTOFF,
-            "inputs": "packed 2-bit reads resident in HBM", "l2": "flushed before every step"}
+            "l2": "flushed (256 MiB write) before every GPU step"}
 
 
 class ClockSampler:
@@ -258,17 +259,8 @@ def batched_samples(n: int = 256, seed: int = 4) -> list[dict]:
     """The batched workload: genome sizes log-uniform 50 kbp-2 Mbp, read length
     from {75, 100, 150, 250}, coverage uniform 10-60x, substitutions uniform
     0.1-1%, k=27, c=3 for every sample."""
-    import math
-    import random
-    rng = random.Random(seed)
-    out = []
-    for i in range(n):
-        g = int(math.exp(rng.uniform(math.log(50_000), math.log(2_000_000))))
-        L = rng.choice([75, 100, 150, 250])
-        cov = rng.uniform(10, 60)
-        out.append(dict(seed=10_000 + i, genome_len=g, n_reads=int(cov * g / L), read_len=L,
-                        sub_rate=rng.uniform(0.001, 0.01)))
-    return out
+    import swapgb
+    return swapgb.batch_workload_specs(n, seed)
 
 
 def batched_metrics(stream_ptr: int, repeats: int = 3) -> dict:
@@ -314,10 +306,13 @@ def batched_metrics(stream_ptr: int, repeats: int = 3) -> dict:
         torch.cuda.synchronize()
         t_batch.append(time.perf_counter() - t0)
         dev_batch.append(batch.info()["ms"][4])
-    # spot check: the last sample of the batch equals its plain build
-    kp, mp = plain.copy_out(sorted=True)
-    kb, mb = batch.batch_copy_out(len(reads) - 1)
-    same = bool(np.array_equal(kp, kb) and np.array_equal(mp, mb))
+    # every sample of the batch against its own plain build (outside the timing)
+    same = 0
+    for i, r in enumerate(reads):
+        plain.build_reads(opts, r)
+        kp, mp = plain.copy_out(sorted=True)
+        kb, mb = batch.batch_copy_out(i)
+        same += bool(np.array_equal(kp, kb) and np.array_equal(mp, mb))
     tp, tb = min(t_plain), min(t_batch)
     return {"workload": "256 samples, genome log-uniform 50 kbp-2 Mbp, reads 75/100/150/250 bp, "
                         "10-60x, 0.1-1% subs, k=27 c=3 (seeded synthetic)",
@@ -327,88 +322,139 @@ def batched_metrics(stream_ptr: int, repeats: int = 3) -> dict:
             "batched_bases_per_s": bases / tb, "speedup": tp / tb,
             "device_ms_plain_sum": min(dev_plain), "device_ms_batched": min(dev_batch),
             "batched_algorithm": {1: "direct", 2: "partitioned", 3: "bucketed"}[batch.info()["algorithm"]],
-            "last_sample_identical": same,
+            "samples_identical": "%d/%d" % (same, len(reads)),
+            "identical_means": "the sample's sorted k-molecules and 8 multiplicities equal its own plain "
+                               "build's, bit for bit",
             "path": "pinned host packed reads -> device-resident graphs; plain = swg_graph_build "
                     "per sample, batched = one swg_batch_build"}
 
 
-def served_metrics(duration_s: float = 10.0, rate: float = 50.0, seed: int = 5) -> dict:
-    """Poisson request stream (mean `rate` req/s) through the request server.
+SERVED_RATES = (50.0, 200.0, 800.0, 3200.0)  # req/s of the served sweep
+SERVED_REQUESTS = 800                         # at most this many requests per rate
+
+
+def served_metrics(stream_ptr: int) -> dict:
+    """Poisson request streams through the request server, one per rate of
+    SERVED_RATES (10 s, or SERVED_REQUESTS requests at the higher rates).
     Request sizes follow the batched workload's per-sample distribution, plus
     2% large requests (10 Mbp genome, 40x, 150 bp reads); k from
-    {21, 25, 27, 31} and c from {2, 3, 5} per request; 150 GiB admission budget.
-    A pool of distinct request inputs is generated once and drawn from."""
+    {21, 25, 27, 31} and c from {2, 3, 5} per request; 150 GiB admission
+    budget. A pool of distinct request inputs is generated once and drawn
+    from. Every result is fetched and its SHA-256 (sorted records) compared,
+    after the stream, with a plain build of the same input, k and c; the
+    plain builds' wall times give the plain form's samples/s for the mix."""
+    import hashlib
     import random
     import threading
+    import numpy as np
+    import torch
     import swapgb
-    rng = random.Random(seed)
-    specs = batched_samples(n=40, seed=seed)
+    specs = batched_samples(n=40, seed=5)
     pool = [swapgb.reads_from_fasta(swapgb.synth_fasta(**p), 21) for p in specs]
     large = swapgb.reads_from_fasta(swapgb.synth_fasta(seed=77, genome_len=10_000_000,
                                                        n_reads=2_666_667, read_len=150,
                                                        sub_rate=0.005), 21)
-    srv = swapgb.Server(memory_budget=150 << 30, workers=2)
-    # warm-up: one request of each kind
-    for r in (pool[0], large):
-        t = srv.submit(r, 27, 3)
-        srv.wait(t, 120.0)
-        srv.release(t)
-    tickets, sizes, kinds = [], [], []
-    lock = threading.Lock()
-    done = threading.Event()
-    lat = {}
+    inputs = pool + [large]
+    digest = lambda k, m: hashlib.sha256(k.tobytes() + m.tobytes()).hexdigest()
 
-    def collector():
-        i = 0
-        while True:
-            with lock:
-                have = i < len(tickets)
-                t = tickets[i] if have else None
-            if not have:
-                if done.is_set():
-                    with lock:
-                        if i >= len(tickets):
-                            return
-                    continue
-                time.sleep(0.0005)
-                continue
-            srv.wait(t, 300.0)
-            lat[t] = srv.poll(t)[1]
+    def one_rate(rate: float, seed: int) -> tuple[dict, list]:
+        rng = random.Random(seed)
+        srv = swapgb.Server(memory_budget=150 << 30, workers=2)
+        for r in (pool[0], large):  # warm-up: one request of each kind
+            t = srv.submit(r, 27, 3)
+            srv.wait(t, 120.0)
             srv.release(t)
-            i += 1
+        base = srv.stats()
+        duration = min(10.0, SERVED_REQUESTS / rate)
+        tickets, reqs = [], []  # reqs: (input index, k, c)
+        lock = threading.Lock()
+        done = threading.Event()
+        got = {}  # ticket -> (latency s, digest)
 
-    th = threading.Thread(target=collector)
-    th.start()
-    t0 = time.perf_counter()
-    t_next = 0.0
-    while t_next < duration_s:
-        now = time.perf_counter() - t0
-        if now < t_next:
-            time.sleep(t_next - now)
-        is_large = rng.random() < 0.02
-        r = large if is_large else pool[rng.randrange(len(pool))]
-        k, c = rng.choice([21, 25, 27, 31]), rng.choice([2, 3, 5])
-        t = srv.submit(r, k, c)
-        with lock:
-            tickets.append(t)
-            sizes.append(r.n_bases)
-            kinds.append(is_large)
-        t_next += rng.expovariate(rate)
-    done.set()
-    th.join()
-    wall = time.perf_counter() - t0
-    st = srv.stats()
-    srv.close()
-    ls = sorted(lat[t] for t in tickets)
-    q = lambda f: ls[min(len(ls) - 1, int(f * len(ls)))]
-    return {"workload": "Poisson %.0f req/s for %.0f s; sizes from the batched workload's per-sample "
-                        "distribution + 2%% large (10 Mbp, 40x, 150 bp); k in {21,25,27,31}, c in "
-                        "{2,3,5}; 150 GiB budget; 2 workers" % (rate, duration_s),
-            "requests": len(tickets), "large_requests": sum(kinds),
-            "p50_ms": 1e3 * q(0.50), "p99_ms": 1e3 * q(0.99), "max_ms": 1e3 * ls[-1],
-            "aggregate_bases_per_s": sum(sizes) / wall, "offered_bases_per_s": sum(sizes) / duration_s,
-            "batches": st["batches"], "max_batch_requests": st["max_batch_requests"],
-            "latency": "submit (including the server's copy of the reads) to the result resident on the device"}
+        def collector():
+            i = 0
+            while True:
+                with lock:
+                    t = tickets[i] if i < len(tickets) else None
+                if t is None:
+                    if done.is_set():
+                        with lock:
+                            if i >= len(tickets):
+                                return
+                        continue
+                    time.sleep(0.0005)
+                    continue
+                srv.wait(t, 300.0)
+                lat = srv.poll(t)[1]
+                k, m = srv.fetch(t, sorted=True)  # outside the latency (taken at completion)
+                got[t] = (lat, digest(k, m))
+                i += 1
+
+        th = threading.Thread(target=collector)
+        th.start()
+        t0 = time.perf_counter()
+        t_next = 0.0
+        while t_next < duration:
+            now = time.perf_counter() - t0
+            if now < t_next:
+                time.sleep(t_next - now)
+            j = len(inputs) - 1 if rng.random() < 0.02 else rng.randrange(len(pool))
+            k, c = rng.choice([21, 25, 27, 31]), rng.choice([2, 3, 5])
+            t = srv.submit(inputs[j], k, c)
+            with lock:
+                tickets.append(t)
+                reqs.append((j, k, c))
+            t_next += rng.expovariate(rate)
+        done.set()
+        th.join()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        lats = sorted(got[t][0] for t in tickets)
+        q = lambda f: lats[min(len(lats) - 1, int(f * len(lats)))]
+        n_batches = st["batches"] - base["batches"]
+        bases = sum(inputs[j].n_bases for j, _, _ in reqs)
+        row = {"rate_req_per_s": rate, "seconds": duration, "requests": len(tickets),
+               "large_requests": sum(j == len(inputs) - 1 for j, _, _ in reqs),
+               "p50_ms": 1e3 * q(0.50), "p99_ms": 1e3 * q(0.99), "max_ms": 1e3 * lats[-1],
+               "aggregate_samples_per_s": len(tickets) / wall, "aggregate_bases_per_s": bases / wall,
+               "offered_bases_per_s": bases / duration, "batches": n_batches,
+               "mean_batch_requests": len(tickets) / max(n_batches, 1),
+               "max_batch_requests": st["max_batch_requests"]}
+        return row, [(reqs[i], got[t][1]) for i, t in enumerate(tickets)]
+
+    rows, checks = [], []
+    for i, rate in enumerate(SERVED_RATES):
+        row, chk = one_rate(rate, seed=5 + i)
+        rows.append(row)
+        checks.append(chk)
+    # every fetched result against a plain build of the same request
+    g = swapgb.Graph()
+    want, plain_s = {}, {}
+    for combo in sorted({c for chk in checks for c, _ in chk}):
+        j, k, c = combo
+        opts = swapgb.Opts(k=k, cutoff=c, stream=stream_ptr)
+        g.build_reads(opts, inputs[j])  # warm (allocations), then timed
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.build_reads(opts, inputs[j])
+        torch.cuda.synchronize()
+        plain_s[combo] = time.perf_counter() - t0
+        want[combo] = digest(*g.copy_out(sorted=True))
+    for row, chk in zip(rows, checks):
+        row["results_identical"] = "%d/%d" % (sum(want[c] == d for c, d in chk), len(chk))
+        row["plain_samples_per_s"] = len(chk) / sum(plain_s[c] for c, _ in chk)
+    return {"workload": "Poisson request streams at %s req/s (10 s or %d requests each); sizes from the "
+                        "batched workload's per-sample distribution + 2%% large (10 Mbp, 40x, 150 bp); k in "
+                        "{21,25,27,31}, c in {2,3,5}; 150 GiB budget; 2 workers"
+                        % ("/".join("%g" % r for r in SERVED_RATES), SERVED_REQUESTS),
+            "latency": "submit (including the server's copy of the reads) to the result resident on the "
+                       "device",
+            "results_identical_means": "SHA-256 of the fetched sorted records equals a plain build's of the "
+                                       "same input, k and c",
+            "plain_samples_per_s_means": "the same requests built one by one with swg_graph_build from host "
+                                         "packed reads (wall time per build, result on the device)",
+            "sweep": rows}
 
 
 def run_reference_arm(args) -> int:
@@ -421,15 +467,15 @@ def run_reference_arm(args) -> int:
     text = swapgb.synth_fasta(**WORKLOAD)
     kind = "port"
     threads = oracle.cores()
-    # bounded sample: about one quarter of the workload's reads per step
-    sample = text[: text.index(b"\n>", len(text) // 4) + 1]
-    nb = oracle.parse(sample, K)["n_bases"]
+    # every step is the whole workload: the FASTA text in host memory framed,
+    # counted and cut off (about 3 s on 16 cores for workload 2)
+    nb = oracle.parse(text, K)["n_bases"]
     for _ in range(max(args.warmup, 0)):
-        oracle.records(sample, K, CUTOFF, threads)
+        oracle.records(text, K, CUTOFF, threads)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        oracle.records(sample, K, CUTOFF, threads)
+        oracle.records(text, K, CUTOFF, threads)
         times.append(time.perf_counter() - t0)
     ms = 1e3 * statistics.mean(times)
     value = nb / (ms * 1e-3)
@@ -437,11 +483,13 @@ def run_reference_arm(args) -> int:
         "impl": "reference", "metric": METRIC, "value": value, "unit": "bases/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-        "data": "synthetic", "config": config_dict(),
+        "data": "synthetic (seeded generator, no dataset)", "config": config_dict(),
+        "arm": {"runs": "the reference's algorithm restated in C (oracle/kmer_oracle.c), one thread "
+                        "per MPI rank of the reference's scheme, on the host cores",
+                "inputs": "the workload's FASTA text in host memory"},
         "cpu_baseline": {"value": value, "unit": "bases/s", "cores": threads, "kind": kind,
-                         "sample": "first %d bases of the workload per step (framing + count + "
-                                   "cutoff), the reference's algorithm restated in C with one "
-                                   "thread per MPI rank" % nb},
+                         "sample": "the whole workload every step: %d bases (framing + count + "
+                                   "cutoff, sorted records)" % nb},
         "e2e": {"value": value, "unit": "bases/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -641,7 +689,10 @@ def main() -> int:
                   "dram_load16_per_s_4_in_flight": r_x4,
                   "l2_load16_cas128_per_s": r_l2, "table_bytes": table_bytes,
                   "ops_per_step": ops, "achieved_ops_per_s": ops / (mean_ms[4] * 1e-3),
-                  "frac_of_R": ops / (mean_ms[4] * 1e-3) / r_red,
+                  # the algorithmic op count over time, against R: context only.
+                  # The bucketed build does not perform these ops as random DRAM
+                  # atomics, so this is no roofline fraction (see "roofline").
+                  "algorithmic_ops_over_R": ops / (mean_ms[4] * 1e-3) / r_red,
                   "occurrences_per_s_counting_phase": n_occ / (count_ms * 1e-3),
                   "frac_counting_phase_vs_" + ("dram" if used == swapgb.ALGO_DIRECT else "l2")
                   + "_load16_cas128": (n_occ / (count_ms * 1e-3))
@@ -651,7 +702,7 @@ def main() -> int:
         batched = batched_metrics(stream.cuda_stream)
     served = None
     if rank == 0 and not args.no_serve and not args.reads:
-        served = served_metrics()
+        served = served_metrics(stream.cuda_stream)
     if merge and atomic:
         achieved = MERGE_RANDOM_PER_NODE * survivors / (merge["ms"] * 1e-3)
         peak = atomic["dram_load16_per_s_4_in_flight"]
@@ -670,8 +721,10 @@ def main() -> int:
             "metric": METRIC, "value": value, "unit": "bases/s", "n_gpus": world,
             "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-            "data": "synthetic (seeded generator, no dataset)", "config": dict(config_dict(args.algo, args.order),
-                                                                    algorithm_used={1: "direct", 2: "partitioned", 3: "bucketed"}[used]),
+            "data": "synthetic (seeded generator, no dataset)", "config": config_dict(),
+            "arm": {"algorithm": args.algo, "read_order": args.order,
+                    "algorithm_used": {1: "direct", 2: "partitioned", 3: "bucketed"}[used],
+                    "inputs": "packed 2-bit reads resident in HBM"},
             "e2e": {"value": aggregate_value(n_bases, world, e2e_s * 1e3), "unit": "bases/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "wall_ms_steps": e2e_steps,
                     "path": "swg_graph_build_fasta on the pinned FASTA text (framing + packing on "

@@ -232,7 +232,9 @@ typedef struct swg_server_stats {
 #define SWG_REQ_FAILED 3
 
 swg_status swg_server_create(const swg_server_opts *o, swg_server **out);
-/* Copies the request's reads; the caller may free them on return. */
+/* Copies the request's reads; the caller may free them on return. If no
+ * worker could set itself up (graph handle or stream creation failed), queued
+ * requests fail with that reason and submit returns SWG_ERR_BAD_STATE. */
 swg_status swg_server_submit(swg_server *srv, const swg_sample *req, uint64_t *ticket);
 /* Non-blocking: state (SWG_REQ_*) and latency so far (submit to completion). */
 swg_status swg_server_poll(swg_server *srv, uint64_t ticket, int *state, double *latency_s);
@@ -365,8 +367,10 @@ swg_status swg_graph_build_info(const swg_graph *g, swg_build_info *info);
  * the caller's device memory. At most 1048576 reads and 2516505 k-mer
  * occurrences per call, else SWG_ERR_BAD_INPUT; more than out_cap survivors
  * gives SWG_ERR_BAD_INPUT with *n_out set to the count needed. The first call
- * on a device resolves the array's address (make it before any stream capture).
- * Calls share the array: calls whose device work overlaps race. */
+ * on a device resolves the array's address, and so does the first call after
+ * the device's context was destroyed (cudaDeviceReset): make those calls
+ * before any stream capture. Calls share the array: calls whose device work
+ * overlaps race. */
 swg_status swg_build_device_noalloc(const swg_opts *o, const uint32_t *d_packed, uint64_t n_words,
                                     const uint64_t *d_read_off, const uint32_t *d_read_len,
                                     uint64_t n_reads, uint64_t *d_keys_out, uint64_t *d_mult_out,

@@ -111,13 +111,14 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict[str, Path]:
     return {"lib": lib, "synth": synth, "swap": swap}
 
 
-def build_oracle(verbose: bool = False) -> None:
-    """CPU restatement (always) and, where the reference tree exists, the
+def build_oracle(verbose: bool = False, ref_dir: str | None = None) -> None:
+    """CPU restatement (always) and, when ref_dir (else the environment
+    variable SWG_REFERENCE_DIR) names the reference's source tree, the
     reference itself (oracle/_ref) — test infrastructure, not the product."""
     oracle = ROOT / "oracle"
     _run(["make", "-s", "-C", str(oracle), "-j4", "restatement"])
-    ref = os.environ.get("SWG_REFERENCE_DIR", "/root/reference")
-    if Path(ref, "graph.cpp").exists():
+    ref = ref_dir or os.environ.get("SWG_REFERENCE_DIR")
+    if ref and Path(ref, "graph.cpp").exists():
         _run(["make", "-s", "-C", str(oracle), "-j4", "reference", "REF=" + ref])
     if verbose:
         print("built oracle")

@@ -763,11 +763,20 @@ __device__ __forceinline__ uint64_t slice_cap_of(const PartArgs &pa, unsigned lo
     return c < pa.slot_cap ? c : pa.slot_cap;
 }
 
+// Where a bin's records go: record j of the block's sorted round (j in the
+// bin's run) is written to dst + j while j < lim (the run's part that fits
+// the bin's region; the rest is dropped and the overflow flagged later).
+struct __align__(16) BinDest {
+    unsigned long long dst;  // global index of the run's first record, minus its start in the round
+    unsigned lim;            // round index past the last record that fits
+    unsigned pad;
+};
+
 // Shared memory of k_p1_scatter: a round's records, their partitions and
 // order, and per partition its count, local offset and global run base.
 size_t p1_scatter_smem(uint32_t n_parts, int round) {
     return (size_t)round * (sizeof(unsigned long long) + sizeof(unsigned short)) +
-           (size_t)n_parts * (sizeof(unsigned long long) + 3 * sizeof(unsigned));
+           (size_t)n_parts * (16 + 2 * sizeof(unsigned));
 }
 
 // One read per thread, rolled base by base: the state of one read's walk.
@@ -955,11 +964,10 @@ template <int NT, int IT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs pa) {
     extern __shared__ __align__(16) unsigned char dyn[];
     unsigned long long *sorted = reinterpret_cast<unsigned long long *>(dyn);
-    unsigned long long *gbase = sorted + NT * IT;
-    unsigned *hist = reinterpret_cast<unsigned *>(gbase + pa.n_parts);
+    BinDest *dest = reinterpret_cast<BinDest *>(sorted + NT * IT);  // per partition: where its run goes
+    unsigned *hist = reinterpret_cast<unsigned *>(dest + pa.n_parts);
     unsigned *loff = hist + pa.n_parts;
-    unsigned *fit = loff + pa.n_parts;  // records of the run that fit the partition's region
-    unsigned short *spart = reinterpret_cast<unsigned short *>(fit + pa.n_parts);
+    unsigned short *spart = reinterpret_cast<unsigned short *>(loff + pa.n_parts);
     __shared__ uint64_t wb[NT / 32];
     const int shift = 64 - pa.bits;
     const uint32_t per = (pa.n_parts + blockDim.x - 1) / blockDim.x;
@@ -1005,16 +1013,19 @@ __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs p
                 if (j < pa.n_parts) {
                     const unsigned c = hist[j];
                     loff[j] = (unsigned)run;
-                    run += c;
-                    unsigned long long g0 = 0;
-                    unsigned f = 0;
+                    BinDest d;
+                    d.dst = 0;
+                    d.lim = (unsigned)run;
+                    d.pad = 0;
                     if (c) {
-                        g0 = atomicAdd(&pa.part_cursor[j], (unsigned long long)c);
+                        const unsigned long long g0 = atomicAdd(&pa.part_cursor[j], (unsigned long long)c);
                         const unsigned long long lim = pa.part_start[j + 1];  // region end
-                        f = g0 + c <= lim ? c : (g0 < lim ? (unsigned)(lim - g0) : 0u);
+                        const unsigned f = g0 + c <= lim ? c : (g0 < lim ? (unsigned)(lim - g0) : 0u);
+                        d.dst = g0 - run;
+                        d.lim = (unsigned)run + f;
                     }
-                    gbase[j] = g0;
-                    fit[j] = f;
+                    dest[j] = d;
+                    run += c;
                 }
             }
             __syncthreads();
@@ -1029,10 +1040,10 @@ __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs p
             }
             __syncthreads();
             for (uint32_t j = threadIdx.x; j < (uint32_t)total; j += blockDim.x) {
-                const unsigned part = spart[j];
+                const BinDest d = dest[spart[j]];
                 // records past the partition's region are dropped (the overflow
                 // is flagged after the scatter and the build recounts)
-                if (j - loff[part] < fit[part]) pa.records[gbase[part] + (j - loff[part])] = sorted[j];
+                if (j < d.lim) pa.records[d.dst + j] = sorted[j];
             }
         }
     }
@@ -1317,6 +1328,94 @@ __global__ void __launch_bounds__(NT, MINB) k_sub_scatter(BucketArgs b) {
             // records past the bucket's region are dropped (the overflow is
             // flagged by the bucket count and the build recounts)
             if (j - loff[bn] < fit[bn]) b.rec2[gbase[bn] + (j - loff[bn])] = w;
+        }
+    }
+}
+
+// Level-2 scatter, one shared atomic per record: the histogram's atomicAdd
+// returns the record's rank within its bin, kept (16 bits each, two per
+// register) until the records are ordered by bin in shared memory.
+constexpr size_t kSubScatter2Dyn = kBkChunk * sizeof(unsigned long long) + kBkBinsMax * sizeof(BinDest) +
+                                   kBkBinsMax * 2 * sizeof(unsigned);
+
+template <int NT, int IT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_sub_scatter2(BucketArgs b) {
+    static_assert(IT % 2 == 0, "ranks are packed two per register");
+    extern __shared__ __align__(16) unsigned char dyn[];
+    unsigned long long *sorted = reinterpret_cast<unsigned long long *>(dyn);
+    BinDest *dest = reinterpret_cast<BinDest *>(sorted + NT * IT);
+    unsigned *hist = reinterpret_cast<unsigned *>(dest + kBkBinsMax);
+    unsigned *loff = hist + kBkBinsMax;
+    __shared__ uint64_t wb[NT / 32];
+    const uint32_t P2 = 1u << b.b2;
+    const uint32_t per = (P2 + NT - 1) / NT;  // bins per thread in the scan
+    const int sh = 64 - b.b1 - b.b2 + 8;      // record >> sh = its bin (b2 > 0)
+    const uint64_t nq = *b.status & kStatusPartOverflow ? 0 : b.chunk_start[b.n_parts];  // recount ahead
+    for (uint32_t j = threadIdx.x; j < P2; j += NT) hist[j] = 0;
+    for (uint64_t q = blockIdx.x; q < nq; q += gridDim.x) {
+        uint64_t r0, r1;
+        const uint32_t p = chunk_range(b, q, r0, r1);
+        const uint32_t n = (uint32_t)(r1 - r0);
+        unsigned long long v[IT];
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+            const uint32_t r = (uint32_t)it * NT + threadIdx.x;
+            v[it] = r < n ? b.rec1[r0 + r] : 0ull;
+        }
+        __syncthreads();  // hist cleared, the previous chunk written out
+        unsigned rk[IT / 2];
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+            unsigned x = 0;
+            if ((uint32_t)it * NT + threadIdx.x < n) x = atomicAdd(&hist[b.b2 ? (uint32_t)(v[it] >> sh) : 0u], 1u);
+            if (it & 1) rk[it / 2] |= x << 16;
+            else rk[it / 2] = x;
+        }
+        __syncthreads();
+        uint64_t mine = 0;
+        for (uint32_t x = 0; x < per; ++x) {
+            const uint32_t j = threadIdx.x * per + x;
+            if (j < P2) mine += hist[j];
+        }
+        uint64_t run = block_exclusive_scan<NT>(mine, wb, nullptr);
+        for (uint32_t x = 0; x < per; ++x) {
+            const uint32_t j = threadIdx.x * per + x;
+            if (j < P2) {
+                const unsigned c = hist[j];
+                loff[j] = (unsigned)run;
+                BinDest d;
+                d.dst = 0;
+                d.lim = (unsigned)run;
+                d.pad = 0;
+                if (c) {
+                    const uint64_t bkj = (uint64_t)p * P2 + j;
+                    const unsigned long long g0 = atomicAdd(&b.cursor2[bkj], (unsigned long long)c);
+                    const unsigned long long lim = b.off2[bkj + 1];  // region end
+                    const unsigned f = g0 + c <= lim ? c : (g0 < lim ? (unsigned)(lim - g0) : 0u);
+                    d.dst = g0 - run;
+                    d.lim = (unsigned)run + f;
+                }
+                dest[j] = d;
+                hist[j] = 0;  // cleared for the next chunk
+                run += c;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+            if ((uint32_t)it * NT + threadIdx.x < n) {
+                const uint32_t bn = b.b2 ? (uint32_t)(v[it] >> sh) : 0u;
+                const unsigned rank = (rk[it / 2] >> (16 * (it & 1))) & 0xffffu;
+                sorted[loff[bn] + rank] = v[it];
+            }
+        }
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < n; j += NT) {
+            const unsigned long long w = sorted[j];
+            const BinDest d = dest[b.b2 ? (uint32_t)(w >> sh) : 0u];
+            // records past the bucket's region are dropped (the overflow is
+            // flagged by the bucket count and the build recounts)
+            if (j < d.lim) b.rec2[d.dst + j] = w;
         }
     }
 }
@@ -2142,7 +2241,14 @@ int launch_sub_scatter(const BucketArgs &b, cudaStream_t s) {
     switch (scatter_shape()) {
         case 1: return launch_sub_scatter_shape<512, 8, 2>(b, s);
         case 2: return launch_sub_scatter_shape<512, 8, 3>(b, s);
-        default: return launch_sub_scatter_shape<256, 16, 3>(b, s);
+        default: {  // one shared atomic per record (the histogram's returns the rank)
+            auto kern = k_sub_scatter2<256, 16, 3>;
+            const uint64_t chunks = b.n_rec / kBkChunk + b.n_parts;
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSubScatter2Dyn);
+            const uint64_t grid = std::min<uint64_t>(chunks, resident_grid(kern, 256, kSubScatter2Dyn));
+            kern<<<(unsigned)grid, 256, kSubScatter2Dyn, s>>>(b);
+            return 1;
+        }
         case 3: {  // bulk-copy staging (measured slower on GB300: 2 blocks/SM instead of 3)
             const uint64_t chunks = b.n_rec / kBkChunk + b.n_parts;
             cudaFuncSetAttribute(k_sub_scatter_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -52,29 +52,82 @@ struct NaScratch {
 // symbol; its device address comes from cudaGetSymbolAddress below.
 static __device__ __align__(256) NaScratch g_noalloc_scratch;
 
+// The array's device address per device, with the id of the context it was
+// resolved in: a context destroyed and made again (cudaDeviceReset) gets a new
+// id, and the address is resolved again in it.
+struct NaSlot {
+    unsigned long long ctx_id;
+    NaScratch *ptr;
+};
 std::mutex g_na_mu;
-NaScratch *g_na_ptr[kNaMaxDevices] = {};
+NaSlot g_na_slot[kNaMaxDevices] = {};
 
-// Once per device, with that device current: resolve the array's device
-// address. The first call on a device does this (it may load this module),
-// so make that first call before any stream capture.
+// The driver's cuCtxGetCurrent / cuCtxGetId, looked up through the runtime
+// (the library does not link the driver library itself). Result codes are the
+// driver's CUresult: 0 = success.
+typedef int (*CtxGetCurrentFn)(void **ctx);
+typedef int (*CtxGetIdFn)(void *ctx, unsigned long long *id);
+
+bool current_context_id(unsigned long long *id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void *f0 = nullptr, *f1 = nullptr;
+        cudaDriverEntryPointQueryResult q0, q1;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1)
+            return false;
+        get_current = reinterpret_cast<CtxGetCurrentFn>(f0);
+        get_id = reinterpret_cast<CtxGetIdFn>(f1);
+    }
+    void *ctx = nullptr;
+    if (get_current(&ctx) != 0 || !ctx) return false;
+    return get_id(ctx, id) == 0;
+}
+
+swg_status na_resolve(NaScratch **p) {
+    void *q = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&q, g_noalloc_scratch);
+    if (e != cudaSuccess || !q) {
+        set_error(std::string("cudaGetSymbolAddress of the no-allocation scratch: ") + cudaGetErrorString(e));
+        return SWG_ERR_CUDA;
+    }
+    *p = static_cast<NaScratch *>(q);
+    return SWG_OK;
+}
+
+// Once per device (and context), with that device current: resolve the
+// array's device address. The first call on a device does this (it may load
+// this module), and so does the first call after the device's context was
+// destroyed; make those calls before any stream capture.
 swg_status na_scratch(int dev, NaScratch **out) {
     if (dev < 0 || dev >= kNaMaxDevices) {
         set_error("device ordinal out of range for the no-allocation scratch");
         return SWG_ERR_BAD_INPUT;
     }
     std::lock_guard<std::mutex> lock(g_na_mu);
-    if (!g_na_ptr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            set_error(std::string("cudaGetSymbolAddress of the no-allocation scratch: ") +
-                      cudaGetErrorString(e));
-            return SWG_ERR_CUDA;
-        }
-        g_na_ptr[dev] = static_cast<NaScratch *>(p);
+    NaSlot &slot = g_na_slot[dev];
+    unsigned long long id = 0;
+    if (!current_context_id(&id)) {
+        // no context current in this thread yet: resolving the symbol makes the
+        // device's primary context current, then its id can be read
+        swg_status st = na_resolve(out);
+        if (st) return st;
+        if (!current_context_id(&id)) return SWG_OK;  // no id to cache by: resolved per call
+        slot.ctx_id = id;
+        slot.ptr = *out;
+        return SWG_OK;
     }
-    *out = g_na_ptr[dev];
+    if (!slot.ptr || slot.ctx_id != id) {
+        swg_status st = na_resolve(&slot.ptr);
+        if (st) {
+            slot.ptr = nullptr;
+            return st;
+        }
+        slot.ctx_id = id;
+    }
+    *out = slot.ptr;
     return SWG_OK;
 }
 

@@ -61,6 +61,8 @@ struct swg_server {
     uint64_t resident = 0;  // results waiting to be fetched
     swg_server_stats st;
     bool stop = false;
+    uint32_t live_workers = 0;  // workers whose set-up succeeded or is still under way
+    std::string dead_error;     // set when every worker failed its set-up
     std::vector<std::thread> workers;
     cudaStream_t fetch_stream = nullptr;
 };
@@ -76,12 +78,43 @@ uint64_t footprint_of(uint64_t reads, uint64_t words, uint64_t occ, double load)
     return words * 4 + reads * (8 + 4 + 8 + 4) + cap * 16 * 2 + (16ull << 20);
 }
 
+// A worker whose set-up failed leaves; when the last one does, every queued
+// request fails with the reason and later submissions are refused with it.
+void worker_setup_failed(swg_server *srv, swg_status st, const std::string &why) {
+    std::lock_guard<std::mutex> lock(srv->mu);
+    if (--srv->live_workers == 0) {
+        srv->dead_error = "request server has no working worker: " + why;
+        for (Request *r : srv->queue) {
+            r->state = SWG_REQ_FAILED;
+            r->status = st;
+            r->error = srv->dead_error;
+            r->t_done = now_s();
+            srv->st.failed++;
+        }
+        srv->queue.clear();
+    }
+    srv->cv_done.notify_all();
+}
+
 void worker_main(swg_server *srv) {
-    cudaSetDevice(srv->device);
+    cudaError_t ce = cudaSetDevice(srv->device);
+    if (ce != cudaSuccess) {
+        worker_setup_failed(srv, SWG_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(ce));
+        return;
+    }
     swg_graph *g = nullptr;
-    if (swg_graph_create(&g) != SWG_OK) return;
+    swg_status gs = swg_graph_create(&g);
+    if (gs != SWG_OK) {
+        worker_setup_failed(srv, gs, std::string("graph handle: ") + swg_last_error());
+        return;
+    }
     cudaStream_t stream = nullptr;
-    cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+    ce = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) {
+        swg_graph_free(g);
+        worker_setup_failed(srv, SWG_ERR_CUDA, std::string("stream creation: ") + cudaGetErrorString(ce));
+        return;
+    }
     swg_opts o;
     std::memset(&o, 0, sizeof(o));
     o.load_factor = srv->opts.load_factor;
@@ -211,6 +244,7 @@ swg_status swg_server_create(const swg_server_opts *o, swg_server **out) {
         swg::set_error("stream creation failed");
         return SWG_ERR_CUDA;
     }
+    srv->live_workers = srv->opts.workers;
     for (uint32_t i = 0; i < srv->opts.workers; i++) srv->workers.emplace_back(worker_main, srv);
     *out = srv;
     return SWG_OK;
@@ -252,6 +286,11 @@ swg_status swg_server_submit(swg_server *srv, const swg_sample *req, uint64_t *t
     }
     if (srv->stop) {
         delete r;
+        return SWG_ERR_BAD_STATE;
+    }
+    if (!srv->dead_error.empty()) {
+        delete r;
+        swg::set_error(srv->dead_error);
         return SWG_ERR_BAD_STATE;
     }
     r->ticket = srv->next_ticket++;

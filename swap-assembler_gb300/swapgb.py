@@ -491,6 +491,23 @@ def synth_fasta(**kw) -> bytes:
         _synth_lib().swg_synth_free(buf)
 
 
+def batch_workload_specs(n: int = 256, seed: int = 4) -> list[dict]:
+    """Generator parameters of the batched workload's samples: genome sizes
+    log-uniform 50 kbp-2 Mbp, read length from {75, 100, 150, 250}, coverage
+    uniform 10-60x, substitutions uniform 0.1-1% (built with k=27, c=3)."""
+    import math
+    import random
+    rng = random.Random(seed)
+    out = []
+    for i in range(n):
+        g = int(math.exp(rng.uniform(math.log(50_000), math.log(2_000_000))))
+        L = rng.choice([75, 100, 150, 250])
+        cov = rng.uniform(10, 60)
+        out.append(dict(seed=10_000 + i, genome_len=g, n_reads=int(cov * g / L), read_len=L,
+                        sub_rate=rng.uniform(0.001, 0.01)))
+    return out
+
+
 def synth_fasta_file(path: str, **kw) -> int:
     p = synth_params(**kw)
     n = _synth_lib().swg_synth_fasta_file(C.byref(p), str(path).encode())

@@ -29,9 +29,17 @@ def test_reference_arm_line():
     assert line["unit"] == "bases/s" and line["value"] > 0 and line["higher_is_better"] is True
     assert line["steps"] == 1 and line["warmup"] == 1 and line["n_gpus"] == 1
     assert "workload" in line["config"] and line["vs_baseline"] is None
+    # the same config dict as the GPU arm's line for the same workload
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", ROOT / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    bench.WORKLOAD, bench.K, bench.CUTOFF, bench.DESC = bench.CONFIGS[1]
+    assert line["config"] == bench.config_dict()
     cpu = line["cpu_baseline"]
     assert cpu["value"] == line["value"] and cpu["kind"] in ("port", "reference")
     assert cpu["cores"] >= 1 and cpu["sample"]
+    assert "whole workload" in cpu["sample"]  # no prefix sample under the full workload's config
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0

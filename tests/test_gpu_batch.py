@@ -116,3 +116,24 @@ def test_tagged_batch_many_samples_and_overflow():
     ok, om = oracle.records(texts[137], 21, 2 + (137 % 3))
     keys, mult = g.batch_copy_out(137)
     assert np.array_equal(keys, ok) and np.array_equal(mult, om)
+
+
+def test_batched_workload_samples_equal_the_restatement():
+    """32 samples of the batched workload's distribution (8 per read length:
+    75, 100, 150 and 250 bp; genomes 50 kbp-2 Mbp at 10-60x), built as one
+    batch with k=27, c=3; each sample's k-molecules and multiplicities equal
+    the CPU restatement of the reference on that sample alone
+    (kmerGraph.cpp:95-310, graph.cpp:1049-1114), bit for bit."""
+    specs = swapgb.batch_workload_specs(256, seed=4)
+    chosen = []
+    for L in (75, 100, 150, 250):
+        chosen += [p for p in specs if p["read_len"] == L][:8]
+    assert len(chosen) == 32
+    texts = [swapgb.synth_fasta(**p) for p in chosen]
+    g = swapgb.Graph()
+    g.build_batch(swapgb.Opts(), [(swapgb.reads_from_fasta(t, 27), 27, 3) for t in texts])
+    assert g.batch_size() == 32
+    for i, t in enumerate(texts):
+        keys, mult = g.batch_copy_out(i)
+        ok, om = oracle.records(t, 27, 3)
+        assert np.array_equal(keys, ok) and np.array_equal(mult, om), "sample %d (%s)" % (i, chosen[i])
