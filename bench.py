@@ -366,10 +366,10 @@ def served_metrics(stream_ptr: int) -> dict:
             srv.release(t)
         base = srv.stats()
         duration = min(10.0, SERVED_REQUESTS / rate)
-        tickets, reqs = [], []  # reqs: (input index, k, c)
+        tickets, reqs, t_sub = [], [], []  # reqs: (input index, k, c); submit times (s)
         lock = threading.Lock()
         done = threading.Event()
-        got = {}  # ticket -> (latency s, digest)
+        got = {}  # ticket -> (latency s, keys, multiplicities), checked after the stream
 
         def collector():
             i = 0
@@ -385,9 +385,9 @@ def served_metrics(stream_ptr: int) -> dict:
                     time.sleep(0.0005)
                     continue
                 srv.wait(t, 300.0)
-                lat = srv.poll(t)[1]
-                k, m = srv.fetch(t, sorted=True)  # outside the latency (taken at completion)
-                got[t] = (lat, digest(k, m))
+                lat = srv.poll(t)[1]  # completion - submission, taken by the server
+                k, m = srv.fetch(t, sorted=False)  # a copy only; sorted and hashed after the stream
+                got[t] = (lat, k, m)
                 i += 1
 
         th = threading.Thread(target=collector)
@@ -400,28 +400,40 @@ def served_metrics(stream_ptr: int) -> dict:
                 time.sleep(t_next - now)
             j = len(inputs) - 1 if rng.random() < 0.02 else rng.randrange(len(pool))
             k, c = rng.choice([21, 25, 27, 31]), rng.choice([2, 3, 5])
+            ts = time.perf_counter() - t0
             t = srv.submit(inputs[j], k, c)
             with lock:
                 tickets.append(t)
                 reqs.append((j, k, c))
+                t_sub.append(ts)
             t_next += rng.expovariate(rate)
         done.set()
         th.join()
-        wall = time.perf_counter() - t0
         st = srv.stats()
         srv.close()
         lats = sorted(got[t][0] for t in tickets)
         q = lambda f: lats[min(len(lats) - 1, int(f * len(lats)))]
+        # the stream's span: first submission to the last result resident
+        span = max(t_sub[i] + got[t][0] for i, t in enumerate(tickets)) - t_sub[0]
         n_batches = st["batches"] - base["batches"]
         bases = sum(inputs[j].n_bases for j, _, _ in reqs)
         row = {"rate_req_per_s": rate, "seconds": duration, "requests": len(tickets),
                "large_requests": sum(j == len(inputs) - 1 for j, _, _ in reqs),
                "p50_ms": 1e3 * q(0.50), "p99_ms": 1e3 * q(0.99), "max_ms": 1e3 * lats[-1],
-               "aggregate_samples_per_s": len(tickets) / wall, "aggregate_bases_per_s": bases / wall,
-               "offered_bases_per_s": bases / duration, "batches": n_batches,
-               "mean_batch_requests": len(tickets) / max(n_batches, 1),
+               "span_s": span, "aggregate_samples_per_s": len(tickets) / span,
+               "aggregate_bases_per_s": bases / span, "offered_bases_per_s": bases / duration,
+               "batches": n_batches, "mean_batch_requests": len(tickets) / max(n_batches, 1),
                "max_batch_requests": st["max_batch_requests"]}
-        return row, [(reqs[i], got[t][1]) for i, t in enumerate(tickets)]
+        from concurrent.futures import ThreadPoolExecutor
+
+        def check(i):
+            _, kk, mm = got[tickets[i]]
+            o = np.argsort(kk, kind="stable")
+            return reqs[i], digest(kk[o], mm[o])
+        with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+            checks = list(ex.map(check, range(len(tickets))))
+        got.clear()
+        return row, checks
 
     rows, checks = [], []
     for i, rate in enumerate(SERVED_RATES):
@@ -450,6 +462,8 @@ def served_metrics(stream_ptr: int) -> dict:
                         % ("/".join("%g" % r for r in SERVED_RATES), SERVED_REQUESTS),
             "latency": "submit (including the server's copy of the reads) to the result resident on the "
                        "device",
+            "aggregate_means": "requests (bases) over the span from the first submission to the last "
+                               "result resident on the device",
             "results_identical_means": "SHA-256 of the fetched sorted records equals a plain build's of the "
                                        "same input, k and c",
             "plain_samples_per_s_means": "the same requests built one by one with swg_graph_build from host "
@@ -631,6 +645,40 @@ def main() -> int:
 
     e2e_s, n_e2e, e2e_steps = timed(e2e_fasta)
     e2e_p_s, _, e2e_p_steps = timed(e2e_packed)
+
+    # the documented drop-in from a FASTA file on local disk,
+    # page cache warm: device framing (swg_graph_build_fasta_file) against host
+    # framing (swg_reads_from_fasta_file + swg_graph_build), result on the device
+    dropin = None
+    if rank == 0 and not args.reads:
+        import tempfile
+        with tempfile.TemporaryDirectory() as td:
+            fa = os.path.join(td, "reads.fa")
+            with open(fa, "wb") as f:
+                f.write(text)
+            g3 = swapgb.Graph()
+
+            def file_device():
+                g3.build_fasta_file(opts, fa)
+                torch.cuda.synchronize()
+
+            def file_host():
+                r = swapgb.reads_from_fasta_file(fa, K)
+                g3.build_reads(opts, r)
+                torch.cuda.synchronize()
+
+            def wall(fn, n=3):
+                fn()
+                ts = []
+                for _ in range(n):
+                    t0 = time.perf_counter()
+                    fn()
+                    ts.append(time.perf_counter() - t0)
+                return 1e3 * statistics.median(ts)
+            dropin = {"what": "one build from the FASTA file (page cache warm) to the filtered graph on the device",
+                      "file_device_framing_ms": wall(file_device), "file_host_framing_ms": wall(file_host),
+                      "file_bytes": len(text)}
+            g3.close()
     h2d = h_text.numel()
     h2d_p = h_packed.numel() * 4 + h_off.numel() * 8 + h_len.numel() * 4
     d2h = n_e2e * 16
@@ -675,6 +723,21 @@ def main() -> int:
                 "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src,
                 "traffic": (tpo * n_occ) if tpo else None, "traffic_source": tsrc,
                 "algorithmic_bytes": algo_bytes, "bytes_model": model, "kernel_ms": k_ms}
+    if kname == "k_bucket_count" and not args.no_probe:
+        # the kernel's own ceiling is on chip: one 64-bit shared CAS per record
+        # (a lower bound: linear probing adds some) and one 32-bit shared add
+        # per arc, at the rates this GPU's shared-memory atomics reach
+        r_add = swapgb.probe_shared_atomics("add_u32", 1 << 31, stream.cuda_stream)
+        r_cas = swapgb.probe_shared_atomics("cas_u64", 1 << 30, stream.cuda_stream)
+        n_arcs = 2 * n_occ - 2 * n_with_occ
+        floor_ms = 1e3 * (n_occ / r_cas + n_arcs / r_add)
+        roofline["on_chip"] = {"bound": "shared-memory atomics", "floor_ms": floor_ms,
+                               "frac": floor_ms / k_ms, "cas64_lane_ops_per_s": r_cas,
+                               "add32_lane_ops_per_s": r_add, "cas_per_build": n_occ,
+                               "adds_per_build": n_arcs,
+                               "model": "one 64-bit shared atomicCAS per record + one 32-bit shared "
+                                        "atomicAdd per arc, at the rates swg_probe_shared_atomics "
+                                        "measures in the same table layout (this run)"}
     atomic = None
     if not args.no_probe and rank == 0:
         table_bytes = 16 << 30
@@ -734,6 +797,7 @@ def main() -> int:
                            "unit": "bases/s", "h2d_bytes_per_step": h2d_p,
                            "d2h_bytes_per_step": d2h, "wall_ms_steps": e2e_p_steps,
                            "path": "swg_graph_build on pinned host packed reads + swg_graph_copy_out"},
+            "dropin": dropin,
             "gpu_launches": launches,
             "build": dict(info, phase_ms_mean=mean_ms),
             "roofline": roofline,

@@ -167,6 +167,14 @@ swg_status swg_graph_build_device(swg_graph *g, const swg_opts *o, const uint32_
  * Environment: SWG_NO_STREAM=1 copies and frames the text in one piece;
  * SWG_STREAM_PIECES=2..16 sets the number of pieces. */
 swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *text, uint64_t len);
+
+/* As swg_graph_build_fasta, on the FASTA file at path: the file is read (in
+ * parallel slices) into a pinned host buffer the handle keeps for later calls,
+ * then uploaded, framed and built on the device. The reference's reader takes
+ * the file by name too (parameter::fastaPath, kmerGraph.cpp:95-156); this is
+ * the one-call replacement for constructDistNodeGraph + cutoffGraph
+ * (graph.cpp:1049-1114) on a file. SWG_ERR_IO if the file cannot be read. */
+swg_status swg_graph_build_fasta_file(swg_graph *g, const swg_opts *o, const char *path);
 /* Convenience: create + build from host packed reads. */
 swg_status swg_build(const swg_opts *o, const uint32_t *packed, uint64_t n_words,
                      const uint64_t *read_off, const uint32_t *read_len, uint64_t n_reads,
@@ -292,6 +300,17 @@ swg_status swg_graph_write_node_lines(const swg_graph *g, const char *path);
  * without a single-sample build; SWG_ERR_BAD_INPUT for an even k (the
  * reference's k is odd, sequence.cpp:44) or more than 2^29 k-molecules. */
 swg_status swg_graph_merge(swg_graph *g);
+/* The same merge with the nodes visited in the caller's order: order_keys
+ * lists every k-molecule of the built graph once (host memory), in the order
+ * the reference's merge loop meets them (its node map's iteration order,
+ * graph.cpp:1412). Each chain's multiplicities are then those of that order
+ * with every edge message applied as it is sent: the chain's merge tree is
+ * the Cartesian tree of the visit times (a node merges the segments that
+ * reach, on each side, the nearest node visited after it); a cycle keeps the
+ * node visited last. Arc strings and surviving nodes are those of
+ * swg_graph_merge. SWG_ERR_BAD_INPUT if the order misses a key, repeats one
+ * or names one the graph does not hold. */
+swg_status swg_graph_merge_in_order(swg_graph *g, const uint64_t *order_keys, uint64_t n_order);
 typedef struct swg_merge_info {
     uint64_t nodes;      /* nodes left (lines of the -d file) */
     uint64_t chains;     /* chains of merged nodes */
@@ -406,6 +425,13 @@ swg_status swg_autotune_apply(const char *cache_path, int k, uint32_t read_len, 
  * 5/6: loads, load+CAS pairs) per second (device time). */
 swg_status swg_probe_random_access(int kind, uint64_t table_bytes, uint64_t n_ops, void *stream,
                                    double *ops_per_s);
+/* Shared-memory atomic throughput on this GPU (lane operations per second,
+ * whole GPU): n_ops random operations in per-CTA tables laid out like the
+ * bucket count's (two CTAs of 512 threads per SM, 4096 64-bit key slots and
+ * 16384 32-bit counter words each). kind: 0 = 32-bit atomicAdd, 1 = 64-bit
+ * atomicCAS. The bucket count's on-chip floor is its CAS and counter adds at
+ * these rates. No counterpart in the reference (a measurement tool). */
+swg_status swg_probe_shared_atomics(int kind, uint64_t n_ops, void *stream, double *ops_per_s);
 
 #ifdef __cplusplus
 }

@@ -12,12 +12,17 @@
 //     detected on the device and the build is repeated with a larger table;
 //   partitioned: record scatter -> waves of L2-resident partition slices.
 // A last synchronisation reads the status and the survivor count.
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <nvtx3/nvToolsExt.h>
@@ -157,6 +162,10 @@ struct swg_graph {
     uint64_t nl_cap = 0;
     uint64_t *d_keep = nullptr, *d_words = nullptr, *d_ridx = nullptr, *d_woff = nullptr;
     uint64_t keep_cap = 0, words_cap = 0, ridx_cap = 0, woff_cap = 0;
+    // swg_graph_build_fasta_file: pinned host buffer the file is read into
+    // (kept and reused by later calls of this handle)
+    char *h_file = nullptr;
+    uint64_t h_file_cap = 0;
 };
 
 namespace {
@@ -1493,6 +1502,7 @@ void swg_graph_free(swg_graph *g) {
     cudaFree(g->d_words);
     cudaFree(g->d_ridx);
     cudaFree(g->d_woff);
+    if (g->h_file) cudaFreeHost(g->h_file);
     if (g->copy) cudaStreamSynchronize(g->copy);
     if (g->frame) cudaStreamSynchronize(g->frame);
     for (auto &e : g->piece_ev)
@@ -1623,6 +1633,65 @@ swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *te
     return st;
 }
 
+swg_status swg_graph_build_fasta_file(swg_graph *g, const swg_opts *o, const char *path) {
+    if (!g || !path) return SWG_ERR_BAD_INPUT;
+    swg_status st = check_opts(o);
+    if (st) return st;
+    const int fd = ::open(path, O_RDONLY);
+    if (fd < 0) {
+        swg::set_error(std::string("cannot open ") + path);
+        return SWG_ERR_IO;
+    }
+    struct stat sb;
+    if (::fstat(fd, &sb) != 0 || sb.st_size <= 0) {
+        ::close(fd);
+        swg::set_error(std::string(sb.st_size == 0 ? "empty FASTA input: " : "cannot stat ") + path);
+        return sb.st_size == 0 ? SWG_ERR_BAD_INPUT : SWG_ERR_IO;
+    }
+    const uint64_t len = (uint64_t)sb.st_size;
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    if (g->h_file_cap < len) {
+        if (g->h_file) cudaFreeHost(g->h_file);
+        g->h_file = nullptr;
+        g->h_file_cap = 0;
+        cudaError_t e = cudaHostAlloc((void **)&g->h_file, len, cudaHostAllocDefault);
+        if (e != cudaSuccess) {
+            ::close(fd);
+            g->h_file = nullptr;
+            return cuda_fail(e, "pinned buffer for the FASTA file");
+        }
+        g->h_file_cap = len;
+    }
+    // read in parallel slices of at least 16 MiB
+    const uint64_t slice = 16ull << 20;
+    const unsigned nt = (unsigned)std::min<uint64_t>(8, (len + slice - 1) / slice);
+    std::vector<int> ok(nt, 1);
+    {
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < nt; t++)
+            th.emplace_back([&, t] {
+                uint64_t a = len * t / nt;
+                const uint64_t b = len * (t + 1) / nt;
+                while (a < b) {
+                    const ssize_t r = ::pread(fd, g->h_file + a, (size_t)std::min<uint64_t>(b - a, 1ull << 30), (off_t)a);
+                    if (r <= 0) {
+                        ok[t] = 0;
+                        return;
+                    }
+                    a += (uint64_t)r;
+                }
+            });
+        for (auto &x : th) x.join();
+    }
+    ::close(fd);
+    for (unsigned t = 0; t < nt; t++)
+        if (!ok[t]) {
+            swg::set_error(std::string("short read from ") + path);
+            return SWG_ERR_IO;
+        }
+    return swg_graph_build_fasta(g, o, g->h_file, len);
+}
+
 swg_status swg_build(const swg_opts *o, const uint32_t *packed, uint64_t n_words,
                      const uint64_t *read_off, const uint32_t *read_len, uint64_t n_reads,
                      swg_graph **out) {
@@ -1645,17 +1714,14 @@ swg_status swg_build_fasta(const swg_opts *o, const char *text, uint64_t len, sw
     *out = nullptr;
     swg_status st = check_opts(o);
     if (st) return st;
-    swg_reads *r = nullptr;
-    st = swg_reads_from_fasta(text, len, o->k, &r);
-    if (st) return st;
-    const uint32_t *p;
-    const uint64_t *off;
-    const uint32_t *ln;
-    uint64_t nw, nr, nb;
-    swg_reads_view(r, &p, &nw, &off, &ln, &nr, &nb);
-    st = swg_build(o, p, nw, off, ln, nr, out);
-    swg_reads_free(r);
-    return st;
+    swg_graph *g = nullptr;
+    if ((st = swg_graph_create(&g))) return st;
+    if ((st = swg_graph_build_fasta(g, o, text, len))) {
+        swg_graph_free(g);
+        return st;
+    }
+    *out = g;
+    return SWG_OK;
 }
 
 swg_status swg_graph_size(const swg_graph *g, uint64_t *n) {
@@ -1749,7 +1815,17 @@ swg_status swg_graph_write_node_lines(const swg_graph *g, const char *path) {
 
 // Merging of semi-extended k-molecules (merge.cu) over the built graph; the
 // result is the -d file's text, kept on the device until the next build.
-swg_status swg_graph_merge(swg_graph *g) {
+static swg_status merge_impl(swg_graph *g, const uint64_t *order, uint64_t n_order);
+
+swg_status swg_graph_merge(swg_graph *g) { return merge_impl(g, nullptr, 0); }
+
+swg_status swg_graph_merge_in_order(swg_graph *g, const uint64_t *order_keys, uint64_t n_order) {
+    if (!order_keys && n_order) return SWG_ERR_BAD_INPUT;
+    static const uint64_t none = 0;
+    return merge_impl(g, order_keys ? order_keys : &none, n_order);
+}
+
+static swg_status merge_impl(swg_graph *g, const uint64_t *order, uint64_t n_order) {
     Phase phase("simplifyDistNodeGraph");
     if (!g) return SWG_ERR_BAD_INPUT;
     swg_status st = writable(g);
@@ -1768,7 +1844,8 @@ swg_status swg_graph_merge(swg_graph *g) {
     }
     cudaEvent_t e0 = g->ev[0], e1 = g->ev[1];
     SWG_CUDA(cudaEventRecord(e0, g->own), "merge timing");
-    st = swg::merge_graph(g->d_out_keys, g->d_out_mult, g->n_out, g->k, g->own, &g->mg, &g->mres);
+    st = swg::merge_graph(g->d_out_keys, g->d_out_mult, g->n_out, g->k, g->own, &g->mg, &g->mres,
+                          reinterpret_cast<const unsigned long long *>(order), n_order);
     if (st) return st;
     SWG_CUDA(cudaEventRecord(e1, g->own), "merge timing");
     SWG_CUDA(cudaEventSynchronize(e1), "merge timing");
@@ -1997,6 +2074,15 @@ swg_status swg_probe_random_access(int kind, uint64_t table_bytes, uint64_t n_op
     if (e != cudaSuccess) return cuda_fail(e, "random-access probe");
     const double per = kind == 5 ? 4.0 : (kind == 6 ? 2.0 : 1.0);  // accesses per operation
     *ops_per_s = ms > 0 ? per * (double)n_ops / (ms * 1e-3) : 0;
+    return SWG_OK;
+}
+
+swg_status swg_probe_shared_atomics(int kind, uint64_t n_ops, void *stream, double *ops_per_s) {
+    if (!ops_per_s || kind < 0 || kind > 1 || n_ops == 0) return SWG_ERR_BAD_INPUT;
+    float ms = 0;
+    cudaError_t e = swg::run_smem_probe(kind, n_ops, (cudaStream_t)stream, &ms);
+    if (e != cudaSuccess) return cuda_fail(e, "shared-memory atomic probe");
+    *ops_per_s = ms > 0 ? (double)n_ops / (ms * 1e-3) : 0;
     return SWG_OK;
 }
 

@@ -2323,6 +2323,63 @@ int launch_big_multi(const BuildArgs &a, const BucketArgs &b, const unsigned lon
 }
 
 
+// Shared-memory atomic probe (the on-chip roofline of the bucket count):
+// two CTAs of 512 threads per SM, each with a zeroed table of kBkTable 64-bit
+// slots and 4 x kBkTable 32-bit words (the bucket table's key and counter
+// arrays), every thread issuing `iters` rounds of four independent operations
+// at random slots. kind 0: 32-bit atomicAdd; kind 1: 64-bit atomicCAS (empty
+// slot -> key; most find the slot taken, as most of a bucket's records do).
+__global__ void __launch_bounds__(kBkThreads, 2) k_smem_probe(int kind, int iters, unsigned long long *sink) {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    unsigned long long *keys = reinterpret_cast<unsigned long long *>(dyn);
+    unsigned *cnt = reinterpret_cast<unsigned *>(keys + kBkTable);
+    for (uint32_t j = threadIdx.x; j < (uint32_t)kBkTable; j += kBkThreads) {
+        keys[j] = 0;
+        reinterpret_cast<uint4 *>(cnt)[j] = make_uint4(0, 0, 0, 0);
+    }
+    __syncthreads();
+    uint32_t x[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) x[q] = (blockIdx.x * kBkThreads + threadIdx.x) * 4u + q + 1u;
+    unsigned long long acc = 0;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            x[q] = x[q] * 0x9e3779b1u + 0x7f4a7c15u;
+            if (kind == 0) atomicAdd(&cnt[x[q] >> 18], 1u);  // 14 bits: 4 x kBkTable words
+            else acc += atomicCAS(&keys[x[q] >> 20], 0ull, (unsigned long long)x[q] | 1ull);
+        }
+    }
+    if (acc == 0x5a5a5a5a5a5a5a5aull) *sink = acc;  // keeps the CAS results live
+}
+
+cudaError_t run_smem_probe(int kind, uint64_t n_ops, cudaStream_t s, float *ms) {
+    unsigned long long *sink = nullptr;
+    cudaError_t err = cudaMalloc(&sink, sizeof(unsigned long long));
+    if (err != cudaSuccess) return err;
+    const size_t smem = (size_t)kBkTable * (sizeof(unsigned long long) + 4 * sizeof(unsigned));
+    cudaFuncSetAttribute(k_smem_probe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const unsigned grid = (unsigned)device_sm_count() * 2;
+    const uint64_t per_round = (uint64_t)grid * kBkThreads * 4;
+    const int iters = (int)std::max<uint64_t>(1, std::min<uint64_t>(n_ops / per_round, 1u << 20));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_smem_probe<<<grid, kBkThreads, smem, s>>>(kind, std::max(1, iters / 8), sink);  // warm-up
+    cudaEventRecord(e0, s);
+    k_smem_probe<<<grid, kBkThreads, smem, s>>>(kind, iters, sink);
+    cudaEventRecord(e1, s);
+    err = cudaEventSynchronize(e1);
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    *ms = t * (float)((double)n_ops / (double)(per_round * (uint64_t)iters));  // scale to n_ops
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    if (err == cudaSuccess) err = cudaGetLastError();
+    return err;
+}
+
 cudaError_t run_probe(int kind, uint64_t table_bytes, uint64_t n_ops, cudaStream_t s, float *ms) {
     Entry *table = nullptr;
     unsigned long long *sink = nullptr;

@@ -52,7 +52,18 @@ constexpr unsigned long long kEmptyKey = ~0ull;
 constexpr int kClasses = 40;  // chain segment size classes 2^0 .. 2^39
 
 // error bits
-constexpr unsigned kErrIndex = 1u, kErrNeighbour = 2u, kErrWalk = 4u, kErrCycle = 8u;
+constexpr unsigned kErrIndex = 1u, kErrNeighbour = 2u, kErrWalk = 4u, kErrCycle = 8u, kErrOrder = 16u;
+
+// Per chain position of a merge in a given visiting order: the visit time of
+// the node at the position, and the two segments that meet there (the first
+// arc of the left one, the last arc of the right one, their multiplicities)
+// once both are merged; `arrive` counts the sides that have arrived.
+struct CartSlot {
+    unsigned t;
+    unsigned lb, rb;
+    unsigned arrive;
+    unsigned char lv, rv;
+};
 
 __device__ __forceinline__ uint64_t fmix64(uint64_t x) {  // MurmurHash3 finaliser
     x ^= x >> 33;
@@ -115,6 +126,9 @@ struct MergeArgs {
     unsigned long long *skey;  // surviving nodes: keys, then (sorted) node indices
     unsigned *sidx;
     unsigned *err;
+    // merge in a given visiting order (null: the fixed tree order)
+    unsigned long long *vt;    // per node: its visit time
+    CartSlot *cart;            // per chain position (the ent layout)
 };
 
 __device__ __forceinline__ unsigned lookup(const MergeArgs &a, uint64_t key) {
@@ -309,11 +323,17 @@ __global__ void k_mg_finish(MergeArgs a, const unsigned long long *__restrict__ 
 }
 
 // ---- cycles of merged nodes: largest key by pointer jumping, cut there
+// A cycle keeps the node the merge visits last: the largest key in the fixed
+// order, the latest visit time in a given one.
+__device__ __forceinline__ unsigned long long cut_rank(const MergeArgs &a, uint64_t node) {
+    return a.vt ? a.vt[node] : a.keys[node];
+}
+
 __global__ void k_mg_cyc_init(MergeArgs a, uint64_t c) {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= c) return;
     const unsigned st = a.clist[t];
-    a.cx0[st] = a.keys[st >> 1];
+    a.cx0[st] = cut_rank(a, st >> 1);
     a.cy0[st] = a.succ[st];
 }
 
@@ -332,7 +352,7 @@ __global__ void k_mg_cyc_cut(MergeArgs a, uint64_t c, const unsigned long long *
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= c) return;
     const unsigned st = a.clist[t];
-    if (a.keys[st >> 1] == mx[st]) {
+    if (cut_rank(a, st >> 1) == mx[st]) {
         a.fl[st >> 1] &= (unsigned char)~1u;  // both states of the node store the same
         if (!(st & 1)) atomicAdd(&a.ctr[3], 1ull);
     }
@@ -436,6 +456,13 @@ __global__ void k_mg_entries(MergeArgs a) {
     const uint64_t m = a.mult[i];
     a.ent[e + c.pos] = (unsigned char)mbyte(m, c.fwd ? rslot(f) : lslot(f));
     a.ent_chain[e + c.pos] = id;
+    if (a.cart) {
+        CartSlot z;
+        z.t = (unsigned)a.vt[i];
+        z.lb = z.rb = z.arrive = 0;
+        z.lv = z.rv = 0;
+        a.cart[e + c.pos] = z;
+    }
     if (c.pos == 1) {
         a.ent[e] = (unsigned char)mbyte(m, c.fwd ? lslot(f) : rslot(f));
         a.ent_chain[e] = id;
@@ -458,6 +485,64 @@ __global__ void k_mg_level(MergeArgs a, uint64_t n_pairs, int t) {
     const uint64_t sum = (uint64_t)a.ent[e] * ll + (uint64_t)a.ent[e + ll] * lr;
     const int pre = (int)(unsigned)sum;
     a.ent[e] = (unsigned char)((uint64_t)(int64_t)pre / (ll + lr));
+}
+
+// Merge in a given visiting order. Visiting the node at position p merges the
+// segment of unit arcs to its left with the one to its right, each spanning
+// up to the nearest node on that side still unvisited (or the chain's end):
+// the chain's merge tree is the Cartesian tree of the visit times. One thread
+// starts at every unit arc; a segment belongs to whichever of its two
+// bounding nodes is visited first; a thread publishes its segment there, and
+// the second of the two sides to arrive combines them (the weighted average
+// of graph.cpp:1322-1324) and carries the merged segment on. The root (no
+// unvisited bound left) writes the chain's multiplicity to its first entry.
+__global__ void k_mg_cart(MergeArgs a, uint64_t total) {
+    const uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total) return;
+    const unsigned id = a.ent_chain[e];
+    if (id == kNone) return;
+    const uint64_t e0 = a.ch_eoff[id], m = a.ch_m[id];
+    uint64_t l = e - e0, r = l;  // the segment: unit arcs l..r
+    unsigned v = a.ent[e];
+    for (uint64_t step = 0; step <= m; ++step) {
+        const unsigned tl = l == 0 ? kNone : a.cart[e0 + l].t;      // node l bounds it on the left
+        const unsigned tr = r == m ? kNone : a.cart[e0 + r + 1].t;  // node r+1 on the right
+        if (tl == kNone && tr == kNone) {
+            a.ent[e0] = (unsigned char)v;
+            return;
+        }
+        const bool as_right = tl < tr;  // node l is visited first: this is its right side
+        const uint64_t p = as_right ? l : r + 1;
+        CartSlot *cs = a.cart + e0 + p;
+        if (as_right) {
+            cs->rv = (unsigned char)v;
+            cs->rb = (unsigned)r;
+        } else {
+            cs->lv = (unsigned char)v;
+            cs->lb = (unsigned)l;
+        }
+        __threadfence();
+        if (atomicAdd(&cs->arrive, 1u) == 0) return;  // the other side carries on
+        __threadfence();
+        volatile CartSlot *vs = cs;
+        const uint64_t L = as_right ? vs->lb : l, R = as_right ? r : vs->rb;
+        const unsigned vl = as_right ? vs->lv : v, vr = as_right ? v : vs->rv;
+        const uint64_t ll = p - L, lr = R - p + 1;
+        const uint64_t sum = (uint64_t)vl * ll + (uint64_t)vr * lr;
+        const int pre = (int)(unsigned)sum;
+        v = (unsigned)(unsigned char)((uint64_t)(int64_t)pre / (ll + lr));
+        l = L;
+        r = R;
+    }
+    atomicOr(a.err, kErrWalk);
+}
+
+// Visit times from a list of keys in visiting order: every node exactly once.
+__global__ void k_mg_vtime(MergeArgs a, const unsigned long long *__restrict__ order, uint64_t n_order) {
+    const uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_order) return;
+    const unsigned i = lookup(a, order[q]);
+    if (i == kNone || atomicCAS(&a.vt[i], ~0ull, (unsigned long long)q) != ~0ull) atomicOr(a.err, kErrOrder);
 }
 
 // ---- the gathered node lines (graph.cpp:615-645): id, per slot " " + arc + "#",
@@ -630,7 +715,8 @@ void merged_free(MergedGraph *m) {
 }
 
 swg_status merge_graph(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n, int k,
-                       cudaStream_t s, MergedGraph *mg, MergeResult *res) {
+                       cudaStream_t s, MergedGraph *mg, MergeResult *res, const unsigned long long *h_order,
+                       uint64_t n_order) {
     *res = MergeResult();
     if (n >= (1ull << 29)) {
         set_error("merge: more than 2^29 k-molecules");
@@ -667,6 +753,28 @@ swg_status merge_graph(const unsigned long long *d_keys, const unsigned long lon
     EMIT_CUDA(cudaMemsetAsync(a.oo, 0xff, 2 * n * sizeof(unsigned long long), s), "merge clear");
     int launches = 0;
     k_mg_index<<<blocks(n), 256, 0, s>>>(a);
+    if (h_order) {  // visit times from the caller's order
+        if (n_order != n) {
+            set_error("merge: the visiting order must list every k-molecule once");
+            return SWG_ERR_BAD_INPUT;
+        }
+        unsigned long long *d_order = nullptr;
+        if (!scr.get(&a.vt, n) || !scr.get(&d_order, n))
+            return cuda_err(cudaErrorMemoryAllocation, "visiting order");
+        EMIT_CUDA(cudaMemsetAsync(a.vt, 0xff, std::max<uint64_t>(n, 1) * sizeof(unsigned long long), s), "merge clear");
+        if (n)
+            EMIT_CUDA(cudaMemcpyAsync(d_order, h_order, n * sizeof(unsigned long long), cudaMemcpyHostToDevice, s),
+                      "visiting order");
+        k_mg_vtime<<<blocks(n), 256, 0, s>>>(a, d_order, n);
+        unsigned herr = 0;
+        EMIT_CUDA(cudaMemcpyAsync(&herr, a.err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "merge status");
+        EMIT_CUDA(cudaStreamSynchronize(s), "visiting order");
+        if (herr & kErrOrder) {
+            set_error("merge: the visiting order names a key twice or a key the graph does not hold");
+            return SWG_ERR_BAD_INPUT;
+        }
+        ++launches;
+    }
     k_mg_classify<<<blocks(n), 256, 0, s>>>(a);
     k_mg_states<<<blocks(n), 256, 0, s>>>(a);
     launches += 3;
@@ -743,14 +851,20 @@ swg_status merge_graph(const unsigned long long *d_keys, const unsigned long lon
         !scr.get(&a.ch_drev, n_chains) || !scr.get(&a.ent, total) || !scr.get(&a.ent_chain, total))
         return cuda_err(cudaErrorMemoryAllocation, "chain workspace");
     EMIT_CUDA(cudaMemsetAsync(a.ent_chain, 0xff, std::max<uint64_t>(total, 1) * sizeof(unsigned), s), "chain clear");
+    if (a.vt && !scr.get(&a.cart, total)) return cuda_err(cudaErrorMemoryAllocation, "merge tree");
     k_mg_chain_alloc<<<blocks(n), 256, 0, s>>>(a);
     k_mg_entries<<<blocks(n), 256, 0, s>>>(a);
     launches += 2;
-    for (int t = 0; t < top; ++t) {
-        const uint64_t pairs = total >> (t + 1);
-        if (!pairs) break;
-        k_mg_level<<<blocks(pairs), 256, 0, s>>>(a, pairs, t);
+    if (a.vt) {
+        if (total) k_mg_cart<<<blocks(total), 256, 0, s>>>(a, total);
         ++launches;
+    } else {
+        for (int t = 0; t < top; ++t) {
+            const uint64_t pairs = total >> (t + 1);
+            if (!pairs) break;
+            k_mg_level<<<blocks(pairs), 256, 0, s>>>(a, pairs, t);
+            ++launches;
+        }
     }
     // the nodes left, in key order
     const uint64_t n_lines = n - h[4] + h[3];
@@ -794,7 +908,12 @@ swg_status merge_graph(const unsigned long long *d_keys, const unsigned long lon
     launches += 3;
     EMIT_CUDA(cudaMemsetAsync(mg->text + bytes, '\n', 1, s), "merged text");
     EMIT_CUDA(cudaGetLastError(), "merge kernels");
+    EMIT_CUDA(cudaMemcpyAsync(&herr, a.err, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "merge status");
     EMIT_CUDA(cudaStreamSynchronize(s), "merge");
+    if (herr) {
+        set_error("merge: a merge tree did not end (internal error)");
+        return SWG_ERR_TIMEOUT;
+    }
     res->text_bytes = bytes + 1;
     mg->text_bytes = bytes + 1;
     mg->nodes = n_lines;

@@ -19,15 +19,37 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "swg_internal.h"
 
+// Allocator that leaves elements uninitialised on resize: the framing threads
+// write every element (the packed words after a parallel clear), so the
+// single-threaded zero fill of std::vector is skipped.
+template <typename T>
+struct NoInitAlloc : std::allocator<T> {
+    template <typename U>
+    struct rebind {
+        using other = NoInitAlloc<U>;
+    };
+    NoInitAlloc() = default;
+    template <typename U>
+    NoInitAlloc(const NoInitAlloc<U> &) {}
+    template <typename U>
+    void construct(U *) noexcept {}
+    template <typename U, typename... A>
+    void construct(U *p, A &&...a) {
+        ::new ((void *)p) U(std::forward<A>(a)...);
+    }
+};
+
 struct swg_reads {
-    std::vector<uint32_t> packed;
-    std::vector<uint64_t> off;
-    std::vector<uint32_t> len;
+    std::vector<uint32_t, NoInitAlloc<uint32_t>> packed;
+    std::vector<uint64_t, NoInitAlloc<uint64_t>> off;
+    std::vector<uint32_t, NoInitAlloc<uint32_t>> len;
     uint64_t n_bases = 0;
     uint64_t n_records = 0;
 };
@@ -55,10 +77,9 @@ struct ChunkStats {
 };
 
 // Pass 1 over the lines that start in [b, e): count them by parity.
-void count_chunk(const char *b, const char *e, const char *end, int k, ChunkStats &st) {
+void count_chunk(const char *b, const char *e, int k, ChunkStats &st) {
     const char *p = b;
     uint64_t line = 0;
-    (void)end;
     while (p < e) {
         // chunks end right after a '\n', so every line starting here ends here
         const char *nl = (const char *)std::memchr(p, '\n', (size_t)(e - p));
@@ -78,6 +99,30 @@ void count_chunk(const char *b, const char *e, const char *end, int k, ChunkStat
         if (!nl) break;
         p = nl + 1;
     }
+}
+
+// Eight sequence bytes (first base in the lowest byte) to their 2-bit codes,
+// first base in bits 15..14, with portable 64-bit arithmetic: a byte's code
+// is ((c >> 1) ^ (c >> 2)) & 3 for A/C/G/T in either case (A=0 C=1 G=2 T=3);
+// every other byte is read as A (kmerGraph.cpp:228-233).
+inline uint64_t bytes_equal(uint64_t v, uint64_t t) {  // 0x80 in each byte of v equal to t's
+    const uint64_t z = v ^ t;
+    return ~(((z & 0x7f7f7f7f7f7f7f7full) + 0x7f7f7f7f7f7f7f7full) | z | 0x7f7f7f7f7f7f7f7full);
+}
+inline uint32_t pack8(uint64_t x) {
+    const uint64_t lc = x | 0x2020202020202020ull;  // lower case (only the four letters count)
+    const uint64_t ok = bytes_equal(lc, 0x6161616161616161ull) | bytes_equal(lc, 0x6363636363636363ull) |
+                        bytes_equal(lc, 0x6767676767676767ull) | bytes_equal(lc, 0x7474747474747474ull);
+    const uint64_t y = ((x >> 1) ^ (x >> 2)) & ((ok >> 7) * 3);  // code i in bits 8i..8i+1
+    const uint64_t y2 = ((y & 0x0003000300030003ull) << 2) | ((y >> 8) & 0x0003000300030003ull);
+    const uint64_t y3 = ((y2 & 0x0000000f0000000full) << 4) | ((y2 >> 16) & 0x0000000f0000000full);
+    return (uint32_t)(((y3 & 0xffu) << 8) | ((y3 >> 32) & 0xffu));
+}
+inline uint32_t pack16(const char *p) {
+    uint64_t a, b;
+    std::memcpy(&a, p, 8);
+    std::memcpy(&b, p + 8, 8);
+    return (pack8(a) << 16) | pack8(b);
 }
 
 inline void put_word(uint32_t *w, uint64_t idx, uint32_t val, bool shared) {
@@ -106,7 +151,8 @@ void pack_chunk(const char *b, const char *e, int parity, int k, uint64_t read0,
             uint64_t widx = base >> 4;
             uint32_t acc = 0;
             int fill = (int)(base & 15);
-            for (uint64_t i = 0; i < L; i++) {
+            uint64_t i = 0;
+            for (; i < L && fill; i++) {  // up to the read's first whole word
                 acc |= (uint32_t)kCodes.v[(unsigned char)p[i]] << (30 - 2 * fill);
                 if (++fill == 16) {
                     put_word(words, widx, acc, widx == first_word || widx == last_word);
@@ -114,6 +160,12 @@ void pack_chunk(const char *b, const char *e, int parity, int k, uint64_t read0,
                     acc = 0;
                     fill = 0;
                 }
+            }
+            for (; i + 16 <= L; i += 16, widx++)  // whole words, 16 bases at a time
+                put_word(words, widx, pack16(p + i), widx == first_word || widx == last_word);
+            for (; i < L; i++) {
+                acc |= (uint32_t)kCodes.v[(unsigned char)p[i]] << (30 - 2 * fill);
+                fill++;
             }
             if (fill) put_word(words, widx, acc, widx == first_word || widx == last_word);
             base += L;
@@ -165,7 +217,7 @@ swg_status pack_fasta(const char *text, uint64_t len, int k, swg_reads **out) {
         for (int t = 0; t < nt; t++)
             th.emplace_back([&, t] {
                 has_nul[t] = std::memchr(cs[t], 0, (size_t)(cs[t + 1] - cs[t])) != nullptr;
-                count_chunk(cs[t], cs[t + 1], end, k, st[t]);
+                count_chunk(cs[t], cs[t + 1], k, st[t]);
             });
         for (auto &x : th) x.join();
     }
@@ -196,14 +248,24 @@ swg_status pack_fasta(const char *text, uint64_t len, int k, swg_reads **out) {
         r->n_records = nrec;
         r->off.resize(read0[nt]);
         r->len.resize(read0[nt]);
-        r->packed.assign((r->n_bases + 15) / 16 + 4, 0u);  // 4 words of tail padding
+        r->packed.resize((r->n_bases + 15) / 16 + 4);  // 4 words of tail padding
     } catch (...) {
         delete r;
         set_error("host allocation failed while packing reads");
         return SWG_ERR_OOM;
     }
     {
+        // every thread clears a share of the words, then (after all have)
+        // packs its chunk: chunks share their boundary words
+        const uint64_t nw = r->packed.size();
         std::vector<std::thread> th;
+        for (int t = 0; t < nt; t++)
+            th.emplace_back([&, t] {
+                const uint64_t w0 = nw * (uint64_t)t / (uint64_t)nt, w1 = nw * (uint64_t)(t + 1) / (uint64_t)nt;
+                std::memset(r->packed.data() + w0, 0, (size_t)(w1 - w0) * sizeof(uint32_t));
+            });
+        for (auto &x : th) x.join();
+        th.clear();
         for (int t = 0; t < nt; t++)
             th.emplace_back([&, t] {
                 pack_chunk(cs[t], cs[t + 1], parity[t], k, read0[t], base0[t], base0[t + 1], r);

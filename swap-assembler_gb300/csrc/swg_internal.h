@@ -184,6 +184,7 @@ int launch_group_by_sample(const unsigned long long *in_keys, const unsigned lon
                            uint64_t n, int tag_bits, uint32_t n_samples, unsigned long long *cursor,
                            unsigned long long *out_keys, unsigned long long *out_mult, cudaStream_t s);
 cudaError_t run_probe(int kind, uint64_t table_bytes, uint64_t n_ops, cudaStream_t s, float *ms);
+cudaError_t run_smem_probe(int kind, uint64_t n_ops, cudaStream_t s, float *ms);
 int device_sm_count();
 
 // Thread-local error message (api.cpp).
@@ -228,8 +229,10 @@ struct MergeResult {
     uint64_t text_bytes = 0, nodes = 0, chains = 0, cycles = 0, rulers = 0;
     int launches = 0;
 };
+// h_order: if set, the n keys in the order the merge visits them (host memory)
 swg_status merge_graph(const unsigned long long *d_keys, const unsigned long long *d_mult, uint64_t n, int k,
-                       cudaStream_t s, MergedGraph *mg, MergeResult *res);
+                       cudaStream_t s, MergedGraph *mg, MergeResult *res,
+                       const unsigned long long *h_order = nullptr, uint64_t n_order = 0);
 // masterTipsRemoval / masterLowCoverageEdgeRemoval on the merged graph
 // (prune.cu); the text is rewritten. *count = tips removed / arcs cut.
 swg_status prune_tips(MergedGraph *mg, cudaStream_t s, uint64_t *count);

@@ -126,6 +126,7 @@ def lib() -> C.CDLL:
             "swg_build": (i32, [C.POINTER(Opts), P, u64, P, P, u64, C.POINTER(P)]),
             "swg_build_fasta": (i32, [C.POINTER(Opts), C.c_char_p, u64, C.POINTER(P)]),
             "swg_graph_build_fasta": (i32, [P, C.POINTER(Opts), P, u64]),
+            "swg_graph_build_fasta_file": (i32, [P, C.POINTER(Opts), C.c_char_p]),
             "swg_graph_size": (i32, [P, pu64]),
             "swg_graph_distinct": (i32, [P, pu64]),
             "swg_graph_device_view": (i32, [P, C.POINTER(P), C.POINTER(P), pu64]),
@@ -134,6 +135,7 @@ def lib() -> C.CDLL:
             "swg_graph_write_kmer_graph": (i32, [P, C.c_char_p]),
             "swg_graph_write_node_lines": (i32, [P, C.c_char_p]),
             "swg_graph_merge": (i32, [P]),
+            "swg_graph_merge_in_order": (i32, [P, P, u64]),
             "swg_graph_merge_info": (i32, [P, C.POINTER(MergeInfo)]),
             "swg_graph_write_merged": (i32, [P, C.c_char_p]),
             "swg_graph_copy_merged": (i32, [P, P, u64, pu64]),
@@ -146,6 +148,7 @@ def lib() -> C.CDLL:
             "swg_graph_last_timings": (i32, [P, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
             "swg_graph_build_info": (i32, [P, C.POINTER(BuildInfo)]),
             "swg_probe_random_access": (i32, [i32, u64, u64, P, C.POINTER(C.c_double)]),
+            "swg_probe_shared_atomics": (i32, [i32, u64, P, C.POINTER(C.c_double)]),
             "swg_batch_build": (i32, [P, C.POINTER(Opts), C.POINTER(Sample), C.c_uint32]),
             "swg_batch_samples": (i32, [P, C.POINTER(C.c_uint32)]),
             "swg_batch_sample_info": (i32, [P, C.c_uint32, pu64, pu64, pu64]),
@@ -307,6 +310,13 @@ class Graph:
         _check(lib().swg_graph_merge(self._h), "swg_graph_merge")
         return self
 
+    def merge_in_order(self, order_keys: np.ndarray) -> "Graph":
+        """The merge with the nodes visited in the given order (every key of the
+        built graph once)."""
+        ok = np.ascontiguousarray(order_keys, dtype=np.uint64)
+        _check(lib().swg_graph_merge_in_order(self._h, _ptr(ok), ok.size), "swg_graph_merge_in_order")
+        return self
+
     def merge_info(self) -> dict:
         info = MergeInfo()
         _check(lib().swg_graph_merge_info(self._h, C.byref(info)), "swg_graph_merge_info")
@@ -357,6 +367,12 @@ class Graph:
             buf = C.create_string_buffer(text, len(text))
             addr, n = C.addressof(buf), len(text)
         _check(lib().swg_graph_build_fasta(self._h, C.byref(opts), addr, n), "swg_graph_build_fasta")
+        return self
+
+    def build_fasta_file(self, opts: Opts, path: str) -> "Graph":
+        """Build from a FASTA file (read into a pinned buffer, framed on the device)."""
+        _check(lib().swg_graph_build_fasta_file(self._h, C.byref(opts), str(path).encode()),
+               "swg_graph_build_fasta_file")
         return self
 
     def build_batch(self, opts: Opts, samples: list) -> "Graph":
@@ -424,6 +440,14 @@ def records_write_node_lines(keys: np.ndarray, mult: np.ndarray, path: str) -> N
 
 PROBE_KINDS = {"red_add_u32": 0, "atom_add_u64": 1, "cas128": 2, "load16": 3, "load16_cas128": 4,
                "load16_x4": 5, "load16_cas128_x2": 6}
+
+
+def probe_shared_atomics(kind: str, n_ops: int, stream: int | None = None) -> float:
+    """Lane operations per second of random shared-memory atomics (whole GPU)."""
+    out = C.c_double()
+    _check(lib().swg_probe_shared_atomics({"add_u32": 0, "cas_u64": 1}[kind], n_ops, stream, C.byref(out)),
+           "swg_probe_shared_atomics")
+    return out.value
 
 
 def probe_random_access(kind: str, table_bytes: int, n_ops: int, stream: int | None = None) -> float:

@@ -260,3 +260,77 @@ def test_contigs_match_oracle(case, tmp_path):
         assert oracle.contig_sequences(p) == oracle.contigs_of_lines(g.merged_text(), k)
         g.remove_tips()
         g.simplify()
+
+
+# ---- merge in a given visiting order (swg_graph_merge_in_order) ----------
+GOLDEN = ROOT / "tests" / "golden"
+
+
+def _ordered(text: bytes, k: int, c: int, order):
+    """GPU merge visiting the nodes in `order` (indices of the key-sorted
+    k-molecules) and the restatement in the same order, every message
+    applied as it is sent (MERGE_TIMING_IMMEDIATE)."""
+    import numpy as np
+    keys, mult = oracle.records(text, k, c)
+    g = swapgb.Graph()
+    g.build_fasta(swapgb.Opts(k=k, cutoff=c), text)
+    g.merge_in_order(keys[np.asarray(order, dtype=np.int64)])
+    want = oracle.merge_text(keys, mult, k, order=order, timing=oracle.MERGE_TIMING_IMMEDIATE)
+    return g.merged_text(), want, g.merge_info()
+
+
+@pytest.mark.parametrize("case", MERGE_CASES, ids=lambda c: c["name"])
+def test_merge_in_the_reference_order(case):
+    """The reference's own visiting order of each merge fixture (its node
+    map's iteration order, stored by tests/golden/make_merge_golden.py from
+    the reference's run): the GPU merge equals the restatement replaying that
+    order line for line, multiplicities included (graph.cpp:1392-1566,
+    averaging at 1322-1324)."""
+    import numpy as np
+    order = np.load(GOLDEN / (case["name"] + ".order.npy")).astype(np.uint64)
+    got, want, info = _ordered(case_text(case), case["k"], case["c"], order)
+    assert len(got) == len(want) == info["text_bytes"]
+    assert _lines(got) == _lines(want)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_merge_in_random_orders(seed):
+    """Random visiting orders on a graph of a few long chains and on the
+    1 Mbp workload's graph (deep and shallow merge trees, cycles)."""
+    import numpy as np
+    for text, k, c in ((swapgb.synth_fasta(seed=77, genome_len=100_000, n_reads=50_000, read_len=100,
+                                           sub_rate=0.0), 31, 3),
+                       (case_text(next(x for x in SYNTH_CASES if x["name"] == "c1_small")), 21, 2)):
+        n = oracle.records(text, k, c)[0].size
+        order = np.random.default_rng(seed).permutation(n).astype(np.uint64)
+        got, want, _ = _ordered(text, k, c, order)
+        assert _lines(got) == _lines(want)
+
+
+def test_merge_in_the_fixed_order_equals_merge():
+    """Given the fixed tree order itself, the ordered merge reproduces
+    swg_graph_merge byte for byte."""
+    case = MERGE_CASES[2]
+    text, k, c = case_text(case), case["k"], case["c"]
+    keys, mult = oracle.records(text, k, c)
+    order = oracle.merge_tree_order(keys, mult, k)
+    a, _ = _gpu_merge(text, k, c)
+    g = swapgb.Graph()
+    g.build_fasta(swapgb.Opts(k=k, cutoff=c), text)
+    g.merge_in_order(keys[order.astype("int64")])
+    assert g.merged_text() == a
+
+
+def test_merge_in_order_rejects_bad_orders():
+    import numpy as np
+    case = MERGE_CASES[1]
+    text, k, c = case_text(case), case["k"], case["c"]
+    keys, _ = oracle.records(text, k, c)
+    g = swapgb.Graph()
+    g.build_fasta(swapgb.Opts(k=k, cutoff=c), text)
+    bad = [keys[:-1], np.concatenate([keys[:-1], keys[:1]]), np.concatenate([keys[:-1], [np.uint64(1)]])]
+    for order in bad:  # a key missing, a key twice, a key the graph does not hold
+        with pytest.raises(swapgb.SwgError) as e:
+            g.merge_in_order(order)
+        assert e.value.status == 1
+    g.merge_in_order(keys[::-1].copy())  # and a good one still works on the same handle

@@ -169,6 +169,23 @@ def test_build_fasta_entry_point():
     assert_same_records(g, text, 19, 1)
 
 
+@pytest.mark.parametrize("case", ["orient_k19", "crlf_k19", "multiline_k19", "saturate_k21"])
+def test_build_fasta_file_entry_point(case, tmp_path):
+    c = kat(case)
+    fa = tmp_path / "in.fa"
+    fa.write_bytes(kat_text(case))
+    g = swapgb.Graph()
+    for _ in range(2):  # the second call reuses the handle's pinned buffer
+        g.build_fasta_file(swapgb.Opts(k=c["k"], cutoff=c["c"]), fa)
+        g.write_kmer_graph(tmp_path / "kg.txt")
+        g.write_node_lines(tmp_path / "nodes.txt")
+        assert sha_lines(sorted_lines(tmp_path / "kg.txt")) == c["kmer_graph_sha256"]
+        assert sha_lines(sorted_lines(tmp_path / "nodes.txt")) == c["nodes_sha256"]
+    with pytest.raises(swapgb.SwgError) as e:
+        g.build_fasta_file(swapgb.Opts(k=c["k"], cutoff=c["c"]), tmp_path / "missing.fa")
+    assert e.value.status == 9  # SWG_ERR_IO
+
+
 def test_cli_matches_reference(tmp_path):
     import subprocess
     c = kat("orient_k31_c3")

@@ -33,7 +33,8 @@ int main(int argc, char *argv[]) {
     parameter parameters;
     parameters.getParameters(argc, argv, &MPIcontrol);
     distNodeGraph *nodeGraph = new distNodeGraph(&parameters, &MPIcontrol);
-    gpuConstructAndCutoff(nodeGraph, &parameters);
+    if (getenv("SWG_HOST_FRAMING")) gpuConstructAndCutoffHostFraming(nodeGraph, &parameters);
+    else gpuConstructAndCutoff(nodeGraph, &parameters);
     nodeGraph->buildKmoleculeGraph(&MPIcontrol, &parameters);
     nodeGraph->graphStatistics(&parameters, &MPIcontrol);
     strcpy(parameters.kmerGraph, parameters.outputPath);
@@ -45,10 +46,14 @@ int main(int argc, char *argv[]) {
 '''
 
 
-def binding_block() -> str:
+def binding_blocks() -> str:
+    """Both bindings INTEGRATION.md shows: device framing from the file (the
+    one main calls) and host framing."""
     text = (ROOT / "INTEGRATION.md").read_text()
     blocks = re.findall(r"```cpp\n(.*?)```", text, flags=re.S)
-    return next(b for b in blocks if "static void gpuConstructAndCutoff" in b)
+    got = [b for b in blocks if "static void gpuConstructAndCutoff" in b]
+    assert len(got) == 2, "expected the device- and host-framing bindings"
+    return "\n".join(got)
 
 
 @pytest.fixture(scope="module")
@@ -63,7 +68,7 @@ def ref_dir() -> Path:
 
 def test_binding_compiles_and_links(ref_dir, tmp_path):
     src = tmp_path / "binding.cpp"
-    src.write_text(DRIVER % binding_block())
+    src.write_text(DRIVER % binding_blocks())
     objs = [ORACLE / "_ref" / n for n in ("kmerGraph.o", "sequence.o", "mympi.o", "mpi_shim.o")]
     for o in objs:
         assert o.exists(), o
