@@ -809,25 +809,29 @@ __device__ __forceinline__ uint32_t walk_next(const BuildArgs &a, ReadWalk &st) 
     return b;
 }
 
+// KC: k fixed at compile time (a single-sample build with that k), so the
+// shifts and masks of the rolling update are constants; 0: k read at run time.
+template <int KC = 0>
 __device__ __forceinline__ void walk_init(const BuildArgs &a, ReadWalk &st, uint64_t r) {
     const uint32_t seg = seg_of(a, r);
-    st.k = k_of(a, seg);
+    st.k = KC ? KC : k_of(a, seg);
     st.tag = a.tag_bits ? (uint64_t)seg << (64 - a.tag_bits) : 0ull;
     st.L = a.read_len[r];
     st.left = st.L >= (uint32_t)st.k ? st.L - (uint32_t)st.k + 1 : 0;
     if (!st.left) return;
     st.kmask = (1ull << (2 * st.k)) - 1;
     st.top = 2 * (st.k - 1);
+    const int top = KC ? 2 * (KC - 1) : st.top;
     const uint64_t g0 = a.read_off[r];
     st.wnext = (g0 >> 4) + 1;
     st.w = ldw(a.packed, g0 >> 4, a.n_words) << (2 * (uint32_t)(g0 & 15));
     st.wn = ldw(a.packed, st.wnext, a.n_words);
     st.wrem = 16 - (uint32_t)(g0 & 15);
     st.fwd = st.rc = 0;
-    for (int i = 0; i < st.k; ++i) {
+    for (int i = 0; i < (KC ? KC : st.k); ++i) {
         const uint32_t b = walk_next(a, st);
         st.fwd = (st.fwd << 2) | b;
-        st.rc = (st.rc >> 2) | ((uint64_t)(3u - b) << st.top);
+        st.rc = (st.rc >> 2) | ((uint64_t)(3u - b) << top);
     }
     st.p = 0;
     st.lb = 0;
@@ -838,18 +842,22 @@ __device__ __forceinline__ void walk_init(const BuildArgs &a, ReadWalk &st, uint
 // Arc slots as make_occ (kmerGraph.cpp:240-296): right (f ? 0 : 4) +
 // base[p+k], left (f ? 4 : 0) + 3 - base[p-1], f = (forward k-mer is the
 // canonical one).
+template <int KC = 0>
 __device__ __forceinline__ void walk_emit(const BuildArgs &a, ReadWalk &st, uint64_t &key,
                                           unsigned &code) {
+    const int top = KC ? 2 * (KC - 1) : st.top;
+    const uint64_t kmask = KC ? (1ull << (2 * KC)) - 1 : st.kmask;
     const bool f = st.fwd >= st.rc;
-    key = (f ? st.fwd : st.rc) | st.tag;
+    key = (f ? st.fwd : st.rc);
+    if (!KC) key |= st.tag;  // KC is used for single-sample builds only
     code = 0;
     if (st.left > 1) code = 0x08u | ((f ? 0u : 4u) + st.nb);  // p + k < L
     if (st.p) code |= 0x80u | (((f ? 4u : 0u) + 3u - st.lb) << 4);
     if (--st.left) {
         const uint32_t b = st.nb;
-        st.lb = (uint32_t)(st.fwd >> st.top);
-        st.fwd = ((st.fwd << 2) | b) & st.kmask;
-        st.rc = (st.rc >> 2) | ((uint64_t)(3u - b) << st.top);
+        st.lb = (uint32_t)(st.fwd >> top);
+        st.fwd = ((st.fwd << 2) | b) & kmask;
+        st.rc = (st.rc >> 2) | ((uint64_t)(3u - b) << top);
         ++st.p;
         if (st.left > 1) st.nb = walk_next(a, st);
     }
@@ -960,7 +968,7 @@ __global__ void k_bucket_caps(const unsigned long long *counts, const unsigned l
 // kK1Items records of its read into registers, taking its rank within the
 // partition from the shared histogram; the block orders the round's records
 // by partition in shared memory and writes one run per partition.
-template <int NT, int IT, int MINB>
+template <int NT, int IT, int MINB, int KC = 0, int B1C = 0>
 __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs pa) {
     extern __shared__ __align__(16) unsigned char dyn[];
     unsigned long long *sorted = reinterpret_cast<unsigned long long *>(dyn);
@@ -969,8 +977,10 @@ __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs p
     unsigned *loff = hist + pa.n_parts;
     unsigned short *spart = reinterpret_cast<unsigned short *>(loff + pa.n_parts);
     __shared__ uint64_t wb[NT / 32];
-    const int shift = 64 - pa.bits;
-    const uint32_t per = (pa.n_parts + blockDim.x - 1) / blockDim.x;
+    const int bits = B1C ? B1C : pa.bits;
+    const int shift = 64 - bits;
+    const uint32_t n_parts = B1C ? (1u << B1C) : pa.n_parts;
+    const uint32_t per = (n_parts + blockDim.x - 1) / blockDim.x;
     __shared__ unsigned long long s_base;
     for (;;) {  // batches of NT reads, handed out as blocks finish them
         if (threadIdx.x == 0) s_base = atomicAdd(&pa.work[1], (unsigned long long)NT);
@@ -980,9 +990,9 @@ __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs p
         const uint64_t r = base + threadIdx.x;
         ReadWalk st;
         st.left = 0;
-        if (r < a.n_reads) walk_init(a, st, r);
+        if (r < a.n_reads) walk_init<KC>(a, st, r);
         while (__syncthreads_or(st.left != 0)) {
-            for (uint32_t j = threadIdx.x; j < pa.n_parts; j += blockDim.x) hist[j] = 0;
+            for (uint32_t j = threadIdx.x; j < n_parts; j += blockDim.x) hist[j] = 0;
             __syncthreads();
             unsigned long long rec[IT];
             unsigned pr[IT];  // partition | rank << 16; ~0 for no record
@@ -993,10 +1003,10 @@ __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs p
                 if (st.left) {
                     uint64_t key;
                     unsigned code;
-                    walk_emit(a, st, key, code);
+                    walk_emit<KC>(a, st, key, code);
                     const uint64_t h = rmix64(key);
                     const unsigned part = (unsigned)(h >> shift);
-                    rec[j] = ((h << pa.bits) >> (pa.bits - 8)) | code;  // low 64-b1 bits << 8
+                    rec[j] = ((h << bits) >> (bits - 8)) | code;  // low 64-b1 bits << 8
                     pr[j] = part | (atomicAdd(&hist[part], 1u) << 16);
                 }
             }
@@ -1004,13 +1014,13 @@ __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs p
             uint64_t mine = 0;
             for (uint32_t x = 0; x < per; ++x) {
                 const uint32_t j = threadIdx.x * per + x;
-                if (j < pa.n_parts) mine += hist[j];
+                if (j < n_parts) mine += hist[j];
             }
             uint64_t total;
             uint64_t run = block_exclusive_scan<NT>(mine, wb, &total);
             for (uint32_t x = 0; x < per; ++x) {
                 const uint32_t j = threadIdx.x * per + x;
-                if (j < pa.n_parts) {
+                if (j < n_parts) {
                     const unsigned c = hist[j];
                     loff[j] = (unsigned)run;
                     BinDest d;
@@ -2175,9 +2185,9 @@ int scatter_shape() {
     return shape;
 }
 
-template <int NT, int IT, int MINB>
+template <int NT, int IT, int MINB, int KC = 0, int B1C = 0>
 int launch_p1_scatter_shape(const BuildArgs &a, const PartArgs &p, cudaStream_t s, bool persistent) {
-    auto kern = k_p1_scatter<NT, IT, MINB>;
+    auto kern = k_p1_scatter<NT, IT, MINB, KC, B1C>;
     const size_t smem = p1_scatter_smem(p.n_parts, NT * IT);
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const uint64_t batches = (a.n_reads + NT - 1) / NT;
@@ -2191,7 +2201,19 @@ int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s, b
     switch (scatter_shape()) {
         case 1: return launch_p1_scatter_shape<512, 8, 2>(a, p, s, persistent);
         case 2: return launch_p1_scatter_shape<256, 8, 4>(a, p, s, persistent);
-        default: return launch_p1_scatter_shape<256, 16, 3>(a, p, s, persistent);
+        default:
+            // single-sample builds with 256 partitions and a common k: the walk's
+            // shifts and masks and the record layout are compile-time constants
+            if (!a.segs && !a.read_seg && !a.tag_bits && p.bits == 8) switch (a.k) {
+                    case 31: return launch_p1_scatter_shape<256, 16, 3, 31, 8>(a, p, s, persistent);
+                    case 27: return launch_p1_scatter_shape<256, 16, 3, 27, 8>(a, p, s, persistent);
+                    case 25: return launch_p1_scatter_shape<256, 16, 3, 25, 8>(a, p, s, persistent);
+                    case 21: return launch_p1_scatter_shape<256, 16, 3, 21, 8>(a, p, s, persistent);
+                    default: break;
+                }
+            if (!a.segs && !a.read_seg && !a.tag_bits && p.bits == 9 && a.k == 31)  // past 400M occurrences
+                return launch_p1_scatter_shape<256, 16, 3, 31, 9>(a, p, s, persistent);
+            return launch_p1_scatter_shape<256, 16, 3>(a, p, s, persistent);
     }
 }
 
