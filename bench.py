@@ -313,6 +313,40 @@ def batched_metrics(stream_ptr: int, repeats: int = 3) -> dict:
         kp, mp = plain.copy_out(sorted=True)
         kb, mb = batch.batch_copy_out(i)
         same += bool(np.array_equal(kp, kb) and np.array_equal(mp, mb))
+    # the autotuner over the bucketed knobs, on two samples of each read length
+    # built as one sample with the batch's k (its choice then runs the batch)
+    pick = []
+    for L in (75, 100, 150, 250):
+        pick += [i for i, p in enumerate(specs) if p["read_len"] == L][:2]
+    words = np.concatenate([reads[i].packed for i in pick])
+    shift = np.cumsum([0] + [reads[i].n_words * 16 for i in pick[:-1]]).astype(np.uint64)
+    offs = np.concatenate([reads[i].off + shift[j] for j, i in enumerate(pick)])
+    lens = np.concatenate([reads[i].len for i in pick])
+    d_w = torch.from_numpy(words.view(np.int32)).cuda()
+    d_o = torch.from_numpy(offs.view(np.int64)).cuda()
+    d_l = torch.from_numpy(lens.view(np.int32)).cuda()
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        best = swapgb.autotune(swapgb.Opts(k=27, cutoff=3, stream=stream_ptr), d_w.data_ptr(), d_w.numel(),
+                               d_o.data_ptr(), d_l.data_ptr(), d_o.numel(), 150, os.path.join(td, "tune.jsonl"))
+    tuned = swapgb.Opts(k=27, cutoff=3, stream=stream_ptr)
+    if best["algorithm"] == swapgb.ALGO_BUCKETED:
+        tuned.bucket_records, tuned.part_bits = best["bucket_records"], best["part_bits"]
+        tuned.scatter_shape = best["scatter_shape"]
+    batch.build_batch(tuned, samples)
+    torch.cuda.synchronize()
+    t_tuned = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        batch.build_batch(tuned, samples)
+        torch.cuda.synchronize()
+        t_tuned.append(time.perf_counter() - t0)
+    tuned_same = 0
+    for i in range(len(reads)):
+        kb, mb = batch.batch_copy_out(i)
+        plain.build_reads(opts, reads[i])
+        kp, mp = plain.copy_out(sorted=True)
+        tuned_same += bool(np.array_equal(kp, kb) and np.array_equal(mp, mb))
     tp, tb = min(t_plain), min(t_batch)
     return {"workload": "256 samples, genome log-uniform 50 kbp-2 Mbp, reads 75/100/150/250 bp, "
                         "10-60x, 0.1-1% subs, k=27 c=3 (seeded synthetic)",
@@ -323,6 +357,10 @@ def batched_metrics(stream_ptr: int, repeats: int = 3) -> dict:
             "device_ms_plain_sum": min(dev_plain), "device_ms_batched": min(dev_batch),
             "batched_algorithm": {1: "direct", 2: "partitioned", 3: "bucketed"}[batch.info()["algorithm"]],
             "samples_identical": "%d/%d" % (same, len(reads)),
+            "autotune": {"picked": best, "on": "2 samples of each read length built as one sample (k=27, c=3)",
+                         "batched_s": min(t_tuned), "batched_samples_per_s": len(reads) / min(t_tuned),
+                         "speedup": tp / min(t_tuned),
+                         "samples_identical": "%d/%d" % (tuned_same, len(reads))},
             "identical_means": "the sample's sorted k-molecules and 8 multiplicities equal its own plain "
                                "build's, bit for bit",
             "path": "pinned host packed reads -> device-resident graphs; plain = swg_graph_build "

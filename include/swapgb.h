@@ -92,6 +92,16 @@ typedef struct swg_opts {
     void *stream;               /* cudaStream_t; NULL = the library's own stream */
     int algorithm;              /* SWG_ALGO_*; 0 = default */
     int read_order;             /* direct: SWG_ORDER_*; 0 = input order */
+    /* Bucketed build knobs (0 = the default; swg_autotune picks them per k and
+     * read-length band): target records per bucket (64..65535), level-1
+     * partition bits (8..10; more are used when the buckets would otherwise
+     * pass twice the target), block shape of the two scatter passes (the
+     * default is 256 threads x 16 records each; 1 = 512 x 8 for both, 2 =
+     * 256 x 8 for level 1 and 512 x 8 for level 2, 3 = level 2 staged by
+     * bulk copies). */
+    uint32_t bucket_records;
+    int part_bits;
+    int scatter_shape;
 } swg_opts;
 
 /* What the last build did (for measurement and tests). */
@@ -179,7 +189,8 @@ swg_status swg_graph_build_fasta_file(swg_graph *g, const swg_opts *o, const cha
 swg_status swg_build(const swg_opts *o, const uint32_t *packed, uint64_t n_words,
                      const uint64_t *read_off, const uint32_t *read_len, uint64_t n_reads,
                      swg_graph **out);
-/* Convenience: frame + pack a FASTA held in host memory, then build. */
+/* Convenience: create a handle and build from a FASTA text in host memory
+ * (swg_graph_build_fasta: framed and packed on the device). */
 swg_status swg_build_fasta(const swg_opts *o, const char *text, uint64_t len, swg_graph **out);
 
 /* ---- batched build ---------------------------------------------------- */
@@ -195,11 +206,15 @@ typedef struct swg_sample {
     int cutoff;
 } swg_sample;
 
-/* Build many independent samples at once: their reads are copied into one
- * device stream, every kernel runs once over all samples, each sample counts
- * into its own partition of one shared table and gets its own output region.
- * Each sample's result equals a plain build of that sample alone. Uses the
- * direct algorithm; opts->k and opts->cutoff are ignored (per sample). */
+/* Build many independent samples at once: their reads (host or device
+ * memory) are copied into one device stream and every kernel runs once over
+ * all samples. By default (2 * largest k + ceil(log2 samples) <= 64, at most
+ * 1024 samples) every key carries its sample's index in its top bits and one
+ * bucketed build counts all samples, each bucket applying each key's own
+ * sample cutoff; otherwise each sample counts into its own partition of one
+ * direct table. Each sample gets its own output region, and its result equals
+ * a plain build of that sample alone. opts->k and opts->cutoff are ignored
+ * (each sample has its own). */
 swg_status swg_batch_build(swg_graph *g, const swg_opts *o, const swg_sample *samples,
                            uint32_t n_samples);
 swg_status swg_batch_samples(const swg_graph *g, uint32_t *n_samples);
@@ -240,7 +255,9 @@ typedef struct swg_server_stats {
 #define SWG_REQ_FAILED 3
 
 swg_status swg_server_create(const swg_server_opts *o, swg_server **out);
-/* Copies the request's reads; the caller may free them on return. If no
+/* Uploads the request's reads to device memory (they wait there until a
+ * worker builds them); the caller may free its buffers on return. SWG_ERR_OOM
+ * if the device cannot hold them. If no
  * worker could set itself up (graph handle or stream creation failed), queued
  * requests fail with that reason and submit returns SWG_ERR_BAD_STATE. */
 swg_status swg_server_submit(swg_server *srv, const swg_sample *req, uint64_t *ticket);
@@ -397,22 +414,28 @@ swg_status swg_build_device_noalloc(const swg_opts *o, const uint32_t *d_packed,
 
 /* ---- autotuner ---------------------------------------------------------- */
 /* Times trial builds of a sample (device packed reads, as for
- * swg_graph_build_device) for each candidate table load factor and counting
- * scheme (direct table in input order, direct table in minimizer order,
- * hash-partitioned slices) and appends the fastest to a cache file as one
- * JSON line keyed by (k, read-length band of read_len_hint). */
+ * swg_graph_build_device) for each candidate: the bucketed build (the default
+ * scheme) with records per bucket 2048 / 4096 / 8192 and each scatter block
+ * shape (the level-1 partition count follows the input's size); the direct table at load factors
+ * 0.5-0.8, in input and in minimizer order; hash-partitioned slices. Appends
+ * the fastest to a cache file as one JSON line keyed by (k, read-length band
+ * of read_len_hint). */
 typedef struct swg_tuning {
     double load_factor;
     int algorithm;
     int read_order;
     float ms;
+    uint32_t bucket_records; /* bucketed knobs, as in swg_opts (0 = default) */
+    int part_bits;
+    int scatter_shape;
 } swg_tuning;
 
 swg_status swg_autotune(const swg_opts *base, const uint32_t *d_packed, uint64_t n_words,
                         const uint64_t *d_read_off, const uint32_t *d_read_len, uint64_t n_reads,
                         uint32_t read_len_hint, const char *cache_path, swg_tuning *best);
-/* Sets o's load factor, algorithm and read order from the cache entry for
- * (k, band of read_len); SWG_ERR_NOT_READY when the cache has none. */
+/* Sets o's load factor, algorithm, read order and bucketed knobs from the
+ * cache entry for (k, band of read_len); SWG_ERR_NOT_READY when the cache has
+ * none. */
 swg_status swg_autotune_apply(const char *cache_path, int k, uint32_t read_len, swg_opts *o);
 
 /* ---- roofline probe ----------------------------------------------------- */

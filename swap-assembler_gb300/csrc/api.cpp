@@ -229,6 +229,12 @@ swg_status check_opts(const swg_opts *o) {
         swg::set_error("load_factor must be in (0, 0.9] (0 = default)");
         return SWG_ERR_BAD_INPUT;
     }
+    if (o->bucket_records > 65535 || (o->part_bits && (o->part_bits < 8 || o->part_bits > 10)) ||
+        o->scatter_shape < 0 || o->scatter_shape > 3) {
+        swg::set_error("bucketed knobs out of range (records per bucket <= 65535, partition bits 8..10, "
+                       "scatter shape 0..3)");
+        return SWG_ERR_BAD_INPUT;
+    }
     return SWG_OK;
 }
 
@@ -476,7 +482,8 @@ swg_status build_partitioned(swg_graph *g, const swg_opts *o, BuildArgs &a, cuda
     std::memset(&pa, 0, sizeof(pa));
     pa.bits = bits;
     pa.n_parts = 1u << bits;
-    pa.work = g->d_ctl->work;  // zeroed with the control block at the start of the build
+    pa.work = g->d_ctl->work;
+    pa.shape = o ? o->scatter_shape : 0;  // zeroed with the control block at the start of the build
     pa.load_num = 3;  // slice capacity = count / 0.6 + 16
     pa.load_den = 5;
     if (load != 0.6) {
@@ -694,14 +701,15 @@ swg_status batch_impl(swg_graph *g, const swg_opts *o, const swg_sample *sm, uin
     SWG_CUDA(cudaEventRecord(g->ev[0], s), "event");
     uint64_t wofs = 0, rofs = 0;
     for (uint32_t i = 0; i < S; i++) {
+        // host or device memory (the request server passes device copies)
         if (sm[i].n_words)
-            SWG_CUDA(cudaMemcpyAsync(g->d_packed + wofs, sm[i].packed, sm[i].n_words * 4,
-                                     cudaMemcpyHostToDevice, s), "copy packed reads");
+            SWG_CUDA(cudaMemcpyAsync(g->d_packed + wofs, sm[i].packed, sm[i].n_words * 4, cudaMemcpyDefault, s),
+                     "copy packed reads");
         if (sm[i].n_reads) {
-            SWG_CUDA(cudaMemcpyAsync(g->d_off + rofs, sm[i].read_off, sm[i].n_reads * 8,
-                                     cudaMemcpyHostToDevice, s), "copy read offsets");
-            SWG_CUDA(cudaMemcpyAsync(g->d_len + rofs, sm[i].read_len, sm[i].n_reads * 4,
-                                     cudaMemcpyHostToDevice, s), "copy read lengths");
+            SWG_CUDA(cudaMemcpyAsync(g->d_off + rofs, sm[i].read_off, sm[i].n_reads * 8, cudaMemcpyDefault, s),
+                     "copy read offsets");
+            SWG_CUDA(cudaMemcpyAsync(g->d_len + rofs, sm[i].read_len, sm[i].n_reads * 4, cudaMemcpyDefault, s),
+                     "copy read lengths");
         }
         wofs += sm[i].n_words;
         rofs += sm[i].n_reads;
@@ -895,17 +903,23 @@ struct BucketPlan {
 // lays out the level-1 partition and bucket regions: from exact counts over
 // the reads of a (counted), else from a sample of them (every stride-th
 // batch, once N reaches 64M occurrences).
-swg_status bucketed_plan(swg_graph *g, const BuildArgs &a, uint64_t N, bool counted, uint32_t stride,
-                         cudaStream_t s, BucketPlan &pl) {
+swg_status bucketed_plan(swg_graph *g, const swg_opts *o, const BuildArgs &a, uint64_t N, bool counted,
+                         uint32_t stride, cudaStream_t s, BucketPlan &pl) {
     swg_status st;
     // level-1 partitions: 256, 512 past 400M occurrences (a level-1 round of
-    // 4096 records still writes runs of 8), 1024 only past 6.4G
+    // 4096 records still writes runs of 8), 1024 only past 6.4G; the options
+    // (then SWG_PART_BITS) override
     int b1 = N <= (400ull << 20) ? 8 : (N <= (6400ull << 20) ? 9 : 10);
     if (const char *e = std::getenv("SWG_PART_BITS")) b1 = std::min(10, std::max(8, std::atoi(e)));
-    const uint64_t P = 1ull << b1;
-    // sub-buckets of about `target` records (SWG_BUCKET_RECORDS overrides)
+    if (o && o->part_bits) b1 = std::min(10, std::max(8, o->part_bits));
+    // sub-buckets of about `target` records (the options, then SWG_BUCKET_RECORDS, override)
     double target = 4096.0;
     if (const char *e = std::getenv("SWG_BUCKET_RECORDS")) target = std::max(64.0, std::atof(e));
+    if (o && o->bucket_records) target = std::min(65535.0, std::max(64.0, (double)o->bucket_records));
+    // more partitions when even 1024 sub-buckets each would leave buckets past
+    // twice the target (they would outgrow the shared-memory tables)
+    while (b1 < 10 && (double)N / (double)((1ull << b1) << 10) > 2 * target) b1++;
+    const uint64_t P = 1ull << b1;
     int b2 = 0;
     while (b2 < 10 && (double)N / (double)(P << b2) > target) b2++;
     // at most 512 sub-buckets (level-2 runs of >= 8 records per 4096-record
@@ -923,6 +937,7 @@ swg_status bucketed_plan(swg_graph *g, const BuildArgs &a, uint64_t N, bool coun
     pa.load_num = 3;
     pa.load_den = 5;
     pa.work = g->d_ctl->work;
+    pa.shape = o ? o->scatter_shape : 0;
     if ((st = ensure(&g->d_part, &g->part_cap, 4 * P + 1, "partition table"))) return st;
     pa.part_count = g->d_part;
     pa.part_start = g->d_part + P;
@@ -941,6 +956,7 @@ swg_status bucketed_plan(swg_graph *g, const BuildArgs &a, uint64_t N, bool coun
     std::memset(&bk, 0, sizeof(bk));
     bk.b1 = b1;
     bk.b2 = b2;
+    bk.shape = o ? o->scatter_shape : 0;
     bk.n_parts = (uint32_t)P;
     bk.part_start = pa.part_start;
     bk.part_cursor = pa.part_cursor;
@@ -1001,7 +1017,7 @@ swg_status build_bucketed(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaStr
     swg_status st;
     g->algorithm = SWG_ALGO_BUCKETED;
     BucketPlan pl;
-    if ((st = bucketed_plan(g, a, a.total_occ, counted, 16, s, pl))) return st;
+    if ((st = bucketed_plan(g, o, a, a.total_occ, counted, 16, s, pl))) return st;
     SWG_CUDA(cudaEventRecord(g->ev[1], s), "event");
     g->launches += swg::launch_part_scatter(a, pl.pa, s);
     SWG_CUDA(cudaEventRecord(g->ev[2], s), "event");
@@ -1335,7 +1351,7 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
                 g->algorithm = SWG_ALGO_BUCKETED;
                 // every stride-th batch of the first piece: 1/16 to 1/8 of all reads
                 const uint32_t stride = (uint32_t)std::max<uint64_t>(1, 16 * first_blocks / nc);
-                if ((st = bucketed_plan(g, a0, N_est, false, stride, s, pl))) return st;
+                if ((st = bucketed_plan(g, o, a0, N_est, false, stride, s, pl))) return st;
                 SWG_CUDA(cudaEventRecord(g->ev[1], s), "event");
             }
         }

@@ -1,9 +1,10 @@
-// Autotuner: picks the table load factor and the counting scheme (direct
-// table in input order, direct table in minimizer order, hash-partitioned
-// slices, or shared-memory buckets) for a (k, read-length band), by timing
-// trial builds of a sample on
-// this GPU, and keeps the choices in a cache file (one JSON object per line:
-// {"k": K, "band": B, "load": X, "algorithm": A, "read_order": O, "ms": T}).
+// Autotuner: picks the counting scheme and its knobs for a (k, read-length
+// band) by timing trial builds of a sample on this GPU: the bucketed build
+// (the default) at several bucket sizes and scatter block shapes; the direct table at several load factors, in input and in
+// minimizer order; hash-partitioned slices. The choices go to a cache file,
+// one JSON object per line: {"k": K, "band": B, "load": X, "algorithm": A,
+// "read_order": O, "ms": T, "bucket_records": R, "part_bits": P,
+// "scatter_shape": S}.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -27,22 +28,30 @@ struct Cand {
     double load;
     int algorithm;
     int order;
+    uint32_t records;  // bucketed knobs (0 = default)
+    int part_bits;
+    int shape;
 };
 
 bool read_entry(const char *line, int *k, int *band, swg_tuning *t) {
     double load = 0, ms = 0;
-    int kk = 0, b = 0, alg = 0, ord = 0;
-    if (std::sscanf(line,
-                    " {\"k\": %d, \"band\": %d, \"load\": %lf, \"algorithm\": %d, \"read_order\": %d, "
-                    "\"ms\": %lf}",
-                    &kk, &b, &load, &alg, &ord, &ms) != 6)
-        return false;
+    int kk = 0, b = 0, alg = 0, ord = 0, pb = 0, sh = 0;
+    unsigned rec = 0;
+    const int got = std::sscanf(line,
+                                " {\"k\": %d, \"band\": %d, \"load\": %lf, \"algorithm\": %d, "
+                                "\"read_order\": %d, \"ms\": %lf, \"bucket_records\": %u, \"part_bits\": %d, "
+                                "\"scatter_shape\": %d}",
+                                &kk, &b, &load, &alg, &ord, &ms, &rec, &pb, &sh);
+    if (got != 6 && got != 9) return false;  // 6: an entry written before the bucketed knobs
     *k = kk;
     *band = b;
     t->load_factor = load;
     t->algorithm = alg;
     t->read_order = ord;
     t->ms = (float)ms;
+    t->bucket_records = got == 9 ? rec : 0;
+    t->part_bits = got == 9 ? pb : 0;
+    t->scatter_shape = got == 9 ? sh : 0;
     return true;
 }
 
@@ -54,13 +63,14 @@ swg_status swg_autotune(const swg_opts *base, const uint32_t *d_packed, uint64_t
                         const uint64_t *d_read_off, const uint32_t *d_read_len, uint64_t n_reads,
                         uint32_t read_len_hint, const char *cache_path, swg_tuning *best) {
     if (!base || !best || !cache_path) return SWG_ERR_BAD_INPUT;
-    const Cand cands[] = {{0.5, SWG_ALGO_DIRECT, SWG_ORDER_INPUT},
-                          {0.6, SWG_ALGO_DIRECT, SWG_ORDER_INPUT},
-                          {0.7, SWG_ALGO_DIRECT, SWG_ORDER_INPUT},
-                          {0.8, SWG_ALGO_DIRECT, SWG_ORDER_INPUT},
-                          {0.6, SWG_ALGO_DIRECT, SWG_ORDER_MINIMIZER},
-                          {0.6, SWG_ALGO_PARTITIONED, SWG_ORDER_INPUT},
-                          {0.6, SWG_ALGO_BUCKETED, SWG_ORDER_INPUT}};
+    // bucketed: bucket size and scatter shape (the partition count follows the
+    // input's size, so a count picked on a sample would not fit the full input)
+    std::vector<Cand> cands;
+    for (uint32_t rec : {4096u, 2048u, 8192u})  // the default first: ties keep it
+        for (int sh : {0, 1, 2}) cands.push_back({0.6, SWG_ALGO_BUCKETED, SWG_ORDER_INPUT, rec, 0, sh});
+    for (double load : {0.5, 0.6, 0.7, 0.8}) cands.push_back({load, SWG_ALGO_DIRECT, SWG_ORDER_INPUT, 0, 0, 0});
+    cands.push_back({0.6, SWG_ALGO_DIRECT, SWG_ORDER_MINIMIZER, 0, 0, 0});
+    cands.push_back({0.6, SWG_ALGO_PARTITIONED, SWG_ORDER_INPUT, 0, 0, 0});
     swg_graph *g = nullptr;
     swg_status st = swg_graph_create(&g);
     if (st) return st;
@@ -73,6 +83,9 @@ swg_status swg_autotune(const swg_opts *base, const uint32_t *d_packed, uint64_t
         o.algorithm = c.algorithm;
         o.read_order = c.order;
         o.expected_distinct = 0;
+        o.bucket_records = c.records;
+        o.part_bits = c.part_bits;
+        o.scatter_shape = c.shape;
         float ms = 0;
         for (int rep = 0; rep < 3 && st == SWG_OK; rep++) {  // first run allocates; best of two
             st = swg_graph_build_device(g, &o, d_packed, n_words, d_read_off, d_read_len, n_reads);
@@ -86,6 +99,9 @@ swg_status swg_autotune(const swg_opts *base, const uint32_t *d_packed, uint64_t
             top.algorithm = c.algorithm;
             top.read_order = c.order;
             top.ms = ms;
+            top.bucket_records = c.records;
+            top.part_bits = c.part_bits;
+            top.scatter_shape = c.shape;
         }
     }
     swg_graph_free(g);
@@ -98,9 +114,9 @@ swg_status swg_autotune(const swg_opts *base, const uint32_t *d_packed, uint64_t
     }
     std::fprintf(fp,
                  "{\"k\": %d, \"band\": %d, \"load\": %.3f, \"algorithm\": %d, \"read_order\": %d, "
-                 "\"ms\": %.4f}\n",
+                 "\"ms\": %.4f, \"bucket_records\": %u, \"part_bits\": %d, \"scatter_shape\": %d}\n",
                  base->k, band_of(read_len_hint), top.load_factor, top.algorithm, top.read_order,
-                 (double)top.ms);
+                 (double)top.ms, top.bucket_records, top.part_bits, top.scatter_shape);
     std::fclose(fp);
     return SWG_OK;
 }
@@ -125,6 +141,9 @@ swg_status swg_autotune_apply(const char *cache_path, int k, uint32_t read_len, 
     o->load_factor = hit.load_factor;
     o->algorithm = hit.algorithm;
     o->read_order = hit.read_order;
+    o->bucket_records = hit.bucket_records;
+    o->part_bits = hit.part_bits;
+    o->scatter_shape = hit.scatter_shape;
     return SWG_OK;
 }
 

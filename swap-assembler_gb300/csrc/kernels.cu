@@ -2198,7 +2198,7 @@ int launch_p1_scatter_shape(const BuildArgs &a, const PartArgs &p, cudaStream_t 
 
 int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s, bool persistent) {
     if (a.total_occ == 0 || a.n_reads == 0) return 0;
-    switch (scatter_shape()) {
+    switch (p.shape ? p.shape : scatter_shape()) {  // shape 3 changes only the level-2 scatter
         case 1: return launch_p1_scatter_shape<512, 8, 2>(a, p, s, persistent);
         case 2: return launch_p1_scatter_shape<256, 8, 4>(a, p, s, persistent);
         default:
@@ -2260,7 +2260,7 @@ int launch_sub_scatter_shape(const BucketArgs &b, cudaStream_t s) {
 
 int launch_sub_scatter(const BucketArgs &b, cudaStream_t s) {
     if (!b.n_rec) return 0;
-    switch (scatter_shape()) {
+    switch (b.shape ? b.shape : scatter_shape()) {
         case 1: return launch_sub_scatter_shape<512, 8, 2>(b, s);
         case 2: return launch_sub_scatter_shape<512, 8, 3>(b, s);
         default: {  // one shared atomic per record (the histogram's returns the rank)

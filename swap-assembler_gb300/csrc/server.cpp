@@ -1,10 +1,13 @@
 // Request server: continuous batching of graph builds on one GPU.
 //
 // Clients submit single-sample requests (packed reads in host memory, their
-// own k and cutoff) at any time. Worker threads, each with its own graph
-// handle and CUDA stream, repeatedly take every queued request that fits the
-// device-memory budget (in arrival order) and build them as one batch
-// (swg_batch_build); with two or more workers, batches overlap on the device.
+// own k and cutoff) at any time. Submission uploads the reads to device
+// memory (an upload runs at the host link's rate; a host copy into fresh
+// pages was the submitting thread's bottleneck), so the caller may free them
+// on return. Worker threads, each with its own graph handle and CUDA stream,
+// repeatedly take every queued request that fits the device-memory budget (in
+// arrival order) and build them as one batch (swg_batch_build on the
+// device-resident reads); with two or more workers, batches overlap on the device.
 // Each request's filtered graph is then copied to its own device buffer and
 // stays resident until the client fetches or releases it. Admission: a
 // request is charged an estimated footprint while its batch runs (inputs,
@@ -32,9 +35,11 @@ double now_s() {
 
 struct Request {
     uint64_t ticket = 0;
-    std::vector<uint32_t> packed;
-    std::vector<uint64_t> off;
-    std::vector<uint32_t> len;
+    uint32_t *d_packed = nullptr;  // the reads, uploaded at submission (freed after the build)
+    uint64_t *d_off = nullptr;
+    uint32_t *d_len = nullptr;
+    uint64_t n_words = 0, n_reads = 0;
+    uint64_t in_bytes = 0;  // device bytes of the uploaded reads
     int k = 0, cutoff = 0;
     uint64_t occ = 0;
     uint64_t footprint = 0;
@@ -59,6 +64,10 @@ struct swg_server {
     uint64_t next_ticket = 1;
     uint64_t reserved = 0;  // in-flight footprints
     uint64_t resident = 0;  // results waiting to be fetched
+    uint64_t queued = 0;    // device bytes of the uploaded reads of queued requests (charged to the
+                            // budget with the rest of the footprint once a worker takes the request)
+    std::mutex upload_mu;   // one upload at a time on upload_stream
+    cudaStream_t upload_stream = nullptr;
     swg_server_stats st;
     bool stop = false;
     uint32_t live_workers = 0;  // workers whose set-up succeeded or is still under way
@@ -78,6 +87,15 @@ uint64_t footprint_of(uint64_t reads, uint64_t words, uint64_t occ, double load)
     return words * 4 + reads * (8 + 4 + 8 + 4) + cap * 16 * 2 + (16ull << 20);
 }
 
+void free_inputs(Request *r, cudaStream_t s) {
+    if (r->d_packed) cudaFreeAsync(r->d_packed, s);
+    if (r->d_off) cudaFreeAsync(r->d_off, s);
+    if (r->d_len) cudaFreeAsync(r->d_len, s);
+    r->d_packed = nullptr;
+    r->d_off = nullptr;
+    r->d_len = nullptr;
+}
+
 // A worker whose set-up failed leaves; when the last one does, every queued
 // request fails with the reason and later submissions are refused with it.
 void worker_setup_failed(swg_server *srv, swg_status st, const std::string &why) {
@@ -85,6 +103,8 @@ void worker_setup_failed(swg_server *srv, swg_status st, const std::string &why)
     if (--srv->live_workers == 0) {
         srv->dead_error = "request server has no working worker: " + why;
         for (Request *r : srv->queue) {
+            srv->queued -= r->in_bytes;
+            free_inputs(r, srv->upload_stream);
             r->state = SWG_REQ_FAILED;
             r->status = st;
             r->error = srv->dead_error;
@@ -125,11 +145,26 @@ void worker_main(swg_server *srv) {
             std::unique_lock<std::mutex> lock(srv->mu);
             for (;;) {
                 if (srv->stop) break;
-                while (!srv->queue.empty()) {
-                    Request *r = srv->queue.front();
+                // Requests in arrival order while they fit the budget. A batch
+                // runs as one tagged bucketed build only while its samples'
+                // indices fit above the largest k-mer (2 k_max + ceil(log2
+                // samples) <= 64 bits): a request that would break that waits
+                // for a later batch, and the requests behind it may join.
+                int kmax = 0;
+                for (auto it = srv->queue.begin(); it != srv->queue.end();) {
+                    Request *r = *it;
                     if (srv->reserved + srv->resident + r->footprint > srv->opts.memory_budget)
                         break;  // waits until memory frees up (arrival order is kept)
-                    srv->queue.pop_front();
+                    const int km = std::max(kmax, r->k);
+                    int tb = 0;
+                    while ((size_t(1) << tb) < batch.size() + 1) tb++;
+                    if (!batch.empty() && (2 * km + tb > 64 || batch.size() + 1 > swg::kMaxTagSamples)) {
+                        ++it;
+                        continue;
+                    }
+                    kmax = km;
+                    it = srv->queue.erase(it);
+                    srv->queued -= r->in_bytes;
                     srv->reserved += r->footprint;
                     r->state = SWG_REQ_RUNNING;
                     batch.push_back(r);
@@ -145,11 +180,11 @@ void worker_main(swg_server *srv) {
         std::vector<swg_sample> samples(batch.size());
         for (size_t i = 0; i < batch.size(); i++) {
             Request *r = batch[i];
-            samples[i].packed = r->packed.data();
-            samples[i].n_words = r->packed.size();
-            samples[i].read_off = r->off.data();
-            samples[i].read_len = r->len.data();
-            samples[i].n_reads = r->off.size();
+            samples[i].packed = r->d_packed;
+            samples[i].n_words = r->n_words;
+            samples[i].read_off = r->d_off;
+            samples[i].read_len = r->d_len;
+            samples[i].n_reads = r->n_reads;
             samples[i].k = r->k;
             samples[i].cutoff = r->cutoff;
         }
@@ -178,6 +213,7 @@ void worker_main(swg_server *srv) {
                 }
             }
         }
+        for (Request *r : batch) free_inputs(r, stream);  // the inputs are no longer needed
         cudaStreamSynchronize(stream);
         {
             std::lock_guard<std::mutex> lock(srv->mu);
@@ -187,10 +223,6 @@ void worker_main(swg_server *srv) {
                 srv->reserved -= r->footprint;
                 r->t_done = t;
                 r->status = rs[i];
-                // the inputs are no longer needed
-                std::vector<uint32_t>().swap(r->packed);
-                std::vector<uint64_t>().swap(r->off);
-                std::vector<uint32_t>().swap(r->len);
                 if (rs[i] == SWG_OK) {
                     r->state = SWG_REQ_DONE;
                     r->resident = r->n_out * 16;
@@ -239,7 +271,9 @@ swg_status swg_server_create(const swg_server_opts *o, swg_server **out) {
     if (srv->opts.load_factor <= 0 || srv->opts.load_factor > 0.9) srv->opts.load_factor = 0.6;
     std::memset(&srv->st, 0, sizeof(srv->st));
     cudaGetDevice(&srv->device);
-    if (cudaStreamCreateWithFlags(&srv->fetch_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&srv->fetch_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&srv->upload_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        if (srv->fetch_stream) cudaStreamDestroy(srv->fetch_stream);
         delete srv;
         swg::set_error("stream creation failed");
         return SWG_ERR_CUDA;
@@ -263,34 +297,71 @@ swg_status swg_server_submit(swg_server *srv, const swg_sample *req, uint64_t *t
     const double t0 = now_s();
     Request *r = new (std::nothrow) Request;
     if (!r) return SWG_ERR_OOM;
-    try {
-        r->packed.assign(req->packed, req->packed + req->n_words);
-        r->off.assign(req->read_off, req->read_off + req->n_reads);
-        r->len.assign(req->read_len, req->read_len + req->n_reads);
-    } catch (...) {
-        delete r;
-        return SWG_ERR_OOM;
-    }
     r->k = req->k;
     r->cutoff = req->cutoff;
-    for (uint64_t i = 0; i < req->n_reads; i++)
-        if (req->read_len[i] >= (uint32_t)req->k) r->occ += req->read_len[i] - req->k + 1;
+    r->n_words = req->n_words;
+    r->n_reads = req->n_reads;
+    r->in_bytes = req->n_words * 4 + req->n_reads * 12;
+    const uint32_t k = (uint32_t)req->k;
+    uint64_t occ = 0;
+    for (uint64_t i = 0; i < req->n_reads; i++) {
+        const uint32_t L = req->read_len[i];
+        occ += L >= k ? L - k + 1 : 0;
+    }
+    r->occ = occ;
     r->footprint = footprint_of(req->n_reads, req->n_words, r->occ, srv->opts.load_factor);
     r->t_submit = t0;
+    {
+        std::lock_guard<std::mutex> lock(srv->mu);
+        swg_status refuse = SWG_OK;
+        if (r->footprint > srv->opts.memory_budget) {
+            srv->st.rejected++;
+            swg::set_error("request footprint exceeds the server's memory budget");
+            refuse = SWG_ERR_ADMISSION;
+        } else if (srv->stop) {
+            refuse = SWG_ERR_BAD_STATE;
+        } else if (!srv->dead_error.empty()) {
+            swg::set_error(srv->dead_error);
+            refuse = SWG_ERR_BAD_STATE;
+        }
+        if (refuse) {
+            delete r;
+            return refuse;
+        }
+        srv->queued += r->in_bytes;
+    }
+    // upload the reads (the caller may free its buffers once this returns)
+    cudaError_t e = cudaSetDevice(srv->device);
+    {
+        std::lock_guard<std::mutex> up(srv->upload_mu);
+        cudaStream_t us = srv->upload_stream;
+        if (e == cudaSuccess && r->n_words) e = cudaMallocAsync((void **)&r->d_packed, r->n_words * 4, us);
+        if (e == cudaSuccess && r->n_reads) e = cudaMallocAsync((void **)&r->d_off, r->n_reads * 8, us);
+        if (e == cudaSuccess && r->n_reads) e = cudaMallocAsync((void **)&r->d_len, r->n_reads * 4, us);
+        if (e == cudaSuccess && r->n_words)
+            e = cudaMemcpyAsync(r->d_packed, req->packed, r->n_words * 4, cudaMemcpyHostToDevice, us);
+        if (e == cudaSuccess && r->n_reads)
+            e = cudaMemcpyAsync(r->d_off, req->read_off, r->n_reads * 8, cudaMemcpyHostToDevice, us);
+        if (e == cudaSuccess && r->n_reads)
+            e = cudaMemcpyAsync(r->d_len, req->read_len, r->n_reads * 4, cudaMemcpyHostToDevice, us);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(us);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            free_inputs(r, us);
+            cudaStreamSynchronize(us);
+        }
+    }
     std::lock_guard<std::mutex> lock(srv->mu);
-    if (r->footprint > srv->opts.memory_budget) {
-        srv->st.rejected++;
+    if (e != cudaSuccess) {
+        srv->queued -= r->in_bytes;
         delete r;
-        swg::set_error("request footprint exceeds the server's memory budget");
-        return SWG_ERR_ADMISSION;
+        swg::set_error(std::string("request upload: ") + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? SWG_ERR_OOM : SWG_ERR_CUDA;
     }
     if (srv->stop) {
+        srv->queued -= r->in_bytes;
+        free_inputs(r, srv->upload_stream);
         delete r;
-        return SWG_ERR_BAD_STATE;
-    }
-    if (!srv->dead_error.empty()) {
-        delete r;
-        swg::set_error(srv->dead_error);
         return SWG_ERR_BAD_STATE;
     }
     r->ticket = srv->next_ticket++;
@@ -437,11 +508,14 @@ void swg_server_free(swg_server *srv) {
     for (auto &t : srv->workers) t.join();
     cudaSetDevice(srv->device);
     for (auto &kv : srv->reqs) {
+        free_inputs(kv.second, srv->fetch_stream);
         free_result(srv, kv.second);
         delete kv.second;
     }
     cudaStreamSynchronize(srv->fetch_stream);
     cudaStreamDestroy(srv->fetch_stream);
+    cudaStreamSynchronize(srv->upload_stream);
+    cudaStreamDestroy(srv->upload_stream);
     delete srv;
 }
 

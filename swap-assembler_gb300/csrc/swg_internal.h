@@ -95,6 +95,7 @@ struct PartArgs {
     uint32_t n_slots;
     int load_num, load_den;            // slice capacity = count * den / num + 16
     unsigned long long *work;          // bucketed: [2] read-batch counters (count, scatter), zeroed
+    int shape;                         // scatter block shape (swg_opts::scatter_shape; 0 = default)
 };
 
 // Bucketed build: the level-1 partition records are split again by the next
@@ -120,6 +121,7 @@ struct BucketArgs {
     unsigned long long *big2;              // ... and for a tier-2 table
     unsigned *big2_count;
     uint32_t big_cap;                      // capacity of each list
+    int shape;                             // scatter block shape (swg_opts::scatter_shape; 0 = default)
 };
 
 // Kernel launchers (kernels.cu). Each returns the number of launches made.

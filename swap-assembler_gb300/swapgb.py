@@ -41,13 +41,15 @@ ORDER_INPUT, ORDER_MINIMIZER = 0, 1
 class Opts(C.Structure):
     _fields_ = [("k", C.c_int), ("cutoff", C.c_int), ("load_factor", C.c_double),
                 ("expected_distinct", C.c_uint64), ("stream", C.c_void_p),
-                ("algorithm", C.c_int), ("read_order", C.c_int)]
+                ("algorithm", C.c_int), ("read_order", C.c_int),
+                ("bucket_records", C.c_uint32), ("part_bits", C.c_int), ("scatter_shape", C.c_int)]
 
     def __init__(self, k: int = 23, cutoff: int = 5, load_factor: float = 0.0,
                  expected_distinct: int = 0, stream: int | None = None, algorithm: int = 0,
-                 read_order: int = 0):
+                 read_order: int = 0, bucket_records: int = 0, part_bits: int = 0,
+                 scatter_shape: int = 0):
         super().__init__(k, cutoff, load_factor, expected_distinct, stream, algorithm,
-                         read_order)
+                         read_order, bucket_records, part_bits, scatter_shape)
 
 
 class BuildInfo(C.Structure):
@@ -95,7 +97,8 @@ REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
 class Tuning(C.Structure):
     _fields_ = [("load_factor", C.c_double), ("algorithm", C.c_int), ("read_order", C.c_int),
-                ("ms", C.c_float)]
+                ("ms", C.c_float), ("bucket_records", C.c_uint32), ("part_bits", C.c_int),
+                ("scatter_shape", C.c_int)]
 
 
 _lib = None
@@ -603,7 +606,8 @@ def autotune(opts: Opts, d_packed: int, n_words: int, d_off: int, d_len: int, n_
     _check(lib().swg_autotune(C.byref(opts), d_packed, n_words, d_off, d_len, n_reads, read_len,
                               str(cache_path).encode(), C.byref(t)), "swg_autotune")
     return {"load_factor": t.load_factor, "algorithm": t.algorithm, "read_order": t.read_order,
-            "ms": t.ms}
+            "ms": t.ms, "bucket_records": t.bucket_records, "part_bits": t.part_bits,
+            "scatter_shape": t.scatter_shape}
 
 
 def autotune_apply(cache_path: str, k: int, read_len: int, opts: Opts) -> bool:

@@ -245,10 +245,29 @@ def test_autotune_then_build(tmp_path):
     best = swapgb.autotune(swapgb.Opts(k=31, cutoff=5), p.data_ptr(), p.numel(), o.data_ptr(),
                            ln.data_ptr(), o.numel(), 100, cache)
     assert best["algorithm"] in (1, 2, 3) and 0.5 <= best["load_factor"] <= 0.8 and best["ms"] > 0
+    assert best["bucket_records"] in (0, 2048, 4096, 8192) and best["part_bits"] == 0
+    assert best["scatter_shape"] in (0, 1, 2)
     opts = swapgb.Opts(k=31, cutoff=5)
     assert swapgb.autotune_apply(cache, 31, 100, opts)
+    assert (opts.bucket_records, opts.part_bits, opts.scatter_shape) == (
+        best["bucket_records"], best["part_bits"], best["scatter_shape"])
     g = swapgb.Graph().build_reads(opts, r)
     assert_same_records(g, text, 31, 5)
+
+
+@pytest.mark.parametrize("knobs", [dict(bucket_records=2048), dict(bucket_records=8192, part_bits=9),
+                                   dict(part_bits=10, scatter_shape=1), dict(scatter_shape=2),
+                                   dict(scatter_shape=3, bucket_records=1024)])
+def test_bucketed_knobs_give_the_same_graph(knobs):
+    """Every bucket size, partition count and scatter shape the autotuner may
+    pick builds the same graph."""
+    text = synth_case_text("c2_small")
+    g = swapgb.Graph().build_reads(swapgb.Opts(k=31, cutoff=5, algorithm=swapgb.ALGO_BUCKETED, **knobs),
+                                   swapgb.reads_from_fasta(text, 31))
+    assert g.info()["algorithm"] == swapgb.ALGO_BUCKETED
+    assert_same_records(g, text, 31, 5)
+    with pytest.raises(swapgb.SwgError):  # out of range
+        swapgb.Graph().build_reads(swapgb.Opts(k=31, cutoff=5, part_bits=11), swapgb.reads_from_fasta(text, 31))
 
 
 def test_bucketed_large_input_and_hot_buckets():

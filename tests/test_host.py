@@ -214,3 +214,11 @@ def test_autotune_cache_lookup(tmp_path):
     assert abs(opts.load_factor - 0.8) < 1e-9 and opts.algorithm == 1 and opts.read_order == 1
     assert swapgb.autotune_apply(cache, 27, 150, opts) and opts.algorithm == 2
     assert not swapgb.autotune_apply(cache, 27, 250, opts)
+    # entries with the bucketed knobs fill them too; the older form leaves them 0
+    with open(cache, "a") as f:
+        f.write('{"k": 27, "band": 3, "load": 0.600, "algorithm": 3, "read_order": 0, "ms": 2.5, '
+                '"bucket_records": 8192, "part_bits": 9, "scatter_shape": 2}\n')
+    assert swapgb.autotune_apply(cache, 27, 250, opts)
+    assert (opts.algorithm, opts.bucket_records, opts.part_bits, opts.scatter_shape) == (3, 8192, 9, 2)
+    assert swapgb.autotune_apply(cache, 27, 150, opts)
+    assert (opts.bucket_records, opts.part_bits, opts.scatter_shape) == (0, 0, 0)
