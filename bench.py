@@ -682,6 +682,20 @@ def main() -> int:
         return max_over_ranks(statistics.mean(ts), world, dev), n, [round(t * 1e3, 3) for t in ts]
 
     e2e_s, n_e2e, e2e_steps = timed(e2e_fasta)
+    # where one end-to-end step goes: the build's event phases (the streamed
+    # build's level-1 phase holds the upload and the framing of the pieces),
+    # then the result copy alone
+    e2e_fasta()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    swapgb._check(lib.swg_graph_build_fasta(g2._h, swapgb.C.byref(opts), h_text.data_ptr(),
+                                            h_text.numel()), "swg_graph_build_fasta")
+    t1 = time.perf_counter()
+    copy_out_e2e()
+    t2 = time.perf_counter()
+    e2e_phases = {"build_wall_ms": 1e3 * (t1 - t0), "copy_out_wall_ms": 1e3 * (t2 - t1),
+                  "build_phase_ms": dict(zip(("setup", "level1_with_upload_and_framing", "level2",
+                                              "bucket_count", "total"), g2.timings()[0]))}
     e2e_p_s, _, e2e_p_steps = timed(e2e_packed)
 
     # the documented drop-in from a FASTA file on local disk,
@@ -830,7 +844,7 @@ def main() -> int:
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "wall_ms_steps": e2e_steps,
                     "path": "swg_graph_build_fasta on the pinned FASTA text (framing + packing on "
                             "the device; texts of 96 MiB and more stream up in pieces) + "
-                            "swg_graph_copy_out"},
+                            "swg_graph_copy_out", "one_step": e2e_phases},
             "e2e_packed": {"value": aggregate_value(n_bases, world, e2e_p_s * 1e3),
                            "unit": "bases/s", "h2d_bytes_per_step": h2d_p,
                            "d2h_bytes_per_step": d2h, "wall_ms_steps": e2e_p_steps,
