@@ -178,6 +178,20 @@ swg_status swg_graph_build_device(swg_graph *g, const swg_opts *o, const uint32_
  * SWG_STREAM_PIECES=2..16 sets the number of pieces. */
 swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *text, uint64_t len);
 
+/* As swg_graph_build_fasta, then the filtered graph into the caller's host
+ * arrays (keys[n], mult[8 n], unordered, as swg_graph_copy_out with sorted =
+ * 0): the end-to-end form of constructDistNodeGraph + cutoffGraph
+ * (graph.cpp:1049-1114) for a caller that wants the graph in host memory.
+ * When keys and mult are pinned host memory the device can address
+ * (cudaHostAlloc, cudaHostRegister) and the bucketed build runs, every
+ * bucket's survivors are written there as the bucket is counted, so the copy
+ * overlaps the counting; the order may then differ between calls. Otherwise
+ * the graph is copied after the build. The graph also stays on the device as
+ * after swg_graph_build_fasta. More than cap survivors: SWG_ERR_BAD_INPUT with
+ * *n_out set to the count needed. */
+swg_status swg_graph_build_fasta_to_host(swg_graph *g, const swg_opts *o, const char *text, uint64_t len,
+                                         uint64_t *keys, uint8_t *mult, uint64_t cap, uint64_t *n_out);
+
 /* As swg_graph_build_fasta, on the FASTA file at path: the file is read (in
  * parallel slices) into a pinned host buffer the handle keeps for later calls,
  * then uploaded, framed and built on the device. The reference's reader takes

@@ -49,6 +49,7 @@ struct Control {  // device-side control block
     unsigned long long work[2];      // bucketed build: read batches handed out (count, scatter)
     unsigned max_len;                // longest read (occurrence scan)
     unsigned pad4;
+    unsigned long long host_written; // survivors written to the caller's host arrays
     uint64_t occ_total;              // last: the memsets of the control block stop before it
 };
 
@@ -166,6 +167,11 @@ struct swg_graph {
     // (kept and reused by later calls of this handle)
     char *h_file = nullptr;
     uint64_t h_file_cap = 0;
+    // swg_graph_build_fasta_to_host: the caller's arrays as the device sees
+    // them, for the duration of the call; host_out_used: the bucket count wrote them
+    unsigned long long *host_keys = nullptr, *host_mult = nullptr;
+    uint64_t host_cap = 0;
+    bool host_out_used = false;
 };
 
 namespace {
@@ -1031,6 +1037,13 @@ swg_status bucketed_finish(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaSt
                            bool counted, BucketPlan &pl) {
     swg_status st;
     g->algorithm = SWG_ALGO_BUCKETED;
+    if (g->host_keys && !a.tag_bits) {  // survivors also straight to the caller's host arrays
+        a.host_keys = g->host_keys;
+        a.host_mult = g->host_mult;
+        a.host_cap = g->host_cap;
+        a.host_written = &g->d_ctl->host_written;
+        g->host_out_used = true;
+    }
     const uint64_t N = a.total_occ;
     const int b1 = pl.b1, b2 = pl.b2;
     const uint64_t P = pl.P, NB = pl.NB;
@@ -1647,6 +1660,40 @@ swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *te
     st = build_impl(g, o, g->d_packed, n_words, g->d_off, g->d_len, n_reads);
     if (st == SWG_OK) g->launches += launches;
     return st;
+}
+
+swg_status swg_graph_build_fasta_to_host(swg_graph *g, const swg_opts *o, const char *text, uint64_t len,
+                                         uint64_t *keys, uint8_t *mult, uint64_t cap, uint64_t *n_out) {
+    if (!g || !n_out || (cap && (!keys || !mult))) return SWG_ERR_BAD_INPUT;
+    *n_out = 0;
+    SWG_CUDA(cudaSetDevice(g->device), "cudaSetDevice");
+    // the arrays as the device sees them (pinned host memory); otherwise the
+    // graph is copied out after the build
+    void *dk = nullptr, *dm = nullptr;
+    const bool mapped = cap && cudaHostGetDevicePointer(&dk, keys, 0) == cudaSuccess &&
+                        cudaHostGetDevicePointer(&dm, mult, 0) == cudaSuccess;
+    if (!mapped) cudaGetLastError();
+    g->host_keys = mapped ? static_cast<unsigned long long *>(dk) : nullptr;
+    g->host_mult = mapped ? static_cast<unsigned long long *>(dm) : nullptr;
+    g->host_cap = mapped ? cap : 0;
+    g->host_out_used = false;
+    swg_status st = swg_graph_build_fasta(g, o, text, len);
+    const bool wrote = g->host_out_used;
+    g->host_keys = g->host_mult = nullptr;
+    g->host_cap = 0;
+    g->host_out_used = false;
+    if (st) return st;
+    *n_out = g->n_out;
+    if (g->n_out > cap) {
+        swg::set_error("output arrays too small: n_out holds the survivor count needed");
+        return SWG_ERR_BAD_INPUT;
+    }
+    if (!wrote) return swg_graph_copy_out(g, keys, mult, cap, 0, n_out);
+    if (g->h_ctl->host_written != g->n_out) {
+        swg::set_error("survivors written to the host arrays disagree with the graph (internal error)");
+        return SWG_ERR_CUDA;
+    }
+    return SWG_OK;
 }
 
 swg_status swg_graph_build_fasta_file(swg_graph *g, const swg_opts *o, const char *path) {

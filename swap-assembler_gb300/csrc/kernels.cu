@@ -1625,6 +1625,23 @@ __global__ void __launch_bounds__(256) k_group_by_sample(const unsigned long lon
     }
 }
 
+// A warp's survivors (kept: their lanes) also go to the caller's host arrays
+// at a global cursor: one atomic per warp, the lanes' slots in lane order;
+// slots past host_cap are counted but not written.
+__device__ __forceinline__ void host_append(const BuildArgs &a, unsigned kept, int lane, uint64_t m,
+                                            uint64_t key) {
+    unsigned long long at = 0;
+    if (lane == __ffs(kept) - 1) at = atomicAdd(a.host_written, (unsigned long long)__popc(kept));
+    at = __shfl_sync(kFull, at, __ffs(kept) - 1);
+    if (m) {
+        const uint64_t q = at + __popc(kept & ((1u << lane) - 1));
+        if (q < a.host_cap) {
+            a.host_keys[q] = key;
+            a.host_mult[q] = m;
+        }
+    }
+}
+
 // Shared memory of a bucket CTA: T keys, T x 8 uint16 counters, and the list
 // of used slots (uint16).
 template <int T>
@@ -1824,6 +1841,7 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
                     b.stage_keys[pos] = runmix64(h);
                     b.rec2[pos] = m;
                 }
+                if (a.host_keys) host_append(a, kept, lane, m, runmix64(h));
             }
         }
         __syncthreads();
@@ -1980,6 +1998,22 @@ __global__ void __launch_bounds__(kCBlock) k_big_compact(BuildArgs a, const Entr
                 a.out_mult[pos] = cnts[it];
             }
             pos++;
+        }
+    }
+    if (a.host_keys) {  // and to the caller's host arrays (see host_append)
+        __shared__ unsigned long long s_hbase;
+        if (threadIdx.x == 0) s_hbase = total ? atomicAdd(a.host_written, (unsigned long long)total) : 0;
+        __syncthreads();
+        uint64_t q = s_hbase + ex;
+#pragma unroll
+        for (int it = 0; it < kCItems; ++it) {
+            if (keep & (1u << it)) {
+                if (q < a.host_cap) {
+                    a.host_keys[q] = keys[it];
+                    a.host_mult[q] = cnts[it];
+                }
+                q++;
+            }
         }
     }
 }

@@ -73,6 +73,13 @@ struct BuildArgs {
     int tag_bits;                      // bucketed batch: the read's sample index sits in the
                                        // top tag_bits bits of every key (0 = no tag)
     unsigned *max_len;                 // if set, the occurrence scan records the longest read
+    // bucketed single-sample build only: survivors also written, as each bucket
+    // is compacted, to host memory the device can reach (unordered, at most
+    // host_cap; host_written counts them), so the copy-out overlaps the count
+    unsigned long long *host_keys;
+    unsigned long long *host_mult;
+    uint64_t host_cap;
+    unsigned long long *host_written;
 };
 
 constexpr uint32_t kMaxTagSamples = 1024;  // samples of one tagged bucketed batch

@@ -130,6 +130,7 @@ def lib() -> C.CDLL:
             "swg_build_fasta": (i32, [C.POINTER(Opts), C.c_char_p, u64, C.POINTER(P)]),
             "swg_graph_build_fasta": (i32, [P, C.POINTER(Opts), P, u64]),
             "swg_graph_build_fasta_file": (i32, [P, C.POINTER(Opts), C.c_char_p]),
+            "swg_graph_build_fasta_to_host": (i32, [P, C.POINTER(Opts), P, u64, P, P, u64, pu64]),
             "swg_graph_size": (i32, [P, pu64]),
             "swg_graph_distinct": (i32, [P, pu64]),
             "swg_graph_device_view": (i32, [P, C.POINTER(P), C.POINTER(P), pu64]),

@@ -133,3 +133,65 @@ def test_sample_miss_recounts_exactly(text2):
     assert info["estimate"] == 1  # the exact-count rerun ran
     gs, ks, ms = build(text, opts, True)
     assert (ms == 255).any()  # the hot k-mers saturate
+
+
+def _to_host(g: swapgb.Graph, opts: swapgb.Opts, text: bytes, keys, mult, cap: int) -> tuple[int, int]:
+    import ctypes as C
+    h = np.frombuffer(text, dtype=np.uint8)
+    n = C.c_uint64()
+    st = swapgb.lib().swg_graph_build_fasta_to_host(g._h, C.byref(opts), h.ctypes.data, h.size, keys, mult,
+                                                     cap, C.byref(n))
+    return st, n.value
+
+
+@pytest.mark.parametrize("case", ["streamed", "one_shot", "hot_keys", "direct"])
+def test_build_to_host_equals_build_then_copy(case, text2):
+    """swg_graph_build_fasta_to_host into pinned arrays (the bucket count
+    writes each bucket's survivors there as it goes) equals
+    swg_graph_build_fasta + swg_graph_copy_out, as a set; twice in a row on
+    one handle; through the streamed and the one-shot framing, with buckets
+    too large for shared memory (the global-table path), and with the direct
+    algorithm (copied after the build)."""
+    import torch
+    opts = swapgb.Opts(k=31, cutoff=5)
+    text = text2
+    if case == "one_shot":
+        text = synth(43, 200_000)
+    elif case == "hot_keys":
+        reads = ["A" * 250, "AC" * 125] * 30000 + ["ACGTTGCA" * 20] * 500
+        text = "".join(">h%d\n%s\n" % (i, r) for i, r in enumerate(reads)).encode() + synth(44, 100_000)
+        opts = swapgb.Opts(k=21, cutoff=2)
+    elif case == "direct":
+        opts = swapgb.Opts(k=31, cutoff=5, algorithm=swapgb.ALGO_DIRECT)
+    want_g = swapgb.Graph().build_fasta(opts, text)
+    wk, wm = want_g.copy_out(sorted=True)
+    cap = wk.size + 16
+    keys = torch.zeros(cap, dtype=torch.int64).pin_memory()
+    mult = torch.zeros(cap * 8, dtype=torch.uint8).pin_memory()
+    g = swapgb.Graph()
+    for _ in range(2):
+        st, n = _to_host(g, opts, text, keys.data_ptr(), mult.data_ptr(), cap)
+        assert st == 0, swapgb.lib().swg_last_error().decode()
+        assert n == wk.size
+        k = keys.numpy().view(np.uint64)[:n]
+        m = mult.numpy().reshape(-1, 8)[:n]
+        o = np.argsort(k, kind="stable")
+        assert np.array_equal(k[o], wk) and np.array_equal(m[o], wm)
+        dk, dm = g.copy_out(sorted=True)  # the graph stays on the device too
+        assert np.array_equal(dk, wk) and np.array_equal(dm, wm)
+    # too small: the count needed comes back
+    st, n = _to_host(g, opts, text, keys.data_ptr(), mult.data_ptr(), max(1, wk.size // 2))
+    assert st == 1 and n == wk.size
+
+
+def test_build_to_host_pageable_arrays(text2):
+    """Arrays the device cannot address (pageable numpy memory): the graph is
+    copied after the build, with the same result."""
+    opts = swapgb.Opts(k=31, cutoff=5)
+    wk, wm = swapgb.Graph().build_fasta(opts, text2).copy_out(sorted=True)
+    keys = np.zeros(wk.size, dtype=np.uint64)
+    mult = np.zeros((wk.size, 8), dtype=np.uint8)
+    st, n = _to_host(swapgb.Graph(), opts, text2, keys.ctypes.data, mult.ctypes.data, wk.size)
+    assert st == 0 and n == wk.size
+    o = np.argsort(keys, kind="stable")
+    assert np.array_equal(keys[o], wk) and np.array_equal(mult[o], wm)
