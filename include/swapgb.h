@@ -98,7 +98,9 @@ typedef struct swg_opts {
      * pass twice the target), block shape of the two scatter passes (the
      * default is 256 threads x 16 records each; 1 = 512 x 8 for both, 2 =
      * 256 x 8 for level 1 and 512 x 8 for level 2, 3 = level 2 staged by
-     * bulk copies). */
+     * bulk copies, 4 = level 1 with warp-cooperative extraction: the lanes of
+     * a warp on consecutive k-mers, each cut from a window of the packed
+     * words; single-sample builds from packed reads). */
     uint32_t bucket_records;
     int part_bits;
     int scatter_shape;

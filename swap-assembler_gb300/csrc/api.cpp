@@ -236,9 +236,9 @@ swg_status check_opts(const swg_opts *o) {
         return SWG_ERR_BAD_INPUT;
     }
     if (o->bucket_records > 65535 || (o->part_bits && (o->part_bits < 8 || o->part_bits > 10)) ||
-        o->scatter_shape < 0 || o->scatter_shape > 3) {
+        o->scatter_shape < 0 || o->scatter_shape > 4) {
         swg::set_error("bucketed knobs out of range (records per bucket <= 65535, partition bits 8..10, "
-                       "scatter shape 0..3)");
+                       "scatter shape 0..4)");
         return SWG_ERR_BAD_INPUT;
     }
     return SWG_OK;

@@ -1060,6 +1060,132 @@ __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs p
 }
 
 
+// Level-1 scatter with warp-cooperative extraction: blocks take tiles of
+// NT * IT consecutive k-mer occurrences (the tiles of the occurrence prefix),
+// and in round j the lanes of a warp take 32 consecutive occurrences —
+// mostly of one read. Each lane cuts its k-mer from a 64-bit window of the
+// packed words (loads its neighbours share through L1), its reverse
+// complement by bit reversal, and its neighbour bases from the window and
+// the word before; no state is carried from one occurrence to the next. The
+// read of an occurrence: lane 0 searches the tile's reads in shared memory,
+// the others step on from it. Records, ranks and the partition sort as in
+// k_p1_scatter. Single-sample builds only (one k).
+template <int NT, int IT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_p1_scatter_wc(BuildArgs a, PartArgs pa) {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    unsigned long long *sorted = reinterpret_cast<unsigned long long *>(dyn);
+    BinDest *dest = reinterpret_cast<BinDest *>(sorted + NT * IT);
+    unsigned *hist = reinterpret_cast<unsigned *>(dest + pa.n_parts);
+    unsigned *loff = hist + pa.n_parts;
+    unsigned short *spart = reinterpret_cast<unsigned short *>(loff + pa.n_parts);
+    __shared__ uint64_t wb[NT / 32];
+    __shared__ TileSmem ts;
+    const int shift = 64 - pa.bits;
+    const uint32_t per = (pa.n_parts + NT - 1) / NT;
+    const int k = a.k;
+    const int lane = threadIdx.x & 31;
+    for (uint64_t t = blockIdx.x; t < a.n_tiles; t += gridDim.x) {
+        __syncthreads();  // the previous tile's rounds are written out
+        const TileView v = load_tile(a, t, ts);
+        for (uint32_t j = threadIdx.x; j < pa.n_parts; j += NT) hist[j] = 0;
+        __syncthreads();
+        unsigned long long rec[IT];
+        unsigned pr[IT];  // partition | rank << 16; ~0 for no record
+        uint64_t hint = 0;  // the read (index in the tile) of this lane's last occurrence
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+            pr[it] = ~0u;
+            rec[it] = 0;
+            const uint64_t i = t * kTileOcc + (uint64_t)it * NT + threadIdx.x;
+            const bool valid = i < a.total_occ;
+            uint64_t pre = 0, off = 0;
+            uint32_t len = 0;
+            if (v.in_smem) {
+                // lane 0 searches; the warp's 32 occurrences span few reads
+                uint64_t r = hint;
+                if (lane == 0 && valid) {
+                    uint64_t lo = hint, hi = v.nr;
+                    while (hi - lo > 1) {
+                        const uint64_t mid = (lo + hi) >> 1;
+                        if (ts.pre[mid] <= i) lo = mid;
+                        else hi = mid;
+                    }
+                    r = lo;
+                }
+                r = __shfl_sync(kFull, r, 0);
+                if (valid) {
+                    while (r + 1 < v.nr && ts.pre[r + 1] <= i) ++r;
+                    pre = ts.pre[r];
+                    off = ts.off[r];
+                    len = ts.len[r];
+                }
+                hint = r;
+            } else if (valid) {
+                uint64_t ridx;
+                uint32_t seg;
+                find_read(a, v, ts, i, pre, off, len, ridx, seg);
+            }
+            if (valid) {
+                const uint64_t p = i - pre, g = off + p;
+                const uint64_t win = window32(a.packed, a.n_words, g);
+                const uint64_t fwd = win >> (64 - 2 * k);
+                const uint64_t rc = revcomp_dev(fwd, k);
+                const bool f = fwd >= rc;
+                unsigned code = 0;
+                if (p + (uint64_t)k < len) code = 0x08u | ((f ? 0u : 4u) + ((uint32_t)(win >> (62 - 2 * k)) & 3u));
+                if (p >= 1) code |= 0x80u | (((f ? 4u : 0u) + 3u - base_at(a.packed, a.n_words, g - 1)) << 4);
+                const uint64_t h = rmix64(f ? fwd : rc);
+                const unsigned part = (unsigned)(h >> shift);
+                rec[it] = ((h << pa.bits) >> (pa.bits - 8)) | code;
+                pr[it] = part | (atomicAdd(&hist[part], 1u) << 16);
+            }
+        }
+        __syncthreads();
+        uint64_t mine = 0;
+        for (uint32_t x = 0; x < per; ++x) {
+            const uint32_t j = threadIdx.x * per + x;
+            if (j < pa.n_parts) mine += hist[j];
+        }
+        uint64_t total;
+        uint64_t run = block_exclusive_scan<NT>(mine, wb, &total);
+        for (uint32_t x = 0; x < per; ++x) {
+            const uint32_t j = threadIdx.x * per + x;
+            if (j < pa.n_parts) {
+                const unsigned c = hist[j];
+                loff[j] = (unsigned)run;
+                BinDest d;
+                d.dst = 0;
+                d.lim = (unsigned)run;
+                d.pad = 0;
+                if (c) {
+                    const unsigned long long g0 = atomicAdd(&pa.part_cursor[j], (unsigned long long)c);
+                    const unsigned long long lim = pa.part_start[j + 1];  // region end
+                    const unsigned f = g0 + c <= lim ? c : (g0 < lim ? (unsigned)(lim - g0) : 0u);
+                    d.dst = g0 - run;
+                    d.lim = (unsigned)run + f;
+                }
+                dest[j] = d;
+                run += c;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+            if (pr[it] != ~0u) {
+                const unsigned part = pr[it] & 0xffffu;
+                const unsigned pos = loff[part] + (pr[it] >> 16);
+                sorted[pos] = rec[it];
+                spart[pos] = (unsigned short)part;
+            }
+        }
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < (uint32_t)total; j += NT) {
+            const BinDest d = dest[spart[j]];
+            if (j < d.lim) pa.records[d.dst + j] = sorted[j];  // past the region: flagged later, recounted
+        }
+    }
+}
+
 // Exclusive prefix over the partitions (n_parts <= 1024, one block).
 __global__ void __launch_bounds__(1024) k_part_prefix(PartArgs pa) {
     __shared__ uint64_t wb[32];
@@ -2214,7 +2340,7 @@ int scatter_shape() {
     static int shape = [] {
         const char *e = std::getenv("SWG_SCATTER_SHAPE");
         const int v = e ? std::atoi(e) : 0;
-        return v >= 0 && v <= 3 ? v : 0;
+        return v >= 0 && v <= 4 ? v : 0;
     }();
     return shape;
 }
@@ -2232,7 +2358,17 @@ int launch_p1_scatter_shape(const BuildArgs &a, const PartArgs &p, cudaStream_t 
 
 int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s, bool persistent) {
     if (a.total_occ == 0 || a.n_reads == 0) return 0;
-    switch (p.shape ? p.shape : scatter_shape()) {  // shape 3 changes only the level-2 scatter
+    const int shape = p.shape ? p.shape : scatter_shape();
+    if (shape == 4 && a.tile_first_read && a.n_tiles && !a.segs && !a.tag_bits) {
+        // warp-cooperative extraction (needs the occurrence prefix and tiles)
+        auto kern = k_p1_scatter_wc<256, 16, 3>;
+        const size_t smem = p1_scatter_smem(p.n_parts, 256 * 16);
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const uint64_t grid = std::min<uint64_t>(a.n_tiles, resident_grid(kern, 256, smem));
+        kern<<<(unsigned)grid, 256, smem, s>>>(a, p);
+        return 1;
+    }
+    switch (shape) {  // shape 3 changes only the level-2 scatter, shape 4 only level 1
         case 1: return launch_p1_scatter_shape<512, 8, 2>(a, p, s, persistent);
         case 2: return launch_p1_scatter_shape<256, 8, 4>(a, p, s, persistent);
         default:

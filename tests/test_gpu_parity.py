@@ -257,7 +257,8 @@ def test_autotune_then_build(tmp_path):
 
 @pytest.mark.parametrize("knobs", [dict(bucket_records=2048), dict(bucket_records=8192, part_bits=9),
                                    dict(part_bits=10, scatter_shape=1), dict(scatter_shape=2),
-                                   dict(scatter_shape=3, bucket_records=1024)])
+                                   dict(scatter_shape=3, bucket_records=1024), dict(scatter_shape=4),
+                                   dict(scatter_shape=4, part_bits=9)])
 def test_bucketed_knobs_give_the_same_graph(knobs):
     """Every bucket size, partition count and scatter shape the autotuner may
     pick builds the same graph."""
