@@ -1808,7 +1808,7 @@ __device__ __forceinline__ uint64_t bucket_mult(const unsigned *cnt, uint32_t s,
 // whose keys do not fit, or with more records than the 16-bit slot counters
 // hold, is appended to the overflow list instead. Buckets are
 // list[0..n_items) if list is given, else 0..n_items.
-template <int kT, int kNT>
+template <int kT, int kNT, int kB = kBkBatch>
 __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_items,
                             const unsigned long long *list, unsigned long long *ovf,
                             unsigned *ovf_count, uint32_t ovf_cap) {
@@ -1830,7 +1830,7 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
     const int c = a.cutoff;
     const bool cut_all = c >= 256;
     const unsigned cbias = (c > 0 && c < 256) ? (0x8000u - (unsigned)c) * 0x00010001u : 0u;
-    unsigned long long v[kBkBatch];
+    unsigned long long v[kB];
     uint64_t v_for = ~0ull;  // bucket whose first batch the registers v hold
     for (uint64_t it = blockIdx.x; it < n_items; it += gridDim.x) {
         const uint64_t bk = list ? list[it] : it;
@@ -1861,7 +1861,7 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
         }
         if (v_for != bk) {
 #pragma unroll
-            for (int i = 0; i < kBkBatch; ++i) {
+            for (int i = 0; i < kB; ++i) {
                 const uint64_t r = rb + (uint64_t)i * kNT + threadIdx.x;
                 v[i] = r < re ? b.rec2[r] : 0ull;
             }
@@ -1869,16 +1869,16 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
         __syncthreads();  // counters reset
         const uint64_t hp = (uint64_t)(bk >> b.b2) << (64 - b.b1);
         bool full = false;
-        for (uint64_t base = rb; base < re; base += (uint64_t)kNT * kBkBatch) {
+        for (uint64_t base = rb; base < re; base += (uint64_t)kNT * kB) {
             if (base != rb) {
 #pragma unroll
-                for (int i = 0; i < kBkBatch; ++i) {  // the batch's loads are in flight together
+                for (int i = 0; i < kB; ++i) {  // the batch's loads are in flight together
                     const uint64_t r = base + (uint64_t)i * kNT + threadIdx.x;
                     v[i] = r < re ? b.rec2[r] : 0ull;
                 }
             }
 #pragma unroll
-            for (int i = 0; i < kBkBatch; ++i) {
+            for (int i = 0; i < kB; ++i) {
                 if (base + (uint64_t)i * kNT >= re) break;  // no thread of the block has a record left
                 const bool valid = !full && base + (uint64_t)i * kNT + threadIdx.x < re;
                 bool fresh = false;
@@ -1929,7 +1929,7 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
             uint64_t nrb, nre;
             bucket_range(b, nbk, nrb, nre);
 #pragma unroll
-            for (int i = 0; i < kBkBatch; ++i) {
+            for (int i = 0; i < kB; ++i) {
                 const uint64_t r = nrb + (uint64_t)i * kNT + threadIdx.x;
                 v[i] = r < nre ? b.rec2[r] : 0ull;
             }
@@ -1996,6 +1996,17 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
 __global__ void __launch_bounds__(kBkThreads, 2) k_bucket_count(BuildArgs a, BucketArgs b, uint64_t n_buckets) {
     if (*b.status & kStatusPartOverflow) return;  // a partition overflowed: the build recounts
     bucket_pass<kBkTable, kBkThreads>(a, b, n_buckets, nullptr, b.big, b.big_count, b.big_cap);
+}
+
+// Tier 1 for small buckets (a plan of at most kBkSmallRecords records per
+// bucket on average): four CTAs of 256 threads per SM with 2048-entry tables
+// and 4 records loaded ahead per thread — as many warps per SM, half as many
+// threads behind each barrier. A bucket whose keys do not fit goes to tier 2.
+constexpr int kBkTableS = 2048, kBkThreadsS = 256;
+constexpr uint64_t kBkSmallRecords = 3072;
+__global__ void __launch_bounds__(kBkThreadsS, 4) k_bucket_count_small(BuildArgs a, BucketArgs b, uint64_t n_buckets) {
+    if (*b.status & kStatusPartOverflow) return;
+    bucket_pass<kBkTableS, kBkThreadsS, 4>(a, b, n_buckets, nullptr, b.big, b.big_count, b.big_cap);
 }
 
 // Tier 2: the buckets tier 1 could not hold, one persistent CTA per SM with
@@ -2457,9 +2468,22 @@ int launch_bucket_count(const BuildArgs &a, const BucketArgs &b, cudaStream_t s)
     const uint64_t nb = (uint64_t)b.n_parts << b.b2;
     const size_t tag = a.tag_bits ? kBucketTagSmem : 0;
     const size_t smem1 = bucket_smem<kBkTable>() + tag, smem2 = bucket_smem<kBkTable2>() + tag;
-    cudaFuncSetAttribute(k_bucket_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
-    const uint64_t grid = std::min<uint64_t>(nb, resident_grid(k_bucket_count, kBkThreads, smem1));
-    k_bucket_count<<<(unsigned)grid, kBkThreads, smem1, s>>>(a, b, nb);
+    // SWG_BUCKET_SMALL: 0 keeps the 4096-entry tables, 2 takes the small ones
+    // for every untagged build, unset or 1 picks by the mean bucket size
+    static const int small_mode = [] {
+        const char *e = std::getenv("SWG_BUCKET_SMALL");
+        return e ? std::atoi(e) : 1;
+    }();
+    if (small_mode && !a.tag_bits && (small_mode == 2 || b.n_rec <= kBkSmallRecords * nb)) {
+        const size_t smemS = bucket_smem<kBkTableS>();
+        cudaFuncSetAttribute(k_bucket_count_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemS);
+        const uint64_t grid = std::min<uint64_t>(nb, resident_grid(k_bucket_count_small, kBkThreadsS, smemS));
+        k_bucket_count_small<<<(unsigned)grid, kBkThreadsS, smemS, s>>>(a, b, nb);
+    } else {
+        cudaFuncSetAttribute(k_bucket_count, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+        const uint64_t grid = std::min<uint64_t>(nb, resident_grid(k_bucket_count, kBkThreads, smem1));
+        k_bucket_count<<<(unsigned)grid, kBkThreads, smem1, s>>>(a, b, nb);
+    }
     cudaFuncSetAttribute(k_bucket_count_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
     k_bucket_count_large<<<(unsigned)device_sm_count(), kBkThreads2, smem2, s>>>(a, b);
     return 2;
