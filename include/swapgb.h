@@ -126,6 +126,9 @@ typedef struct swg_build_info {
                              bucketed: 1 when a partition or bucket outgrew its
                              sampled region and the build reran with exact counts */
     float ms[5];          /* as swg_graph_last_timings */
+    uint32_t bucket_table; /* bucketed: entries of the shared table the first
+                              counting pass used (2048 when the buckets average
+                              at most 3072 records, else 4096); 0 otherwise */
 } swg_build_info;
 
 typedef struct swg_reads swg_reads; /* host-side packed reads */

@@ -101,6 +101,7 @@ struct swg_graph {
     Entry *d_slices = nullptr;
     uint64_t slices_cap = 0;
     uint32_t parts = 0, slots = 0, waves = 0;
+    uint32_t bucket_table = 0;  // bucketed: entries of the tier-1 shared table
     uint64_t slot_cap = 0;
     // read-order workspace
     unsigned *d_minhash = nullptr;
@@ -1064,6 +1065,7 @@ swg_status bucketed_finish(swg_graph *g, const swg_opts *o, BuildArgs &a, cudaSt
     SWG_CUDA(cudaGetLastError(), "bucket scatter launch");
     SWG_CUDA(cudaEventRecord(g->ev[3], s), "event");
     g->launches += swg::launch_bucket_count(a, bk, s);
+    g->bucket_table = (uint32_t)swg::bucket_count_table(a, bk);
     SWG_CUDA(cudaEventRecord(g->ev[5], s), "event");
     g->launches += swg::launch_gscan(reinterpret_cast<const uint64_t *>(bk.surv),
                                      reinterpret_cast<uint64_t *>(bk.surv_off), NB,
@@ -2125,6 +2127,7 @@ swg_status swg_graph_build_info(const swg_graph *g, swg_build_info *info) {
     info->retries = g->retries;
     info->estimate = g->estimate;
     std::memcpy(info->ms, g->ms, sizeof(g->ms));
+    info->bucket_table = g->algorithm == SWG_ALGO_BUCKETED ? g->bucket_table : 0;
     return SWG_OK;
 }
 

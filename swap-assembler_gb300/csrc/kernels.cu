@@ -2464,17 +2464,20 @@ int launch_sub_scatter(const BucketArgs &b, cudaStream_t s) {
     }
 }
 
+int bucket_count_table(const BuildArgs &a, const BucketArgs &b) {
+    // SWG_BUCKET_SMALL: 0 keeps the 4096-entry tables, 2 takes the small ones
+    // for every untagged build, unset or 1 picks by the mean bucket size
+    const char *e = std::getenv("SWG_BUCKET_SMALL");
+    const int small_mode = e ? std::atoi(e) : 1;
+    const uint64_t nb = (uint64_t)b.n_parts << b.b2;
+    return small_mode && !a.tag_bits && (small_mode == 2 || b.n_rec <= kBkSmallRecords * nb) ? kBkTableS : kBkTable;
+}
+
 int launch_bucket_count(const BuildArgs &a, const BucketArgs &b, cudaStream_t s) {
     const uint64_t nb = (uint64_t)b.n_parts << b.b2;
     const size_t tag = a.tag_bits ? kBucketTagSmem : 0;
     const size_t smem1 = bucket_smem<kBkTable>() + tag, smem2 = bucket_smem<kBkTable2>() + tag;
-    // SWG_BUCKET_SMALL: 0 keeps the 4096-entry tables, 2 takes the small ones
-    // for every untagged build, unset or 1 picks by the mean bucket size
-    static const int small_mode = [] {
-        const char *e = std::getenv("SWG_BUCKET_SMALL");
-        return e ? std::atoi(e) : 1;
-    }();
-    if (small_mode && !a.tag_bits && (small_mode == 2 || b.n_rec <= kBkSmallRecords * nb)) {
+    if (bucket_count_table(a, b) == kBkTableS) {  // small buckets on average
         const size_t smemS = bucket_smem<kBkTableS>();
         cudaFuncSetAttribute(k_bucket_count_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemS);
         const uint64_t grid = std::min<uint64_t>(nb, resident_grid(k_bucket_count_small, kBkThreadsS, smemS));

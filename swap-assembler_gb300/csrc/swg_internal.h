@@ -188,6 +188,9 @@ int launch_chunk_prefix(const BucketArgs &b, cudaStream_t s);
 int launch_sub_hist(const BucketArgs &b, cudaStream_t s);
 int launch_sub_scatter(const BucketArgs &b, cudaStream_t s);
 int launch_bucket_count(const BuildArgs &a, const BucketArgs &b, cudaStream_t s);
+// Entries of the tier-1 shared table launch_bucket_count uses for this build
+// (2048 for small untagged buckets, else 4096).
+int bucket_count_table(const BuildArgs &a, const BucketArgs &b);
 int launch_bucket_gather(const BuildArgs &a, const BucketArgs &b, uint64_t n_buckets, cudaStream_t s);
 int launch_group_by_sample(const unsigned long long *in_keys, const unsigned long long *in_mult,
                            uint64_t n, int tag_bits, uint32_t n_samples, unsigned long long *cursor,

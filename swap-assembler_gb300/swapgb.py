@@ -57,7 +57,7 @@ class BuildInfo(C.Structure):
                 ("distinct", C.c_uint64), ("survivors", C.c_uint64),
                 ("table_entries", C.c_uint64), ("partitions", C.c_uint32),
                 ("slots", C.c_uint32), ("waves", C.c_uint32), ("retries", C.c_uint32),
-                ("estimate", C.c_double), ("ms", C.c_float * 5)]
+                ("estimate", C.c_double), ("ms", C.c_float * 5), ("bucket_table", C.c_uint32)]
 
     def as_dict(self) -> dict:
         d = {name: getattr(self, name) for name, _ in self._fields_ if name != "ms"}

@@ -271,6 +271,26 @@ def test_bucketed_knobs_give_the_same_graph(knobs):
         swapgb.Graph().build_reads(swapgb.Opts(k=31, cutoff=5, part_bits=11), swapgb.reads_from_fasta(text, 31))
 
 
+@pytest.mark.parametrize("mode", ["auto", "0", "2"])
+@pytest.mark.parametrize("records", [2048, 8192])
+def test_tier1_table_choice(mode, records, monkeypatch):
+    """The first counting pass takes 2048-entry tables when the plan's buckets
+    average at most 3072 records (SWG_BUCKET_SMALL=0 / 2 force 4096 / 2048),
+    and either gives the same graph, with hot repeats overflowing to the later tiers."""
+    if mode != "auto":
+        monkeypatch.setenv("SWG_BUCKET_SMALL", mode)
+    text = synth_case_text("c2_small")
+    hot = "".join(">h%d\n%s\n" % (i, r) for i, r in enumerate(["ACGTTGCA" * 20] * 3000)).encode()
+    text = text + hot
+    g = swapgb.Graph().build_reads(swapgb.Opts(k=31, cutoff=5, algorithm=swapgb.ALGO_BUCKETED,
+                                               bucket_records=records), swapgb.reads_from_fasta(text, 31))
+    info = g.info()
+    small = info["occurrences"] <= 3072 * info["table_entries"]
+    want = {"auto": 2048 if small else 4096, "0": 4096, "2": 2048}[mode]
+    assert info["bucket_table"] == want, info
+    assert_same_records(g, text, 31, 5)
+
+
 def test_bucketed_large_input_and_hot_buckets():
     text = swapgb.synth_fasta(seed=23, genome_len=2_000_000, n_reads=1_000_000, read_len=100,
                               sub_rate=0.01, indel_rate=0.001)
