@@ -1471,19 +1471,22 @@ __global__ void __launch_bounds__(NT, MINB) k_sub_scatter(BucketArgs b) {
 // Level-2 scatter, one shared atomic per record: the histogram's atomicAdd
 // returns the record's rank within its bin, kept (16 bits each, two per
 // register) until the records are ordered by bin in shared memory.
-constexpr size_t kSubScatter2Dyn = kBkChunk * sizeof(unsigned long long) + kBkBinsMax * sizeof(BinDest) +
-                                   kBkBinsMax * 2 * sizeof(unsigned);
+// Its shared memory: the chunk, then per bin (2^b2 of them) its destination,
+// count and local offset.
+size_t sub_scatter2_smem(int b2) {
+    return kBkChunk * sizeof(unsigned long long) + ((size_t)1 << b2) * (sizeof(BinDest) + 2 * sizeof(unsigned));
+}
 
 template <int NT, int IT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) k_sub_scatter2(BucketArgs b) {
     static_assert(IT % 2 == 0, "ranks are packed two per register");
     extern __shared__ __align__(16) unsigned char dyn[];
+    const uint32_t P2 = 1u << b.b2;
     unsigned long long *sorted = reinterpret_cast<unsigned long long *>(dyn);
     BinDest *dest = reinterpret_cast<BinDest *>(sorted + NT * IT);
-    unsigned *hist = reinterpret_cast<unsigned *>(dest + kBkBinsMax);
-    unsigned *loff = hist + kBkBinsMax;
+    unsigned *hist = reinterpret_cast<unsigned *>(dest + P2);
+    unsigned *loff = hist + P2;
     __shared__ uint64_t wb[NT / 32];
-    const uint32_t P2 = 1u << b.b2;
     const uint32_t per = (P2 + NT - 1) / NT;  // bins per thread in the scan
     const int sh = 64 - b.b1 - b.b2 + 8;      // record >> sh = its bin (b2 > 0)
     const uint64_t nq = *b.status & kStatusPartOverflow ? 0 : b.chunk_start[b.n_parts];  // recount ahead
@@ -2439,19 +2442,25 @@ int launch_sub_scatter_shape(const BucketArgs &b, cudaStream_t s) {
     return 1;
 }
 
+// One shared atomic per record (the histogram's returns the rank).
+template <int NT, int IT, int MINB>
+int launch_sub_scatter2_shape(const BucketArgs &b, cudaStream_t s) {
+    static_assert(NT * IT == kBkChunk, "a level-2 chunk is one block's round");
+    auto kern = k_sub_scatter2<NT, IT, MINB>;
+    const uint64_t chunks = b.n_rec / kBkChunk + b.n_parts;
+    const size_t smem = sub_scatter2_smem(b.b2);
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const uint64_t grid = std::min<uint64_t>(chunks, resident_grid(kern, NT, smem));
+    kern<<<(unsigned)grid, NT, smem, s>>>(b);
+    return 1;
+}
+
 int launch_sub_scatter(const BucketArgs &b, cudaStream_t s) {
     if (!b.n_rec) return 0;
     switch (b.shape ? b.shape : scatter_shape()) {
         case 1: return launch_sub_scatter_shape<512, 8, 2>(b, s);
         case 2: return launch_sub_scatter_shape<512, 8, 3>(b, s);
-        default: {  // one shared atomic per record (the histogram's returns the rank)
-            auto kern = k_sub_scatter2<256, 16, 3>;
-            const uint64_t chunks = b.n_rec / kBkChunk + b.n_parts;
-            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSubScatter2Dyn);
-            const uint64_t grid = std::min<uint64_t>(chunks, resident_grid(kern, 256, kSubScatter2Dyn));
-            kern<<<(unsigned)grid, 256, kSubScatter2Dyn, s>>>(b);
-            return 1;
-        }
+        default: return launch_sub_scatter2_shape<256, 16, 3>(b, s);
         case 3: {  // bulk-copy staging (measured slower on GB300: 2 blocks/SM instead of 3)
             const uint64_t chunks = b.n_rec / kBkChunk + b.n_parts;
             cudaFuncSetAttribute(k_sub_scatter_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
