@@ -82,6 +82,16 @@ __device__ __forceinline__ uint32_t base_at(const uint32_t *__restrict__ p, uint
 
 __device__ __forceinline__ uint64_t umin64(uint64_t a, uint64_t b) { return a < b ? a : b; }
 
+// Asks L2 to fetch records [r0, r1) of a record array ahead of their loads
+// (one bulk prefetch from the calling thread). The range is narrowed to
+// whole 16-byte pairs of records inside it, as the bulk prefetch requires.
+__device__ __forceinline__ void prefetch_records_l2(const unsigned long long *rec, uint64_t r0, uint64_t r1) {
+    const uint64_t a = (r0 + 1) & ~1ull, e = r1 & ~1ull;
+    if (e <= a) return;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(rec + a), "r"((uint32_t)((e - a) * 8))
+                 : "memory");
+}
+
 __device__ __forceinline__ uint64_t occ_of(uint32_t len, int k) {
     return len >= (uint32_t)k ? (uint64_t)(len - (uint32_t)k + 1) : 0ull;
 }
@@ -1841,6 +1851,11 @@ __device__ void bucket_pass(const BuildArgs &a, const BucketArgs &b, uint64_t n_
         bucket_range(b, bk, rb, re);
         const uint64_t nrec = re - rb;
         if (threadIdx.x == 0 && b.cursor2[bk] > re) atomicOr(b.status, kStatusPartOverflow);
+        if (threadIdx.x == 0 && it + gridDim.x < n_items) {  // the next bucket, into L2
+            uint64_t nrb, nre;
+            bucket_range(b, list ? list[it + gridDim.x] : it + gridDim.x, nrb, nre);
+            prefetch_records_l2(b.rec2, nrb, nre);
+        }
         __syncthreads();  // the previous bucket's compaction (and the clear) is done
         if (threadIdx.x == 0) {
             s_over = 0;
