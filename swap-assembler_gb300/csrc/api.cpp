@@ -1380,7 +1380,10 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
             ac.n_reads = reads_c - reads;
             ac.total_occ = occ_c - occ;
             SWG_CUDA(cudaMemsetAsync(&g->d_ctl->work[1], 0, sizeof(unsigned long long), s), "clear work");
-            g->launches += swg::launch_part_scatter(ac, pl.pa, s, false);
+            // all but the last piece leave room for the framing of the next
+            // one (its kernels would otherwise wait for this scatter to end)
+            g->launches += swg::launch_part_scatter(ac, pl.pa, s,
+                                                    c + 1 < C ? swg::kScatterShared : swg::kScatterPerBatch);
             SWG_CUDA(cudaGetLastError(), "scatter launch");
         }
         NL = NLc;

@@ -116,16 +116,19 @@ __global__ void __launch_bounds__(kFBlock) k_gscan_reduce(const uint64_t *__rest
     if (threadIdx.x == 0) sums[blockIdx.x] = total;
 }
 
-__global__ void __launch_bounds__(1024) k_gscan_blocks(uint64_t *sums, uint64_t nb, uint64_t *total) {
-    __shared__ uint64_t wb[32];
+// One block of kFBlock threads: a block this size finds room on an SM that
+// a concurrent kernel of the same block size leaves (the streamed build's
+// framing runs beside the level-1 scatter).
+__global__ void __launch_bounds__(kFBlock) k_gscan_blocks(uint64_t *sums, uint64_t nb, uint64_t *total) {
+    __shared__ uint64_t wb[kFBlock / 32];
     __shared__ uint64_t carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    for (uint64_t base = 0; base < nb; base += 1024) {
+    for (uint64_t base = 0; base < nb; base += kFBlock) {
         const uint64_t i = base + threadIdx.x;
         const uint64_t v = i < nb ? sums[i] : 0;
         uint64_t t;
-        const uint64_t ex = block_exclusive_scan<1024>(v, wb, &t);
+        const uint64_t ex = block_exclusive_scan<kFBlock>(v, wb, &t);
         const uint64_t c = carry;
         if (i < nb) sums[i] = c + ex;
         __syncthreads();
@@ -300,7 +303,7 @@ int launch_gscan(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t *scratc
         return 0;
     }
     k_gscan_reduce<<<(unsigned)nb, kFBlock, 0, s>>>(in, n, scratch);
-    k_gscan_blocks<<<1, 1024, 0, s>>>(scratch, nb, total);
+    k_gscan_blocks<<<1, kFBlock, 0, s>>>(scratch, nb, total);
     k_gscan_write<<<(unsigned)nb, kFBlock, 0, s>>>(in, n, scratch, out);
     return 3;
 }

@@ -2375,17 +2375,20 @@ int scatter_shape() {
 }
 
 template <int NT, int IT, int MINB, int KC = 0, int B1C = 0>
-int launch_p1_scatter_shape(const BuildArgs &a, const PartArgs &p, cudaStream_t s, bool persistent) {
+int launch_p1_scatter_shape(const BuildArgs &a, const PartArgs &p, cudaStream_t s, int grid_mode) {
     auto kern = k_p1_scatter<NT, IT, MINB, KC, B1C>;
     const size_t smem = p1_scatter_smem(p.n_parts, NT * IT);
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const uint64_t batches = (a.n_reads + NT - 1) / NT;
-    const uint64_t grid = persistent ? std::min<uint64_t>(batches, resident_grid(kern, NT, smem)) : batches;
+    const uint64_t resident = resident_grid(kern, NT, smem), sms = device_sm_count();
+    uint64_t grid = batches;  // kScatterPerBatch
+    if (grid_mode == kScatterResident) grid = std::min(batches, resident);
+    if (grid_mode == kScatterShared) grid = std::min(batches, resident > sms ? resident - sms : resident);
     kern<<<(unsigned)grid, NT, smem, s>>>(a, p);
     return 1;
 }
 
-int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s, bool persistent) {
+int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s, int grid_mode) {
     if (a.total_occ == 0 || a.n_reads == 0) return 0;
     const int shape = p.shape ? p.shape : scatter_shape();
     if (shape == 4 && a.tile_first_read && a.n_tiles && !a.segs && !a.tag_bits) {
@@ -2398,21 +2401,21 @@ int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s, b
         return 1;
     }
     switch (shape) {  // shape 3 changes only the level-2 scatter, shape 4 only level 1
-        case 1: return launch_p1_scatter_shape<512, 8, 2>(a, p, s, persistent);
-        case 2: return launch_p1_scatter_shape<256, 8, 4>(a, p, s, persistent);
+        case 1: return launch_p1_scatter_shape<512, 8, 2>(a, p, s, grid_mode);
+        case 2: return launch_p1_scatter_shape<256, 8, 4>(a, p, s, grid_mode);
         default:
             // single-sample builds with 256 partitions and a common k: the walk's
             // shifts and masks and the record layout are compile-time constants
             if (!a.segs && !a.read_seg && !a.tag_bits && p.bits == 8) switch (a.k) {
-                    case 31: return launch_p1_scatter_shape<256, 16, 3, 31, 8>(a, p, s, persistent);
-                    case 27: return launch_p1_scatter_shape<256, 16, 3, 27, 8>(a, p, s, persistent);
-                    case 25: return launch_p1_scatter_shape<256, 16, 3, 25, 8>(a, p, s, persistent);
-                    case 21: return launch_p1_scatter_shape<256, 16, 3, 21, 8>(a, p, s, persistent);
+                    case 31: return launch_p1_scatter_shape<256, 16, 3, 31, 8>(a, p, s, grid_mode);
+                    case 27: return launch_p1_scatter_shape<256, 16, 3, 27, 8>(a, p, s, grid_mode);
+                    case 25: return launch_p1_scatter_shape<256, 16, 3, 25, 8>(a, p, s, grid_mode);
+                    case 21: return launch_p1_scatter_shape<256, 16, 3, 21, 8>(a, p, s, grid_mode);
                     default: break;
                 }
             if (!a.segs && !a.read_seg && !a.tag_bits && p.bits == 9 && a.k == 31)  // past 400M occurrences
-                return launch_p1_scatter_shape<256, 16, 3, 31, 9>(a, p, s, persistent);
-            return launch_p1_scatter_shape<256, 16, 3>(a, p, s, persistent);
+                return launch_p1_scatter_shape<256, 16, 3, 31, 9>(a, p, s, grid_mode);
+            return launch_p1_scatter_shape<256, 16, 3>(a, p, s, grid_mode);
     }
 }
 

@@ -161,7 +161,12 @@ int launch_big_multi(const BuildArgs &a, const BucketArgs &b, const unsigned lon
 // persistent: at most the resident blocks, each taking read batches until
 // none is left; else one block per batch (blocks retire as they finish, so
 // other streams' kernels get SMs during the scatter)
-int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s, bool persistent = true);
+// Grid of the level-1 scatter: one block per batch of reads (blocks retire
+// as they finish), as many blocks as stay resident (each takes batches until
+// none are left), or one block per SM fewer than that, leaving room on every
+// SM for the kernels of a concurrent stream (the streamed build's framing).
+enum { kScatterPerBatch = 0, kScatterResident = 1, kScatterShared = 2 };
+int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s, int grid_mode = kScatterResident);
 int launch_part_wave(const BuildArgs &a, const PartArgs &p, uint32_t p0, uint32_t n,
                      uint64_t rec_begin, uint64_t rec_end, cudaStream_t s);
 // Device FASTA framing (framing.cu).
