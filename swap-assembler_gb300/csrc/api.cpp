@@ -1225,7 +1225,7 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
         cut[c] = (first_blocks + (nc - first_blocks) * (c - 1) / (C - 1)) * swg::kFramingChunk;
     cut[C] = n;
     if (!g->copy) SWG_CUDA(cudaStreamCreateWithFlags(&g->copy, cudaStreamNonBlocking), "copy stream");
-    if (!g->frame) {  // the framing stream's blocks go first as the scatter's retire
+    if (!g->frame) {  // highest priority; the scatters of earlier pieces leave it an SM slot
         int least = 0, greatest = 0;
         SWG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
         SWG_CUDA(cudaStreamCreateWithPriority(&g->frame, cudaStreamNonBlocking, greatest), "framing stream");
