@@ -162,8 +162,8 @@ struct swg_graph {
     uint64_t sfw_cap = 0;
     uint64_t *d_nl = nullptr;
     uint64_t nl_cap = 0;
-    uint64_t *d_keep = nullptr, *d_words = nullptr, *d_ridx = nullptr, *d_woff = nullptr;
-    uint64_t keep_cap = 0, words_cap = 0, ridx_cap = 0, woff_cap = 0;
+    uint64_t *d_ridx = nullptr, *d_woff = nullptr;  // per record: read index, first word
+    uint64_t ridx_cap = 0, woff_cap = 0;
     // swg_graph_build_fasta_file: pinned host buffer the file is read into
     // (kept and reused by later calls of this handle)
     char *h_file = nullptr;
@@ -1261,7 +1261,7 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
     } drain{g->copy, F};
     // workspace: block counts [nc] | block bases [nc] | scan scratch [S] | totals [8]
     // totals: newlines, reads, words, occurrences, longest read, NUL flag
-    const uint64_t S = std::max(swg::gscan_scratch(nc), swg::gscan_scratch(n / 2 + 1));
+    const uint64_t S = std::max(swg::gscan_scratch(nc), swg::rec_scan_scratch(n / 2 + 1));
     if ((st = ensure(&g->d_sfw, &g->sfw_cap, 2 * nc + S + 8, "framing workspace"))) return st;
     uint64_t *counts = g->d_sfw, *cbase = counts + nc, *scratch = cbase + nc, *tot = scratch + S;
     auto *acc = reinterpret_cast<unsigned long long *>(tot + 3);
@@ -1311,17 +1311,13 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
         if ((st = grow_keep(&g->d_nl, &g->nl_cap, g->nl_cap >= NLc ? NLc : nl_want, NL, "newline positions")))
             return st;
         const uint64_t r_want = std::max<uint64_t>(Rc, (uint64_t)(scale * 1.1 * (double)Rc) + 1024);
-        const uint64_t rw = g->keep_cap >= Rc ? Rc : r_want;
-        if ((st = grow_keep(&g->d_keep, &g->keep_cap, rw, R, "record flags")) ||
-            (st = grow_keep(&g->d_words, &g->words_cap, rw, R, "record words")) ||
-            (st = grow_keep(&g->d_ridx, &g->ridx_cap, rw, R, "read index")) ||
+        const uint64_t rw = g->ridx_cap >= Rc ? Rc : r_want;
+        if ((st = grow_keep(&g->d_ridx, &g->ridx_cap, rw, R, "read index")) ||
             (st = grow_keep(&g->d_woff, &g->woff_cap, rw, R, "word offsets")))
             return st;
         launches += swg::launch_nl_pos(g->d_text, end, cbase, g->d_nl, F, j0);
-        launches += swg::launch_rec_len(g->d_nl, Rc, o->k, g->d_keep, g->d_words, F, R, acc);
         // this piece's records only: prefixes from 0, the totals so far added when packing
-        launches += swg::launch_gscan(g->d_keep + R, g->d_ridx + R, Rc - R, scratch, tot + 1, F);
-        launches += swg::launch_gscan(g->d_words + R, g->d_woff + R, Rc - R, scratch, tot + 2, F);
+        launches += swg::launch_rec_scan(g->d_nl, R, Rc, o->k, scratch, g->d_ridx, g->d_woff, tot + 1, acc, F);
         SWG_CUDA(cudaGetLastError(), "framing launch");
         SWG_CUDA(cudaMemcpyAsync(h, tot, sizeof(h), cudaMemcpyDeviceToHost, F), "read framing totals");
         SWG_CUDA(cudaStreamSynchronize(F), "framing scan");
@@ -1532,8 +1528,6 @@ void swg_graph_free(swg_graph *g) {
     cudaFree(g->d_slices);
     cudaFree(g->d_sfw);
     cudaFree(g->d_nl);
-    cudaFree(g->d_keep);
-    cudaFree(g->d_words);
     cudaFree(g->d_ridx);
     cudaFree(g->d_woff);
     if (g->h_file) cudaFreeHost(g->h_file);
@@ -1612,7 +1606,7 @@ swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *te
     SWG_CUDA(cudaMemcpyAsync(g->d_text, first, n, cudaMemcpyHostToDevice, s), "copy FASTA text");
     const uint64_t nc = swg::framing_chunks(n);
     // workspace: counts [nc] | scratch [S] | total [2] | newline positions [nl] | records x3
-    const uint64_t S = std::max(swg::gscan_scratch(nc), swg::gscan_scratch(n / 2 + 1));
+    const uint64_t S = std::max(swg::gscan_scratch(nc), swg::rec_scan_scratch(n / 2 + 1));
     uint64_t want = nc + S + 2;
     if ((st = ensure(&g->d_fw, &g->fw_cap, want, "framing workspace"))) return st;
     uint64_t *counts = g->d_fw, *scratch = counts + nc, *tot = scratch + S;
@@ -1634,7 +1628,7 @@ swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *te
         return SWG_ERR_BAD_INPUT;
     }
     const uint64_t R = NL / 2;
-    want = nc + S + 2 + NL + 3 * std::max<uint64_t>(R, 1);
+    want = nc + S + 2 + NL + 2 * std::max<uint64_t>(R, 1);
     if (want > g->fw_cap) {  // grow, keeping the chunk bases computed above
         uint64_t *nw = nullptr;
         SWG_CUDA(cudaMalloc(&nw, want * 8), "framing workspace");
@@ -1648,11 +1642,9 @@ swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *te
         scratch = counts + nc;
         tot = scratch + S;
     }
-    uint64_t *nl = tot + 2, *keep = nl + NL, *words = keep + R, *idx = words + R;
+    uint64_t *nl = tot + 2, *idx = nl + NL, *words = idx + R;
     launches += swg::launch_nl_pos(g->d_text, n, counts, nl, s);
-    launches += swg::launch_rec_len(nl, R, o->k, keep, words, s);
-    launches += swg::launch_gscan(keep, idx, R, scratch, tot, s);
-    launches += swg::launch_gscan(words, words, R, scratch, tot + 1, s);
+    launches += swg::launch_rec_scan(nl, 0, R, o->k, scratch, idx, words, tot, nullptr, s);
     SWG_CUDA(cudaGetLastError(), "framing launch");
     SWG_CUDA(cudaMemcpyAsync(h, tot, 16, cudaMemcpyDeviceToHost, s), "read framing totals");
     SWG_CUDA(cudaStreamSynchronize(s), "framing scan");

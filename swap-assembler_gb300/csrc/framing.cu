@@ -101,6 +101,33 @@ __global__ void __launch_bounds__(kFBlock) k_nl_pos(const unsigned char *__restr
     }
 }
 
+// Exclusive scan of at most a few kGChunk items by one block (in place
+// allowed): one launch where the three-kernel scan would take three.
+__global__ void __launch_bounds__(kFBlock) k_gscan_small(const uint64_t *in, uint64_t n, uint64_t *out,
+                                                         uint64_t *total) {
+    __shared__ uint64_t wb[kFBlock / 32];
+    uint64_t carry = 0;
+    for (uint64_t b0 = 0; b0 < n; b0 += kGChunk) {
+        const uint64_t base = b0 + (uint64_t)threadIdx.x * kGItems;
+        uint64_t v[kGItems];
+        uint64_t s = 0;
+#pragma unroll
+        for (int it = 0; it < kGItems; ++it) {
+            v[it] = base + it < n ? in[base + it] : 0;
+            s += v[it];
+        }
+        uint64_t t;
+        uint64_t run = carry + block_exclusive_scan<kFBlock>(s, wb, &t);
+#pragma unroll
+        for (int it = 0; it < kGItems; ++it) {
+            if (base + it < n) out[base + it] = run;
+            run += v[it];
+        }
+        carry += t;
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
 // Generic exclusive scan of uint64 (in place allowed).
 __global__ void __launch_bounds__(kFBlock) k_gscan_reduce(const uint64_t *__restrict__ in, uint64_t n,
                                                           uint64_t *__restrict__ sums) {
@@ -158,28 +185,46 @@ __global__ void __launch_bounds__(kFBlock) k_gscan_write(const uint64_t *in, uin
     }
 }
 
-// Records r0 <= r < r1: header line 2r, sequence line 2r+1 (line 0 starts at
-// byte 0). With acc, the kept reads' k-mer occurrences are added to acc[0]
-// and their longest length maxed into acc[1].
-__global__ void k_rec_len(const uint64_t *__restrict__ nl, uint64_t r0, uint64_t r1, int k,
-                          uint64_t *__restrict__ keep, uint64_t *__restrict__ words,
-                          unsigned long long *__restrict__ acc) {
-    const uint64_t r = r0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// Record r's sequence length (line 2r+1; header line 2r before it).
+__device__ __forceinline__ uint64_t rec_length(const uint64_t *__restrict__ nl, uint64_t r) {
+    return nl[2 * r + 1] - nl[2 * r] - 1;
+}
+
+// The record scan in three kernels (a scan of records r0 <= r < r1 in blocks
+// of kGChunk): per block the kept records (length >= k) and their 16-base
+// words are summed (and, with acc, the kept reads' k-mer occurrences added
+// to acc[0] and their longest length maxed into acc[1]); one block scans the
+// two columns of block sums (totals to tot[0], tot[1]); then every record
+// gets its read index (kept records before it) and first word, from r0 on.
+__global__ void __launch_bounds__(kFBlock) k_rec_reduce(const uint64_t *__restrict__ nl, uint64_t r0,
+                                                        uint64_t r1, int k, uint64_t *__restrict__ sums,
+                                                        unsigned long long *__restrict__ acc) {
+    __shared__ uint64_t wb[kFBlock / 32];
+    const uint64_t base = r0 + (uint64_t)blockIdx.x * kGChunk;
+    uint64_t keep = 0, words = 0;
     unsigned long long occ = 0, mx = 0;
-    if (r < r1) {
-        const uint64_t start = nl[2 * r] + 1, end = nl[2 * r + 1];
-        const uint64_t L = end - start;
-        const bool ok = L >= (uint64_t)k;
-        keep[r] = ok ? 1 : 0;
-        words[r] = ok ? (L + 15) / 16 : 0;
-        if (ok) {
-            occ = L - (uint64_t)k + 1;
-            mx = L;
+    for (int it = 0; it < kGItems; ++it) {
+        const uint64_t r = base + (uint64_t)it * kFBlock + threadIdx.x;
+        if (r < r1) {
+            const uint64_t L = rec_length(nl, r);
+            if (L >= (uint64_t)k) {
+                keep++;
+                words += (L + 15) / 16;
+                occ += L - (uint64_t)k + 1;
+                mx = L > mx ? L : mx;
+            }
         }
+    }
+    uint64_t tk, tw;
+    block_exclusive_scan<kFBlock>(keep, wb, &tk);
+    block_exclusive_scan<kFBlock>(words, wb, &tw);
+    if (threadIdx.x == 0) {
+        sums[2 * blockIdx.x] = tk;
+        sums[2 * blockIdx.x + 1] = tw;
     }
     if (!acc) return;
 #pragma unroll
-    for (int d = 16; d; d >>= 1) {  // blockDim is a multiple of 32: whole warps
+    for (int d = 16; d; d >>= 1) {
         occ += __shfl_down_sync(0xffffffffu, occ, d);
         const unsigned long long y = __shfl_down_sync(0xffffffffu, mx, d);
         mx = y > mx ? y : mx;
@@ -187,6 +232,63 @@ __global__ void k_rec_len(const uint64_t *__restrict__ nl, uint64_t r0, uint64_t
     if ((threadIdx.x & 31) == 0 && occ) {
         atomicAdd(&acc[0], occ);
         atomicMax(&acc[1], mx);
+    }
+}
+
+__global__ void __launch_bounds__(kFBlock) k_rec_blocks(uint64_t *sums, uint64_t nb, uint64_t *tot) {
+    __shared__ uint64_t wb[kFBlock / 32];
+    __shared__ uint64_t carry[2];
+    if (threadIdx.x < 2) carry[threadIdx.x] = 0;
+    __syncthreads();
+    for (uint64_t b0 = 0; b0 < nb; b0 += kFBlock) {
+        const uint64_t i = b0 + threadIdx.x;
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const uint64_t v = i < nb ? sums[2 * i + c] : 0;
+            uint64_t t;
+            const uint64_t ex = block_exclusive_scan<kFBlock>(v, wb, &t);
+            const uint64_t cc = carry[c];
+            if (i < nb) sums[2 * i + c] = cc + ex;
+            __syncthreads();
+            if (threadIdx.x == 0) carry[c] = cc + t;
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x < 2) tot[threadIdx.x] = carry[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kFBlock) k_rec_write(const uint64_t *__restrict__ nl, uint64_t r0,
+                                                       uint64_t r1, int k, const uint64_t *__restrict__ sums,
+                                                       uint64_t *__restrict__ read_idx,
+                                                       uint64_t *__restrict__ word_off) {
+    __shared__ uint64_t wb[kFBlock / 32];
+    const uint64_t base = r0 + (uint64_t)blockIdx.x * kGChunk + (uint64_t)threadIdx.x * kGItems;
+    uint32_t kept = 0;  // bit i: record base + i kept
+    uint64_t wds[kGItems];
+    uint64_t sk = 0, sw = 0;
+#pragma unroll
+    for (int it = 0; it < kGItems; ++it) {
+        wds[it] = 0;
+        if (base + it < r1) {
+            const uint64_t L = rec_length(nl, base + it);
+            if (L >= (uint64_t)k) {
+                kept |= 1u << it;
+                wds[it] = (L + 15) / 16;
+            }
+        }
+        sk += (kept >> it) & 1u;
+        sw += wds[it];
+    }
+    uint64_t rk = sums[2 * blockIdx.x] + block_exclusive_scan<kFBlock>(sk, wb, nullptr);
+    uint64_t rw = sums[2 * blockIdx.x + 1] + block_exclusive_scan<kFBlock>(sw, wb, nullptr);
+#pragma unroll
+    for (int it = 0; it < kGItems; ++it) {
+        if (base + it < r1) {
+            read_idx[base + it] = rk;
+            word_off[base + it] = rw;
+        }
+        rk += (kept >> it) & 1u;
+        rw += wds[it];
     }
 }
 
@@ -302,9 +404,29 @@ int launch_gscan(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t *scratc
         cudaMemsetAsync(total, 0, sizeof(uint64_t), s);
         return 0;
     }
+    if (nb <= 2) {
+        k_gscan_small<<<1, kFBlock, 0, s>>>(in, n, out, total);
+        return 1;
+    }
     k_gscan_reduce<<<(unsigned)nb, kFBlock, 0, s>>>(in, n, scratch);
     k_gscan_blocks<<<1, kFBlock, 0, s>>>(scratch, nb, total);
     k_gscan_write<<<(unsigned)nb, kFBlock, 0, s>>>(in, n, scratch, out);
+    return 3;
+}
+
+uint64_t rec_scan_scratch(uint64_t n_rec) { return 2 * ((n_rec + kGChunk - 1) / kGChunk) + 2; }
+
+int launch_rec_scan(const uint64_t *nl, uint64_t r0, uint64_t n_rec, int k, uint64_t *scratch,
+                    uint64_t *read_idx, uint64_t *word_off, uint64_t *tot, unsigned long long *acc,
+                    cudaStream_t s) {
+    const uint64_t nb = n_rec > r0 ? (n_rec - r0 + kGChunk - 1) / kGChunk : 0;
+    if (nb == 0) {
+        cudaMemsetAsync(tot, 0, 2 * sizeof(uint64_t), s);
+        return 0;
+    }
+    k_rec_reduce<<<(unsigned)nb, kFBlock, 0, s>>>(nl, r0, n_rec, k, scratch, acc);
+    k_rec_blocks<<<1, kFBlock, 0, s>>>(scratch, nb, tot);
+    k_rec_write<<<(unsigned)nb, kFBlock, 0, s>>>(nl, r0, n_rec, k, scratch, read_idx, word_off);
     return 3;
 }
 
@@ -321,13 +443,6 @@ int launch_nl_pos(const unsigned char *t, uint64_t n, const uint64_t *chunk_base
     const uint64_t nc = framing_chunks(n);
     if (nc <= j0) return 0;
     k_nl_pos<<<(unsigned)(nc - j0), kFBlock, 0, s>>>(t, n, chunk_base, nl, j0);
-    return 1;
-}
-
-int launch_rec_len(const uint64_t *nl, uint64_t n_rec, int k, uint64_t *keep, uint64_t *words,
-                   cudaStream_t s, uint64_t r0, unsigned long long *acc) {
-    if (n_rec <= r0) return 0;
-    k_rec_len<<<(unsigned)((n_rec - r0 + 255) / 256), 256, 0, s>>>(nl, r0, n_rec, k, keep, words, acc);
     return 1;
 }
 

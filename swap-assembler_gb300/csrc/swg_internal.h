@@ -182,8 +182,14 @@ int launch_nl_count(const unsigned char *t, uint64_t n, uint64_t *counts, unsign
                     cudaStream_t s, uint64_t j0 = 0);
 int launch_nl_pos(const unsigned char *t, uint64_t n, const uint64_t *chunk_base, uint64_t *nl,
                   cudaStream_t s, uint64_t j0 = 0);
-int launch_rec_len(const uint64_t *nl, uint64_t n_rec, int k, uint64_t *keep, uint64_t *words,
-                   cudaStream_t s, uint64_t r0 = 0, unsigned long long *acc = nullptr);
+// Records r0 <= r < n_rec: read_idx[r] / word_off[r] = kept records (length
+// >= k) / their 16-base words before r, from r0; totals to tot[0], tot[1];
+// with acc, the kept reads' k-mer occurrences added to acc[0] and their
+// longest length maxed into acc[1]. scratch holds rec_scan_scratch(n) words.
+uint64_t rec_scan_scratch(uint64_t n_rec);
+int launch_rec_scan(const uint64_t *nl, uint64_t r0, uint64_t n_rec, int k, uint64_t *scratch,
+                    uint64_t *read_idx, uint64_t *word_off, uint64_t *tot, unsigned long long *acc,
+                    cudaStream_t s);
 int launch_rec_pack(const unsigned char *t, const uint64_t *nl, uint64_t n_rec, int k,
                     const uint64_t *read_idx, const uint64_t *word_off, uint64_t *off,
                     uint32_t *len, uint32_t *packed, cudaStream_t s, uint64_t r0 = 0,
