@@ -115,7 +115,7 @@ struct swg_graph {
     // device framing workspace
     unsigned char *d_text = nullptr;
     uint64_t text_cap = 0;
-    uint64_t *d_fw = nullptr;  // chunk counts | scan scratch | newline positions | records x3
+    uint64_t *d_fw = nullptr;  // chunk counts | scan scratch | newline masks and positions | records x2
     uint64_t fw_cap = 0;
     // bucketed workspace
     unsigned long long *d_rec2 = nullptr;
@@ -1260,10 +1260,12 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
         }
     } drain{g->copy, F};
     // workspace: block counts [nc] | block bases [nc] | scan scratch [S] | totals [8]
-    // totals: newlines, reads, words, occurrences, longest read, NUL flag
+    // | newline masks; totals: newlines, reads, words, occurrences, longest read, NUL flag
     const uint64_t S = std::max(swg::gscan_scratch(nc), swg::rec_scan_scratch(n / 2 + 1));
-    if ((st = ensure(&g->d_sfw, &g->sfw_cap, 2 * nc + S + 8, "framing workspace"))) return st;
+    if ((st = ensure(&g->d_sfw, &g->sfw_cap, 2 * nc + S + 8 + swg::newline_mask_words(n), "framing workspace")))
+        return st;
     uint64_t *counts = g->d_sfw, *cbase = counts + nc, *scratch = cbase + nc, *tot = scratch + S;
+    uint64_t *masks = tot + 8;
     auto *acc = reinterpret_cast<unsigned long long *>(tot + 3);
     unsigned *nul_flag = reinterpret_cast<unsigned *>(tot + 5);
     SWG_CUDA(cudaMemsetAsync(tot, 0, 8 * 8, F), "clear framing totals");
@@ -1295,7 +1297,7 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
     for (uint64_t c = 0; c < C; ++c) {
         SWG_CUDA(cudaStreamWaitEvent(F, copied[c], 0), "piece wait");
         const uint64_t j0 = cut[c] / swg::kFramingChunk, end = cut[c + 1];
-        launches += swg::launch_nl_count(g->d_text, end, counts, nul_flag, F, j0);
+        launches += swg::launch_nl_count(g->d_text, end, counts, masks, nul_flag, F, j0);
         launches += swg::launch_gscan(counts, cbase, swg::framing_chunks(end), scratch, tot, F);
         uint64_t h[6] = {0, 0, 0, 0, 0, 0};
         SWG_CUDA(cudaMemcpyAsync(h, tot, sizeof(h), cudaMemcpyDeviceToHost, F), "read newline count");
@@ -1315,7 +1317,7 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
         if ((st = grow_keep(&g->d_ridx, &g->ridx_cap, rw, R, "read index")) ||
             (st = grow_keep(&g->d_woff, &g->woff_cap, rw, R, "word offsets")))
             return st;
-        launches += swg::launch_nl_pos(g->d_text, end, cbase, g->d_nl, F, j0);
+        launches += swg::launch_nl_pos(masks, end, cbase, g->d_nl, F, j0);
         // this piece's records only: prefixes from 0, the totals so far added when packing
         launches += swg::launch_rec_scan(g->d_nl, R, Rc, o->k, scratch, g->d_ridx, g->d_woff, tot + 1, acc, F);
         SWG_CUDA(cudaGetLastError(), "framing launch");
@@ -1605,13 +1607,15 @@ swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *te
     if ((st = ensure(&g->d_text, &g->text_cap, n + 64, "FASTA text"))) return st;
     SWG_CUDA(cudaMemcpyAsync(g->d_text, first, n, cudaMemcpyHostToDevice, s), "copy FASTA text");
     const uint64_t nc = swg::framing_chunks(n);
-    // workspace: counts [nc] | scratch [S] | total [2] | newline positions [nl] | records x3
+    // workspace: counts [nc] | scratch [S] | total [2] | newline masks [MW] |
+    // newline positions [nl] | per record: read index, first word
     const uint64_t S = std::max(swg::gscan_scratch(nc), swg::rec_scan_scratch(n / 2 + 1));
-    uint64_t want = nc + S + 2;
+    const uint64_t MW = swg::newline_mask_words(n);
+    uint64_t want = nc + S + 2 + MW;
     if ((st = ensure(&g->d_fw, &g->fw_cap, want, "framing workspace"))) return st;
     uint64_t *counts = g->d_fw, *scratch = counts + nc, *tot = scratch + S;
     SWG_CUDA(cudaMemsetAsync(g->d_ctl, 0, sizeof(unsigned), s), "clear flag");
-    int launches = swg::launch_nl_count(g->d_text, n, counts, &g->d_ctl->status, s);
+    int launches = swg::launch_nl_count(g->d_text, n, counts, tot + 2, &g->d_ctl->status, s);
     launches += swg::launch_gscan(counts, counts, nc, scratch, tot, s);
     uint64_t h[2] = {0, 0};
     unsigned nul = 0;
@@ -1628,11 +1632,11 @@ swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *te
         return SWG_ERR_BAD_INPUT;
     }
     const uint64_t R = NL / 2;
-    want = nc + S + 2 + NL + 2 * std::max<uint64_t>(R, 1);
-    if (want > g->fw_cap) {  // grow, keeping the chunk bases computed above
+    want = nc + S + 2 + MW + NL + 2 * std::max<uint64_t>(R, 1);
+    if (want > g->fw_cap) {  // grow, keeping the chunk bases and the newline masks computed above
         uint64_t *nw = nullptr;
         SWG_CUDA(cudaMalloc(&nw, want * 8), "framing workspace");
-        SWG_CUDA(cudaMemcpyAsync(nw, g->d_fw, (nc + S + 2) * 8, cudaMemcpyDeviceToDevice, s),
+        SWG_CUDA(cudaMemcpyAsync(nw, g->d_fw, (nc + S + 2 + MW) * 8, cudaMemcpyDeviceToDevice, s),
                  "copy framing workspace");
         SWG_CUDA(cudaStreamSynchronize(s), "framing workspace");
         cudaFree(g->d_fw);
@@ -1642,8 +1646,8 @@ swg_status swg_graph_build_fasta(swg_graph *g, const swg_opts *o, const char *te
         scratch = counts + nc;
         tot = scratch + S;
     }
-    uint64_t *nl = tot + 2, *idx = nl + NL, *words = idx + R;
-    launches += swg::launch_nl_pos(g->d_text, n, counts, nl, s);
+    uint64_t *masks = tot + 2, *nl = masks + MW, *idx = nl + NL, *words = idx + R;
+    launches += swg::launch_nl_pos(masks, n, counts, nl, s);
     launches += swg::launch_rec_scan(nl, 0, R, o->k, scratch, idx, words, tot, nullptr, s);
     SWG_CUDA(cudaGetLastError(), "framing launch");
     SWG_CUDA(cudaMemcpyAsync(h, tot, 16, cudaMemcpyDeviceToHost, s), "read framing totals");

@@ -57,47 +57,47 @@ __device__ __forceinline__ void load_words(const unsigned char *__restrict__ t, 
 // 0xff in every byte of x equal to '\n'.
 __device__ __forceinline__ uint32_t nl_mask(uint32_t x) { return __vcmpeq4(x, 0x0a0a0a0au); }
 
-// Newlines per chunk (chunks j0 + blockIdx.x); any NUL byte raises flag.
+// Newlines per chunk (chunks j0 + blockIdx.x), and per thread's kFBytes
+// bytes a bit mask of them (bit b: byte b is a newline) for k_nl_pos, which
+// then reads 1/8 of what the text is; any NUL byte raises flag.
+static_assert(kFBytes == 64, "one 64-bit newline mask per thread");
 __global__ void __launch_bounds__(kFBlock) k_nl_count(const unsigned char *__restrict__ t, uint64_t n,
                                                       uint64_t *__restrict__ counts,
+                                                      unsigned long long *__restrict__ masks,
                                                       unsigned *__restrict__ flag, uint64_t j0) {
     __shared__ uint64_t wb[kFBlock / 32];
     const uint64_t j = j0 + blockIdx.x;
     uint32_t w[kFBytes / 4];
     load_words(t, n, j * kFChunk + (uint64_t)threadIdx.x * kFBytes, w);
-    unsigned c = 0, z = 0;
+    unsigned z = 0;
+    unsigned long long m = 0;
 #pragma unroll
     for (int q = 0; q < kFBytes / 4; ++q) {
-        c += __popc(nl_mask(w[q])) >> 3;
+        const uint32_t e = nl_mask(w[q]);  // 0xff per newline byte
+        const uint32_t b = ((e >> 7) & 1u) | ((e >> 14) & 2u) | ((e >> 21) & 4u) | ((e >> 28) & 8u);
+        m |= (unsigned long long)b << (4 * q);
         z |= __vcmpeq4(w[q], 0u);
     }
+    masks[j * kFBlock + threadIdx.x] = m;
     uint64_t total;
-    block_exclusive_scan<kFBlock>(c, wb, &total);
+    block_exclusive_scan<kFBlock>((uint64_t)__popcll(m), wb, &total);
     if (threadIdx.x == 0) counts[j] = total;
     if (z) atomicOr(flag, 1u);
 }
 
-// Position of every newline of chunks j0 + blockIdx.x, in order.
-__global__ void __launch_bounds__(kFBlock) k_nl_pos(const unsigned char *__restrict__ t, uint64_t n,
+// Position of every newline of chunks j0 + blockIdx.x, in order, from the
+// masks k_nl_count left.
+__global__ void __launch_bounds__(kFBlock) k_nl_pos(const unsigned long long *__restrict__ masks,
                                                     const uint64_t *__restrict__ chunk_base,
                                                     uint64_t *__restrict__ nl, uint64_t j0) {
     __shared__ uint64_t wb[kFBlock / 32];
     const uint64_t j = j0 + blockIdx.x;
     const uint64_t base = j * kFChunk + (uint64_t)threadIdx.x * kFBytes;
-    uint32_t w[kFBytes / 4];
-    load_words(t, n, base, w);
-    unsigned c = 0;
-#pragma unroll
-    for (int q = 0; q < kFBytes / 4; ++q) c += __popc(nl_mask(w[q])) >> 3;
-    uint64_t pos = chunk_base[j] + block_exclusive_scan<kFBlock>(c, wb, nullptr);
-#pragma unroll
-    for (int q = 0; q < kFBytes / 4; ++q) {
-        uint32_t m = nl_mask(w[q]);
-        while (m) {
-            const int bit = __ffs(m) - 1;  // lowest set byte: bits bit..bit+7
-            nl[pos++] = base + 4 * q + (bit >> 3);
-            m &= ~(0xffu << bit);
-        }
+    unsigned long long m = masks[j * kFBlock + threadIdx.x];
+    uint64_t pos = chunk_base[j] + block_exclusive_scan<kFBlock>((uint64_t)__popcll(m), wb, nullptr);
+    while (m) {
+        nl[pos++] = base + (uint64_t)(__ffsll((long long)m) - 1);
+        m &= m - 1;
     }
 }
 
@@ -430,19 +430,23 @@ int launch_rec_scan(const uint64_t *nl, uint64_t r0, uint64_t n_rec, int k, uint
     return 3;
 }
 
-int launch_nl_count(const unsigned char *t, uint64_t n, uint64_t *counts, unsigned *flag,
+uint64_t newline_mask_words(uint64_t n) { return framing_chunks(n) * kFBlock; }
+
+int launch_nl_count(const unsigned char *t, uint64_t n, uint64_t *counts, uint64_t *masks, unsigned *flag,
                     cudaStream_t s, uint64_t j0) {
     const uint64_t nc = framing_chunks(n);
     if (nc <= j0) return 0;
-    k_nl_count<<<(unsigned)(nc - j0), kFBlock, 0, s>>>(t, n, counts, flag, j0);
+    k_nl_count<<<(unsigned)(nc - j0), kFBlock, 0, s>>>(t, n, counts, reinterpret_cast<unsigned long long *>(masks),
+                                                      flag, j0);
     return 1;
 }
 
-int launch_nl_pos(const unsigned char *t, uint64_t n, const uint64_t *chunk_base, uint64_t *nl,
-                  cudaStream_t s, uint64_t j0) {
+int launch_nl_pos(const uint64_t *masks, uint64_t n, const uint64_t *chunk_base, uint64_t *nl, cudaStream_t s,
+                  uint64_t j0) {
     const uint64_t nc = framing_chunks(n);
     if (nc <= j0) return 0;
-    k_nl_pos<<<(unsigned)(nc - j0), kFBlock, 0, s>>>(t, n, chunk_base, nl, j0);
+    k_nl_pos<<<(unsigned)(nc - j0), kFBlock, 0, s>>>(reinterpret_cast<const unsigned long long *>(masks),
+                                                    chunk_base, nl, j0);
     return 1;
 }
 

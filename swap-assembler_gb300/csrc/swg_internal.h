@@ -178,9 +178,12 @@ int launch_gscan(const uint64_t *in, uint64_t *out, uint64_t n, uint64_t *scratc
 // n_rec (a streamed build frames the text a piece at a time); a record's
 // read index and first word are read_base + read_idx[r], word_base +
 // word_off[r].
-int launch_nl_count(const unsigned char *t, uint64_t n, uint64_t *counts, unsigned *flag,
+// The newline count leaves a bit mask of the newlines (newline_mask_words(n)
+// words for a text of n bytes) that the newline positions are read from.
+uint64_t newline_mask_words(uint64_t n);
+int launch_nl_count(const unsigned char *t, uint64_t n, uint64_t *counts, uint64_t *masks, unsigned *flag,
                     cudaStream_t s, uint64_t j0 = 0);
-int launch_nl_pos(const unsigned char *t, uint64_t n, const uint64_t *chunk_base, uint64_t *nl,
+int launch_nl_pos(const uint64_t *masks, uint64_t n, const uint64_t *chunk_base, uint64_t *nl,
                   cudaStream_t s, uint64_t j0 = 0);
 // Records r0 <= r < n_rec: read_idx[r] / word_off[r] = kept records (length
 // >= k) / their 16-base words before r, from r0; totals to tot[0], tot[1];
