@@ -307,9 +307,10 @@ __device__ __forceinline__ uint32_t code_of(unsigned char ch) {
 // words out, and the lanes then build those words round-robin — every lane
 // busy, each on the record its word falls in (binary search over the 33
 // prefixes). A word (16 bases, first base in the top bits) comes from two
-// aligned 16-byte loads of the text shifted by the record's alignment, every
-// byte mapped through a 256-entry table. The text buffer has 64 bytes of
-// slack past its end.
+// aligned 16-byte loads of the text shifted by the record's alignment; four
+// upper-case ACGT bytes at a time are mapped arithmetically, any other group
+// of four byte by byte through a 256-entry table. Bases past the read are
+// cleared. The text buffer has 64 bytes of slack past its end.
 __global__ void __launch_bounds__(256) k_rec_pack(const unsigned char *__restrict__ t,
                                                   const uint64_t *__restrict__ nl, uint64_t r0,
                                                   uint64_t n_rec, int k,
@@ -378,13 +379,21 @@ __global__ void __launch_bounds__(256) k_rec_pack(const unsigned char *__restric
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 const uint32_t x = __funnelshift_r(sel[i], sel[i + 1], sh);
+                // upper-case A, C, G, T give ((b >> 1) ^ (b >> 2)) & 3 = 0, 1, 2, 3: four
+                // such bytes are recognised by mapping their codes back to letters
+                const uint32_t c = ((x >> 1) ^ (x >> 2)) & 0x03030303u;
+                const uint32_t pick = __byte_perm(c | (c >> 4), 0, 0x0020);  // codes as selector nibbles
+                uint32_t q4;
+                if (__byte_perm(0x54474341u, 0, pick) == x) {  // "ACGT" indexed by the codes
+                    q4 = (c * 0x40100401u) >> 24;                // code of byte b to bits 6-2b
+                } else {
+                    q4 = 0;
 #pragma unroll
-                for (int bb = 0; bb < 4; ++bb) {
-                    const int jj = 4 * i + bb;
-                    const uint32_t c = (uint32_t)jj < left ? (uint32_t)lut[(x >> (8 * bb)) & 0xffu] : 0u;
-                    word |= c << (30 - 2 * jj);
+                    for (int bb = 0; bb < 4; ++bb) q4 |= (uint32_t)lut[(x >> (8 * bb)) & 0xffu] << (6 - 2 * bb);
                 }
+                word |= q4 << (24 - 8 * i);
             }
+            if (left < 16) word &= 0xffffffffu << (32 - 2 * left);  // 1 <= left: bases past the read
             packed[s_w0[wp][lo] + w] = word;
         }
         __syncwarp();
