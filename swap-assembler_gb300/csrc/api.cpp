@@ -1191,7 +1191,7 @@ swg_status grow_keep(T **p, uint64_t *cap, uint64_t want, uint64_t keep, const c
 }
 
 constexpr uint64_t kStreamMin = 96ull << 20;    // shorter texts go up and are framed in one piece
-constexpr uint64_t kStreamPiece = 64ull << 20;  // target bytes per piece
+constexpr uint64_t kStreamPiece = 40ull << 20;  // target bytes per piece
 constexpr uint64_t kStreamMaxPieces = 16;
 
 // Streamed FASTA build (texts of kStreamMin bytes and more). The text goes
@@ -1199,17 +1199,20 @@ constexpr uint64_t kStreamMaxPieces = 16;
 // lands — newline counts, newline positions, the records completed so far,
 // their packing — and, on the bucketed path, the build stream scatters that
 // piece's reads to the level-1 partitions while the next pieces are copied
-// and framed. The framing stream's host round trips (record and word totals)
-// never wait for a scatter. The partition and bucket regions are sized from
-// the first piece: its occurrences per text byte scale to the whole text (a
+// and framed. The first piece is framed with host round trips: its totals
+// size the build. Its occurrences per text byte scale to the whole text (a
 // region that the estimate or the sample misses overflows, and the build
-// recounts exactly, as the one-shot build does), and its reads are the
-// sample. Any piece with a read longer than the bucketed build takes,
-// another algorithm or read order, or a graph the bucketed workspace does not
-// fit, falls back to the one-shot build over the reads framed here. Results
-// are those of the one-shot build.
+// recounts exactly, as the one-shot build does), its reads are the sample,
+// and its densities, with slack, size the framing arrays for the whole text.
+// The later pieces of a bucketed build are then framed on the device alone
+// (the running totals and each piece's reads kept in device memory); a text
+// that outgrows the arrays is framed again with round trips (synced). Any
+// piece with a read longer than the bucketed build takes, another algorithm
+// or read order, or a graph the bucketed workspace does not fit, falls back
+// to the one-shot build over the reads framed here. Results are those of the
+// one-shot build.
 swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *first, uint64_t n,
-                                cudaStream_t s) {
+                                cudaStream_t s, bool synced = false) {
     swg_status st;
     const uint64_t nc = swg::framing_chunks(n);
     uint64_t C = std::min<uint64_t>(kStreamMaxPieces, std::max<uint64_t>(2, n / kStreamPiece));
@@ -1259,16 +1262,22 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
             cudaStreamSynchronize(f);
         }
     } drain{g->copy, F};
-    // workspace: block counts [nc] | block bases [nc] | scan scratch [S] | totals [8]
-    // | newline masks; totals: newlines, reads, words, occurrences, longest read, NUL flag
+    // workspace: block counts [nc] | block bases [nc] | scan scratch [S] |
+    // framing state [16] | each piece's reads [2 kStreamMaxPieces] | newline masks
     const uint64_t S = std::max(swg::gscan_scratch(nc), swg::rec_scan_scratch(n / 2 + 1));
-    if ((st = ensure(&g->d_sfw, &g->sfw_cap, 2 * nc + S + 8 + swg::newline_mask_words(n), "framing workspace")))
+    constexpr uint64_t kStateWords = 16;
+    static_assert(sizeof(swg::StreamState) <= kStateWords * 8, "framing state");
+    if ((st = ensure(&g->d_sfw, &g->sfw_cap,
+                     2 * nc + S + kStateWords + 2 * kStreamMaxPieces + swg::newline_mask_words(n),
+                     "framing workspace")))
         return st;
     uint64_t *counts = g->d_sfw, *cbase = counts + nc, *scratch = cbase + nc, *tot = scratch + S;
-    uint64_t *masks = tot + 8;
+    auto *fs = reinterpret_cast<swg::StreamState *>(tot);  // tot[0..5]: newlines, piece reads, words, occ, longest, NUL
+    auto *piece_reads = reinterpret_cast<unsigned long long *>(tot + kStateWords);
+    uint64_t *masks = tot + kStateWords + 2 * kStreamMaxPieces;
     auto *acc = reinterpret_cast<unsigned long long *>(tot + 3);
     unsigned *nul_flag = reinterpret_cast<unsigned *>(tot + 5);
-    SWG_CUDA(cudaMemsetAsync(tot, 0, 8 * 8, F), "clear framing totals");
+    SWG_CUDA(cudaMemsetAsync(tot, 0, kStateWords * 8, F), "clear framing state");
 
     // build state, as build_impl sets it
     g->built = false;
@@ -1294,9 +1303,43 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
                   (o->algorithm == SWG_ALGO_DEFAULT && o->read_order == SWG_ORDER_INPUT);
     int launches = 0;
     uint64_t NL = 0, R = 0, reads = 0, words = 0, occ = 0, longest = 0;
+    // after the first piece (framed with host round trips: it sizes the
+    // build), the pieces of a bucketed build are framed on the device alone,
+    // into capacities for the whole text estimated from the first piece; a
+    // text that outgrows them is framed again with round trips (synced)
+    bool fast = stream && !synced;
+    uint64_t nl_cap = 0, rec_cap = 0;
     for (uint64_t c = 0; c < C; ++c) {
         SWG_CUDA(cudaStreamWaitEvent(F, copied[c], 0), "piece wait");
         const uint64_t j0 = cut[c] / swg::kFramingChunk, end = cut[c + 1];
+        if (fast && c > 0) {
+            launches += swg::launch_nl_count(g->d_text, end, counts, masks, nul_flag, F, j0);
+            launches += swg::launch_gscan(counts, cbase, swg::framing_chunks(end), scratch, tot, F);
+            launches += swg::launch_nl_pos(masks, end, cbase, g->d_nl, F, j0, nl_cap,
+                                           reinterpret_cast<uint64_t *>(&fs->overflow));
+            launches += swg::launch_frame_piece(g->d_nl, nl_cap, fs, rec_cap, o->k, scratch, g->d_ridx, g->d_woff,
+                                                g->d_text, g->d_off, g->d_len, g->d_packed, g->reads_cap,
+                                                g->packed_cap, piece_reads + 2 * c, F);
+            SWG_CUDA(cudaGetLastError(), "framing launch");
+            SWG_CUDA(cudaEventRecord(packed_ev[c], F), "packed event");
+            // the piece's reads to the level-1 partitions (the range the
+            // framing left on the device), leaving room for the next piece's
+            // framing but for the last piece
+            SWG_CUDA(cudaStreamWaitEvent(s, packed_ev[c], 0), "build stream wait");
+            BuildArgs ac = a;
+            ac.packed = g->d_packed;
+            ac.n_words = g->packed_cap;
+            ac.read_off = g->d_off;
+            ac.read_len = g->d_len;
+            ac.n_reads = g->reads_cap;  // bounds only: the piece's reads are in piece_reads
+            ac.total_occ = 1;
+            ac.read_range = piece_reads + 2 * c;
+            SWG_CUDA(cudaMemsetAsync(&g->d_ctl->work[1], 0, sizeof(unsigned long long), s), "clear work");
+            g->launches += swg::launch_part_scatter(ac, pl.pa, s,
+                                                    c + 1 < C ? swg::kScatterShared : swg::kScatterResident);
+            SWG_CUDA(cudaGetLastError(), "scatter launch");
+            continue;
+        }
         launches += swg::launch_nl_count(g->d_text, end, counts, masks, nul_flag, F, j0);
         launches += swg::launch_gscan(counts, cbase, swg::framing_chunks(end), scratch, tot, F);
         uint64_t h[6] = {0, 0, 0, 0, 0, 0};
@@ -1308,12 +1351,14 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
         }
         const uint64_t NLc = h[0], Rc = NLc / 2;
         // capacities from the first piece, scaled to the whole text with slack
-        const double scale = (double)n / (double)end;
-        const uint64_t nl_want = std::max<uint64_t>(NLc, (uint64_t)(scale * 1.1 * (double)NLc) + 1024);
-        if ((st = grow_keep(&g->d_nl, &g->nl_cap, g->nl_cap >= NLc ? NLc : nl_want, NL, "newline positions")))
+        // (the device-framed pieces need the whole text's from the start)
+        const double scale = (double)n / (double)end, slack = fast ? 1.25 : 1.1;
+        const uint64_t nl_want = std::max<uint64_t>(NLc, (uint64_t)(scale * slack * (double)NLc) + 4096);
+        if ((st = grow_keep(&g->d_nl, &g->nl_cap, g->nl_cap >= NLc && !fast ? NLc : nl_want, NL,
+                            "newline positions")))
             return st;
-        const uint64_t r_want = std::max<uint64_t>(Rc, (uint64_t)(scale * 1.1 * (double)Rc) + 1024);
-        const uint64_t rw = g->ridx_cap >= Rc ? Rc : r_want;
+        const uint64_t r_want = std::max<uint64_t>(Rc, (uint64_t)(scale * slack * (double)Rc) + 4096);
+        const uint64_t rw = g->ridx_cap >= Rc && !fast ? Rc : r_want;
         if ((st = grow_keep(&g->d_ridx, &g->ridx_cap, rw, R, "read index")) ||
             (st = grow_keep(&g->d_woff, &g->woff_cap, rw, R, "word offsets")))
             return st;
@@ -1327,15 +1372,15 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
         longest = std::max<uint64_t>(longest, h[4]);
         // the reads' arrays grow only with the build stream idle: its
         // scatters of earlier pieces read them
-        const bool grow_packed = g->packed_cap < words_c + 4 || !g->d_packed;
-        const bool grow_reads = g->reads_cap < reads_c || !g->d_off || !g->d_len;
+        const uint64_t p_want = std::max<uint64_t>(words_c + 4, (uint64_t)(scale * slack * (double)words_c) + 4096);
+        const uint64_t rd_want = std::max<uint64_t>(reads_c, (uint64_t)(scale * slack * (double)reads_c) + 4096);
+        const bool grow_packed = g->packed_cap < (fast ? p_want : words_c + 4) || !g->d_packed;
+        const bool grow_reads = g->reads_cap < (fast ? rd_want : reads_c) || !g->d_off || !g->d_len;
         if (grow_packed || grow_reads) SWG_CUDA(cudaStreamSynchronize(s), "build stream");
         if (grow_packed) {
-            const uint64_t p_want = std::max<uint64_t>(words_c + 4, (uint64_t)(scale * 1.1 * (double)words_c) + 1024);
             if ((st = grow_keep(&g->d_packed, &g->packed_cap, p_want, words, "packed reads"))) return st;
         }
         if (grow_reads) {
-            const uint64_t rd_want = std::max<uint64_t>(reads_c, (uint64_t)(scale * 1.1 * (double)reads_c) + 1024);
             uint64_t c1 = g->reads_cap, c2 = g->reads_cap;
             if ((st = grow_keep(&g->d_off, &c1, rd_want, reads, "read offsets")) ||
                 (st = grow_keep(&g->d_len, &c2, rd_want, reads, "read lengths")))
@@ -1389,6 +1434,32 @@ swg_status build_fasta_streamed(swg_graph *g, const swg_opts *o, const char *fir
         reads = reads_c;
         words = words_c;
         occ = occ_c;
+        fast = fast && stream;
+        if (fast && c == 0) {  // the device-framed pieces go on from this piece's totals
+            nl_cap = g->nl_cap;
+            rec_cap = std::min(g->ridx_cap, g->woff_cap);
+            const uint64_t from[4] = {Rc, reads_c, words_c, 0};  // records, reads, words, overflow
+            SWG_CUDA(cudaMemcpyAsync(&fs->records, from, sizeof(from), cudaMemcpyHostToDevice, F), "framing state");
+        }
+    }
+    if (fast) {  // the device-framed pieces' totals
+        uint64_t hs[12];
+        SWG_CUDA(cudaMemcpyAsync(hs, tot, sizeof(hs), cudaMemcpyDeviceToHost, F), "read framing state");
+        SWG_CUDA(cudaStreamSynchronize(F), "framing");
+        if ((unsigned)hs[5]) {
+            swg::set_error("NUL byte in the FASTA input");
+            return SWG_ERR_BAD_INPUT;
+        }
+        if (hs[9]) {  // the text outgrew the capacities from the first piece
+            SWG_CUDA(cudaStreamSynchronize(s), "build stream");
+            return build_fasta_streamed(g, o, first, n, s, true);
+        }
+        NL = hs[0];
+        occ = hs[3];
+        longest = std::max<uint64_t>(longest, hs[4]);
+        reads = hs[7];
+        words = hs[8];
+        if (o->algorithm == SWG_ALGO_DEFAULT && longest > kBucketedMaxRead) stream = false;
     }
     // the build stream goes on after all framing
     SWG_CUDA(cudaStreamWaitEvent(s, packed_ev[C - 1], 0), "build stream wait");

@@ -86,17 +86,20 @@ __global__ void __launch_bounds__(kFBlock) k_nl_count(const unsigned char *__res
 }
 
 // Position of every newline of chunks j0 + blockIdx.x, in order, from the
-// masks k_nl_count left.
+// masks k_nl_count left; positions from cap on are not written and set *ovf.
 __global__ void __launch_bounds__(kFBlock) k_nl_pos(const unsigned long long *__restrict__ masks,
                                                     const uint64_t *__restrict__ chunk_base,
-                                                    uint64_t *__restrict__ nl, uint64_t j0) {
+                                                    uint64_t *__restrict__ nl, uint64_t j0, uint64_t cap,
+                                                    uint64_t *__restrict__ ovf) {
     __shared__ uint64_t wb[kFBlock / 32];
     const uint64_t j = j0 + blockIdx.x;
     const uint64_t base = j * kFChunk + (uint64_t)threadIdx.x * kFBytes;
     unsigned long long m = masks[j * kFBlock + threadIdx.x];
     uint64_t pos = chunk_base[j] + block_exclusive_scan<kFBlock>((uint64_t)__popcll(m), wb, nullptr);
     while (m) {
-        nl[pos++] = base + (uint64_t)(__ffsll((long long)m) - 1);
+        if (pos < cap) nl[pos] = base + (uint64_t)(__ffsll((long long)m) - 1);
+        else if (ovf) *ovf = 1;
+        pos++;
         m &= m - 1;
     }
 }
@@ -196,48 +199,66 @@ __device__ __forceinline__ uint64_t rec_length(const uint64_t *__restrict__ nl, 
 // to acc[0] and their longest length maxed into acc[1]); one block scans the
 // two columns of block sums (totals to tot[0], tot[1]); then every record
 // gets its read index (kept records before it) and first word, from r0 on.
-__global__ void __launch_bounds__(kFBlock) k_rec_reduce(const uint64_t *__restrict__ nl, uint64_t r0,
-                                                        uint64_t r1, int k, uint64_t *__restrict__ sums,
-                                                        unsigned long long *__restrict__ acc) {
-    __shared__ uint64_t wb[kFBlock / 32];
-    const uint64_t base = r0 + (uint64_t)blockIdx.x * kGChunk;
-    uint64_t keep = 0, words = 0;
-    unsigned long long occ = 0, mx = 0;
-    for (int it = 0; it < kGItems; ++it) {
-        const uint64_t r = base + (uint64_t)it * kFBlock + threadIdx.x;
-        if (r < r1) {
-            const uint64_t L = rec_length(nl, r);
-            if (L >= (uint64_t)k) {
-                keep++;
-                words += (L + 15) / 16;
-                occ += L - (uint64_t)k + 1;
-                mx = L > mx ? L : mx;
-            }
-        }
-    }
-    uint64_t tk, tw;
-    block_exclusive_scan<kFBlock>(keep, wb, &tk);
-    block_exclusive_scan<kFBlock>(words, wb, &tw);
-    if (threadIdx.x == 0) {
-        sums[2 * blockIdx.x] = tk;
-        sums[2 * blockIdx.x + 1] = tw;
-    }
-    if (!acc) return;
-#pragma unroll
-    for (int d = 16; d; d >>= 1) {
-        occ += __shfl_down_sync(0xffffffffu, occ, d);
-        const unsigned long long y = __shfl_down_sync(0xffffffffu, mx, d);
-        mx = y > mx ? y : mx;
-    }
-    if ((threadIdx.x & 31) == 0 && occ) {
-        atomicAdd(&acc[0], occ);
-        atomicMax(&acc[1], mx);
+// With rr, the range is rr[0] <= r < rr[1] (device values, a streamed
+// piece's records); the blocks stride over the range's blocks of records.
+__device__ __forceinline__ void rec_range(const uint64_t *rr, uint64_t &r0, uint64_t &r1) {
+    if (rr) {
+        r0 = rr[0];
+        r1 = rr[1];
     }
 }
 
-__global__ void __launch_bounds__(kFBlock) k_rec_blocks(uint64_t *sums, uint64_t nb, uint64_t *tot) {
+__global__ void __launch_bounds__(kFBlock) k_rec_reduce(const uint64_t *__restrict__ nl, uint64_t r0,
+                                                        uint64_t r1, const uint64_t *rr, int k,
+                                                        uint64_t *__restrict__ sums,
+                                                        unsigned long long *__restrict__ acc) {
+    __shared__ uint64_t wb[kFBlock / 32];
+    rec_range(rr, r0, r1);
+    const uint64_t nb = r1 > r0 ? (r1 - r0 + kGChunk - 1) / kGChunk : 0;
+    for (uint64_t q = blockIdx.x; q < nb; q += gridDim.x) {
+        const uint64_t base = r0 + q * kGChunk;
+        uint64_t keep = 0, words = 0;
+        unsigned long long occ = 0, mx = 0;
+        for (int it = 0; it < kGItems; ++it) {
+            const uint64_t r = base + (uint64_t)it * kFBlock + threadIdx.x;
+            if (r < r1) {
+                const uint64_t L = rec_length(nl, r);
+                if (L >= (uint64_t)k) {
+                    keep++;
+                    words += (L + 15) / 16;
+                    occ += L - (uint64_t)k + 1;
+                    mx = L > mx ? L : mx;
+                }
+            }
+        }
+        uint64_t tk, tw;
+        block_exclusive_scan<kFBlock>(keep, wb, &tk);
+        block_exclusive_scan<kFBlock>(words, wb, &tw);
+        if (threadIdx.x == 0) {
+            sums[2 * q] = tk;
+            sums[2 * q + 1] = tw;
+        }
+        if (acc) {
+#pragma unroll
+            for (int d = 16; d; d >>= 1) {
+                occ += __shfl_down_sync(0xffffffffu, occ, d);
+                const unsigned long long y = __shfl_down_sync(0xffffffffu, mx, d);
+                mx = y > mx ? y : mx;
+            }
+            if ((threadIdx.x & 31) == 0 && occ) {
+                atomicAdd(&acc[0], occ);
+                atomicMax(&acc[1], mx);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kFBlock) k_rec_blocks(uint64_t *sums, uint64_t r0, uint64_t r1,
+                                                        const uint64_t *rr, uint64_t *tot) {
     __shared__ uint64_t wb[kFBlock / 32];
     __shared__ uint64_t carry[2];
+    rec_range(rr, r0, r1);
+    const uint64_t nb = r1 > r0 ? (r1 - r0 + kGChunk - 1) / kGChunk : 0;
     if (threadIdx.x < 2) carry[threadIdx.x] = 0;
     __syncthreads();
     for (uint64_t b0 = 0; b0 < nb; b0 += kFBlock) {
@@ -258,38 +279,69 @@ __global__ void __launch_bounds__(kFBlock) k_rec_blocks(uint64_t *sums, uint64_t
 }
 
 __global__ void __launch_bounds__(kFBlock) k_rec_write(const uint64_t *__restrict__ nl, uint64_t r0,
-                                                       uint64_t r1, int k, const uint64_t *__restrict__ sums,
+                                                       uint64_t r1, const uint64_t *rr, int k,
+                                                       const uint64_t *__restrict__ sums,
                                                        uint64_t *__restrict__ read_idx,
                                                        uint64_t *__restrict__ word_off) {
     __shared__ uint64_t wb[kFBlock / 32];
-    const uint64_t base = r0 + (uint64_t)blockIdx.x * kGChunk + (uint64_t)threadIdx.x * kGItems;
-    uint32_t kept = 0;  // bit i: record base + i kept
-    uint64_t wds[kGItems];
-    uint64_t sk = 0, sw = 0;
+    rec_range(rr, r0, r1);
+    const uint64_t nb = r1 > r0 ? (r1 - r0 + kGChunk - 1) / kGChunk : 0;
+    for (uint64_t q = blockIdx.x; q < nb; q += gridDim.x) {
+        const uint64_t base = r0 + q * kGChunk + (uint64_t)threadIdx.x * kGItems;
+        uint32_t kept = 0;  // bit i: record base + i kept
+        uint64_t wds[kGItems];
+        uint64_t sk = 0, sw = 0;
 #pragma unroll
-    for (int it = 0; it < kGItems; ++it) {
-        wds[it] = 0;
-        if (base + it < r1) {
-            const uint64_t L = rec_length(nl, base + it);
-            if (L >= (uint64_t)k) {
-                kept |= 1u << it;
-                wds[it] = (L + 15) / 16;
+        for (int it = 0; it < kGItems; ++it) {
+            wds[it] = 0;
+            if (base + it < r1) {
+                const uint64_t L = rec_length(nl, base + it);
+                if (L >= (uint64_t)k) {
+                    kept |= 1u << it;
+                    wds[it] = (L + 15) / 16;
+                }
             }
+            sk += (kept >> it) & 1u;
+            sw += wds[it];
         }
-        sk += (kept >> it) & 1u;
-        sw += wds[it];
-    }
-    uint64_t rk = sums[2 * blockIdx.x] + block_exclusive_scan<kFBlock>(sk, wb, nullptr);
-    uint64_t rw = sums[2 * blockIdx.x + 1] + block_exclusive_scan<kFBlock>(sw, wb, nullptr);
+        uint64_t rk = sums[2 * q] + block_exclusive_scan<kFBlock>(sk, wb, nullptr);
+        uint64_t rw = sums[2 * q + 1] + block_exclusive_scan<kFBlock>(sw, wb, nullptr);
 #pragma unroll
-    for (int it = 0; it < kGItems; ++it) {
-        if (base + it < r1) {
-            read_idx[base + it] = rk;
-            word_off[base + it] = rw;
+        for (int it = 0; it < kGItems; ++it) {
+            if (base + it < r1) {
+                read_idx[base + it] = rk;
+                word_off[base + it] = rw;
+            }
+            rk += (kept >> it) & 1u;
+            rw += wds[it];
         }
-        rk += (kept >> it) & 1u;
-        rw += wds[it];
     }
+}
+
+// Streamed framing state (one thread). k_frame_prep: this piece's records
+// are rr = [records framed so far, complete records through the piece),
+// capped at rec_cap and at the newline positions written (nl_cap; past
+// either, st->overflow). k_frame_advance: the piece's kept reads
+// and words are added to the running totals, and its reads' range is put
+// in piece_reads for the level-1 scatter (empty after an overflow).
+__global__ void k_frame_prep(StreamState *st, uint64_t rec_cap, uint64_t nl_cap) {
+    uint64_t r1 = st->newlines / 2;
+    const uint64_t cap = rec_cap < nl_cap / 2 ? rec_cap : nl_cap / 2;
+    if (r1 > cap || st->newlines > nl_cap) {
+        r1 = r1 < cap ? r1 : cap;
+        st->overflow = 1;
+    }
+    st->rec_range[0] = st->records;
+    st->rec_range[1] = r1 > st->records ? r1 : st->records;
+}
+
+__global__ void k_frame_advance(StreamState *st, unsigned long long *piece_reads) {
+    const uint64_t before = st->reads;
+    st->reads += st->piece_reads;
+    st->words += st->piece_words;
+    st->records = st->rec_range[1];
+    piece_reads[0] = before;
+    piece_reads[1] = st->overflow ? before : st->reads;
 }
 
 __device__ __forceinline__ uint32_t code_of(unsigned char ch) {
@@ -318,7 +370,8 @@ __global__ void __launch_bounds__(256) k_rec_pack(const unsigned char *__restric
                                                   const uint64_t *__restrict__ word_off,
                                                   uint64_t read_base, uint64_t word_base,
                                                   uint64_t *__restrict__ off, uint32_t *__restrict__ len,
-                                                  uint32_t *__restrict__ packed) {
+                                                  uint32_t *__restrict__ packed, StreamState *sst,
+                                                  uint64_t reads_cap, uint64_t words_cap) {
     __shared__ unsigned char lut[256];
     __shared__ uint32_t s_pre[8][33];
     __shared__ uint64_t s_start[8][32], s_w0[8][32];
@@ -327,6 +380,12 @@ __global__ void __launch_bounds__(256) k_rec_pack(const unsigned char *__restric
     __syncthreads();
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    if (sst) {  // a streamed piece: its records, and the reads and words framed before it
+        r0 = sst->rec_range[0];
+        n_rec = sst->rec_range[1];
+        read_base = sst->reads;
+        word_base = sst->words;
+    }
     for (uint64_t g0 = r0 + (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; g0 < n_rec;
          g0 += nwarps * 32) {
         const uint64_t r = g0 + lane;
@@ -336,12 +395,17 @@ __global__ void __launch_bounds__(256) k_rec_pack(const unsigned char *__restric
             my_start = nl[2 * r] + 1;
             const uint64_t L = nl[2 * r + 1] - my_start;
             if (L >= (uint64_t)k) {
-                my_len = (uint32_t)L;
-                my_nw = (uint32_t)((L + 15) / 16);
-                my_w0 = word_base + word_off[r];
-                const uint64_t ri = read_base + read_idx[r];
-                off[ri] = my_w0 * 16;
-                len[ri] = my_len;
+                const uint64_t ri = read_base + read_idx[r], w0 = word_base + word_off[r];
+                const uint32_t nw = (uint32_t)((L + 15) / 16);
+                if (ri < reads_cap && w0 + nw <= words_cap) {
+                    my_len = (uint32_t)L;
+                    my_nw = nw;
+                    my_w0 = w0;
+                    off[ri] = my_w0 * 16;
+                    len[ri] = my_len;
+                } else if (sst) {
+                    sst->overflow = 1;  // only a streamed piece has caps below its totals
+                }
             }
         }
         uint32_t inc = my_nw;  // inclusive warp scan of the word counts
@@ -433,10 +497,31 @@ int launch_rec_scan(const uint64_t *nl, uint64_t r0, uint64_t n_rec, int k, uint
         cudaMemsetAsync(tot, 0, 2 * sizeof(uint64_t), s);
         return 0;
     }
-    k_rec_reduce<<<(unsigned)nb, kFBlock, 0, s>>>(nl, r0, n_rec, k, scratch, acc);
-    k_rec_blocks<<<1, kFBlock, 0, s>>>(scratch, nb, tot);
-    k_rec_write<<<(unsigned)nb, kFBlock, 0, s>>>(nl, r0, n_rec, k, scratch, read_idx, word_off);
+    k_rec_reduce<<<(unsigned)nb, kFBlock, 0, s>>>(nl, r0, n_rec, nullptr, k, scratch, acc);
+    k_rec_blocks<<<1, kFBlock, 0, s>>>(scratch, r0, n_rec, nullptr, tot);
+    k_rec_write<<<(unsigned)nb, kFBlock, 0, s>>>(nl, r0, n_rec, nullptr, k, scratch, read_idx, word_off);
     return 3;
+}
+
+int launch_frame_piece(const uint64_t *nl, uint64_t nl_cap, StreamState *st, uint64_t rec_cap, int k,
+                       uint64_t *scratch,
+                       uint64_t *read_idx, uint64_t *word_off, const unsigned char *t, uint64_t *off,
+                       uint32_t *len, uint32_t *packed, uint64_t reads_cap, uint64_t words_cap,
+                       unsigned long long *piece_reads, cudaStream_t s) {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned grid = (unsigned)std::max(sms, 1) * 4;
+    const uint64_t *rr = reinterpret_cast<const uint64_t *>(st->rec_range);
+    uint64_t *piece_tot = reinterpret_cast<uint64_t *>(&st->piece_reads);  // piece_reads, piece_words
+    k_frame_prep<<<1, 1, 0, s>>>(st, rec_cap, nl_cap);
+    k_rec_reduce<<<grid, kFBlock, 0, s>>>(nl, 0, 0, rr, k, scratch, &st->occ);
+    k_rec_blocks<<<1, kFBlock, 0, s>>>(scratch, 0, 0, rr, piece_tot);
+    k_rec_write<<<grid, kFBlock, 0, s>>>(nl, 0, 0, rr, k, scratch, read_idx, word_off);
+    k_rec_pack<<<grid * 4, 256, 0, s>>>(t, nl, 0, 0, k, read_idx, word_off, 0, 0, off, len, packed, st,
+                                        reads_cap, words_cap);
+    k_frame_advance<<<1, 1, 0, s>>>(st, piece_reads);
+    return 6;
 }
 
 uint64_t newline_mask_words(uint64_t n) { return framing_chunks(n) * kFBlock; }
@@ -451,11 +536,11 @@ int launch_nl_count(const unsigned char *t, uint64_t n, uint64_t *counts, uint64
 }
 
 int launch_nl_pos(const uint64_t *masks, uint64_t n, const uint64_t *chunk_base, uint64_t *nl, cudaStream_t s,
-                  uint64_t j0) {
+                  uint64_t j0, uint64_t cap, uint64_t *ovf) {
     const uint64_t nc = framing_chunks(n);
     if (nc <= j0) return 0;
     k_nl_pos<<<(unsigned)(nc - j0), kFBlock, 0, s>>>(reinterpret_cast<const unsigned long long *>(masks),
-                                                    chunk_base, nl, j0);
+                                                    chunk_base, nl, j0, cap, ovf);
     return 1;
 }
 
@@ -469,7 +554,7 @@ int launch_rec_pack(const unsigned char *t, const uint64_t *nl, uint64_t n_rec, 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint64_t blocks = std::min<uint64_t>((n_rec - r0 + 255) / 256, (uint64_t)std::max(sms, 1) * 16);
     k_rec_pack<<<(unsigned)blocks, 256, 0, s>>>(t, nl, r0, n_rec, k, read_idx, word_off, read_base, word_base,
-                                                off, len, packed);
+                                                off, len, packed, nullptr, ~0ull, ~0ull);
     return 1;
 }
 

@@ -991,16 +991,18 @@ __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs p
     const int shift = 64 - bits;
     const uint32_t n_parts = B1C ? (1u << B1C) : pa.n_parts;
     const uint32_t per = (n_parts + blockDim.x - 1) / blockDim.x;
+    const uint64_t r_first = a.read_range ? a.read_range[0] : 0;
+    const uint64_t n_reads = a.read_range ? a.read_range[1] - r_first : a.n_reads;
     __shared__ unsigned long long s_base;
     for (;;) {  // batches of NT reads, handed out as blocks finish them
         if (threadIdx.x == 0) s_base = atomicAdd(&pa.work[1], (unsigned long long)NT);
         __syncthreads();
         const uint64_t base = s_base;
-        if (base >= a.n_reads) break;
+        if (base >= n_reads) break;
         const uint64_t r = base + threadIdx.x;
         ReadWalk st;
         st.left = 0;
-        if (r < a.n_reads) walk_init<KC>(a, st, r);
+        if (r < n_reads) walk_init<KC>(a, st, r_first + r);
         while (__syncthreads_or(st.left != 0)) {
             for (uint32_t j = threadIdx.x; j < n_parts; j += blockDim.x) hist[j] = 0;
             __syncthreads();
@@ -2399,6 +2401,20 @@ int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s, i
         const uint64_t grid = std::min<uint64_t>(a.n_tiles, resident_grid(kern, 256, smem));
         kern<<<(unsigned)grid, 256, smem, s>>>(a, p);
         return 1;
+    }
+    if (grid_mode == kScatterShared && !a.segs && !a.read_seg && !a.tag_bits && p.bits == 8) {
+        // beside a concurrent stream, with 256 partitions: 8 records per
+        // thread a round and at most 64 registers, so that four blocks fit an
+        // SM and the three resident ones leave a fourth block's room (with 512
+        // partitions a round of 2048 records would write runs of 4: the
+        // 3-block shape below keeps its rounds and leaves one of its blocks)
+        switch (a.k) {
+            case 31: return launch_p1_scatter_shape<256, 8, 4, 31, 8>(a, p, s, grid_mode);
+            case 27: return launch_p1_scatter_shape<256, 8, 4, 27, 8>(a, p, s, grid_mode);
+            case 25: return launch_p1_scatter_shape<256, 8, 4, 25, 8>(a, p, s, grid_mode);
+            case 21: return launch_p1_scatter_shape<256, 8, 4, 21, 8>(a, p, s, grid_mode);
+            default: return launch_p1_scatter_shape<256, 8, 4>(a, p, s, grid_mode);
+        }
     }
     switch (shape) {  // shape 3 changes only the level-2 scatter, shape 4 only level 1
         case 1: return launch_p1_scatter_shape<512, 8, 2>(a, p, s, grid_mode);

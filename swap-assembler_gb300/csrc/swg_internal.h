@@ -73,6 +73,10 @@ struct BuildArgs {
     int tag_bits;                      // bucketed batch: the read's sample index sits in the
                                        // top tag_bits bits of every key (0 = no tag)
     unsigned *max_len;                 // if set, the occurrence scan records the longest read
+    // level-1 scatter of a streamed piece: if set, the reads read_range[0] <=
+    // r < read_range[1] (device values; n_reads and total_occ are then only
+    // bounds for the launch)
+    const unsigned long long *read_range;
     // bucketed single-sample build only: survivors also written, as each bucket
     // is compacted, to host memory the device can reach (unordered, at most
     // host_cap; host_written counts them), so the copy-out overlaps the count
@@ -164,7 +168,8 @@ int launch_big_multi(const BuildArgs &a, const BucketArgs &b, const unsigned lon
 // Grid of the level-1 scatter: one block per batch of reads (blocks retire
 // as they finish), as many blocks as stay resident (each takes batches until
 // none are left), or one block per SM fewer than that, leaving room on every
-// SM for the kernels of a concurrent stream (the streamed build's framing).
+// SM for the kernels of a concurrent stream (the streamed build's framing;
+// with 256 partitions this mode takes a block shape of at most 64 registers).
 enum { kScatterPerBatch = 0, kScatterResident = 1, kScatterShared = 2 };
 int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s, int grid_mode = kScatterResident);
 int launch_part_wave(const BuildArgs &a, const PartArgs &p, uint32_t p0, uint32_t n,
@@ -184,7 +189,31 @@ uint64_t newline_mask_words(uint64_t n);
 int launch_nl_count(const unsigned char *t, uint64_t n, uint64_t *counts, uint64_t *masks, unsigned *flag,
                     cudaStream_t s, uint64_t j0 = 0);
 int launch_nl_pos(const uint64_t *masks, uint64_t n, const uint64_t *chunk_base, uint64_t *nl,
-                  cudaStream_t s, uint64_t j0 = 0);
+                  cudaStream_t s, uint64_t j0 = 0, uint64_t cap = ~0ull, uint64_t *ovf = nullptr);
+// Device state of a streamed framing, in the order the framing kernels write
+// it (the chunk-count scan's total, the record scan's two totals, the
+// occurrence and longest-read accumulators, the NUL flag first).
+struct StreamState {
+    unsigned long long newlines;                  // through the current piece
+    unsigned long long piece_reads, piece_words;  // kept reads and their words in the piece
+    unsigned long long occ, longest;              // kept reads' k-mer occurrences, longest read
+    unsigned long long nul;                       // a NUL byte was seen (low 32 bits)
+    unsigned long long records;                   // records framed before the piece
+    unsigned long long reads, words;              // kept reads and words framed so far
+    unsigned long long overflow;                  // a capacity below the text's needs
+    unsigned long long rec_range[2];              // the piece's records
+};
+// One streamed piece framed with no host round trip (its newlines counted,
+// scanned and located already): the records it completes are scanned and
+// packed with the running totals as bases, the totals advanced, and the
+// piece's reads written to piece_reads as [first, end) for the level-1
+// scatter. Capacities the text outgrows set st->overflow instead of being
+// written past.
+int launch_frame_piece(const uint64_t *nl, uint64_t nl_cap, StreamState *st, uint64_t rec_cap, int k,
+                       uint64_t *scratch,
+                       uint64_t *read_idx, uint64_t *word_off, const unsigned char *t, uint64_t *off,
+                       uint32_t *len, uint32_t *packed, uint64_t reads_cap, uint64_t words_cap,
+                       unsigned long long *piece_reads, cudaStream_t s);
 // Records r0 <= r < n_rec: read_idx[r] / word_off[r] = kept records (length
 // >= k) / their 16-base words before r, from r0; totals to tot[0], tot[1];
 // with acc, the kept reads' k-mer occurrences added to acc[0] and their

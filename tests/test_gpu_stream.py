@@ -2,10 +2,13 @@
 framed and scattered to the level-1 partitions as it lands, with the regions
 sized from the first piece. Its graph must equal the one-shot build's (the
 text copied whole, framed, then built; SWG_NO_STREAM selects it) bit for bit:
-on plain inputs of 2 and 4 pieces, with each algorithm, with a read too long
-for the bucketed build in a later piece (the fallback), with the multi-line
-quirk shifting the header/sequence alternation mid-text, on a reused handle,
-and with the same errors for a NUL byte or an unpaired last header."""
+on plain inputs of 3 and 6 pieces (40 MiB each; the first framed with host
+round trips, the rest on the device alone), with each algorithm, with a read
+too long for the bucketed build in a later piece (the fallback), with the
+multi-line quirk shifting the header/sequence alternation mid-text, with
+later pieces denser than the first (framed again with round trips), on a
+reused handle, and with the same errors for a NUL byte or an unpaired last
+header."""
 import os
 
 import numpy as np
@@ -49,19 +52,19 @@ def assert_same(text: bytes, opts: swapgb.Opts) -> dict:
 
 @pytest.fixture(scope="module")
 def text2():
-    # 1.1M x 100 bp reads: about 120 MB of text, two pieces
+    # 1.1M x 100 bp reads: about 120 MB of text, three pieces
     return synth(41, 1_100_000)
 
 
-def test_two_pieces_equal_one_shot(text2):
+def test_few_pieces_equal_one_shot(text2):
     info = assert_same(text2, swapgb.Opts(k=31, cutoff=5))
     assert info["algorithm"] == swapgb.ALGO_BUCKETED and info["survivors"] > 0
     assert info["estimate"] == 0  # the first piece's sample sized every region
 
 
-def test_four_pieces_equal_one_shot_and_host_framing():
-    text = synth(42, 2_600_000, genome_len=5_000_000)  # about 286 MB
-    assert len(text) >= 4 * (64 << 20)
+def test_many_pieces_equal_one_shot_and_host_framing():
+    text = synth(42, 2_600_000, genome_len=5_000_000)  # about 287 MB: six pieces
+    assert len(text) >= 6 * (40 << 20)
     opts = swapgb.Opts(k=21, cutoff=2)
     assert assert_same(text, opts)["estimate"] == 0
     _, ks, ms = build(text, opts, True)
@@ -133,6 +136,19 @@ def test_sample_miss_recounts_exactly(text2):
     assert info["estimate"] == 1  # the exact-count rerun ran
     gs, ks, ms = build(text, opts, True)
     assert (ms == 255).any()  # the hot k-mers saturate
+
+
+def test_denser_later_pieces_frame_again():
+    """Pieces after the first are framed on the device into capacities
+    estimated from the first piece. Here the first piece holds 250 bp reads
+    and the rest 40 bp reads (about five times the newlines per byte): the
+    estimate is outgrown, the build frames the text again with host round
+    trips, and the graph still equals the one-shot build's."""
+    long_part = swapgb.synth_fasta(seed=51, genome_len=3_000_000, n_reads=140_000, read_len=250)
+    short_part = swapgb.synth_fasta(seed=52, genome_len=3_000_000, n_reads=2_000_000, read_len=40)
+    text = long_part + short_part
+    assert len(text) >= STREAM_MIN and len(long_part) > len(text) // 4  # the first piece: long reads only
+    assert_same(text, swapgb.Opts(k=21, cutoff=2))
 
 
 def _to_host(g: swapgb.Graph, opts: swapgb.Opts, text: bytes, keys, mult, cap: int) -> tuple[int, int]:
