@@ -991,18 +991,21 @@ __global__ void __launch_bounds__(NT, MINB) k_p1_scatter(BuildArgs a, PartArgs p
     const int shift = 64 - bits;
     const uint32_t n_parts = B1C ? (1u << B1C) : pa.n_parts;
     const uint32_t per = (n_parts + blockDim.x - 1) / blockDim.x;
-    const uint64_t r_first = a.read_range ? a.read_range[0] : 0;
-    const uint64_t n_reads = a.read_range ? a.read_range[1] - r_first : a.n_reads;
-    __shared__ unsigned long long s_base;
+    // the reads: [0, n_reads), or read_range (kept in shared memory, read
+    // once per batch: no registers held through the rounds)
+    __shared__ unsigned long long s_base, s_first, s_end;
+    if (threadIdx.x == 0) {
+        s_first = a.read_range ? a.read_range[0] : 0;
+        s_end = a.read_range ? a.read_range[1] : a.n_reads;
+    }
     for (;;) {  // batches of NT reads, handed out as blocks finish them
         if (threadIdx.x == 0) s_base = atomicAdd(&pa.work[1], (unsigned long long)NT);
         __syncthreads();
-        const uint64_t base = s_base;
-        if (base >= n_reads) break;
-        const uint64_t r = base + threadIdx.x;
+        const uint64_t r = s_first + s_base + threadIdx.x;
+        if (s_first + s_base >= s_end) break;
         ReadWalk st;
         st.left = 0;
-        if (r < n_reads) walk_init<KC>(a, st, r_first + r);
+        if (r < s_end) walk_init<KC>(a, st, r);
         while (__syncthreads_or(st.left != 0)) {
             for (uint32_t j = threadIdx.x; j < n_parts; j += blockDim.x) hist[j] = 0;
             __syncthreads();
