@@ -329,7 +329,7 @@ swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, u
     SWG_CUDA(cudaMemsetAsync(g->d_ctl, 0, sizeof(Control), s), "memset control");
     SWG_CUDA(cudaMemsetAsync(g->d_prefix, 0, sizeof(uint64_t), s), "memset prefix");
     a.max_len = &g->d_ctl->max_len;
-    g->launches += swg::launch_occ_scan(a, s);
+    g->launches += swg::launch_occ_scan(a, s, false);  // the total; the per-read prefix below if needed
     a.max_len = nullptr;
     SWG_CUDA(cudaGetLastError(), "occurrence scan launch");
     SWG_CUDA(cudaMemcpyAsync(&g->h_ctl->occ_total, g->d_prefix + n_reads, sizeof(uint64_t),
@@ -343,19 +343,23 @@ swg_status build_impl(swg_graph *g, const swg_opts *o, const uint32_t *packed, u
     g->occurrences = a.total_occ;
     g->retries = 0;
     g->estimate = 0;
-    a.n_tiles = (a.total_occ + swg::kTileOcc - 1) / swg::kTileOcc;
-    if ((st = ensure(&g->d_tiles, &g->tiles_cap, a.n_tiles, "tile table"))) return st;
-    a.tile_first_read = g->d_tiles;
-    g->launches += swg::launch_tiles(a, s);
-    SWG_CUDA(cudaGetLastError(), "tile launch");
-
-    if (o->algorithm == SWG_ALGO_PARTITIONED) return build_partitioned(g, o, a, s, load);
-    if (o->algorithm == SWG_ALGO_BUCKETED) return build_bucketed(g, o, a, s, load);
     // the bucketed build walks one read per thread: reads of more than 16 kbp
     // (long-read data) would leave the GPU waiting on a few threads
-    if (o->algorithm == SWG_ALGO_DEFAULT && o->read_order == SWG_ORDER_INPUT &&
-        g->h_ctl->max_len <= kBucketedMaxRead && bucketed_fits(g, a.total_occ))
-        return build_bucketed(g, o, a, s, load);
+    const bool bucketed = o->algorithm == SWG_ALGO_BUCKETED ||
+                          (o->algorithm == SWG_ALGO_DEFAULT && o->read_order == SWG_ORDER_INPUT &&
+                           g->h_ctl->max_len <= kBucketedMaxRead && bucketed_fits(g, a.total_occ));
+    // the per-read occurrence prefix and the tiles of kTileOcc occurrences:
+    // every algorithm but the bucketed build's thread-per-read scatter uses them
+    if (!bucketed || swg::level1_shape(o->scatter_shape) == 4) {
+        g->launches += swg::launch_occ_scan_write(a, s);
+        a.n_tiles = (a.total_occ + swg::kTileOcc - 1) / swg::kTileOcc;
+        if ((st = ensure(&g->d_tiles, &g->tiles_cap, a.n_tiles, "tile table"))) return st;
+        a.tile_first_read = g->d_tiles;
+        g->launches += swg::launch_tiles(a, s);
+        SWG_CUDA(cudaGetLastError(), "tile launch");
+    }
+    if (o->algorithm == SWG_ALGO_PARTITIONED) return build_partitioned(g, o, a, s, load);
+    if (bucketed) return build_bucketed(g, o, a, s, load);
     return build_direct(g, o, a, s, load);
 }
 

@@ -2257,14 +2257,23 @@ int device_sm_count() {
 
 uint64_t scan_block_count(uint64_t n_reads) { return (n_reads + kScanChunk - 1) / kScanChunk; }
 
-int launch_occ_scan(const BuildArgs &a, cudaStream_t s) {
+int launch_occ_scan(const BuildArgs &a, cudaStream_t s, bool write) {
     const uint64_t nb = scan_block_count(a.n_reads);
     if (nb == 0) return 0;
     k_scan_reduce<<<(unsigned)nb, kScanBlock, 0, s>>>(a);
     k_scan_blocks<<<1, 1024, 0, s>>>(a.scan_blocks, nb, a.occ_prefix + a.n_reads);
+    if (!write) return 2;
     k_scan_write<<<(unsigned)nb, kScanBlock, 0, s>>>(a);
     return 3;
 }
+
+int launch_occ_scan_write(const BuildArgs &a, cudaStream_t s) {
+    const uint64_t nb = scan_block_count(a.n_reads);
+    if (nb == 0) return 0;
+    k_scan_write<<<(unsigned)nb, kScanBlock, 0, s>>>(a);
+    return 1;
+}
+
 
 int launch_tiles(const BuildArgs &a, cudaStream_t s) {
     if (a.n_tiles == 0) return 0;
@@ -2370,6 +2379,9 @@ int launch_part_prefix(const PartArgs &p, cudaStream_t s) {
 // Block shape of the two scatter passes: threads, records per thread per
 // round, resident blocks per SM (SWG_SCATTER_SHAPE = 0..3 selects one; 3 is
 // the level-2 scatter with bulk-copy staging).
+int scatter_shape();
+int level1_shape(int opt_shape) { return opt_shape ? opt_shape : scatter_shape(); }
+
 int scatter_shape() {
     static int shape = [] {
         const char *e = std::getenv("SWG_SCATTER_SHAPE");

@@ -136,7 +136,14 @@ struct BucketArgs {
 };
 
 // Kernel launchers (kernels.cu). Each returns the number of launches made.
-int launch_occ_scan(const BuildArgs &a, cudaStream_t s);
+// The occurrence total (into occ_prefix[n_reads]) and, with write, the
+// per-read prefix; launch_occ_scan_write adds the prefix to a scan made
+// without it.
+int launch_occ_scan(const BuildArgs &a, cudaStream_t s, bool write = true);
+int launch_occ_scan_write(const BuildArgs &a, cudaStream_t s);
+// The level-1 scatter's block shape for swg_opts::scatter_shape (0: the
+// SWG_SCATTER_SHAPE default).
+int level1_shape(int opt_shape);
 uint64_t scan_block_count(uint64_t n_reads);
 int launch_tiles(const BuildArgs &a, cudaStream_t s);
 int launch_hll(const BuildArgs &a, cudaStream_t s);
