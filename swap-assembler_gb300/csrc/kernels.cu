@@ -2417,34 +2417,30 @@ int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s, i
         kern<<<(unsigned)grid, 256, smem, s>>>(a, p);
         return 1;
     }
-    if (grid_mode == kScatterShared && !a.segs && !a.read_seg && !a.tag_bits && p.bits == 8) {
-        // beside a concurrent stream, with 256 partitions: 8 records per
-        // thread a round and at most 64 registers, so that four blocks fit an
-        // SM and the three resident ones leave a fourth block's room (with 512
-        // partitions a round of 2048 records would write runs of 4: the
-        // 3-block shape below keeps its rounds and leaves one of its blocks)
+    const bool single = !a.segs && !a.read_seg && !a.tag_bits;
+    // Single-sample builds with 256 partitions and a common k: the walk's
+    // shifts and masks and the record layout are compile-time constants, and
+    // rounds of 12 records a thread fit 64 registers, so four blocks share an
+    // SM (three in the shared grid, leaving a fourth block's room). Shapes 1
+    // and 2 replace it in a resident or per-batch grid.
+    if (single && p.bits == 8 && (grid_mode == kScatterShared || shape == 0 || shape == 3 || shape == 4))
         switch (a.k) {
-            case 31: return launch_p1_scatter_shape<256, 8, 4, 31, 8>(a, p, s, grid_mode);
-            case 27: return launch_p1_scatter_shape<256, 8, 4, 27, 8>(a, p, s, grid_mode);
-            case 25: return launch_p1_scatter_shape<256, 8, 4, 25, 8>(a, p, s, grid_mode);
-            case 21: return launch_p1_scatter_shape<256, 8, 4, 21, 8>(a, p, s, grid_mode);
-            default: return launch_p1_scatter_shape<256, 8, 4>(a, p, s, grid_mode);
+            case 31: return launch_p1_scatter_shape<256, 12, 4, 31, 8>(a, p, s, grid_mode);
+            case 27: return launch_p1_scatter_shape<256, 12, 4, 27, 8>(a, p, s, grid_mode);
+            case 25: return launch_p1_scatter_shape<256, 12, 4, 25, 8>(a, p, s, grid_mode);
+            case 21: return launch_p1_scatter_shape<256, 12, 4, 21, 8>(a, p, s, grid_mode);
+            default: break;
         }
-    }
+    // beside a concurrent stream otherwise: a 64-register shape of four blocks
+    // an SM for 256 partitions; with 512 a round of 2048 records would write
+    // runs of 4, so the 3-block shape below keeps its rounds and leaves one
+    // of its blocks
+    if (grid_mode == kScatterShared && p.bits == 8) return launch_p1_scatter_shape<256, 8, 4>(a, p, s, grid_mode);
     switch (shape) {  // shape 3 changes only the level-2 scatter, shape 4 only level 1
         case 1: return launch_p1_scatter_shape<512, 8, 2>(a, p, s, grid_mode);
         case 2: return launch_p1_scatter_shape<256, 8, 4>(a, p, s, grid_mode);
         default:
-            // single-sample builds with 256 partitions and a common k: the walk's
-            // shifts and masks and the record layout are compile-time constants
-            if (!a.segs && !a.read_seg && !a.tag_bits && p.bits == 8) switch (a.k) {
-                    case 31: return launch_p1_scatter_shape<256, 16, 3, 31, 8>(a, p, s, grid_mode);
-                    case 27: return launch_p1_scatter_shape<256, 16, 3, 27, 8>(a, p, s, grid_mode);
-                    case 25: return launch_p1_scatter_shape<256, 16, 3, 25, 8>(a, p, s, grid_mode);
-                    case 21: return launch_p1_scatter_shape<256, 16, 3, 21, 8>(a, p, s, grid_mode);
-                    default: break;
-                }
-            if (!a.segs && !a.read_seg && !a.tag_bits && p.bits == 9 && a.k == 31)  // past 400M occurrences
+            if (single && p.bits == 9 && a.k == 31)  // past 400M occurrences: 512 partitions
                 return launch_p1_scatter_shape<256, 16, 3, 31, 9>(a, p, s, grid_mode);
             return launch_p1_scatter_shape<256, 16, 3>(a, p, s, grid_mode);
     }
