@@ -2432,10 +2432,12 @@ int launch_part_scatter(const BuildArgs &a, const PartArgs &p, cudaStream_t s, i
             default: break;
         }
     // beside a concurrent stream otherwise: a 64-register shape of four blocks
-    // an SM for 256 partitions; with 512 a round of 2048 records would write
-    // runs of 4, so the 3-block shape below keeps its rounds and leaves one
-    // of its blocks
+    // an SM, so that three work while a fourth block's room stays free (for
+    // 512 partitions with rounds of 16 records, which spill some registers:
+    // a round of 2048 would write runs of 4)
     if (grid_mode == kScatterShared && p.bits == 8) return launch_p1_scatter_shape<256, 8, 4>(a, p, s, grid_mode);
+    if (grid_mode == kScatterShared && single && p.bits == 9 && a.k == 31)
+        return launch_p1_scatter_shape<256, 16, 4, 31, 9>(a, p, s, grid_mode);
     switch (shape) {  // shape 3 changes only the level-2 scatter, shape 4 only level 1
         case 1: return launch_p1_scatter_shape<512, 8, 2>(a, p, s, grid_mode);
         case 2: return launch_p1_scatter_shape<256, 8, 4>(a, p, s, grid_mode);
