@@ -3,11 +3,14 @@
 // Same framing as the host path (and the reference, kmerGraph.cpp:113-114,
 // 160-233): from the first '>', lines alternate header / ONE sequence line;
 // acgt upper-cased, any other byte read as 'A'; sequences shorter than k
-// dropped. Steps: newlines per 16 KiB chunk -> scan -> every newline's
-// position -> record r = (line 2r, line 2r+1) -> keep sequences of length >= k
-// -> scan of kept reads and of their 16-base words -> pack. Every read starts
-// on a word boundary of the packed stream (read_off is a multiple of 16), so
-// each packed word belongs to one read and is written by one thread.
+// dropped. Steps: newlines per 16 KiB chunk (and a newline bit mask) -> scan
+// -> every newline's position -> record r = (line 2r, line 2r+1) -> keep
+// sequences of length >= k -> one scan of kept reads and of their 16-base
+// words -> pack. Every read starts on a word boundary of the packed stream
+// (read_off is a multiple of 16), so each packed word belongs to one read and
+// is written by one thread. A streamed text is framed a piece at a time; past
+// its first piece the records' ranges and the running totals can stay in
+// device memory (StreamState), with no host round trip per piece.
 #include <cuda_runtime.h>
 
 #include <algorithm>
