@@ -1,5 +1,6 @@
 """Host-side parts of the library that need no GPU: FASTA framing and 2-bit
 packing, the output writers, the C-ABI surface and the command line."""
+import ctypes as C
 import os
 import re
 import subprocess
@@ -140,6 +141,36 @@ def test_header_is_plain_c_and_links(tmp_path):
                         "-Wl,-rpath," + str(swapgb.LIB_PATH.parent), "-o", str(tmp_path / "caller")],
                        stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     assert r.returncode == 0, r.stdout
+
+
+STRUCTS = [("swg_opts", swapgb.Opts), ("swg_build_info", swapgb.BuildInfo), ("swg_merge_info", swapgb.MergeInfo),
+           ("swg_sample", swapgb.Sample), ("swg_server_opts", swapgb.ServerOpts),
+           ("swg_server_stats", swapgb.ServerStats), ("swg_tuning", swapgb.Tuning)]
+
+
+def test_ctypes_mirrors_match_the_header(tmp_path):
+    """Every struct swapgb.py mirrors has the header's size and field offsets
+    (a C program compiled against include/swapgb.h prints them)."""
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "swapgb.h"', "int main(void) {"]
+    for cname, py in STRUCTS:
+        lines.append('    printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for field, _ in py._fields_:
+            lines.append('    printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, field, cname, field))
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-I" + str(ROOT / "include"), str(src), "-o", str(exe)],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout
+    got = {}
+    for line in subprocess.run([str(exe)], stdout=subprocess.PIPE, text=True, check=True).stdout.splitlines():
+        cname, field, value = line.split()
+        got[(cname, field)] = int(value)
+    for cname, py in STRUCTS:
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for field, _ in py._fields_:
+            assert got[(cname, field)] == getattr(py, field).offset, (cname, field)
 
 
 def test_host_code_under_address_and_undefined_sanitizers(tmp_path):
